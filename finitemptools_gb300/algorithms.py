@@ -1,0 +1,337 @@
+"""DMRG and TDVP drivers on device-resident tensors (algorithms/dmrg.jl,
+algorithms/tdvp.jl, algorithms/dmrgexcited.jl:219-223) and expectation
+values (mpo/arithmetics.jl:267-276, mpohamiltonian/arithmetics.jl:5-19,
+operators/expecs.jl:29-55).
+
+Functions ending in ``_`` mutate their first argument like the reference's
+``!`` functions.  Sites are 1-based.  Every sweep keeps the MPS, the
+environments and the Krylov vectors on the GPU; only scalars come back.
+"""
+
+import numpy as np
+
+from .auxiliary import (MPSTruncation, default_truncation, dot, gemm, leftorth, norm,
+                        rightorth, scal, scale_cols, scale_rows, stable_tsvd)
+from .derivatives import HeffOp
+from .device import DeviceTensor
+from .envs import ExpectationCache, environments, increase_bond_env_, updateleft_, updateright_
+from .transfer import updateleft, updateright
+from .utilities import MPOHamiltonian
+
+__all__ = ["Defaults", "DMRG1", "DMRG2", "TDVP1", "leftsweep_", "rightsweep_", "sweep_",
+           "compute_", "ground_state_", "expectation", "expectation_local"]
+
+
+class Defaults:
+    """module Defaults (FiniteMPTools.jl:53-63)."""
+    maxiter = 100
+    D = 50
+    tol = 1e-12
+    dmrg_eig_tol = 1.0e-12
+    tdvp_exp_tol = 1.0e-8
+    verbosity = 1
+
+
+class DMRG2:
+    """@with_kw struct DMRG2 (algorithms/dmrg.jl:79-86) plus the device
+    options: ``precision`` of the contractions and FP64 Krylov
+    reorthogonalisation (``reorth``, not in the reference; off by default)."""
+
+    def __init__(self, maxiter=Defaults.maxiter, tol=Defaults.tol, eig_maxiter=10,
+                 eig_tol=Defaults.dmrg_eig_tol, verbosity=Defaults.verbosity, trunc=None,
+                 precision="fp64", reorth=False):
+        self.maxiter, self.tol = maxiter, tol
+        self.eig_maxiter, self.eig_tol = eig_maxiter, eig_tol
+        self.verbosity = verbosity
+        self.trunc = trunc if trunc is not None else default_truncation()
+        self.precision, self.reorth = precision, reorth
+
+
+class DMRG1:
+    """@with_kw struct DMRG1 (algorithms/dmrg.jl:8-15)."""
+
+    def __init__(self, D=Defaults.D, maxiter=Defaults.maxiter, tol=Defaults.tol, eig_maxiter=10,
+                 eig_tol=Defaults.dmrg_eig_tol, verbosity=Defaults.verbosity, precision="fp64",
+                 reorth=False):
+        self.D, self.maxiter, self.tol = D, maxiter, tol
+        self.eig_maxiter, self.eig_tol = eig_maxiter, eig_tol
+        self.verbosity = verbosity
+        self.precision, self.reorth = precision, reorth
+
+
+class TDVP1:
+    """struct TDVP1 (algorithms/tdvp.jl:8-17); stepsize is complex for real
+    time (-1j*dt).  ``krylovdim`` is the Krylov subspace of exponentiate."""
+
+    def __init__(self, stepsize, D=Defaults.D, exptol=Defaults.tdvp_exp_tol, ishermitian=False,
+                 verbosity=1, krylovdim=30, precision="fp64"):
+        self.stepsize = stepsize
+        self.D, self.exptol, self.ishermitian = D, exptol, ishermitian
+        self.verbosity, self.krylovdim, self.precision = verbosity, krylovdim, precision
+
+
+# ----------------------------------------------------------------- DMRG2
+def _two_site(A, B):
+    """twositemps[a,s1,s2,b] := A[a,s1,c] B[c,s2,b] (dmrg.jl:98)."""
+    Dl, d1, Dm = A.shape
+    _, d2, Dr = B.shape
+    return gemm(A, B, (Dl, d1, d2, Dr), Dl * d1, d2 * Dr, Dm)
+
+
+def _dmrg2_bond_left(m, site, alg):
+    """leftsweep! bond body (dmrg.jl:95-113): mps[site] = u, mps[site+1] = s*v."""
+    mps, mpo, hs = m.mps, m.mpo, m.hstorage
+    x2 = _two_site(mps[site], mps[site + 1])
+    Dl, d1, d2, Dr = x2.shape
+    op = HeffOp("ac2", hs[site], hs[site + 2], W1=mpo[site], W2=mpo[site + 1],
+                precision=alg.precision, dtype=x2.dtype)
+    E, vecs, info, k = op.lanczos(x2, alg.eig_maxiter, alg.eig_tol, alg.reorth)
+    del op
+    u, s, vt, err = stable_tsvd(vecs, Dl * d1, d2 * Dr, alg.trunc)
+    kk = s.shape[0]
+    scal(1.0 / norm(s), s)                                      # normalize!(s)
+    svt = scale_rows(vt, kk, d2 * Dr, s)                        # s * v (in place)
+    usv = gemm(u, svt, (Dl, d1, d2, Dr), Dl * d1, d2 * Dr, kk)
+    delta = abs(1 - abs(dot(usv, x2)))   # sum x2 * conj(u s v)  (dmrg.jl:109-110)
+    mps[site] = u.view_as((Dl, d1, kk))
+    mps[site + 1] = svt.view_as((kk, d2, Dr))
+    updateleft_(m, site)
+    if alg.verbosity > 2:
+        print("bond %d (left): E=%.15g lanczos k=%d info=%d D=%d" % (site, E, k, info, kk))
+    return E, delta
+
+
+def leftsweep_(m, alg):
+    """leftsweep!(m, alg) for DMRG2 (dmrg.jl:89-115) and DMRG1 (:27-52)."""
+    if isinstance(alg, DMRG1):
+        return _dmrg1_leftsweep(m, alg)
+    Es, delta = [], 0.0
+    for site in range(1, len(m.mps) - 1):
+        E, dl = _dmrg2_bond_left(m, site, alg)
+        Es.append(E)
+        delta = max(delta, dl)
+    return Es, delta
+
+
+def rightsweep_(m, alg):
+    """rightsweep!(m, alg) for DMRG2 (dmrg.jl:117-144) and DMRG1 (:54-76)."""
+    if isinstance(alg, DMRG1):
+        return _dmrg1_rightsweep(m, alg)
+    Es, delta = [], 0.0
+    for site in range(len(m.mps) - 1, 0, -1):
+        E, dl = _dmrg2_bond_right(m, site, alg)
+        Es.append(E)
+        delta = max(delta, dl)
+    return Es, delta
+
+
+def _dmrg2_bond_right(m, site, alg):
+    """rightsweep! bond body (dmrg.jl:123-142): mps[site] = u*s,
+    mps[site+1] = v, mps.s[site+1] = s."""
+    mps, mpo, hs = m.mps, m.mpo, m.hstorage
+    x2 = _two_site(mps[site], mps[site + 1])
+    Dl, d1, d2, Dr = x2.shape
+    op = HeffOp("ac2", hs[site], hs[site + 2], W1=mpo[site], W2=mpo[site + 1],
+                precision=alg.precision, dtype=x2.dtype)
+    E, vecs, info, k = op.lanczos(x2, alg.eig_maxiter, alg.eig_tol, alg.reorth)
+    del op
+    u, s, vt, err = stable_tsvd(vecs, Dl * d1, d2 * Dr, alg.trunc)
+    kk = s.shape[0]
+    scal(1.0 / norm(s), s)
+    # fidelity first (needs u, s, v before they are absorbed)
+    svt = scale_rows(vt.copy(), kk, d2 * Dr, s)
+    usv = gemm(u, svt, (Dl, d1, d2, Dr), Dl * d1, d2 * Dr, kk)
+    delta = abs(1 - abs(dot(usv, x2)))
+    del svt, usv
+    mps[site] = scale_cols(u, Dl * d1, kk, s).view_as((Dl, d1, kk))
+    mps[site + 1] = vt.view_as((kk, d2, Dr))
+    mps.s[site + 1] = s
+    updateright_(m, site + 1)
+    if alg.verbosity > 2:
+        print("bond %d (right): E=%.15g lanczos k=%d D=%d" % (site, E, k, kk))
+    return E, delta
+
+
+# ----------------------------------------------------------------- DMRG1
+def _galerkin(m, site, precision):
+    """calc_galerkin (dmrg.jl:17-24): || leftnull(A)^H * ac_prime(A) ||, zero when
+    the left null space is empty.  leftnull spans the complement of the thin
+    QR factor Q of A, so the norm is ||y - Q Q^H y||."""
+    A = m.mps[site]
+    Dl, d, Dr = A.shape
+    if Dl * d <= Dr:
+        return 0.0
+    op = HeffOp("ac", m.hstorage[site], m.hstorage[site + 1], W1=m.mpo[site],
+                precision=precision, dtype=A.dtype)
+    y = op(A)
+    Q, _ = leftorth(A, Dl * d, Dr)
+    r = Q.shape[1]
+    # y - Q (Q^H y)
+    qy = gemm(Q, y, (r, Dr), r, Dr, Dl * d, ta="C")
+    gemm(Q, qy, None, Dl * d, Dr, r, alpha=-1.0, beta=1.0, C=y)
+    return norm(y)
+
+
+def _dmrg1_leftsweep(m, alg):
+    increase_bond_env_(m, alg.D)
+    mps, mpo, hs = m.mps, m.mpo, m.hstorage
+    Es, delta = [], 0.0
+    for site in range(1, len(mps)):
+        A = mps[site]
+        op = HeffOp("ac", hs[site], hs[site + 1], W1=mpo[site], precision=alg.precision,
+                    dtype=A.dtype)
+        E, vec, _, _ = op.lanczos(A, alg.eig_maxiter, alg.eig_tol, alg.reorth)
+        Es.append(E)
+        delta = max(delta, _galerkin(m, site, alg.precision))
+        Dl, d, Dr = A.shape
+        Q, R = leftorth(vec, Dl * d, Dr)
+        r = Q.shape[1]
+        mps[site] = Q.view_as((Dl, d, r))
+        B = mps[site + 1]
+        mps[site + 1] = gemm(R, B, (r, B.shape[1], B.shape[2]), r, B.shape[1] * B.shape[2], Dr)
+        updateleft_(m, site)
+    return Es, delta
+
+
+def _dmrg1_rightsweep(m, alg):
+    mps, mpo, hs = m.mps, m.mpo, m.hstorage
+    Es, delta = [], 0.0
+    for site in range(len(mps), 1, -1):
+        A = mps[site]
+        op = HeffOp("ac", hs[site], hs[site + 1], W1=mpo[site], precision=alg.precision,
+                    dtype=A.dtype)
+        E, vec, _, _ = op.lanczos(A, alg.eig_maxiter, alg.eig_tol, alg.reorth)
+        Es.append(E)
+        delta = max(delta, _galerkin(m, site, alg.precision))
+        Dl, d, Dr = A.shape
+        Lm, Q = rightorth(vec, Dl, d * Dr)
+        r = Q.shape[0]
+        mps[site] = Q.view_as((r, d, Dr))
+        P = mps[site - 1]
+        mps[site - 1] = gemm(P, Lm, (P.shape[0], P.shape[1], r), P.shape[0] * P.shape[1], r, Dl)
+        updateright_(m, site)
+    return Es, delta
+
+
+# ----------------------------------------------------------------- TDVP1
+def _tdvp1_leftsweep(m, alg):
+    """_leftsweep!(m, ::TDVP1) (tdvp.jl:19-44)."""
+    increase_bond_env_(m, alg.D)
+    mps, mpo, hs = m.mps, m.mpo, m.hstorage
+    dt = alg.stepsize
+    L = len(mps)
+    for site in range(1, L):
+        A = mps[site]
+        op = HeffOp("ac", hs[site], hs[site + 1], W1=mpo[site], precision=alg.precision,
+                    dtype=A.dtype)
+        tmp = op.exponentiate(dt / 2, A, alg.exptol / abs(dt / 2), alg.krylovdim)
+        del op
+        Dl, d, Dr = A.shape
+        Q, v = leftorth(tmp, Dl * d, Dr)
+        r = Q.shape[1]
+        mps[site] = Q.view_as((Dl, d, r))
+        hnew = updateleft(hs[site], mps[site], mpo[site], mps[site], alg.precision)
+        opc = HeffOp("c", hnew, hs[site + 1], precision=alg.precision, dtype=A.dtype)
+        v = opc.exponentiate(-dt / 2, v, alg.exptol / abs(dt / 2), alg.krylovdim)
+        del opc
+        B = mps[site + 1]
+        mps[site + 1] = gemm(v, B, (r, B.shape[1], B.shape[2]), r, B.shape[1] * B.shape[2], Dr)
+        hs[site + 1] = hnew
+    site = L
+    op = HeffOp("ac", hs[site], hs[site + 1], W1=mpo[site], precision=alg.precision,
+                dtype=mps[site].dtype)
+    mps[site] = op.exponentiate(dt, mps[site], alg.exptol / abs(dt), alg.krylovdim)
+
+
+def _tdvp1_rightsweep(m, alg):
+    """_rightsweep!(m, ::TDVP1) (tdvp.jl:46-69)."""
+    mps, mpo, hs = m.mps, m.mpo, m.hstorage
+    dt = alg.stepsize
+    L = len(mps)
+    for site in range(L - 1, 0, -1):
+        B = mps[site + 1]
+        Dl, d, Dr = B.shape
+        v, Q = rightorth(B, Dl, d * Dr)
+        r = Q.shape[0]
+        mps[site + 1] = Q.view_as((r, d, Dr))
+        hnew = updateright(hs[site + 2], mps[site + 1], mpo[site + 1], mps[site + 1],
+                           alg.precision)
+        opc = HeffOp("c", hs[site + 1], hnew, precision=alg.precision, dtype=B.dtype)
+        v = opc.exponentiate(-dt / 2, v, alg.exptol / abs(dt / 2), alg.krylovdim)
+        del opc
+        hs[site + 1] = hnew
+        P = mps[site]
+        mps[site] = gemm(P, v, (P.shape[0], P.shape[1], r), P.shape[0] * P.shape[1], r, Dl)
+        op = HeffOp("ac", hs[site], hs[site + 1], W1=mpo[site], precision=alg.precision,
+                    dtype=P.dtype)
+        mps[site] = op.exponentiate(dt / 2, mps[site], alg.exptol / abs(dt / 2), alg.krylovdim)
+
+
+# --------------------------------------------------------------- drivers
+def sweep_(m, alg):
+    """sweep!(m, alg): DMRG returns (Energies, delta) (dmrgexcited.jl:219-223);
+    TDVP evolves in place (tdvp.jl:219-222)."""
+    if isinstance(alg, TDVP1):
+        _tdvp1_leftsweep(m, alg)
+        _tdvp1_rightsweep(m, alg)
+        return None
+    E1, d1 = leftsweep_(m, alg)
+    E2, d2 = rightsweep_(m, alg)
+    return E1 + E2, max(d1, d2)
+
+
+def compute_(env, alg):
+    """compute!(env, alg) (dmrg.jl:221-234)."""
+    all_E = []
+    it = 0
+    delta = 2 * alg.tol
+    while it < alg.maxiter and delta > alg.tol:
+        Es, delta = sweep_(env, alg)
+        all_E.extend(Es)
+        it += 1
+    return all_E, delta
+
+
+def ground_state_(state, h, alg=None):
+    """ground_state!(state, h, alg) (dmrg.jl:240)."""
+    alg = alg if alg is not None else DMRG2()
+    return compute_(environments(h, state, alg.precision), alg)
+
+
+# ------------------------------------------------------------ observables
+def expectation(psiA, h, psiB=None, precision="fp64"):
+    """expectation(psiA, h::FiniteMPO | MPOHamiltonian, psiB): a chain of
+    updateright from r_RR, closed with l_LL."""
+    psiB = psiA if psiB is None else psiB
+    L = len(psiA)
+    if isinstance(h, MPOHamiltonian):
+        Ws = h.site_tensors(L)
+    else:
+        Ws = list(h)
+    dt = np.complex128 if (psiA.dtype == np.complex128 or psiB.dtype == np.complex128 or
+                           any(np.iscomplexobj(W) for W in Ws)) else np.float64
+    w = Ws[-1].shape[2]
+    e = np.zeros((1, w, 1), dtype=dt)
+    e[0, w - 1, 0] = 1
+    hold = DeviceTensor.from_numpy(e, psiA.handle, dt)
+    for i in range(L, 0, -1):
+        hold = updateright(hold, psiA[i], Ws[i - 1].astype(dt), psiB[i], precision)
+    v = hold.numpy().reshape(-1)
+    return v[0]
+
+
+def expectation_local(psi, site, op):
+    """<psi|O_site|psi>/<psi|psi> for a one-site operator, by overlap chains
+    (operators/expecs.jl:29-55 with a one-site QTerm)."""
+    L = len(psi)
+    d = psi[1].shape[1]
+    dt = np.complex128 if (psi.dtype == np.complex128 or np.iscomplexobj(op)) else np.float64
+    one = np.ones((1, 1, 1), dtype=dt)
+    hold = DeviceTensor.from_numpy(one, psi.handle, dt)
+    nrm = DeviceTensor.from_numpy(one, psi.handle, dt)
+    I = np.eye(d, dtype=dt).reshape(1, d, 1, d)
+    O = np.asarray(op, dtype=dt).reshape(1, d, 1, d)
+    for i in range(L, 0, -1):
+        hold = updateright(hold, psi[i], O if i == site else I, psi[i])
+        nrm = updateright(nrm, psi[i], None, psi[i])
+    return hold.numpy().reshape(-1)[0] / nrm.numpy().reshape(-1)[0]

@@ -1,0 +1,140 @@
+// Internal declarations shared by the libfmpt translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cusolverDn.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/fmpt.h"
+
+struct fmpt_handle {
+  int device = 0;
+  cudaStream_t stream = nullptr;       // stream in use
+  cudaStream_t own_stream = nullptr;   // stream created by fmpt_create
+  cusolverDnHandle_t solver = nullptr;
+  uint64_t launches = 0;
+  std::string err;
+  // small pinned host staging area for scalars read back by the solvers
+  double* pinned = nullptr;
+  size_t pinned_len = 0;
+  int sm_count = 0;
+};
+
+namespace fmpt {
+
+int set_error(fmpt_handle* h, int status, const char* fmt, ...);
+
+#define FMPT_CUDA(h, expr)                                                              \
+  do {                                                                                  \
+    cudaError_t _e = (expr);                                                            \
+    if (_e != cudaSuccess)                                                              \
+      return ::fmpt::set_error((h), _e == cudaErrorMemoryAllocation ? FMPT_ERR_NOMEM    \
+                                                                    : FMPT_ERR_CUDA,    \
+                               "%s:%d %s: %s", __FILE__, __LINE__, #expr,              \
+                               cudaGetErrorString(_e));                                 \
+  } while (0)
+
+#define FMPT_TRY(expr)          \
+  do {                          \
+    int _s = (expr);            \
+    if (_s != FMPT_OK) return _s; \
+  } while (0)
+
+#define FMPT_LAUNCHED(h)                                                                \
+  do {                                                                                  \
+    (h)->launches++;                                                                    \
+    cudaError_t _e = cudaGetLastError();                                                \
+    if (_e != cudaSuccess)                                                              \
+      return ::fmpt::set_error((h), FMPT_ERR_CUDA, "%s:%d launch: %s", __FILE__,        \
+                               __LINE__, cudaGetErrorString(_e));                       \
+  } while (0)
+
+// Stream-ordered device scratch owned by a C++ scope.
+struct DevBuf {
+  fmpt_handle* h = nullptr;
+  void* p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  int alloc(fmpt_handle* hh, size_t nbytes);
+  void release();
+  double* d() const { return static_cast<double*>(p); }
+};
+
+int ensure_pinned(fmpt_handle* h, size_t n_doubles);
+
+// -------- generic FP64 / split-complex GEMM (gemm_f64.cu)
+// C = alpha op(A) op(B) + beta C ; planes: element offsets between re and im planes.
+struct GemmArgs {
+  int cplx;                 // 0 real, 1 split complex
+  int ta, tb;               // fmpt_trans
+  int m, n, k;
+  double alpha[2], beta[2];
+  const double* A; int64_t lda; int64_t planeA;
+  const double* B; int64_t ldb; int64_t planeB;
+  double* C; int64_t ldc; int64_t planeC;
+  int batch;                // batched over blockIdx.z with the strides below
+  int64_t strideA, strideB, strideC;
+};
+int gemm_f64(fmpt_handle* h, const GemmArgs& g);
+
+// -------- block-sparse MPO "middle" contraction (heff.cu)
+// out[o1, o2, wo, so] = sum_{blocks (wi -> wo)} sum_si coef[so, si] in[o1, o2, wi, si]
+struct MidSchedule {
+  int nw_in = 0, nw_out = 0, p_in = 0, p_out = 0, cplx = 0;
+  std::vector<int> blk_win;      // per block: input w
+  std::vector<int> wout_start;   // nw_out + 1 prefix offsets into the blocks (sorted by wo)
+  std::vector<double> coef;      // per block: p_out x p_in (row-major so, si), re then im if cplx
+  // device copies
+  int* d_win = nullptr;
+  int* d_wstart = nullptr;
+  double* d_coef = nullptr;
+  int nblocks() const { return (int)blk_win.size(); }
+};
+int mid_upload(fmpt_handle* h, MidSchedule& s);
+void mid_free(fmpt_handle* h, MidSchedule& s);
+struct MidStrides { int64_t o1, o2, w, s; };
+int mid_apply(fmpt_handle* h, const MidSchedule& s, const double* in, int64_t plane_in,
+              MidStrides si, double* out, int64_t plane_out, MidStrides so, int n1, int n2);
+
+// Schedules from dense host MPO tensors (W[wl, s_out, wr, s_in]).
+int schedule_ac2(fmpt_handle* h, int cplx, const double* W1, const double* W2, int d1, int d2,
+                 int wl, int wm, int wr, MidSchedule& s);
+int schedule_ac(fmpt_handle* h, int cplx, const double* W, int d, int wl, int wr, MidSchedule& s);
+// updateright maps the right index w2 (input) to the left index w (output)
+int schedule_env(fmpt_handle* h, int cplx, const double* W, int d, int wl, int wr, bool right,
+                 MidSchedule& s);
+
+// -------- vector kernels (krylov.cu)
+int vec_dot_dev(fmpt_handle* h, int cplx, int64_t n, const double* x, const double* y,
+                double* out_dev /* re, im */);
+int vec_nrm2_dev(fmpt_handle* h, int cplx, int64_t n, const double* x, double* out_dev);
+
+}  // namespace fmpt
+
+// The opaque operator type of the C ABI.
+struct fmpt_op {
+  fmpt_handle* h = nullptr;
+  int kind = 0;          // 0 ac2, 1 ac, 2 c
+  int dtype = FMPT_F64;
+  int precision = FMPT_PREC_FP64;
+  int Dl = 0, Dr = 0, d1 = 1, d2 = 1, wl = 1, wm = 1, wr = 1;
+  const double* hleft = nullptr;
+  const double* hright = nullptr;
+  fmpt::MidSchedule sched;
+  int64_t n = 0;          // vector length (complex elements for C128)
+  void* tc = nullptr;     // tensor-core state (mixed precision), owned
+};
+
+namespace fmpt {
+int op_apply_fp64(fmpt_op* op, const double* x, double* y);
+int op_tc_prepare(fmpt_op* op);
+int op_tc_apply(fmpt_op* op, const double* x, double* y);
+void op_tc_free(fmpt_op* op);
+}  // namespace fmpt

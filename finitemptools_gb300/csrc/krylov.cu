@@ -1,0 +1,614 @@
+// Krylov solvers on device-resident vectors: the reference's plain Lanczos
+// for the lowest eigenpair and a Krylov exponential for TDVP.
+//
+// Vectors stay in HBM for the whole solve; only the scalars that steer the
+// host loop (beta for the stopping test, the first column of the small
+// exponential for the step-size control) come back to the host.  All
+// reductions are deterministic two-level sums (warp shuffles inside a block,
+// a fixed-order sum over the block partials, recomputed by every consumer
+// block so that no separate finalisation launch is needed).
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "internal.h"
+
+namespace fmpt {
+namespace {
+
+constexpr int KT = 256;
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ double block_sum(double v) {
+  __shared__ double red[KT / 32];
+  __shared__ double total;
+  v = warp_sum(v);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double w = threadIdx.x < KT / 32 ? red[threadIdx.x] : 0.0;
+    w = warp_sum(w);
+    if (threadIdx.x == 0) total = w;
+  }
+  __syncthreads();
+  double r = total;
+  __syncthreads();
+  return r;
+}
+
+// fixed-order sum of G partials (every block computes the same value)
+__device__ double sum_parts(const double* part, int G) {
+  double s = 0.0;
+  for (int i = threadIdx.x; i < G; i += KT) s += part[i];
+  return block_sum(s);
+}
+
+// part[b] = sum x*y over a grid-stride slice (real view of length n)
+__global__ void rdot_partial(int64_t n, const double* __restrict__ x, const double* __restrict__ y,
+                             double* __restrict__ part) {
+  double s = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * KT + threadIdx.x; i < n; i += (int64_t)gridDim.x * KT)
+    s = fma(x[i], y[i], s);
+  s = block_sum(s);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+// x = v / ||v|| with ||v||^2 = sum(part); stores the norm in *nrm
+__global__ void normalize_from_parts(int64_t n, const double* __restrict__ v, double* __restrict__ x,
+                                     const double* __restrict__ part, int G, double* nrm) {
+  double s = sqrt(sum_parts(part, G));
+  if (blockIdx.x == 0 && threadIdx.x == 0) *nrm = s;
+  double inv = 1.0 / s;
+  for (int64_t i = (int64_t)blockIdx.x * KT + threadIdx.x; i < n; i += (int64_t)gridDim.x * KT)
+    x[i] = v[i] * inv;
+}
+
+// a = sum(part_a); alpha_out = a; y -= (q*a + qm1*b_old); part_b = partial |y|^2
+__global__ void lanczos_axpy(int64_t n, double* __restrict__ y, const double* __restrict__ q,
+                             const double* __restrict__ qm1, const double* __restrict__ part_a,
+                             int G, const double* b_old, double* alpha_out,
+                             double* __restrict__ part_b) {
+  const double a = sum_parts(part_a, G);
+  const double b = (qm1 != nullptr) ? *b_old : 0.0;
+  if (blockIdx.x == 0 && threadIdx.x == 0) *alpha_out = a;
+  double s = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * KT + threadIdx.x; i < n; i += (int64_t)gridDim.x * KT) {
+    double t = q[i] * a;
+    if (qm1) t += qm1[i] * b;
+    double v = y[i] - t;
+    y[i] = v;
+    s = fma(v, v, s);
+  }
+  s = block_sum(s);
+  if (threadIdx.x == 0) part_b[blockIdx.x] = s;
+}
+
+// b = sqrt(sum(part_b)); beta_out = b; if b != 0: y /= b
+__global__ void lanczos_scale(int64_t n, double* __restrict__ y, const double* __restrict__ part_b,
+                              int G, double* beta_out) {
+  const double b = sqrt(sum_parts(part_b, G));
+  if (blockIdx.x == 0 && threadIdx.x == 0) *beta_out = b;
+  if (b == 0.0) return;
+  // Julia's qi /= b divides element-wise; so does this (no reciprocal)
+  for (int64_t i = (int64_t)blockIdx.x * KT + threadIdx.x; i < n; i += (int64_t)gridDim.x * KT)
+    y[i] = y[i] / b;
+}
+
+// ---- multi-vector kernels over the Krylov basis V (j vectors of length n,
+// complex split planes when cplx: V_i re at V + i*2n, im at V + i*2n + n)
+// partial dots h_i = <V_i, z> ; part layout [G][j][2]
+__global__ void multidot_partial(int cplx, int64_t n, int j, const double* __restrict__ V,
+                                 int64_t vstride, const double* __restrict__ z,
+                                 double* __restrict__ part) {
+  for (int i = 0; i < j; i++) {
+    const double* v = V + (int64_t)i * vstride;
+    double sr = 0.0, si = 0.0;
+    for (int64_t e = (int64_t)blockIdx.x * KT + threadIdx.x; e < n; e += (int64_t)gridDim.x * KT) {
+      double vr = v[e], zr = z[e];
+      sr = fma(vr, zr, sr);
+      if (cplx) {
+        double vi = v[n + e], zi = z[n + e];
+        sr = fma(vi, zi, sr);
+        si = fma(vr, zi, si);
+        si = fma(-vi, zr, si);
+      }
+    }
+    sr = block_sum(sr);
+    if (cplx) si = block_sum(si);
+    if (threadIdx.x == 0) {
+      part[((int64_t)blockIdx.x * j + i) * 2] = sr;
+      part[((int64_t)blockIdx.x * j + i) * 2 + 1] = si;
+    }
+  }
+}
+
+// coef[i] (re, im) = sum over G partials; written by one block
+__global__ void multidot_finalize(int j, int G, const double* __restrict__ part,
+                                  double* __restrict__ coef, double* __restrict__ accum) {
+  for (int i = 0; i < j; i++) {
+    double sr = 0.0, si = 0.0;
+    for (int g = threadIdx.x; g < G; g += KT) {
+      sr += part[((int64_t)g * j + i) * 2];
+      si += part[((int64_t)g * j + i) * 2 + 1];
+    }
+    sr = block_sum(sr);
+    si = block_sum(si);
+    if (threadIdx.x == 0) {
+      coef[2 * i] = sr;
+      coef[2 * i + 1] = si;
+      if (accum) { accum[2 * i] += sr; accum[2 * i + 1] += si; }
+    }
+  }
+}
+
+// z -= sum_i coef_i V_i ; part = partial |z|^2
+__global__ void multi_axpy_sub(int cplx, int64_t n, int j, const double* __restrict__ V,
+                               int64_t vstride, const double* __restrict__ coef,
+                               double* __restrict__ z, double* __restrict__ part) {
+  double s = 0.0;
+  for (int64_t e = (int64_t)blockIdx.x * KT + threadIdx.x; e < n; e += (int64_t)gridDim.x * KT) {
+    double zr = z[e], zi = cplx ? z[n + e] : 0.0;
+    for (int i = 0; i < j; i++) {
+      const double* v = V + (int64_t)i * vstride;
+      double cr = coef[2 * i], ci = coef[2 * i + 1];
+      double vr = v[e];
+      if (cplx) {
+        double vi = v[n + e];
+        zr -= cr * vr - ci * vi;
+        zi -= cr * vi + ci * vr;
+      } else {
+        zr -= cr * vr;
+      }
+    }
+    z[e] = zr;
+    if (cplx) z[n + e] = zi;
+    s = fma(zr, zr, s);
+    if (cplx) s = fma(zi, zi, s);
+  }
+  s = block_sum(s);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+// out = sum_i c_i V_i (c complex when cplx, real otherwise); scale multiplies
+__global__ void combine_basis(int cplx, int64_t n, int j, const double* __restrict__ V,
+                              int64_t vstride, const double* __restrict__ c, int cstride,
+                              double scale, int last_first, double* __restrict__ out) {
+  for (int64_t e = (int64_t)blockIdx.x * KT + threadIdx.x; e < n; e += (int64_t)gridDim.x * KT) {
+    double r = 0.0, im = 0.0;
+    // lanczos_linear_transformation_single (simple_lanczos.jl:70-78) adds the
+    // last basis vector first
+    for (int t = 0; t < j; t++) {
+      int i = last_first ? (t == 0 ? j - 1 : t - 1) : t;
+      const double* v = V + (int64_t)i * vstride;
+      double cr = c[i * cstride], ci = cplx ? c[i * cstride + 1] : 0.0;
+      double vr = v[e];
+      if (cplx) {
+        double vi = v[n + e];
+        r += cr * vr - ci * vi;
+        im += cr * vi + ci * vr;
+      } else {
+        r += cr * vr;
+      }
+    }
+    out[e] = r * scale;
+    if (cplx) out[n + e] = im * scale;
+  }
+}
+
+// scale vector by 1/sqrt(sum parts) and store that norm
+__global__ void normalize_inplace(int64_t n_real, double* __restrict__ z,
+                                  const double* __restrict__ part, int G, double* nrm_out) {
+  double s = sqrt(sum_parts(part, G));
+  if (blockIdx.x == 0 && threadIdx.x == 0) *nrm_out = s;
+  if (s == 0.0) return;
+  for (int64_t e = (int64_t)blockIdx.x * KT + threadIdx.x; e < n_real;
+       e += (int64_t)gridDim.x * KT)
+    z[e] = z[e] / s;
+}
+
+// Lowest eigenpair of the symmetric tridiagonal (alpha[0..k-1], beta[0..k-2])
+// by Sturm-sequence bisection and inverse iteration with a partially pivoted
+// tridiagonal solve (the LAPACK dgtsv elimination).  One thread: k <= 128.
+__global__ void tridiag_lowest(int k, const double* __restrict__ alpha,
+                               const double* __restrict__ beta, double* eval_out,
+                               double* __restrict__ evec_out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double lo = alpha[0], hi = alpha[0];
+  for (int i = 0; i < k; i++) {
+    double r = (i > 0 ? fabs(beta[i - 1]) : 0.0) + (i < k - 1 ? fabs(beta[i]) : 0.0);
+    lo = fmin(lo, alpha[i] - r);
+    hi = fmax(hi, alpha[i] + r);
+  }
+  const double tiny = 1e-300;
+  for (int it = 0; it < 200; it++) {
+    double mid = 0.5 * (lo + hi);
+    if (mid <= lo || mid >= hi) break;
+    int cnt = 0;
+    double q = alpha[0] - mid;
+    if (q < 0) cnt++;
+    for (int i = 1; i < k; i++) {
+      if (q == 0.0) q = tiny;
+      q = (alpha[i] - mid) - beta[i - 1] * beta[i - 1] / q;
+      if (q < 0) cnt++;
+    }
+    if (cnt >= 1) hi = mid; else lo = mid;
+  }
+  const double lam = 0.5 * (lo + hi);
+  *eval_out = lam;
+  if (k == 1) { evec_out[0] = 1.0; return; }
+  double dl[128], dd[128], du[128], du2[128], x[128];
+  for (int i = 0; i < k; i++) x[i] = 1.0 / sqrt((double)k) * (1.0 + 0.01 * i);
+  double scale_ref = fmax(fabs(lo), fabs(hi)) + 1e-300;
+  for (int iter = 0; iter < 3; iter++) {
+    for (int i = 0; i < k; i++) {
+      dd[i] = alpha[i] - lam;
+      if (i < k - 1) { dl[i] = beta[i]; du[i] = beta[i]; }
+      du2[i] = 0.0;
+    }
+    // forward elimination with row interchanges
+    for (int i = 0; i < k - 1; i++) {
+      if (fabs(dd[i]) >= fabs(dl[i])) {
+        if (dd[i] == 0.0) dd[i] = 1e-300 * scale_ref + 1e-300;
+        double f = dl[i] / dd[i];
+        dd[i + 1] -= f * du[i];
+        x[i + 1] -= f * x[i];
+        dl[i] = 0.0;
+      } else {
+        double f = dd[i] / dl[i];
+        dd[i] = dl[i];
+        double t = dd[i + 1];
+        dd[i + 1] = du[i] - f * t;
+        if (i < k - 2) {
+          du2[i] = du[i + 1];
+          du[i + 1] = -f * du2[i];
+        }
+        du[i] = t;
+        double xt = x[i];
+        x[i] = x[i + 1];
+        x[i + 1] = xt - f * x[i + 1];
+      }
+    }
+    if (dd[k - 1] == 0.0) dd[k - 1] = 1e-300 * scale_ref + 1e-300;
+    // back substitution
+    x[k - 1] = x[k - 1] / dd[k - 1];
+    x[k - 2] = (x[k - 2] - du[k - 2] * x[k - 1]) / dd[k - 2];
+    for (int i = k - 3; i >= 0; i--) x[i] = (x[i] - du[i] * x[i + 1] - du2[i] * x[i + 2]) / dd[i];
+    double nrm = 0.0;
+    for (int i = 0; i < k; i++) nrm += x[i] * x[i];
+    nrm = sqrt(nrm);
+    for (int i = 0; i < k; i++) x[i] /= nrm;
+  }
+  for (int i = 0; i < k; i++) evec_out[i] = x[i];
+}
+
+// E = exp(H) for a small complex matrix (m <= 32, column-major, re/im pairs)
+// by Taylor scaling and squaring (Moler & Van Loan, method 3): scale so that
+// the 1-norm is <= 1/2, sum 20 Taylor terms, square back.
+__global__ void small_expm(int m, const double* __restrict__ H, double* __restrict__ E) {
+  __shared__ double Ar[32][33], Ai[32][33], Pr[32][33], Pi[32][33], Sr[32][33], Si[32][33];
+  __shared__ int s_sq;
+  const int r = threadIdx.x, c = threadIdx.y;
+  const bool in = (r < m && c < m);
+  Ar[r][c] = in ? H[2 * (r + c * m)] : 0.0;
+  Ai[r][c] = in ? H[2 * (r + c * m) + 1] : 0.0;
+  __syncthreads();
+  if (r == 0 && c == 0) {
+    double nrm = 0.0;
+    for (int j = 0; j < m; j++) {
+      double col = 0.0;
+      for (int i = 0; i < m; i++) col += hypot(Ar[i][j], Ai[i][j]);
+      nrm = fmax(nrm, col);
+    }
+    int s = 0;
+    while (nrm > 0.5 && s < 60) { nrm *= 0.5; s++; }
+    s_sq = s;
+  }
+  __syncthreads();
+  const double sc = ldexp(1.0, -s_sq);
+  Ar[r][c] *= sc;
+  Ai[r][c] *= sc;
+  const double id = (r == c && in) ? 1.0 : 0.0;
+  Pr[r][c] = id; Pi[r][c] = 0.0;
+  Sr[r][c] = id; Si[r][c] = 0.0;
+  __syncthreads();
+  for (int t = 1; t <= 20; t++) {
+    double nr = 0.0, ni = 0.0;
+    for (int q = 0; q < m; q++) {
+      nr += Pr[r][q] * Ar[q][c] - Pi[r][q] * Ai[q][c];
+      ni += Pr[r][q] * Ai[q][c] + Pi[r][q] * Ar[q][c];
+    }
+    __syncthreads();
+    Pr[r][c] = nr / t;
+    Pi[r][c] = ni / t;
+    Sr[r][c] += Pr[r][c];
+    Si[r][c] += Pi[r][c];
+    __syncthreads();
+  }
+  for (int t = 0; t < s_sq; t++) {
+    double nr = 0.0, ni = 0.0;
+    for (int q = 0; q < m; q++) {
+      nr += Sr[r][q] * Sr[q][c] - Si[r][q] * Si[q][c];
+      ni += Sr[r][q] * Si[q][c] + Si[r][q] * Sr[q][c];
+    }
+    __syncthreads();
+    Sr[r][c] = nr;
+    Si[r][c] = ni;
+    __syncthreads();
+  }
+  if (in) {
+    E[2 * (r + c * m)] = Sr[r][c];
+    E[2 * (r + c * m) + 1] = Si[r][c];
+  }
+}
+
+int grid_for(fmpt_handle* h, int64_t n) {
+  int64_t g = (n + KT - 1) / KT;
+  int64_t cap = (int64_t)h->sm_count * 4;
+  if (cap < 1) cap = 1;
+  return (int)std::max<int64_t>(1, std::min(g, cap));
+}
+
+}  // namespace
+}  // namespace fmpt
+
+using namespace fmpt;
+
+extern "C" {
+
+int fmpt_lanczos_ground(fmpt_op* op, const double* x0, int kmax, double btol, int reorth,
+                        double* eigval, double* xout, int* info, int* niter) {
+  if (!op) return FMPT_ERR_ARG;
+  fmpt_handle* h = op->h;
+  if (!x0 || !xout || !eigval) return set_error(h, FMPT_ERR_ARG, "lanczos: null pointer");
+  if (kmax < 1 || kmax > 128) return set_error(h, FMPT_ERR_ARG, "lanczos: kmax must be 1..128");
+  const int cp = op->dtype == FMPT_C128;
+  const int64_t n = op->n * (cp ? 2 : 1);   // real view of the vector
+  const int G = grid_for(h, n);
+  DevBuf Vb, Yb, scal, partA, partB, partM, coef;
+  FMPT_TRY(Vb.alloc(h, (size_t)(kmax + 1) * n * sizeof(double)));
+  FMPT_TRY(Yb.alloc(h, (size_t)n * sizeof(double)));
+  // scal: [0] vm, [1..kmax] alpha, [kmax+1 .. 2kmax] beta, [2kmax+1] eval, then evec (kmax)
+  FMPT_TRY(scal.alloc(h, (size_t)(3 * kmax + 8) * sizeof(double)));
+  FMPT_TRY(partA.alloc(h, (size_t)G * sizeof(double)));
+  FMPT_TRY(partB.alloc(h, (size_t)G * sizeof(double)));
+  FMPT_TRY(partM.alloc(h, (size_t)G * (kmax + 1) * 2 * sizeof(double)));
+  FMPT_TRY(coef.alloc(h, (size_t)(kmax + 1) * 2 * sizeof(double)));
+  FMPT_TRY(ensure_pinned(h, 4));
+  double* V = Vb.d();
+  double* y = Yb.d();
+  double* s_vm = scal.d();
+  double* s_alpha = scal.d() + 1;
+  double* s_beta = scal.d() + 1 + kmax;
+  double* s_eval = scal.d() + 1 + 2 * kmax;
+  double* s_evec = scal.d() + 2 + 2 * kmax;
+  auto V_ = [&](int i) { return V + (int64_t)i * n; };
+
+  // reorthogonalise y against V_0..V_{j-1} (classical Gram-Schmidt, one pass)
+  auto reorthogonalise = [&](int j) -> int {
+    multidot_partial<<<G, KT, 0, h->stream>>>(0, n, j, V, n, y, partM.d());
+    FMPT_LAUNCHED(h);
+    multidot_finalize<<<1, KT, 0, h->stream>>>(j, G, partM.d(), coef.d(), nullptr);
+    FMPT_LAUNCHED(h);
+    multi_axpy_sub<<<G, KT, 0, h->stream>>>(0, n, j, V, n, coef.d(), y, partB.d());
+    FMPT_LAUNCHED(h);
+    return FMPT_OK;
+  };
+
+  // ---- lanczos_make_first_step (simple_lanczos.jl:27-42)
+  rdot_partial<<<G, KT, 0, h->stream>>>(n, x0, x0, partA.d());
+  FMPT_LAUNCHED(h);
+  normalize_from_parts<<<G, KT, 0, h->stream>>>(n, x0, V_(0), partA.d(), G, s_vm);
+  FMPT_LAUNCHED(h);
+  FMPT_TRY(fmpt_op_apply(op, V_(0), y));
+  rdot_partial<<<G, KT, 0, h->stream>>>(n, V_(0), y, partA.d());
+  FMPT_LAUNCHED(h);
+  lanczos_axpy<<<G, KT, 0, h->stream>>>(n, y, V_(0), nullptr, partA.d(), G, nullptr, s_alpha,
+                                        partB.d());
+  FMPT_LAUNCHED(h);
+  if (reorth) FMPT_TRY(reorthogonalise(1));
+  lanczos_scale<<<G, KT, 0, h->stream>>>(n, y, partB.d(), G, s_beta);
+  FMPT_LAUNCHED(h);
+  FMPT_CUDA(h, cudaMemcpyAsync(h->pinned, s_beta, sizeof(double), cudaMemcpyDeviceToHost,
+                               h->stream));
+  FMPT_CUDA(h, cudaStreamSynchronize(h->stream));
+  double b = h->pinned[0];
+  int k = 1;
+  int inf = 0;
+  if (!std::isfinite(b)) return set_error(h, FMPT_ERR_NONFINITE, "lanczos: beta is not finite");
+  if (b < btol) {
+    // converged after the first step: Rayleigh quotient and the start vector
+    FMPT_CUDA(h, cudaMemcpyAsync(h->pinned, s_alpha, sizeof(double), cudaMemcpyDeviceToHost,
+                                 h->stream));
+    FMPT_CUDA(h, cudaMemcpyAsync(xout, V_(0), n * sizeof(double), cudaMemcpyDeviceToDevice,
+                                 h->stream));
+    FMPT_CUDA(h, cudaStreamSynchronize(h->stream));
+    *eigval = h->pinned[0];
+    if (info) *info = 0;
+    if (niter) *niter = 1;
+    return FMPT_OK;
+  }
+  // y holds q_1 (normalised); move it into V_1
+  FMPT_CUDA(h, cudaMemcpyAsync(V_(1), y, n * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+  bool converged = false;
+  while (k < kmax) {
+    // lanczos_make_step(A, V[k-1], V[k], beta[k-1])  (simple_lanczos.jl:49-68)
+    FMPT_TRY(fmpt_op_apply(op, V_(k), y));
+    rdot_partial<<<G, KT, 0, h->stream>>>(n, V_(k), y, partA.d());
+    FMPT_LAUNCHED(h);
+    lanczos_axpy<<<G, KT, 0, h->stream>>>(n, y, V_(k), V_(k - 1), partA.d(), G, s_beta + (k - 1),
+                                          s_alpha + k, partB.d());
+    FMPT_LAUNCHED(h);
+    if (reorth) FMPT_TRY(reorthogonalise(k + 1));
+    lanczos_scale<<<G, KT, 0, h->stream>>>(n, y, partB.d(), G, s_beta + k);
+    FMPT_LAUNCHED(h);
+    FMPT_CUDA(h, cudaMemcpyAsync(h->pinned, s_beta + k, sizeof(double), cudaMemcpyDeviceToHost,
+                                 h->stream));
+    FMPT_CUDA(h, cudaStreamSynchronize(h->stream));
+    b = h->pinned[0];
+    k += 1;
+    if (!std::isfinite(b)) return set_error(h, FMPT_ERR_NONFINITE, "lanczos: beta is not finite");
+    if (b < btol) { converged = true; break; }
+    if (k < kmax)
+      FMPT_CUDA(h, cudaMemcpyAsync(V_(k), y, n * sizeof(double), cudaMemcpyDeviceToDevice,
+                                   h->stream));
+  }
+  if (!converged) inf = -1;
+  // eigen(Symmetric(T[1:k,1:k])) on the device, lowest pair (find_lanczos "SR")
+  tridiag_lowest<<<1, 1, 0, h->stream>>>(k, s_alpha, s_beta, s_eval, s_evec);
+  FMPT_LAUNCHED(h);
+  combine_basis<<<G, KT, 0, h->stream>>>(0, n, k, V, n, s_evec, 1, 1.0, 1, xout);
+  FMPT_LAUNCHED(h);
+  FMPT_CUDA(h, cudaMemcpyAsync(h->pinned, s_eval, sizeof(double), cudaMemcpyDeviceToHost,
+                               h->stream));
+  FMPT_CUDA(h, cudaStreamSynchronize(h->stream));
+  *eigval = h->pinned[0];
+  if (info) *info = inf;
+  if (niter) *niter = k;
+  return FMPT_OK;
+}
+
+int fmpt_exponentiate(fmpt_op* op, double t_re, double t_im, const double* x, double* xout,
+                      int krylovdim, double tol, int* info) {
+  if (!op) return FMPT_ERR_ARG;
+  fmpt_handle* h = op->h;
+  if (!x || !xout) return set_error(h, FMPT_ERR_ARG, "exponentiate: null pointer");
+  if (krylovdim < 1 || krylovdim > 31)
+    return set_error(h, FMPT_ERR_ARG, "exponentiate: krylovdim must be 1..31");
+  const int cp = op->dtype == FMPT_C128;
+  if (!cp && t_im != 0.0)
+    return set_error(h, FMPT_ERR_ARG, "exponentiate: complex time step needs dtype C128");
+  const int64_t n = op->n;                     // elements (complex for C128)
+  const int64_t nr = n * (cp ? 2 : 1);         // real view
+  const int G = grid_for(h, nr);
+  const int M = krylovdim;
+  DevBuf Vb, zb, part, partM, coef, hcol, Hd, Ed, nrm;
+  FMPT_TRY(Vb.alloc(h, (size_t)(M + 1) * nr * sizeof(double)));
+  FMPT_TRY(zb.alloc(h, (size_t)nr * sizeof(double)));
+  FMPT_TRY(part.alloc(h, (size_t)G * sizeof(double)));
+  FMPT_TRY(partM.alloc(h, (size_t)G * (M + 1) * 2 * sizeof(double)));
+  FMPT_TRY(coef.alloc(h, (size_t)(M + 1) * 2 * sizeof(double)));
+  FMPT_TRY(hcol.alloc(h, (size_t)(M + 1) * 2 * sizeof(double)));
+  FMPT_TRY(Hd.alloc(h, (size_t)32 * 32 * 2 * sizeof(double)));
+  FMPT_TRY(Ed.alloc(h, (size_t)32 * 32 * 2 * sizeof(double)));
+  FMPT_TRY(nrm.alloc(h, 2 * sizeof(double)));
+  FMPT_TRY(ensure_pinned(h, (size_t)(M + 2) * 2 + 4));
+  double* V = Vb.d();
+  auto V_ = [&](int i) { return V + (int64_t)i * nr; };
+  const double tabs = std::hypot(t_re, t_im);
+  if (tabs == 0.0) {
+    FMPT_CUDA(h, cudaMemcpyAsync(xout, x, nr * sizeof(double), cudaMemcpyDeviceToDevice,
+                                 h->stream));
+    if (info) *info = 0;
+    return FMPT_OK;
+  }
+  const double sg_r = t_re / tabs, sg_i = t_im / tabs;
+  // w = x / ||x||
+  rdot_partial<<<G, KT, 0, h->stream>>>(nr, x, x, part.d());
+  FMPT_LAUNCHED(h);
+  normalize_from_parts<<<G, KT, 0, h->stream>>>(nr, x, V_(0), part.d(), G, nrm.d());
+  FMPT_LAUNCHED(h);
+  FMPT_CUDA(h, cudaMemcpyAsync(h->pinned, nrm.d(), sizeof(double), cudaMemcpyDeviceToHost,
+                               h->stream));
+  FMPT_CUDA(h, cudaStreamSynchronize(h->stream));
+  double scale = h->pinned[0];
+  if (scale == 0.0) {
+    FMPT_CUDA(h, cudaMemsetAsync(xout, 0, nr * sizeof(double), h->stream));
+    if (info) *info = 0;
+    return FMPT_OK;
+  }
+  double tau_done = 0.0, dtau = tabs;
+  int steps = 0;
+  std::vector<double> Hh((size_t)(M + 1) * M * 2);     // Hessenberg, column-major (re, im)
+  while (tau_done < tabs * (1.0 - 1e-15)) {
+    if (++steps > 1000) return set_error(h, FMPT_ERR_NOCONV, "exponentiate: too many steps");
+    std::fill(Hh.begin(), Hh.end(), 0.0);
+    int m = M;
+    bool happy = false;
+    double hmax = 0.0;
+    for (int j = 0; j < M; j++) {
+      FMPT_TRY(fmpt_op_apply(op, V_(j), zb.d()));
+      // two passes of classical Gram-Schmidt; hcol accumulates the coefficients
+      FMPT_CUDA(h, cudaMemsetAsync(hcol.d(), 0, (size_t)(M + 1) * 2 * sizeof(double), h->stream));
+      for (int pass = 0; pass < 2; pass++) {
+        multidot_partial<<<G, KT, 0, h->stream>>>(cp, n, j + 1, V, nr, zb.d(), partM.d());
+        FMPT_LAUNCHED(h);
+        multidot_finalize<<<1, KT, 0, h->stream>>>(j + 1, G, partM.d(), coef.d(), hcol.d());
+        FMPT_LAUNCHED(h);
+        multi_axpy_sub<<<G, KT, 0, h->stream>>>(cp, n, j + 1, V, nr, coef.d(), zb.d(), part.d());
+        FMPT_LAUNCHED(h);
+      }
+      normalize_inplace<<<G, KT, 0, h->stream>>>(nr, zb.d(), part.d(), G, nrm.d());
+      FMPT_LAUNCHED(h);
+      FMPT_CUDA(h, cudaMemcpyAsync(h->pinned, hcol.d(), (size_t)(j + 1) * 2 * sizeof(double),
+                                   cudaMemcpyDeviceToHost, h->stream));
+      FMPT_CUDA(h, cudaMemcpyAsync(h->pinned + 2 * (M + 1), nrm.d(), sizeof(double),
+                                   cudaMemcpyDeviceToHost, h->stream));
+      FMPT_CUDA(h, cudaStreamSynchronize(h->stream));
+      for (int i = 0; i <= j; i++) {
+        Hh[2 * (i + (size_t)(M + 1) * j)] = h->pinned[2 * i];
+        Hh[2 * (i + (size_t)(M + 1) * j) + 1] = h->pinned[2 * i + 1];
+        hmax = std::max(hmax, std::hypot(h->pinned[2 * i], h->pinned[2 * i + 1]));
+      }
+      const double hn = h->pinned[2 * (M + 1)];
+      if (!std::isfinite(hn)) return set_error(h, FMPT_ERR_NONFINITE, "exponentiate: NaN");
+      Hh[2 * (j + 1 + (size_t)(M + 1) * j)] = hn;
+      if (hn < 1e-14 * std::max(1.0, hmax)) { m = j + 1; happy = true; break; }
+      if (j + 1 < M + 1)
+        FMPT_CUDA(h, cudaMemcpyAsync(V_(j + 1), zb.d(), nr * sizeof(double),
+                                     cudaMemcpyDeviceToDevice, h->stream));
+    }
+    dtau = happy ? (tabs - tau_done) : std::min(dtau, tabs - tau_done);
+    std::vector<double> Hs((size_t)m * m * 2);
+    double err = 0.0;
+    for (int tries = 0; tries < 200; tries++) {
+      // Hs = (sign(t) * dtau) * H[0:m, 0:m]
+      const double fr = sg_r * dtau, fi = sg_i * dtau;
+      for (int c = 0; c < m; c++)
+        for (int r = 0; r < m; r++) {
+          double hr = Hh[2 * (r + (size_t)(M + 1) * c)], hi = Hh[2 * (r + (size_t)(M + 1) * c) + 1];
+          Hs[2 * (r + (size_t)m * c)] = fr * hr - fi * hi;
+          Hs[2 * (r + (size_t)m * c) + 1] = fr * hi + fi * hr;
+        }
+      FMPT_CUDA(h, cudaMemcpyAsync(Hd.d(), Hs.data(), Hs.size() * sizeof(double),
+                                   cudaMemcpyHostToDevice, h->stream));
+      small_expm<<<1, dim3(32, 32), 0, h->stream>>>(m, Hd.d(), Ed.d());
+      FMPT_LAUNCHED(h);
+      // first column of exp -> host (error estimate uses its last entry)
+      FMPT_CUDA(h, cudaMemcpyAsync(h->pinned, Ed.d(), (size_t)m * 2 * sizeof(double),
+                                   cudaMemcpyDeviceToHost, h->stream));
+      FMPT_CUDA(h, cudaStreamSynchronize(h->stream));
+      if (happy) { err = 0.0; break; }
+      const double hlast = Hh[2 * (m + (size_t)(M + 1) * (m - 1))];
+      err = std::abs(hlast * dtau) * std::hypot(h->pinned[2 * (m - 1)], h->pinned[2 * (m - 1) + 1]);
+      if (err <= 0.9 * tol * dtau) break;
+      dtau *= 0.5;
+    }
+    // w = sum_i E[i, 0] V_i (first column stays on the device in Ed)
+    combine_basis<<<G, KT, 0, h->stream>>>(cp, n, m, V, nr, Ed.d(), 2, 1.0, 0, zb.d());
+    FMPT_LAUNCHED(h);
+    rdot_partial<<<G, KT, 0, h->stream>>>(nr, zb.d(), zb.d(), part.d());
+    FMPT_LAUNCHED(h);
+    normalize_from_parts<<<G, KT, 0, h->stream>>>(nr, zb.d(), V_(0), part.d(), G, nrm.d());
+    FMPT_LAUNCHED(h);
+    FMPT_CUDA(h, cudaMemcpyAsync(h->pinned, nrm.d(), sizeof(double), cudaMemcpyDeviceToHost,
+                                 h->stream));
+    FMPT_CUDA(h, cudaStreamSynchronize(h->stream));
+    scale *= h->pinned[0];
+    tau_done += dtau;
+    if (!happy && tau_done < tabs) dtau = std::min(2.0 * dtau, tabs - tau_done);
+  }
+  // xout = scale * V_0
+  FMPT_CUDA(h, cudaMemcpyAsync(xout, V_(0), nr * sizeof(double), cudaMemcpyDeviceToDevice,
+                               h->stream));
+  double sc[2] = {scale, 0.0};
+  FMPT_TRY(fmpt_scal(h, FMPT_F64, nr, sc, xout));
+  if (info) *info = steps;
+  return FMPT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,279 @@
+// Dense FP64 factorisations on the device through cuSOLVER: the truncated
+// two-site SVD (auxiliary/stable_svd.jl + truncation.jl) and the QR/LQ gauge
+// moves (leftorth!/rightorth with QR()/LQ()).  cuSOLVER is a library call;
+// the truncation rule, the layout plumbing and the gesvd -> gesvdj fallback
+// (the reference retries gesdd with gesvd) are here.
+#include <cuComplex.h>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "internal.h"
+
+namespace fmpt {
+namespace {
+
+// dst(i, j) = op(src)(i, j) for a rows x cols destination.
+//   src/dst plane < 0: interleaved complex (re, im pairs); >= 0: split planes
+//   trans: read src(j, i); conj: negate the imaginary part
+__global__ void mat_copy(int cplx, int rows, int cols, const double* __restrict__ src,
+                         int64_t s_ld, int64_t s_plane, int trans, int conj,
+                         double* __restrict__ dst, int64_t d_ld, int64_t d_plane) {
+  int64_t tot = (int64_t)rows * cols;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < tot;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    int i = (int)(t % rows), j = (int)(t / rows);
+    int64_t si = trans ? (int64_t)j + (int64_t)i * s_ld : (int64_t)i + (int64_t)j * s_ld;
+    int64_t di = (int64_t)i + (int64_t)j * d_ld;
+    double re, im = 0.0;
+    if (!cplx) {
+      re = src[si];
+    } else if (s_plane < 0) {
+      re = src[2 * si]; im = src[2 * si + 1];
+    } else {
+      re = src[si]; im = src[s_plane + si];
+    }
+    if (conj) im = -im;
+    if (!cplx) {
+      dst[di] = re;
+    } else if (d_plane < 0) {
+      dst[2 * di] = re; dst[2 * di + 1] = im;
+    } else {
+      dst[di] = re; dst[d_plane + di] = im;
+    }
+  }
+}
+
+// zero the strictly lower triangle of a rows x cols (ld) matrix (split planes)
+__global__ void zero_lower(int cplx, int rows, int cols, double* M, int64_t ld, int64_t plane) {
+  int64_t tot = (int64_t)rows * cols;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < tot;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    int i = (int)(t % rows), j = (int)(t / rows);
+    if (i > j) {
+      M[i + j * ld] = 0.0;
+      if (cplx) M[plane + i + j * ld] = 0.0;
+    }
+  }
+}
+
+int copy_mat(fmpt_handle* h, int cplx, int rows, int cols, const double* src, int64_t s_ld,
+             int64_t s_plane, int trans, int conj, double* dst, int64_t d_ld, int64_t d_plane) {
+  int64_t tot = (int64_t)rows * cols;
+  if (tot == 0) return FMPT_OK;
+  int64_t g = std::min<int64_t>((tot + 255) / 256, (int64_t)h->sm_count * 8);
+  mat_copy<<<(unsigned)std::max<int64_t>(g, 1), 256, 0, h->stream>>>(
+      cplx, rows, cols, src, s_ld, s_plane, trans, conj, dst, d_ld, d_plane);
+  FMPT_LAUNCHED(h);
+  return FMPT_OK;
+}
+
+#define FMPT_SOLVER(h, expr)                                                         \
+  do {                                                                               \
+    cusolverStatus_t _s = (expr);                                                    \
+    if (_s != CUSOLVER_STATUS_SUCCESS)                                               \
+      return set_error((h), FMPT_ERR_CUSOLVER, "%s:%d %s -> cusolver status %d",     \
+                       __FILE__, __LINE__, #expr, (int)_s);                          \
+  } while (0)
+
+int read_info(fmpt_handle* h, const int* dinfo, int* out) {
+  FMPT_TRY(ensure_pinned(h, 1));
+  FMPT_CUDA(h, cudaMemcpyAsync(h->pinned, dinfo, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  FMPT_CUDA(h, cudaStreamSynchronize(h->stream));
+  *out = *reinterpret_cast<int*>(h->pinned);
+  return FMPT_OK;
+}
+
+// Full thin SVD of a tall (m >= n) matrix given in solver layout (real, or
+// interleaved complex) in Awork (overwritten).  U: m x n, S: n, VT: n x n.
+int svd_tall(fmpt_handle* h, int cplx, int m, int n, double* Awork, double* S, double* U,
+             double* VT) {
+  DevBuf work, rwork, dinfo;
+  FMPT_TRY(dinfo.alloc(h, sizeof(int)));
+  int lwork = 0;
+  if (cplx)
+    FMPT_SOLVER(h, cusolverDnZgesvd_bufferSize(h->solver, m, n, &lwork));
+  else
+    FMPT_SOLVER(h, cusolverDnDgesvd_bufferSize(h->solver, m, n, &lwork));
+  // gesvd destroys A: keep a copy for the Jacobi fallback
+  DevBuf Acopy;
+  const size_t abytes = (size_t)m * n * sizeof(double) * (cplx ? 2 : 1);
+  FMPT_TRY(Acopy.alloc(h, abytes));
+  FMPT_CUDA(h, cudaMemcpyAsync(Acopy.p, Awork, abytes, cudaMemcpyDeviceToDevice, h->stream));
+  FMPT_TRY(work.alloc(h, (size_t)std::max(lwork, 1) * sizeof(double) * (cplx ? 2 : 1)));
+  FMPT_TRY(rwork.alloc(h, (size_t)std::max(n, 1) * 5 * sizeof(double)));
+  if (cplx)
+    FMPT_SOLVER(h, cusolverDnZgesvd(h->solver, 'S', 'S', m, n, (cuDoubleComplex*)Awork, m, S,
+                                    (cuDoubleComplex*)U, m, (cuDoubleComplex*)VT, n,
+                                    (cuDoubleComplex*)work.p, lwork, rwork.d(), (int*)dinfo.p));
+  else
+    FMPT_SOLVER(h, cusolverDnDgesvd(h->solver, 'S', 'S', m, n, Awork, m, S, U, m, VT, n,
+                                    work.d(), lwork, rwork.d(), (int*)dinfo.p));
+  int info = 0;
+  FMPT_TRY(read_info(h, (const int*)dinfo.p, &info));
+  if (info == 0) return FMPT_OK;
+  if (info < 0) return set_error(h, FMPT_ERR_CUSOLVER, "gesvd: illegal argument %d", -info);
+  // not converged: retry with the one-sided Jacobi SVD (stable_svd.jl:12-18 pattern)
+  gesvdjInfo_t params;
+  FMPT_SOLVER(h, cusolverDnCreateGesvdjInfo(&params));
+  DevBuf V;
+  FMPT_TRY(V.alloc(h, (size_t)n * n * sizeof(double) * (cplx ? 2 : 1)));
+  int lw2 = 0;
+  cusolverStatus_t st;
+  if (cplx)
+    st = cusolverDnZgesvdj_bufferSize(h->solver, CUSOLVER_EIG_MODE_VECTOR, 1, m, n,
+                                      (cuDoubleComplex*)Acopy.p, m, S, (cuDoubleComplex*)U, m,
+                                      (cuDoubleComplex*)V.p, n, &lw2, params);
+  else
+    st = cusolverDnDgesvdj_bufferSize(h->solver, CUSOLVER_EIG_MODE_VECTOR, 1, m, n, Acopy.d(), m,
+                                      S, U, m, V.d(), n, &lw2, params);
+  DevBuf w2;
+  if (st == CUSOLVER_STATUS_SUCCESS) {
+    int s2 = w2.alloc(h, (size_t)std::max(lw2, 1) * sizeof(double) * (cplx ? 2 : 1));
+    if (s2 != FMPT_OK) { cusolverDnDestroyGesvdjInfo(params); return s2; }
+    if (cplx)
+      st = cusolverDnZgesvdj(h->solver, CUSOLVER_EIG_MODE_VECTOR, 1, m, n,
+                             (cuDoubleComplex*)Acopy.p, m, S, (cuDoubleComplex*)U, m,
+                             (cuDoubleComplex*)V.p, n, (cuDoubleComplex*)w2.p, lw2,
+                             (int*)dinfo.p, params);
+    else
+      st = cusolverDnDgesvdj(h->solver, CUSOLVER_EIG_MODE_VECTOR, 1, m, n, Acopy.d(), m, S, U, m,
+                             V.d(), n, w2.d(), lw2, (int*)dinfo.p, params);
+  }
+  cusolverDnDestroyGesvdjInfo(params);
+  if (st != CUSOLVER_STATUS_SUCCESS)
+    return set_error(h, FMPT_ERR_CUSOLVER, "gesvdj fallback failed (status %d)", (int)st);
+  FMPT_TRY(read_info(h, (const int*)dinfo.p, &info));
+  if (info != 0) return set_error(h, FMPT_ERR_CUSOLVER, "gesvd and gesvdj failed (info %d)", info);
+  // VT = V^H (interleaved layout, n x n)
+  return copy_mat(h, cplx, n, n, V.d(), n, cplx ? -1 : 0, 1, cplx, VT, n, cplx ? -1 : 0);
+}
+
+}  // namespace
+}  // namespace fmpt
+
+using namespace fmpt;
+
+extern "C" {
+
+int fmpt_svd_trunc(fmpt_handle* h, int dtype, const double* M, int m, int n, int maxD,
+                   double eps, double* U, double* S, double* Vt, int* kout, double* errout) {
+  if (!h || !M || !U || !S || !Vt || !kout) return FMPT_ERR_ARG;
+  if (m < 1 || n < 1 || maxD < 1) return set_error(h, FMPT_ERR_SHAPE, "svd: bad extents");
+  const int cp = dtype == FMPT_C128;
+  const int r = std::min(m, n);
+  const bool tall = m >= n;
+  const int mm = tall ? m : n, nn = tall ? n : m;   // solver problem is mm x nn, mm >= nn
+  const int64_t planeM = (int64_t)m * n;
+  DevBuf A, Uw, VTw, Sw;
+  const size_t es = sizeof(double) * (cp ? 2 : 1);
+  FMPT_TRY(A.alloc(h, (size_t)mm * nn * es));
+  FMPT_TRY(Uw.alloc(h, (size_t)mm * nn * es));
+  FMPT_TRY(VTw.alloc(h, (size_t)nn * nn * es));
+  FMPT_TRY(Sw.alloc(h, (size_t)nn * sizeof(double)));
+  // solver input: M (tall) or M^H (wide), interleaved for complex
+  FMPT_TRY(copy_mat(h, cp, mm, nn, M, m, planeM, tall ? 0 : 1, tall ? 0 : cp, A.d(), mm,
+                    cp ? -1 : 0));
+  FMPT_TRY(svd_tall(h, cp, mm, nn, A.d(), Sw.d(), Uw.d(), VTw.d()));
+  // singular values to the host, MPSTruncation rule
+  std::vector<double> s(r);
+  FMPT_CUDA(h, cudaMemcpyAsync(s.data(), Sw.d(), r * sizeof(double), cudaMemcpyDeviceToHost,
+                               h->stream));
+  FMPT_CUDA(h, cudaStreamSynchronize(h->stream));
+  double nrm = 0.0;
+  for (double v : s) nrm += v * v;
+  nrm = std::sqrt(nrm);
+  int keep = 0;
+  for (double v : s) keep += (v >= eps * nrm) ? 1 : 0;   // s is sorted descending
+  double e1 = 0.0, e2 = 0.0;
+  for (int i = keep; i < r; i++) e1 += s[i] * s[i];
+  int k = keep;
+  if (keep > maxD) {
+    for (int i = maxD; i < keep; i++) e2 += s[i] * s[i];
+    k = maxD;
+  }
+  if (errout) *errout = std::sqrt(e1 + e2);
+  *kout = k;
+  FMPT_CUDA(h, cudaMemcpyAsync(S, Sw.d(), k * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+  if (tall) {
+    // U = Uw[:, :k] (m x k), Vt = VTw[:k, :] (k x n)
+    FMPT_TRY(copy_mat(h, cp, m, k, Uw.d(), mm, cp ? -1 : 0, 0, 0, U, m, (int64_t)m * k));
+    FMPT_TRY(copy_mat(h, cp, k, n, VTw.d(), nn, cp ? -1 : 0, 0, 0, Vt, k, (int64_t)k * n));
+  } else {
+    // M^H = Uw S VTw  ->  M = VTw^H S Uw^H : U = (VTw[:k, :])^H, Vt = (Uw[:, :k])^H
+    FMPT_TRY(copy_mat(h, cp, m, k, VTw.d(), nn, cp ? -1 : 0, 1, cp, U, m, (int64_t)m * k));
+    FMPT_TRY(copy_mat(h, cp, k, n, Uw.d(), mm, cp ? -1 : 0, 1, cp, Vt, k, (int64_t)k * n));
+  }
+  return FMPT_OK;
+}
+
+int fmpt_qr(fmpt_handle* h, int dtype, const double* M, int m, int n, double* Q, double* R) {
+  if (!h || !M || !Q || !R) return FMPT_ERR_ARG;
+  if (m < 1 || n < 1) return set_error(h, FMPT_ERR_SHAPE, "qr: bad extents");
+  const int cp = dtype == FMPT_C128;
+  const int r = std::min(m, n);
+  const size_t es = sizeof(double) * (cp ? 2 : 1);
+  DevBuf A, tau, work, dinfo;
+  FMPT_TRY(A.alloc(h, (size_t)m * std::max(n, r) * es));
+  FMPT_TRY(tau.alloc(h, (size_t)r * es));
+  FMPT_TRY(dinfo.alloc(h, sizeof(int)));
+  FMPT_TRY(copy_mat(h, cp, m, n, M, m, (int64_t)m * n, 0, 0, A.d(), m, cp ? -1 : 0));
+  int lw1 = 0, lw2 = 0;
+  if (cp) {
+    FMPT_SOLVER(h, cusolverDnZgeqrf_bufferSize(h->solver, m, n, (cuDoubleComplex*)A.p, m, &lw1));
+    FMPT_SOLVER(h, cusolverDnZungqr_bufferSize(h->solver, m, r, r, (cuDoubleComplex*)A.p, m,
+                                               (cuDoubleComplex*)tau.p, &lw2));
+  } else {
+    FMPT_SOLVER(h, cusolverDnDgeqrf_bufferSize(h->solver, m, n, A.d(), m, &lw1));
+    FMPT_SOLVER(h, cusolverDnDorgqr_bufferSize(h->solver, m, r, r, A.d(), m, tau.d(), &lw2));
+  }
+  int lw = std::max(std::max(lw1, lw2), 1);
+  FMPT_TRY(work.alloc(h, (size_t)lw * es));
+  if (cp)
+    FMPT_SOLVER(h, cusolverDnZgeqrf(h->solver, m, n, (cuDoubleComplex*)A.p, m,
+                                    (cuDoubleComplex*)tau.p, (cuDoubleComplex*)work.p, lw,
+                                    (int*)dinfo.p));
+  else
+    FMPT_SOLVER(h, cusolverDnDgeqrf(h->solver, m, n, A.d(), m, tau.d(), work.d(), lw,
+                                    (int*)dinfo.p));
+  // R = upper triangle of A[0:r, 0:n]
+  FMPT_TRY(copy_mat(h, cp, r, n, A.d(), m, cp ? -1 : 0, 0, 0, R, r, (int64_t)r * n));
+  {
+    int64_t tot = (int64_t)r * n;
+    zero_lower<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>((tot + 255) / 256, 4096)), 256, 0,
+                 h->stream>>>(cp, r, n, R, r, (int64_t)r * n);
+    FMPT_LAUNCHED(h);
+  }
+  if (cp)
+    FMPT_SOLVER(h, cusolverDnZungqr(h->solver, m, r, r, (cuDoubleComplex*)A.p, m,
+                                    (cuDoubleComplex*)tau.p, (cuDoubleComplex*)work.p, lw,
+                                    (int*)dinfo.p));
+  else
+    FMPT_SOLVER(h, cusolverDnDorgqr(h->solver, m, r, r, A.d(), m, tau.d(), work.d(), lw,
+                                    (int*)dinfo.p));
+  int info = 0;
+  FMPT_TRY(read_info(h, (const int*)dinfo.p, &info));
+  if (info != 0) return set_error(h, FMPT_ERR_CUSOLVER, "qr: info %d", info);
+  return copy_mat(h, cp, m, r, A.d(), m, cp ? -1 : 0, 0, 0, Q, m, (int64_t)m * r);
+}
+
+int fmpt_lq(fmpt_handle* h, int dtype, const double* M, int m, int n, double* Lout, double* Q) {
+  if (!h || !M || !Lout || !Q) return FMPT_ERR_ARG;
+  if (m < 1 || n < 1) return set_error(h, FMPT_ERR_SHAPE, "lq: bad extents");
+  const int cp = dtype == FMPT_C128;
+  const int r = std::min(m, n);
+  const size_t es = sizeof(double) * (cp ? 2 : 1);
+  // M^H (n x m) = Q' R'  ->  M = R'^H Q'^H
+  DevBuf MH, Qp, Rp;
+  FMPT_TRY(MH.alloc(h, (size_t)n * m * es));
+  FMPT_TRY(Qp.alloc(h, (size_t)n * r * es));
+  FMPT_TRY(Rp.alloc(h, (size_t)r * m * es));
+  FMPT_TRY(copy_mat(h, cp, n, m, M, m, (int64_t)m * n, 1, cp, MH.d(), n, (int64_t)n * m));
+  FMPT_TRY(fmpt_qr(h, dtype, MH.d(), n, m, Qp.d(), Rp.d()));
+  FMPT_TRY(copy_mat(h, cp, m, r, Rp.d(), r, (int64_t)r * m, 1, cp, Lout, m, (int64_t)m * r));
+  FMPT_TRY(copy_mat(h, cp, r, n, Qp.d(), n, (int64_t)n * r, 1, cp, Q, r, (int64_t)r * n));
+  return FMPT_OK;
+}
+
+}  // extern "C"

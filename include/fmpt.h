@@ -1,0 +1,181 @@
+/*
+ * libfmpt -- GB300 (sm_103a) kernels for the DMRG/TDVP inner loop of
+ * FiniteMPTools, behind a plain C ABI.
+ *
+ * Conventions
+ *   - Every entry point returns an int status (FMPT_OK == 0, negative on
+ *     error); nothing is thrown across the ABI.  fmpt_last_error() gives the
+ *     message of the last failure on a handle.
+ *   - Tensor arguments are DEVICE pointers in the reference's column-major
+ *     layout and index order (Julia storage of the TensorKit tensors):
+ *       MPS site tensor   A[a, s, b]            -> A[a + Dl*(s + d*b)]
+ *       MPO site tensor   W[wl, s_out, wr, s_in] (HOST pointer, see below)
+ *       environment       L[a', w, a], R[b', w, b] (bra, mpo, ket)
+ *       two-site tensor   x[a, s1, s2, b]
+ *   - MPO tensors are tiny and are the only HOST pointers: the library
+ *     derives the nonzero (w, w') block schedule from them on the host.
+ *   - dtype FMPT_F64 is real double; FMPT_C128 is complex double held as
+ *     split planes: a tensor of n elements is 2n doubles, the n real parts
+ *     followed by the n imaginary parts (also for the host MPO tensors).
+ *   - A handle owns one CUDA stream, a cuSOLVER handle and a stream-ordered
+ *     memory pool.  It is not thread-safe: use one handle per host thread.
+ *     Calls are asynchronous on the handle's stream unless they return a
+ *     host scalar (eigenvalues, truncation results), which synchronise.
+ */
+#ifndef FMPT_H
+#define FMPT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct fmpt_handle fmpt_handle;
+typedef struct fmpt_op fmpt_op;
+
+enum fmpt_status {
+  FMPT_OK = 0,
+  FMPT_ERR_ARG = -1,          /* bad argument (null pointer, unknown enum)  ~ ArgumentError   */
+  FMPT_ERR_SHAPE = -2,        /* inconsistent dimensions                   ~ DimensionMismatch */
+  FMPT_ERR_CUDA = -3,         /* CUDA runtime error                                            */
+  FMPT_ERR_CUSOLVER = -4,     /* cuSOLVER error or non-converged factorisation                 */
+  FMPT_ERR_TIMEOUT = -5,      /* a bounded device wait gave up                                 */
+  FMPT_ERR_NONFINITE = -6,    /* NaN/Inf met in a reduction                                    */
+  FMPT_ERR_NOMEM = -7,        /* device allocation failed                                      */
+  FMPT_ERR_UNSUPPORTED = -8,  /* valid request this build does not implement                   */
+  FMPT_ERR_NOCONV = -9        /* Krylov exponential did not reach its tolerance                */
+};
+
+enum fmpt_dtype { FMPT_F64 = 0, FMPT_C128 = 1 };
+
+/* Arithmetic of the contractions (H_eff*x and environment updates).
+ * FP64 is the plain form; the others run on tcgen05 tensor cores with FP32
+ * accumulation (3xTF32 = hi/lo split products). */
+enum fmpt_precision { FMPT_PREC_FP64 = 0, FMPT_PREC_TF32X3 = 1, FMPT_PREC_TF32 = 2, FMPT_PREC_BF16 = 3 };
+
+enum fmpt_trans { FMPT_N = 0, FMPT_T = 1, FMPT_C = 2, FMPT_R = 3 /* conj, no transpose */ };
+
+/* ------------------------------------------------------------ handle */
+int fmpt_create(int device, fmpt_handle** out);
+int fmpt_destroy(fmpt_handle* h);
+const char* fmpt_status_string(int status);
+const char* fmpt_last_error(fmpt_handle* h);
+int fmpt_synchronize(fmpt_handle* h);
+/* Run subsequent work of this handle on an external cudaStream_t (NULL: the
+ * handle's own stream). */
+int fmpt_set_stream(fmpt_handle* h, void* cuda_stream);
+void* fmpt_get_stream(fmpt_handle* h);
+/* Number of kernels this handle has launched (own kernels only). */
+uint64_t fmpt_launch_count(fmpt_handle* h);
+int fmpt_version(void);
+
+/* ------------------------------------------------------------ memory */
+int fmpt_malloc(fmpt_handle* h, size_t bytes, void** dptr);
+int fmpt_free(fmpt_handle* h, void* dptr);
+int fmpt_memcpy_h2d(fmpt_handle* h, void* dst, const void* src, size_t bytes);
+int fmpt_memcpy_d2h(fmpt_handle* h, void* dst, const void* src, size_t bytes);
+int fmpt_memcpy_d2d(fmpt_handle* h, void* dst, const void* src, size_t bytes);
+int fmpt_memset_zero(fmpt_handle* h, void* dst, size_t bytes);
+
+/* ------------------------------------------------- BLAS-like helpers */
+/* C = alpha*op(A)*op(B) + beta*C, column-major, op from fmpt_trans.  For
+ * C128 the operands are split planes with plane strides (in elements)
+ * given by the matrix extents: A has lda*cols(A) elements per plane, etc.
+ * alpha/beta are {re, im}. */
+int fmpt_gemm(fmpt_handle* h, int dtype, int transa, int transb, int m, int n, int k,
+              const double* alpha, const double* A, int lda, const double* B, int ldb,
+              const double* beta, double* C, int ldc);
+/* out = <x, y> = sum conj(x_i) y_i, written to HOST out[0..1] (re, im). */
+int fmpt_dot(fmpt_handle* h, int dtype, int64_t n, const double* x, const double* y, double* out);
+int fmpt_nrm2(fmpt_handle* h, int dtype, int64_t n, const double* x, double* out);
+/* y = a*x + y ; x = a*x  (a = {re, im}) */
+int fmpt_axpy(fmpt_handle* h, int dtype, int64_t n, const double* a, const double* x, double* y);
+int fmpt_scal(fmpt_handle* h, int dtype, int64_t n, const double* a, double* x);
+/* M[i, j] *= s[i] (side 0) or s[j] (side 1); s is a real DEVICE vector. */
+int fmpt_scale_dim(fmpt_handle* h, int dtype, int side, int m, int n, const double* s, double* M);
+
+/* ------------------------------------------------------ H_eff * x
+ * ac2_prime (algorithms/derivatives.jl:20-22):
+ *   y[a',s1',s2',b'] = sum L[a',w,a] x[a,s1,s2,b] W1[w,s1',m,s1] W2[m,s2',w2,s2] R[b',w2,b]
+ * hleft [Dl, wl, Dl], hright [Dr, wr, Dr], W1 [wl, d1, wm, d1], W2 [wm, d2, wr, d2]. */
+int fmpt_ac2_prime(fmpt_handle* h, int dtype, int precision, const double* x,
+                   const double* W1_host, const double* W2_host, const double* hleft,
+                   const double* hright, double* y, int Dl, int d1, int d2, int Dr,
+                   int wl, int wm, int wr);
+/* ac_prime (derivatives.jl:2-4): y[a',s',b'] = sum L[a',w,a] x[a,s,b] W[w,s',w2,s] R[b',w2,b] */
+int fmpt_ac_prime(fmpt_handle* h, int dtype, int precision, const double* x,
+                  const double* W_host, const double* hleft, const double* hright, double* y,
+                  int Dl, int d, int Dr, int wl, int wr);
+/* c_prime (derivatives.jl:52-54): y[a',b'] = sum L[a',w,a] C[a,b] R[b',w,b] */
+int fmpt_c_prime(fmpt_handle* h, int dtype, int precision, const double* C,
+                 const double* hleft, const double* hright, double* y, int Dl, int Dr, int w);
+
+/* ------------------------------------------------ environment updates
+ * updateleft (mpo/transfer.jl:31-34):
+ *   hnew[b',w2,b] = sum hold[a',w,a] B[a,s,b] W[w,s',w2,s] conj(A[a',s',b'])
+ *   hold [Dl, wl, Dl], A/B [Dl, d, Dr], hnew [Dr, wr, Dr].
+ * updateright (mpo/transfer.jl:26-29):
+ *   hnew[a',w,a] = sum hold[b',w2,b] B[a,s,b] W[w,s',w2,s] conj(A[a',s',b'])
+ *   hold [Dr, wr, Dr], hnew [Dl, wl, Dl].
+ * W_host == NULL selects the operator-less overlap update (transfer.jl:37-45)
+ * with wl == wr. */
+int fmpt_updateleft(fmpt_handle* h, int dtype, int precision, const double* hold,
+                    const double* A, const double* W_host, const double* B, double* hnew,
+                    int Dl, int d, int Dr, int wl, int wr);
+int fmpt_updateright(fmpt_handle* h, int dtype, int precision, const double* hold,
+                     const double* A, const double* W_host, const double* B, double* hnew,
+                     int Dl, int d, int Dr, int wl, int wr);
+
+/* ---------------------------------------- prepared operators (solvers)
+ * An fmpt_op captures one effective Hamiltonian (its environments are
+ * referenced, not copied, and must stay alive and unchanged) so that the
+ * Krylov solvers can apply it repeatedly without re-deriving schedules or
+ * re-converting operands. */
+int fmpt_op_ac2(fmpt_handle* h, int dtype, int precision, const double* W1_host,
+                const double* W2_host, const double* hleft, const double* hright, int Dl,
+                int d1, int d2, int Dr, int wl, int wm, int wr, fmpt_op** out);
+int fmpt_op_ac(fmpt_handle* h, int dtype, int precision, const double* W_host,
+               const double* hleft, const double* hright, int Dl, int d, int Dr, int wl,
+               int wr, fmpt_op** out);
+int fmpt_op_c(fmpt_handle* h, int dtype, int precision, const double* hleft,
+              const double* hright, int Dl, int Dr, int w, fmpt_op** out);
+int fmpt_op_apply(fmpt_op* op, const double* x, double* y);
+int64_t fmpt_op_size(fmpt_op* op);
+int fmpt_op_destroy(fmpt_op* op);
+
+/* Lowest eigenpair by the reference's plain Lanczos
+ * (auxiliary/simple_lanczos.jl:83-120): three-term recurrence, stop when
+ * beta < btol, at most kmax Krylov vectors, lowest Ritz pair of the
+ * tridiagonal matrix (solved on the device in FP64).  reorth != 0 adds full
+ * FP64 reorthogonalisation (not in the reference; off for parity runs).
+ * eigval/info/niter are HOST outputs; xout is a device vector. */
+int fmpt_lanczos_ground(fmpt_op* op, const double* x0, int kmax, double btol, int reorth,
+                        double* eigval, double* xout, int* info, int* niter);
+
+/* xout = exp(t * op) x  (t = t_re + i t_im) by a Krylov projection of at
+ * most krylovdim vectors with adaptive time stepping to ``tol`` (the
+ * tolerance _exp_evolve hands KrylovKit.exponentiate, algorithms/tdvp.jl:3-6,
+ * already divided by |t|).  The op must be Hermitian.  A complex t needs
+ * dtype C128.  info (HOST) = number of Krylov restarts used. */
+int fmpt_exponentiate(fmpt_op* op, double t_re, double t_im, const double* x, double* xout,
+                      int krylovdim, double tol, int* info);
+
+/* ------------------------------------------------- dense factorisations
+ * Truncated SVD of M (m x n, column-major) with MPSTruncation semantics
+ * (auxiliary/truncation.jl:27-47, stable_svd.jl:12-18): drop sigma below
+ * eps*||sigma||_2, then keep at most maxD.  U (m x k, ld m), S (k, real),
+ * Vt (k x n, ld k) are device buffers sized for k = min(m, n).  k and err
+ * (2-norm of the dropped sigma) are HOST outputs. */
+int fmpt_svd_trunc(fmpt_handle* h, int dtype, const double* M, int m, int n, int maxD,
+                   double eps, double* U, double* S, double* Vt, int* k, double* err);
+/* Thin QR (leftorth!, QR()): M (m x n) = Q (m x r) R (r x n), r = min(m, n). */
+int fmpt_qr(fmpt_handle* h, int dtype, const double* M, int m, int n, double* Q, double* R);
+/* Thin LQ (rightorth, LQ()): M (m x n) = L (m x r) Q (r x n). */
+int fmpt_lq(fmpt_handle* h, int dtype, const double* M, int m, int n, double* Lout, double* Q);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FMPT_H */
