@@ -1,0 +1,403 @@
+#!/usr/bin/env python
+"""Benchmark of the DMRG/TDVP inner loop: two-site H_eff*x throughput.
+
+Workload (the H_eff*x microbenchmark configuration): x[D,2,2,D], L[D,5,D],
+R[D,5,D] iid N(0,1) from a fixed numpy seed, L and R symmetrised in (a, a'),
+the Heisenberg Schur MPO W[5,2,5,2] with its exact zero pattern; D = 2048
+(the largest size of the set) unless --D is given.  A step is one
+H_eff*x = ac2_prime(x, W, W, L, R) with the environments prepared once (as
+inside a Lanczos solve).  Algorithmic flops per step: F2 = 4 w d^2 D^3 +
+4 w^2 d^3 D^2 (the reference's dense pairwise order, derivatives.jl:21).
+
+Arms:
+  default            this library (libfmpt) at --precision (default bf16,
+                     FP32 accumulation); also reports every precision form
+                     (fp64, tf32x3, tf32, bf16) at D in {256..2048} with its
+                     relative Frobenius error against the FP64 form.
+  --impl reference   the reference's algorithm on the host cores: the numpy
+                     restatement of ac2_prime in the reference's pairwise
+                     order (OpenBLAS, all host threads).  The reference itself
+                     is Julia and cannot run on this machine.
+
+Multi-GPU: the path does not shard (each sweep is sequential over bonds), so
+--gpus N under torchrun runs N independent replicas; value = all replicas'
+flops over the slowest replica's time.
+"""
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "DMRG sweep s & H_eff·x TFLOP/s, mixed vs FP64 on one GB300 at ΔE≤1e-8"
+UNIT = "TFLOP/s"
+W_MPO, D_PHYS = 5, 2
+
+
+def flops_ac2(D, w=W_MPO, d=D_PHYS):
+    return 4 * w * d * d * D ** 3 + 4 * w * w * d ** 3 * D ** 2
+
+
+def workload(D, seed=2024):
+    from finitemptools_gb300.utilities import heisenberg_xxz_mpo
+    rng = np.random.default_rng(seed)
+    x = rng.standard_normal((D, 2, 2, D))
+    L = rng.standard_normal((D, W_MPO, D))
+    L = 0.5 * (L + L.transpose(2, 1, 0))
+    R = rng.standard_normal((D, W_MPO, D))
+    R = 0.5 * (R + R.transpose(2, 1, 0))
+    W = heisenberg_xxz_mpo(1.0, 1.0, 0.0)[1].dense()
+    return x, L, R, W
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return None
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                p = [q.strip() for q in line.split(",")]
+                if len(p) < 8:
+                    continue
+                try:
+                    sm.append(float(p[0]))
+                    mx = float(p[1])
+                except ValueError:
+                    continue
+                for nm, v in zip(names, p[4:8]):
+                    if v.lower().startswith("active"):
+                        reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(D, budget_s=12.0):
+    """The oracle's ac2_prime (numpy, reference pairwise order) on the host:
+    repeated full applications at D until about budget_s seconds."""
+    import oracle as O
+    x, L, R, W = workload(D)
+    O.ac2_prime(x, W, W, L, R)              # warm BLAS threads
+    n, t0 = 0, time.perf_counter()
+    while True:
+        O.ac2_prime(x, W, W, L, R)
+        n += 1
+        el = time.perf_counter() - t0
+        if el > budget_s or n >= 20:
+            break
+    return {"value": flops_ac2(D) * n / el / 1e12, "unit": UNIT, "cores": os.cpu_count(),
+            "kind": "port",
+            "sample": "%d full two-site H_eff*x applications at D=%d, float64, numpy/OpenBLAS "
+                      "with all %d host threads, %.1f s" % (n, D, os.cpu_count(), el)}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    import oracle as O
+    D = args.D
+    x, L, R, W = workload(D)
+    # bound the run: estimate one step, shrink the per-step sample if needed
+    t0 = time.perf_counter()
+    O.ac2_prime(x, W, W, L, R)
+    est = time.perf_counter() - t0
+    steps = args.steps + args.warmup
+    frac = 1.0
+    if est * steps > 150.0:
+        frac = max(150.0 / (est * steps), 1.0 / D)
+    nb = max(1, int(round(D * frac)))
+    Rs = R[:nb]                               # right-environment bra rows b' of the sample
+    f_step = (flops_ac2(D) - 2 * 4 * W_MPO * D ** 3) + 2 * 4 * W_MPO * D * D * nb
+    for _ in range(args.warmup):
+        O.ac2_prime(x, W, W, L, Rs)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        O.ac2_prime(x, W, W, L, Rs)
+        times.append(time.perf_counter() - t0)
+    ms = 1e3 * sum(times) / len(times)
+    v = f_step / (ms / 1e3) / 1e12
+    sample = ("two-site H_eff*x at D=%d, float64, numpy/OpenBLAS on %d host threads%s" %
+              (D, os.cpu_count(), "" if nb == D else
+               ", output columns b' sampled: %d of %d per step" % (nb, D)))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": config_dict(args, "fp64"),
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def config_dict(args, prec):
+    return {"workload": "two-site H_eff*x (ac2_prime), Heisenberg Schur MPO w=5, "
+                        "x[D,2,2,D], L/R[D,5,D] iid N(0,1) symmetrised",
+            "D": args.D, "w": W_MPO, "d": D_PHYS, "precision": prec,
+            "flops_per_step": flops_ac2(args.D), "seed": 2024,
+            "l2": "L2 flushed (256 MB write) between timed steps",
+            "parallelism": "replicas" if args.gpus > 1 else "single GPU"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--D", type=int, default=2048)
+    ap.add_argument("--precision", default="bf16", choices=["fp64", "tf32x3", "tf32", "bf16"])
+    ap.add_argument("--no-table", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    import finitemptools_gb300 as fm
+    from finitemptools_gb300 import DeviceTensor as DT
+    from finitemptools_gb300._native import lib, PREC
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    pg = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        pg = dist
+    # one explicit stream shared by torch (events, L2 flush) and libfmpt
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    h = fm.Handle(local)
+    h.set_stream(stream.cuda_stream)
+
+    D, prec = args.D, args.precision
+    x, L, R, W = workload(D)
+    xd, Ld, Rd = DT.from_numpy(x, h), DT.from_numpy(L, h), DT.from_numpy(R, h)
+    op = fm.HeffOp("ac2", Ld, Rd, W1=W, W2=W, precision=prec)
+    y = DT(x.shape, np.float64, h)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def barrier():
+        torch.cuda.synchronize()
+        if pg:
+            pg.barrier()
+
+    for _ in range(args.warmup):
+        op(xd, out=y)
+    barrier()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    with ClockSampler(local) as clk:
+        h.profile(True)
+        h.profile_read(0), h.profile_read(1), h.profile_read(2), h.profile_read(3)
+        n_launch0 = h.launch_count()
+        for k in range(args.steps):
+            flush.zero_()                      # evict L2 before every step (not timed)
+            ev[k][0].record(stream)
+            op(xd, out=y)
+            ev[k][1].record(stream)
+        barrier()
+        n_launch = h.launch_count() - n_launch0
+        tc_n, tc_ms = h.profile_read(0)
+        mid_n, mid_ms = h.profile_read(2)
+        cv_n, cv_ms = h.profile_read(3)
+        h.profile(False)
+        time.sleep(0.25)
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    tot_ms = sum(step_ms)
+    if pg:
+        t = torch.tensor([tot_ms], dtype=torch.float64)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        tot_ms = float(t[0])
+    F = flops_ac2(D)
+    value = F * args.steps * ws / (tot_ms / 1e3) / 1e12
+    clocks = clk.summary()
+
+    # ---- roofline of the dominant kernel (the tcgen05 GEMM: 2 launches per step,
+    # each 2*w*d^2*D^3 algorithmic flops)
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    if prec == "bf16":
+        peak, peak_note = peaks.get("bf16_tflops", 1900.0), "bf16_tflops (burst) of measured"
+    elif prec in ("tf32", "tf32x3"):
+        peak = peaks.get("bf16_tflops", 1900.0) / 2
+        peak_note = "half of measured bf16_tflops (dense TF32 rate is half of BF16)"
+    else:
+        peak, peak_note = None, None
+    roof = None
+    if tc_n:
+        per_launch = 2 * W_MPO * D_PHYS ** 2 * D ** 3
+        achieved = per_launch / (tc_ms / tc_n / 1e3) / 1e12
+        if prec == "tf32x3":
+            achieved *= 1.0          # algorithmic flops only (3 products are not credited)
+        roof = {"bound": "tensor", "kernel": "tc_gemm (tcgen05 %s)" % prec,
+                "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak if peak else None, "peak_source": peak_note,
+                "traffic": None, "launches": tc_n, "avg_launch_ms": tc_ms / tc_n,
+                "share_of_step": tc_ms / tot_ms if tot_ms else None,
+                "other_kernels_ms_per_step": {"mpo_step": mid_ms / args.steps,
+                                              "convert": cv_ms / args.steps}}
+
+    # ---- end to end through the C ABI with host buffers (pinned)
+    e2e = None
+    if rank == 0 or ws > 1:
+        hx = torch.from_numpy(x.ravel(order="F").copy()).pin_memory()
+        hL = torch.from_numpy(L.ravel(order="F").copy()).pin_memory()
+        hR = torch.from_numpy(R.ravel(order="F").copy()).pin_memory()
+        hy = torch.empty(x.size, dtype=torch.float64).pin_memory()
+        Wb = np.ascontiguousarray(W.ravel(order="F"))
+        dx, dL, dR, dy = DT(x.shape, np.float64, h), DT(L.shape, np.float64, h), \
+            DT(R.shape, np.float64, h), DT(x.shape, np.float64, h)
+        LIB = lib()
+
+        def e2e_step():
+            h.check(LIB.fmpt_memcpy_h2d(h.ptr, dx.ptr, hx.data_ptr(), hx.numel() * 8))
+            h.check(LIB.fmpt_memcpy_h2d(h.ptr, dL.ptr, hL.data_ptr(), hL.numel() * 8))
+            h.check(LIB.fmpt_memcpy_h2d(h.ptr, dR.ptr, hR.data_ptr(), hR.numel() * 8))
+            h.check(LIB.fmpt_ac2_prime(h.ptr, 0, PREC[prec], dx.ptr, Wb.ctypes.data,
+                                       Wb.ctypes.data, dL.ptr, dR.ptr, dy.ptr, D, 2, 2, D,
+                                       W_MPO, W_MPO, W_MPO))
+            h.check(LIB.fmpt_memcpy_d2h(h.ptr, hy.data_ptr(), dy.ptr, hy.numel() * 8))
+
+        for _ in range(2):
+            e2e_step()
+        n_e2e = max(3, min(args.steps, 10))
+        t_e2e = []
+        for _ in range(n_e2e):
+            flush.zero_()
+            torch.cuda.synchronize()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            e2e_step()
+            b.record(stream)
+            torch.cuda.synchronize()
+            t_e2e.append(a.elapsed_time(b))
+        e_ms = sum(t_e2e) / len(t_e2e)
+        e2e = {"value": F / (e_ms / 1e3) / 1e12, "unit": UNIT, "ms_per_step": e_ms,
+               "h2d_bytes_per_step": (x.size + L.size + R.size) * 8,
+               "d2h_bytes_per_step": x.size * 8,
+               "path": "fmpt_ac2_prime through the C ABI, pinned host x/L/R in, y out"}
+
+    # ---- every precision form at every size (config table), rank 0 only
+    table = None
+    if rank == 0 and not args.no_table:
+        table = []
+        for Dt in (256, 512, 1024, 2048):
+            xt, Lt, Rt, Wt = workload(Dt, seed=7)
+            xdt, Ldt, Rdt = DT.from_numpy(xt, h), DT.from_numpy(Lt, h), DT.from_numpy(Rt, h)
+            ref = None
+            for p in ("fp64", "tf32x3", "tf32", "bf16"):
+                opt = fm.HeffOp("ac2", Ldt, Rdt, W1=Wt, W2=Wt, precision=p)
+                yt = opt(xdt)
+                reps = 2 if (p == "fp64" and Dt >= 1024) else 5
+                for _ in range(1):
+                    opt(xdt, out=yt)
+                ts = []
+                for _ in range(reps):
+                    flush.zero_()
+                    a = torch.cuda.Event(enable_timing=True)
+                    b = torch.cuda.Event(enable_timing=True)
+                    a.record(stream)
+                    opt(xdt, out=yt)
+                    b.record(stream)
+                    torch.cuda.synchronize()
+                    ts.append(a.elapsed_time(b))
+                ms = min(ts)
+                yn = yt.numpy()
+                if p == "fp64":
+                    ref = yn
+                    err = 0.0
+                else:
+                    err = float(np.linalg.norm(yn - ref) / np.linalg.norm(ref))
+                table.append({"D": Dt, "dtype": p, "ms": ms,
+                              "tflops": flops_ac2(Dt) / (ms / 1e3) / 1e12,
+                              "rel_frobenius_err_vs_fp64": err})
+                del opt, yt
+        fp64 = {r["D"]: r["ms"] for r in table if r["dtype"] == "fp64"}
+        for r in table:
+            r["speedup_vs_fp64"] = fp64[r["D"]] / r["ms"]
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_baseline(D)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": tot_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": prec, "data": "synthetic",
+            "config": config_dict(args, prec), "clocks": clocks, "e2e": e2e,
+            "gpu_launches": n_launch, "roofline": roof, "cpu_baseline": cpu,
+            "per_dtype": table,
+        }
+        print(json.dumps(line), flush=True)
+    if pg:
+        pg.barrier()
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

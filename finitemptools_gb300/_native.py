@@ -38,6 +38,8 @@ SIGNATURES = {
     "fmpt_get_stream": (c_void_p, [c_void_p]),
     "fmpt_launch_count": (c_uint64, [c_void_p]),
     "fmpt_version": (c_int, []),
+    "fmpt_profile_enable": (c_int, [c_void_p, c_int]),
+    "fmpt_profile_read": (c_int, [c_void_p, c_int, P(c_int64), P(c_double)]),
     "fmpt_malloc": (c_int, [c_void_p, c_size_t, P(c_void_p)]),
     "fmpt_free": (c_int, [c_void_p, c_void_p]),
     "fmpt_memcpy_h2d": (c_int, [c_void_p, dptr, hptr, c_size_t]),

@@ -26,6 +26,30 @@ void DevBuf::release() {
   bytes = 0;
 }
 
+static cudaEvent_t pool_event(fmpt_handle* h) {
+  if (!h->ev_pool.empty()) {
+    cudaEvent_t e = h->ev_pool.back();
+    h->ev_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+ProfScope::ProfScope(fmpt_handle* hh, int c) : h(hh), cls(c) {
+  if (!h || !h->prof) return;
+  b = pool_event(h);
+  e = pool_event(h);
+  cudaEventRecord(b, h->stream);
+}
+
+ProfScope::~ProfScope() {
+  if (!b) return;
+  cudaEventRecord(e, h->stream);
+  h->prof_ev[cls].push_back({b, e});
+}
+
 int ensure_pinned(fmpt_handle* h, size_t n) {
   if (h->pinned_len >= n) return FMPT_OK;
   if (h->pinned) {
@@ -230,9 +254,35 @@ int fmpt_create(int device, fmpt_handle** out) {
   return FMPT_OK;
 }
 
+int fmpt_profile_enable(fmpt_handle* h, int on) {
+  if (!h) return FMPT_ERR_ARG;
+  h->prof = on != 0;
+  return FMPT_OK;
+}
+
+int fmpt_profile_read(fmpt_handle* h, int cls, int64_t* launches, double* total_ms) {
+  if (!h || cls < 0 || cls >= FMPT_K_COUNT) return FMPT_ERR_ARG;
+  FMPT_CUDA(h, cudaStreamSynchronize(h->stream));
+  double tot = 0.0;
+  for (auto& pr : h->prof_ev[cls]) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, pr.first, pr.second);
+    tot += ms;
+    h->ev_pool.push_back(pr.first);
+    h->ev_pool.push_back(pr.second);
+  }
+  if (launches) *launches = (int64_t)h->prof_ev[cls].size();
+  if (total_ms) *total_ms = tot;
+  h->prof_ev[cls].clear();
+  return FMPT_OK;
+}
+
 int fmpt_destroy(fmpt_handle* h) {
   if (!h) return FMPT_OK;
   cudaStreamSynchronize(h->stream);
+  for (auto& v : h->prof_ev)
+    for (auto& pr : v) { h->ev_pool.push_back(pr.first); h->ev_pool.push_back(pr.second); }
+  for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
   if (h->solver) cusolverDnDestroy(h->solver);
   if (h->pinned) cudaFreeHost(h->pinned);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);

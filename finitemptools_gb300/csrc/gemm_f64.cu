@@ -140,6 +140,7 @@ int gemm_f64(fmpt_handle* h, const GemmArgs& g) {
   if (grid.y > 65535 || grid.z > 65535)
     return set_error(h, FMPT_ERR_SHAPE, "gemm: grid too large (%d x %d x %d)", grid.x, grid.y,
                      grid.z);
+  ProfScope prof(h, FMPT_K_F64_GEMM);
   if (g.cplx)
     gemm_kernel<true><<<grid, NT, 0, h->stream>>>(g);
   else

@@ -207,6 +207,7 @@ int mid_apply(fmpt_handle* h, const MidSchedule& s, const double* in, int64_t pl
   if (blocks > 2147483647LL) return set_error(h, FMPT_ERR_SHAPE, "mid: too many threads");
   int P = std::max(s.p_in, s.p_out);
   if (P > 16) return set_error(h, FMPT_ERR_UNSUPPORTED, "physical dimension product %d > 16", P);
+  ProfScope prof(h, FMPT_K_MPO_STEP);
 #define MIDL(MP, CP)                                                                          \
   mid_kernel<MP, CP><<<(unsigned)blocks, threads, 0, h->stream>>>(                            \
       in, plane_in, si, out, plane_out, so, n1, n2, s.nw_out, s.p_in, s.p_out, s.d_win,       \

@@ -22,6 +22,10 @@ struct fmpt_handle {
   double* pinned = nullptr;
   size_t pinned_len = 0;
   int sm_count = 0;
+  // device timers (fmpt_profile_*)
+  bool prof = false;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof_ev[FMPT_K_COUNT];
+  std::vector<cudaEvent_t> ev_pool;
 };
 
 namespace fmpt {
@@ -68,6 +72,15 @@ struct DevBuf {
 };
 
 int ensure_pinned(fmpt_handle* h, size_t n_doubles);
+
+// Scoped device timer for one launch of a kernel class (no-op unless profiling).
+struct ProfScope {
+  fmpt_handle* h;
+  int cls;
+  cudaEvent_t b = nullptr, e = nullptr;
+  ProfScope(fmpt_handle* hh, int c);
+  ~ProfScope();
+};
 
 // -------- generic FP64 / split-complex GEMM (gemm_f64.cu)
 // C = alpha op(A) op(B) + beta C ; planes: element offsets between re and im planes.
@@ -136,5 +149,19 @@ namespace fmpt {
 int op_apply_fp64(fmpt_op* op, const double* x, double* y);
 int op_tc_prepare(fmpt_op* op);
 int op_tc_apply(fmpt_op* op, const double* x, double* y);
+int op_tc_check(fmpt_op* op);   // reads the device timeout flag (synchronises)
 void op_tc_free(fmpt_op* op);
+
+// K-major tensor-core operand: TF32 (float storage) or BF16 plane, optional
+// TF32 low plane (3xTF32), row stride and batch stride in elements.
+struct TcOperand {
+  const void* hi;
+  const void* lo;
+  int64_t ld;
+  int64_t bstride;
+};
+// C[m, n] (+ batch) = sum_k A[m, k] B[n, k] on tcgen05; mode 0 TF32, 1 3xTF32, 2 BF16;
+// C is FP32 (out_f64 = 0) or FP64, column-major with ldc.
+int tc_gemm(fmpt_handle* h, int mode, int M, int N, int K, int batch, const TcOperand& A,
+            const TcOperand& B, void* C, int out_f64, int64_t ldc, int64_t strideC, int* err_dev);
 }  // namespace fmpt

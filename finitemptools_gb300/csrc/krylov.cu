@@ -243,7 +243,8 @@ __global__ void tridiag_lowest(int k, const double* __restrict__ alpha,
   if (k == 1) { evec_out[0] = 1.0; return; }
   double dl[128], dd[128], du[128], du2[128], x[128];
   for (int i = 0; i < k; i++) x[i] = 1.0 / sqrt((double)k) * (1.0 + 0.01 * i);
-  double scale_ref = fmax(fabs(lo), fabs(hi)) + 1e-300;
+  // a zero pivot is replaced by eps*|T| (the LAPACK dlagts perturbation idea)
+  const double pert = 2.2e-16 * (fmax(fabs(lo), fabs(hi)) + 1e-300);
   for (int iter = 0; iter < 3; iter++) {
     for (int i = 0; i < k; i++) {
       dd[i] = alpha[i] - lam;
@@ -253,7 +254,7 @@ __global__ void tridiag_lowest(int k, const double* __restrict__ alpha,
     // forward elimination with row interchanges
     for (int i = 0; i < k - 1; i++) {
       if (fabs(dd[i]) >= fabs(dl[i])) {
-        if (dd[i] == 0.0) dd[i] = 1e-300 * scale_ref + 1e-300;
+        if (dd[i] == 0.0) dd[i] = pert;
         double f = dl[i] / dd[i];
         dd[i + 1] -= f * du[i];
         x[i + 1] -= f * x[i];
@@ -273,13 +274,17 @@ __global__ void tridiag_lowest(int k, const double* __restrict__ alpha,
         x[i + 1] = xt - f * x[i + 1];
       }
     }
-    if (dd[k - 1] == 0.0) dd[k - 1] = 1e-300 * scale_ref + 1e-300;
+    if (dd[k - 1] == 0.0) dd[k - 1] = pert;
     // back substitution
     x[k - 1] = x[k - 1] / dd[k - 1];
     x[k - 2] = (x[k - 2] - du[k - 2] * x[k - 1]) / dd[k - 2];
     for (int i = k - 3; i >= 0; i--) x[i] = (x[i] - du[i] * x[i + 1] - du2[i] * x[i + 2]) / dd[i];
+    // normalise without overflow: scale by the largest entry first
+    double mx = 0.0;
+    for (int i = 0; i < k; i++) mx = fmax(mx, fabs(x[i]));
+    if (!(mx > 0.0) || !isfinite(mx)) { for (int i = 0; i < k; i++) x[i] = (i == 0); mx = 1.0; }
     double nrm = 0.0;
-    for (int i = 0; i < k; i++) nrm += x[i] * x[i];
+    for (int i = 0; i < k; i++) { x[i] /= mx; nrm += x[i] * x[i]; }
     nrm = sqrt(nrm);
     for (int i = 0; i < k; i++) x[i] /= nrm;
   }
@@ -467,6 +472,7 @@ int fmpt_lanczos_ground(fmpt_op* op, const double* x0, int kmax, double btol, in
                                h->stream));
   FMPT_CUDA(h, cudaStreamSynchronize(h->stream));
   *eigval = h->pinned[0];
+  if (op->precision != FMPT_PREC_FP64) FMPT_TRY(op_tc_check(op));
   if (info) *info = inf;
   if (niter) *niter = k;
   return FMPT_OK;

@@ -1,0 +1,403 @@
+// Tensor-core (tcgen05 + TMA + TMEM) GEMM engine for the mixed-precision
+// forms of the contractions, and the mixed-precision H_eff*x built on it.
+//
+//   C[m, n] = sum_k A[m, k] B[n, k]      (A, B "K-major": k contiguous)
+//
+// One CTA owns a 128 x BN output tile.  Warp 0 streams A/B K-slices into a
+// STAGES-deep shared-memory ring with cp.async.bulk.tensor (128-byte
+// swizzle, no multicast), warp 1 allocates the TMEM accumulator and issues
+// tcgen05.mma from one thread (kind::tf32 or kind::f16 with BF16 operands,
+// FP32 accumulation), warps 2-5 drain TMEM with tcgen05.ld and store.
+// 3xTF32 issues three MMAs per K-step (hi*hi + hi*lo + lo*hi) into the same
+// accumulator from operands pre-split into TF32 hi/lo planes.
+//
+// Every mbarrier wait is bounded (wall clock, ~2 s): on expiry the kernel
+// raises a flag that the host turns into FMPT_ERR_TIMEOUT, drains its own
+// MMAs and TMA loads with bounded waits, frees TMEM and returns.
+#include <cuda.h>
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "internal.h"
+
+namespace fmpt {
+namespace tc {
+
+constexpr int BM = 128;
+constexpr int NTHREADS = 192;
+constexpr unsigned long long WAIT_NS = 2000000000ull;
+
+enum Mode { TF32 = 0, TF32X3 = 1, BF16 = 2 };
+
+// --------------------------------------------------------------- PTX helpers
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ unsigned long long globaltimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// bounded wait; false (and the abort flag set) when it gave up
+__device__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag,
+                          int* err) {
+  if (mbar_try(bar, parity)) return true;
+  const unsigned long long t0 = globaltimer();
+  while (true) {
+    if (mbar_try(bar, parity)) return true;
+    if (*abort_flag) return false;
+    if (globaltimer() - t0 > WAIT_NS) {
+      *abort_flag = 1;
+      atomicExch(err, 1);
+      return false;
+    }
+  }
+}
+
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, uint32_t bar,
+                                            int c0, int c1, int c2) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%3, %4, %5}], [%2];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(bar), "r"(c0), "r"(c1), "r"(c2)
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+// K-major operand tile, 128-byte rows, 128-byte swizzle, 8-row groups 1024 B apart
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr >> 4) & 0x3FFF);          // start address
+  d |= (uint64_t)1 << 16;                         // leading byte offset (unused for SW128 K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;               // stride byte offset: 8 rows x 128 B
+  d |= (uint64_t)1 << 46;                         // descriptor version (sm_100 family)
+  d |= (uint64_t)2 << 61;                         // SWIZZLE_128B
+  return d;
+}
+
+// instruction descriptor: D=F32, A/B format, K-major A and B, N, M
+__host__ __device__ constexpr uint32_t make_idesc(int mode, int M, int N) {
+  return (1u << 4) |                                      // D format F32
+         ((mode == BF16 ? 1u : 2u) << 7) |               // A: BF16 (kind::f16) / TF32
+         ((mode == BF16 ? 1u : 2u) << 10) |              // B
+         ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+template <int MODE>
+__device__ __forceinline__ void mma(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                    uint32_t accum) {
+  if (MODE == BF16) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(accum));
+  } else {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(accum));
+  }
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                   bar)
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
+      "%11, %12, %13, %14, %15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+struct EpiArgs {
+  void* C;            // float or double
+  int64_t ldc;        // column stride (elements)
+  int64_t strideC;    // batch stride (elements)
+  int M, N;
+  int* err;
+};
+
+template <int MODE, int BN, int STAGES, int OUT>
+struct Cfg {
+  static constexpr int KBYTES = 128;                            // bytes of K per stage row
+  static constexpr int KELEMS = MODE == BF16 ? 64 : 32;
+  static constexpr int A_BYTES = BM * KBYTES;
+  static constexpr int B_BYTES = BN * KBYTES;
+  static constexpr int SPLIT = MODE == TF32X3 ? 2 : 1;
+  static constexpr int STAGE_BYTES = (A_BYTES + B_BYTES) * SPLIT;
+  static constexpr int SMEM = STAGES * STAGE_BYTES + 1024 + 256;
+  static constexpr int TMEM_COLS = BN <= 32 ? 32 : BN <= 64 ? 64 : BN <= 128 ? 128 : 256;
+  static_assert(BN % 16 == 0 && BN >= 16 && BN <= 256, "N tile");
+  static_assert(SMEM <= 227 * 1024, "shared memory");
+};
+
+template <int MODE, int BN, int STAGES, int OUT>
+__global__ void __launch_bounds__(NTHREADS, 1)
+    gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
+                const __grid_constant__ CUtensorMap mapA2, const __grid_constant__ CUtensorMap mapB2,
+                int K, EpiArgs ep) {
+  using C_ = Cfg<MODE, BN, STAGES, OUT>;
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                             ~uintptr_t(1023));
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * C_::STAGE_BYTES);
+  // bars[0..S): full, [S..2S): empty, [2S]: accumulator ready, [2S+1]: drain
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 2);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN, z = blockIdx.z;
+  const int nk = (K + C_::KELEMS - 1) / C_::KELEMS;
+
+  auto stageA = [&](int s, int part) { return smem + s * C_::STAGE_BYTES + part * (C_::A_BYTES + C_::B_BYTES); };
+  auto stageB = [&](int s, int part) { return stageA(s, part) + C_::A_BYTES; };
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; s++) {
+      mbar_init(smem_u32(&bars[s]), 1);
+      mbar_init(smem_u32(&bars[STAGES + s]), 1);
+    }
+    mbar_init(smem_u32(&bars[2 * STAGES]), 1);
+    mbar_init(smem_u32(&bars[2 * STAGES + 1]), 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&mapA)) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&mapB)) : "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "r"(C_::TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      int issued_stage_last = -1;
+      for (int kb = 0; kb < nk; kb++) {
+        const int s = kb % STAGES;
+        const uint32_t ph = (kb / STAGES) & 1;
+        if (!mbar_wait(smem_u32(&bars[STAGES + s]), ph ^ 1, abort_flag, ep.err)) break;
+        const uint32_t full = smem_u32(&bars[s]);
+        mbar_expect_tx(full, C_::STAGE_BYTES);
+        const int kc = kb * C_::KELEMS;
+        tma_load_3d(smem_u32(stageA(s, 0)), &mapA, full, kc, m0, z);
+        tma_load_3d(smem_u32(stageB(s, 0)), &mapB, full, kc, n0, z);
+        if (MODE == TF32X3) {
+          tma_load_3d(smem_u32(stageA(s, 1)), &mapA2, full, kc, m0, z);
+          tma_load_3d(smem_u32(stageB(s, 1)), &mapB2, full, kc, n0, z);
+        }
+        issued_stage_last = kb;
+      }
+      if (*abort_flag) {
+        // drain: every load this thread issued must land before the CTA exits
+        for (int kb = max(0, issued_stage_last - STAGES + 1); kb <= issued_stage_last; kb++) {
+          const uint32_t bar = smem_u32(&bars[kb % STAGES]);
+          const unsigned long long t0 = globaltimer();
+          while (!mbar_try(bar, (kb / STAGES) & 1) && globaltimer() - t0 < WAIT_NS) {
+          }
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      constexpr uint32_t idesc = make_idesc(MODE, BM, BN);
+      for (int kb = 0; kb < nk; kb++) {
+        const int s = kb % STAGES;
+        const uint32_t ph = (kb / STAGES) & 1;
+        if (!mbar_wait(smem_u32(&bars[s]), ph, abort_flag, ep.err)) break;
+        tc_fence_after();
+        const uint32_t a0 = smem_u32(stageA(s, 0)), b0 = smem_u32(stageB(s, 0));
+#pragma unroll
+        for (int ks = 0; ks < 4; ks++) {                     // 4 x 32 bytes of K per stage
+          const uint32_t acc = (kb > 0 || ks > 0) ? 1u : 0u;
+          const uint64_t ad = smem_desc(a0 + ks * 32), bd = smem_desc(b0 + ks * 32);
+          mma<MODE>(tmem, ad, bd, idesc, acc);
+          if (MODE == TF32X3) {
+            const uint32_t a1 = smem_u32(stageA(s, 1)), b1 = smem_u32(stageB(s, 1));
+            mma<MODE>(tmem, ad, smem_desc(b1 + ks * 32), idesc, 1u);
+            mma<MODE>(tmem, smem_desc(a1 + ks * 32), bd, idesc, 1u);
+          }
+        }
+        mma_commit(smem_u32(&bars[STAGES + s]));             // frees the stage when done
+      }
+      mma_commit(smem_u32(&bars[2 * STAGES]));               // accumulator ready
+    }
+  } else {
+    // epilogue warps 2..5: TMEM lane quarter = warp % 4
+    const int q = warp & 3;
+    const bool ok = mbar_wait(smem_u32(&bars[2 * STAGES]), 0, abort_flag, ep.err);
+    tc_fence_after();
+    if (ok && !*abort_flag) {
+      const int row = m0 + 32 * q + lane;
+      const uint32_t tbase = tmem + ((uint32_t)(32 * q) << 16);
+#pragma unroll 1
+      for (int c0 = 0; c0 < BN; c0 += 16) {
+        uint32_t r[16];
+        tmem_ld16(tbase + c0, r);
+        if (row < ep.M) {
+#pragma unroll
+          for (int j = 0; j < 16; j++) {
+            const int n = n0 + c0 + j;
+            if (n < ep.N) {
+              const int64_t idx = (int64_t)row + ep.ldc * n + ep.strideC * z;
+              const float v = __uint_as_float(r[j]);
+              if (OUT == 1)
+                static_cast<double*>(ep.C)[idx] = (double)v;
+              else
+                static_cast<float*>(ep.C)[idx] = v;
+            }
+          }
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    if (lane == 0) {
+      // all MMAs issued by this CTA have retired before TMEM is released
+      mma_commit(smem_u32(&bars[2 * STAGES + 1]));
+      const unsigned long long t0 = globaltimer();
+      while (!mbar_try(smem_u32(&bars[2 * STAGES + 1]), 0) && globaltimer() - t0 < WAIT_NS) {
+      }
+    }
+    __syncwarp();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(C_::TMEM_COLS)
+                 : "memory");
+  }
+}
+
+// ---------------------------------------------------------- tensor maps
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn(fmpt_handle* h) {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  }
+  (void)h;
+  return fn;
+}
+
+// 3-D K-major operand map: dims {K, rows, batch}, box {K slice of 128 B, box_rows, 1}
+int make_map(fmpt_handle* h, CUtensorMap* map, const void* base, int mode, int64_t K,
+             int64_t rows, int64_t ld, int64_t batch, int64_t bstride, int box_rows) {
+  EncodeTiledFn fn = encode_fn(h);
+  if (!fn) return set_error(h, FMPT_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+  const int es = mode == BF16 ? 2 : 4;
+  if ((reinterpret_cast<uintptr_t>(base) & 15) || (ld * es) % 16 || (bstride * es) % 16)
+    return set_error(h, FMPT_ERR_SHAPE, "tensor map: operand not 16-byte aligned");
+  cuuint64_t dims[3] = {(cuuint64_t)K, (cuuint64_t)rows, (cuuint64_t)std::max<int64_t>(batch, 1)};
+  cuuint64_t strides[2] = {(cuuint64_t)(ld * es), (cuuint64_t)(std::max<int64_t>(bstride, ld * rows) * es)};
+  cuuint32_t box[3] = {(cuuint32_t)(128 / es), (cuuint32_t)box_rows, 1};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = fn(map, mode == BF16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
+                  3, const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return set_error(h, FMPT_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+  return FMPT_OK;
+}
+
+}  // namespace tc
+
+// ----------------------------------------------------- public engine call
+int tc_gemm(fmpt_handle* h, int mode, int M, int N, int K, int batch, const TcOperand& A,
+            const TcOperand& B, void* C, int out_f64, int64_t ldc, int64_t strideC, int* err_dev) {
+  using namespace tc;
+  if (M <= 0 || N <= 0 || K <= 0 || batch <= 0) return FMPT_OK;
+  CUtensorMap ma, mb, ma2, mb2;
+  const int BN = mode == TF32X3 ? 128 : 256;
+  FMPT_TRY(make_map(h, &ma, A.hi, mode, K, M, A.ld, batch, A.bstride, BM));
+  FMPT_TRY(make_map(h, &mb, B.hi, mode, K, N, B.ld, batch, B.bstride, BN));
+  if (mode == TF32X3) {
+    if (!A.lo || !B.lo) return set_error(h, FMPT_ERR_ARG, "3xTF32 needs lo planes");
+    FMPT_TRY(make_map(h, &ma2, A.lo, mode, K, M, A.ld, batch, A.bstride, BM));
+    FMPT_TRY(make_map(h, &mb2, B.lo, mode, K, N, B.ld, batch, B.bstride, BN));
+  } else {
+    ma2 = ma;
+    mb2 = mb;
+  }
+  EpiArgs ep{C, ldc, strideC, M, N, err_dev};
+  dim3 grid((M + BM - 1) / BM, (N + BN - 1) / BN, batch);
+  if (grid.y > 65535 || grid.z > 65535) return set_error(h, FMPT_ERR_SHAPE, "tc_gemm grid");
+  ProfScope prof(h, FMPT_K_TC_GEMM);
+#define LAUNCH(MODE_, BN_, ST_, OUT_)                                                         \
+  do {                                                                                        \
+    auto kfn = gemm_kernel<MODE_, BN_, ST_, OUT_>;                                            \
+    constexpr int SM_ = Cfg<MODE_, BN_, ST_, OUT_>::SMEM;                                      \
+    static bool attr_done = false;                                                            \
+    if (!attr_done) {                                                                         \
+      FMPT_CUDA(h, cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, SM_)); \
+      attr_done = true;                                                                       \
+    }                                                                                         \
+    kfn<<<grid, NTHREADS, SM_, h->stream>>>(ma, mb, ma2, mb2, K, ep);                         \
+  } while (0)
+  if (mode == TF32) {
+    if (out_f64) LAUNCH(TF32, 256, 4, 1); else LAUNCH(TF32, 256, 4, 0);
+  } else if (mode == TF32X3) {
+    if (out_f64) LAUNCH(TF32X3, 128, 3, 1); else LAUNCH(TF32X3, 128, 3, 0);
+  } else {
+    if (out_f64) LAUNCH(BF16, 256, 4, 1); else LAUNCH(BF16, 256, 4, 0);
+  }
+#undef LAUNCH
+  FMPT_LAUNCHED(h);
+  return FMPT_OK;
+}
+
+}  // namespace fmpt

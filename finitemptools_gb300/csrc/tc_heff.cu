@@ -1,0 +1,352 @@
+// Mixed-precision H_eff*x (two-site, one-site, zero-site) on the tcgen05
+// GEMM engine.
+//
+// Device layouts (K contiguous for both tensor-core operands, K padded to a
+// multiple of 8 so every TMA row starts on a 16-byte boundary):
+//   xg [a][(s, b)]            the state itself (x[a, s, b] is already K-major)
+//   Lg [a][(a', w)]           Lg[a + Kp*(a' + Dl*w)]      = L[a', w, a]
+//   Rg [(b, w2)][b']          Rg[(b + Drp*w2) + K2*b']    = R[b', w2, b]
+//   T1 [(s, b)][(a', w)]      FP32 accumulator output of GEMM 1
+//   T3 [(b, w2)][(a', s')]    MPO step output, operand of GEMM 2
+//   y  [(a', s')][b']         FP64, the reference layout of y[a', s', b']
+// GEMM 1:  T1 = xg^T . Lg          M = P*Dr, N = wl*Dl, K = Kp
+// MPO step: T3[a', s', w2, b] = sum_blocks O[s', s] T1[a', w, s, b]
+// GEMM 2:  y  = T3 . Rg^T          M = P*Dl, N = Dr,    K = K2 = wr*Drp
+// Environments are converted once per operator (they are fixed during a
+// Krylov solve); x is converted on every application.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+
+#include "internal.h"
+
+namespace fmpt {
+
+namespace {
+
+enum { M_TF32 = 0, M_TF32X3 = 1, M_BF16 = 2 };
+
+int tc_mode_of(int precision) {
+  return precision == FMPT_PREC_TF32 ? M_TF32 : precision == FMPT_PREC_TF32X3 ? M_TF32X3 : M_BF16;
+}
+
+__device__ __forceinline__ float tf32_rna(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+
+// write one converted value: TF32 (hi, optional lo) or BF16
+template <int MODE>
+__device__ __forceinline__ void put(void* hi, void* lo, int64_t i, double v) {
+  if (MODE == M_BF16) {
+    static_cast<__nv_bfloat16*>(hi)[i] = __float2bfloat16_rn((float)v);
+  } else {
+    const float h = tf32_rna((float)v);
+    static_cast<float*>(hi)[i] = h;
+    if (MODE == M_TF32X3) static_cast<float*>(lo)[i] = tf32_rna((float)(v - (double)h));
+  }
+}
+
+// xg[a + Kp*m] = x[a + Dl*m] (zero for a >= Dl)
+template <int MODE>
+__global__ void conv_state(const double* __restrict__ x, int Dl, int Kp, int64_t M, void* hi,
+                           void* lo) {
+  const int64_t tot = (int64_t)Kp * M;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < tot;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int a = (int)(t % Kp);
+    const int64_t m = t / Kp;
+    put<MODE>(hi, lo, t, a < Dl ? x[a + (int64_t)Dl * m] : 0.0);
+  }
+}
+
+// batched transpose with conversion:
+//   dst[c + dld*r + dz*z] = src[r + sld*c + sz*z]   for r < R, c < Cp (zero for c >= C)
+template <int MODE>
+__global__ void conv_transpose(const double* __restrict__ src, int64_t sld, int64_t sz, int R,
+                               int C, int Cp, void* hi, void* lo, int64_t dld, int64_t dz) {
+  __shared__ double tile[32][33];
+  const int z = blockIdx.z;
+  const int r0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
+  const int tx = threadIdx.x, ty = threadIdx.y;      // 32 x 8
+  for (int j = ty; j < 32; j += 8) {
+    const int r = r0 + tx, c = c0 + j;
+    tile[j][tx] = (r < R && c < C) ? src[r + sld * c + sz * z] : 0.0;
+  }
+  __syncthreads();
+  for (int j = ty; j < 32; j += 8) {
+    const int c = c0 + tx, r = r0 + j;
+    if (r < R && c < Cp) put<MODE>(hi, lo, (int64_t)c + dld * r + dz * z, tile[tx][j]);
+  }
+}
+
+// MPO step on the FP32 GEMM-1 output, converted for GEMM 2.
+//   in : T1[(s + P*b) + P*Dr*(a' + Dl*w)]
+//   out: T3[(b + Drp*w2) + K2*(a' + Dl*s')]
+template <int MODE, int MAXP>
+__global__ void mid_tc(const float* __restrict__ T1, int P, int Dl, int Dr, int Drp, int64_t K2,
+                       int nw_out, const int* __restrict__ win, const int* __restrict__ wstart,
+                       const double* __restrict__ coef, void* hi, void* lo) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)Dl * Dr) return;
+  const int b = (int)(t % Dr), ap = (int)(t / Dr);
+  const int64_t in_w = (int64_t)P * Dr * Dl;
+  const float* ib = T1 + (int64_t)P * b + (int64_t)P * Dr * ap;
+  for (int wo = 0; wo < nw_out; wo++) {
+    float acc[MAXP];
+#pragma unroll
+    for (int q = 0; q < MAXP; q++) acc[q] = 0.f;
+    const int e1 = __ldg(wstart + wo + 1);
+    for (int e = __ldg(wstart + wo); e < e1; e++) {
+      const int wi = __ldg(win + e);
+      const double* c = coef + (int64_t)e * P * P;
+      float v[MAXP];
+#pragma unroll
+      for (int s = 0; s < MAXP; s++) v[s] = s < P ? ib[in_w * wi + s] : 0.f;
+#pragma unroll
+      for (int q = 0; q < MAXP; q++) {
+        if (q >= P) break;
+#pragma unroll
+        for (int s = 0; s < MAXP; s++) {
+          if (s >= P) break;
+          acc[q] = fmaf((float)__ldg(c + q * P + s), v[s], acc[q]);
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < MAXP; q++) {
+      if (q >= P) break;
+      put<MODE>(hi, lo, (int64_t)b + (int64_t)Drp * wo + K2 * (ap + (int64_t)Dl * q), (double)acc[q]);
+    }
+  }
+}
+
+// Fast path of the MPO step for two spin-1/2 sites (P = 4) and MPO bonds
+// w <= 8: the nonzero (w, w') block pattern is a bitmask, every loop is
+// unrolled with static indices (registers only), T1 is read once as float4
+// and the block coefficients sit in shared memory.
+template <int MODE>
+__global__ void __launch_bounds__(256) mid_tc_p4(const float4* __restrict__ T1, int Dl, int Dr,
+                                                 int Drp, int64_t K2, int nw_in, int nw_out,
+                                                 uint64_t mask, const float* __restrict__ cdev,
+                                                 void* hi, void* lo) {
+  __shared__ float c[64][16];                     // [wi*8 + wo][q*4 + s]
+  for (int i = threadIdx.x; i < 64 * 16; i += blockDim.x) c[i / 16][i % 16] = cdev[i];
+  __syncthreads();
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)Dl * Dr) return;
+  const int b = (int)(t % Dr), ap = (int)(t / Dr);
+  const int64_t in_w = (int64_t)Dr * Dl;          // float4 stride between w planes
+  const float4* ib = T1 + b + (int64_t)Dr * ap;
+  float4 v[8];
+#pragma unroll
+  for (int wi = 0; wi < 8; wi++)
+    v[wi] = wi < nw_in ? ib[in_w * wi] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+  for (int wo = 0; wo < 8; wo++) {
+    if (wo >= nw_out) break;
+    float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+#pragma unroll
+    for (int wi = 0; wi < 8; wi++) {
+      if (!((mask >> (wi * 8 + wo)) & 1ull)) continue;
+      const float* cc = c[wi * 8 + wo];
+      a0 = fmaf(cc[0], v[wi].x, fmaf(cc[1], v[wi].y, fmaf(cc[2], v[wi].z, fmaf(cc[3], v[wi].w, a0))));
+      a1 = fmaf(cc[4], v[wi].x, fmaf(cc[5], v[wi].y, fmaf(cc[6], v[wi].z, fmaf(cc[7], v[wi].w, a1))));
+      a2 = fmaf(cc[8], v[wi].x, fmaf(cc[9], v[wi].y, fmaf(cc[10], v[wi].z, fmaf(cc[11], v[wi].w, a2))));
+      a3 = fmaf(cc[12], v[wi].x, fmaf(cc[13], v[wi].y, fmaf(cc[14], v[wi].z, fmaf(cc[15], v[wi].w, a3))));
+    }
+    const int64_t o = (int64_t)b + (int64_t)Drp * wo + K2 * ap;
+    const int64_t qs = K2 * Dl;
+    put<MODE>(hi, lo, o, (double)a0);
+    put<MODE>(hi, lo, o + qs, (double)a1);
+    put<MODE>(hi, lo, o + 2 * qs, (double)a2);
+    put<MODE>(hi, lo, o + 3 * qs, (double)a3);
+  }
+}
+
+struct TcState {
+  int mode = 0, P = 1, es = 4;
+  int Kp = 0, Drp = 0;
+  int64_t K2 = 0;
+  DevBuf Lg[2], Rg[2], xg[2], T1, T3[2];
+  int* err = nullptr;
+  // fast MPO step (P = 4, w <= 8): block bitmask and dense float coefficients
+  bool fast_mid = false;
+  uint64_t mask = 0;
+  DevBuf cfast;
+};
+
+inline int round_up8(int v) { return (v + 7) / 8 * 8; }
+
+int grid1(fmpt_handle* h, int64_t n) {
+  int64_t g = (n + 255) / 256, cap = (int64_t)h->sm_count * 16;
+  return (int)std::max<int64_t>(1, std::min(g, cap));
+}
+
+template <int MODE>
+int launch_transpose(fmpt_handle* h, const double* src, int64_t sld, int64_t sz, int R, int C,
+                     int Cp, int Z, void* hi, void* lo, int64_t dld, int64_t dz) {
+  dim3 grid((R + 31) / 32, (Cp + 31) / 32, Z);
+  ProfScope prof(h, FMPT_K_CONVERT);
+  conv_transpose<MODE><<<grid, dim3(32, 8), 0, h->stream>>>(src, sld, sz, R, C, Cp, hi, lo, dld, dz);
+  FMPT_LAUNCHED(h);
+  return FMPT_OK;
+}
+
+int transpose_any(fmpt_handle* h, int mode, const double* src, int64_t sld, int64_t sz, int R,
+                  int C, int Cp, int Z, void* hi, void* lo, int64_t dld, int64_t dz) {
+  if (mode == M_TF32) return launch_transpose<M_TF32>(h, src, sld, sz, R, C, Cp, Z, hi, lo, dld, dz);
+  if (mode == M_TF32X3) return launch_transpose<M_TF32X3>(h, src, sld, sz, R, C, Cp, Z, hi, lo, dld, dz);
+  return launch_transpose<M_BF16>(h, src, sld, sz, R, C, Cp, Z, hi, lo, dld, dz);
+}
+
+}  // namespace
+
+int op_tc_prepare(fmpt_op* op) {
+  fmpt_handle* h = op->h;
+  if (op->dtype != FMPT_F64)
+    return set_error(h, FMPT_ERR_UNSUPPORTED, "mixed precision: complex operators not built");
+  TcState* st = new TcState();
+  op->tc = st;
+  st->mode = tc_mode_of(op->precision);
+  st->es = st->mode == M_BF16 ? 2 : 4;
+  const int Dl = op->Dl, Dr = op->Dr, wl = op->wl, wr = op->wr;
+  if (op->kind == 2) {
+    // c_prime: identity MPO step over w (wl == wr), one "physical" index
+    st->P = 1;
+    MidSchedule& s = op->sched;
+    s.nw_in = wl; s.nw_out = wl; s.p_in = 1; s.p_out = 1; s.cplx = 0;
+    s.blk_win.resize(wl); s.wout_start.resize(wl + 1); s.coef.assign(wl, 1.0);
+    for (int w = 0; w < wl; w++) { s.blk_win[w] = w; s.wout_start[w] = w; }
+    s.wout_start[wl] = wl;
+    FMPT_TRY(mid_upload(h, s));
+  } else {
+    st->P = op->kind == 0 ? op->d1 * op->d2 : op->d1;
+  }
+  if (st->P > 16) return set_error(h, FMPT_ERR_UNSUPPORTED, "physical dimension product > 16");
+  const int P = st->P;
+  st->Kp = round_up8(Dl);
+  st->Drp = round_up8(Dr);
+  st->K2 = (int64_t)wr * st->Drp;
+  const int split = st->mode == M_TF32X3 ? 2 : 1;
+  const size_t es = st->es;
+  for (int p = 0; p < split; p++) {
+    FMPT_TRY(st->Lg[p].alloc(h, (size_t)st->Kp * Dl * wl * es));
+    FMPT_TRY(st->Rg[p].alloc(h, (size_t)st->K2 * Dr * es));
+    FMPT_TRY(st->xg[p].alloc(h, (size_t)st->Kp * P * Dr * es));
+    FMPT_TRY(st->T3[p].alloc(h, (size_t)st->K2 * P * Dl * es));
+    FMPT_CUDA(h, cudaMemsetAsync(st->T3[p].p, 0, st->T3[p].bytes, h->stream));  // K padding
+  }
+  FMPT_TRY(st->T1.alloc(h, (size_t)P * Dr * wl * Dl * sizeof(float)));
+  {
+    const MidSchedule& ms = op->sched;
+    if (P == 4 && ms.nw_in <= 8 && ms.nw_out <= 8) {
+      std::vector<float> cf(64 * 16, 0.f);
+      uint64_t mask = 0;
+      for (int wo = 0; wo < ms.nw_out; wo++)
+        for (int e = ms.wout_start[wo]; e < ms.wout_start[wo + 1]; e++) {
+          const int wi = ms.blk_win[e];
+          mask |= 1ull << (wi * 8 + wo);
+          for (int q = 0; q < 16; q++) cf[(wi * 8 + wo) * 16 + q] += (float)ms.coef[(size_t)e * 16 + q];
+        }
+      FMPT_TRY(st->cfast.alloc(h, cf.size() * sizeof(float)));
+      FMPT_CUDA(h, cudaMemcpyAsync(st->cfast.p, cf.data(), cf.size() * sizeof(float),
+                                   cudaMemcpyHostToDevice, h->stream));
+      FMPT_CUDA(h, cudaStreamSynchronize(h->stream));
+      st->mask = mask;
+      st->fast_mid = true;
+    }
+  }
+  FMPT_CUDA(h, cudaMallocAsync((void**)&st->err, sizeof(int), h->stream));
+  FMPT_CUDA(h, cudaMemsetAsync(st->err, 0, sizeof(int), h->stream));
+  void* lo_L = split > 1 ? st->Lg[1].p : nullptr;
+  void* lo_R = split > 1 ? st->Rg[1].p : nullptr;
+  // Lg[a + Kp*(a' + Dl*w)] = L[a' + Dl*w + Dl*wl*a]: per w, (r=a', c=a)
+  FMPT_TRY(transpose_any(h, st->mode, op->hleft, (int64_t)Dl * wl, Dl, Dl, Dl, st->Kp, wl,
+                         st->Lg[0].p, lo_L, st->Kp, (int64_t)st->Kp * Dl));
+  // Rg[b + Drp*w2 + K2*b'] = R[b' + Dr*w2 + Dr*wr*b]: per w2, (r=b', c=b)
+  FMPT_TRY(transpose_any(h, st->mode, op->hright, (int64_t)Dr * wr, Dr, Dr, Dr, st->Drp, wr,
+                         st->Rg[0].p, lo_R, st->K2, st->Drp));
+  return FMPT_OK;
+}
+
+int op_tc_apply(fmpt_op* op, const double* x, double* y) {
+  fmpt_handle* h = op->h;
+  TcState* st = static_cast<TcState*>(op->tc);
+  if (!st) return set_error(h, FMPT_ERR_ARG, "operator has no tensor-core state");
+  const int Dl = op->Dl, Dr = op->Dr, wl = op->wl, P = st->P;
+  const int split = st->mode == M_TF32X3 ? 2 : 1;
+  void* xlo = split > 1 ? st->xg[1].p : nullptr;
+  void* tlo = split > 1 ? st->T3[1].p : nullptr;
+  const int64_t nx = (int64_t)st->Kp * P * Dr;
+  {
+  ProfScope prof(h, FMPT_K_CONVERT);
+  if (st->mode == M_TF32)
+    conv_state<M_TF32><<<grid1(h, nx), 256, 0, h->stream>>>(x, Dl, st->Kp, (int64_t)P * Dr, st->xg[0].p, xlo);
+  else if (st->mode == M_TF32X3)
+    conv_state<M_TF32X3><<<grid1(h, nx), 256, 0, h->stream>>>(x, Dl, st->Kp, (int64_t)P * Dr, st->xg[0].p, xlo);
+  else
+    conv_state<M_BF16><<<grid1(h, nx), 256, 0, h->stream>>>(x, Dl, st->Kp, (int64_t)P * Dr, st->xg[0].p, xlo);
+  FMPT_LAUNCHED(h);
+  }
+  // GEMM 1: T1[(s b), (a' w)] = sum_a xg[a, (s b)] Lg[a, (a' w)]
+  TcOperand A1{st->xg[0].p, xlo, st->Kp, 0};
+  TcOperand B1{st->Lg[0].p, split > 1 ? st->Lg[1].p : nullptr, st->Kp, 0};
+  FMPT_TRY(tc_gemm(h, st->mode, P * Dr, wl * Dl, st->Kp, 1, A1, B1, st->T1.p, 0, (int64_t)P * Dr,
+                   0, st->err));
+  // MPO step
+  {
+    const int64_t nt = (int64_t)Dl * Dr;
+    const unsigned blocks = (unsigned)((nt + 255) / 256);
+    const MidSchedule& s = op->sched;
+    ProfScope prof(h, FMPT_K_MPO_STEP);
+    if (st->fast_mid) {
+      const float4* t1 = (const float4*)st->T1.p;
+      const float* cf = (const float*)st->cfast.p;
+      if (st->mode == M_TF32)
+        mid_tc_p4<M_TF32><<<blocks, 256, 0, h->stream>>>(t1, Dl, Dr, st->Drp, st->K2, s.nw_in, s.nw_out, st->mask, cf, st->T3[0].p, tlo);
+      else if (st->mode == M_TF32X3)
+        mid_tc_p4<M_TF32X3><<<blocks, 256, 0, h->stream>>>(t1, Dl, Dr, st->Drp, st->K2, s.nw_in, s.nw_out, st->mask, cf, st->T3[0].p, tlo);
+      else
+        mid_tc_p4<M_BF16><<<blocks, 256, 0, h->stream>>>(t1, Dl, Dr, st->Drp, st->K2, s.nw_in, s.nw_out, st->mask, cf, st->T3[0].p, tlo);
+    } else
+#define MIDTC(MODE_, MP_)                                                                    \
+  mid_tc<MODE_, MP_><<<blocks, 256, 0, h->stream>>>((const float*)st->T1.p,                \
+                                                    P, Dl, Dr, st->Drp, st->K2, s.nw_out,      \
+                                                    s.d_win, s.d_wstart, s.d_coef, st->T3[0].p, tlo)
+    if (P <= 4) {
+      if (st->mode == M_TF32) MIDTC(M_TF32, 4); else if (st->mode == M_TF32X3) MIDTC(M_TF32X3, 4); else MIDTC(M_BF16, 4);
+    } else {
+      if (st->mode == M_TF32) MIDTC(M_TF32, 16); else if (st->mode == M_TF32X3) MIDTC(M_TF32X3, 16); else MIDTC(M_BF16, 16);
+    }
+#undef MIDTC
+    FMPT_LAUNCHED(h);
+  }
+  // GEMM 2: y[(a' s'), b'] = sum_(b w2) T3[(b w2), (a' s')] Rg[(b w2), b']
+  TcOperand A2{st->T3[0].p, tlo, st->K2, 0};
+  TcOperand B2{st->Rg[0].p, split > 1 ? st->Rg[1].p : nullptr, st->K2, 0};
+  FMPT_TRY(tc_gemm(h, st->mode, P * Dl, Dr, (int)st->K2, 1, A2, B2, y, 1, (int64_t)P * Dl, 0,
+                   st->err));
+  return FMPT_OK;
+}
+
+int op_tc_check(fmpt_op* op) {
+  TcState* st = static_cast<TcState*>(op->tc);
+  if (!st || !st->err) return FMPT_OK;
+  int e = 0;
+  FMPT_CUDA(op->h, cudaMemcpyAsync(&e, st->err, sizeof(int), cudaMemcpyDeviceToHost, op->h->stream));
+  FMPT_CUDA(op->h, cudaStreamSynchronize(op->h->stream));
+  if (e) return set_error(op->h, FMPT_ERR_TIMEOUT, "tensor-core GEMM wait timed out");
+  return FMPT_OK;
+}
+
+void op_tc_free(fmpt_op* op) {
+  TcState* st = static_cast<TcState*>(op->tc);
+  if (!st) return;
+  if (st->err) cudaFreeAsync(st->err, op->h->stream);
+  delete st;
+  op->tc = nullptr;
+}
+
+}  // namespace fmpt

@@ -31,6 +31,19 @@ class Handle:
     def launch_count(self):
         return int(lib().fmpt_launch_count(self.ptr))
 
+    def profile(self, on=True):
+        """Enable/disable the per-kernel-class device timers."""
+        check(lib().fmpt_profile_enable(self.ptr, 1 if on else 0), self.ptr)
+
+    def profile_read(self, kernel_class):
+        """(launches, device ms) of one class since the last read
+        (0 tensor-core GEMM, 1 FP64 GEMM, 2 MPO step, 3 conversion)."""
+        n = ctypes.c_int64()
+        ms = ctypes.c_double()
+        check(lib().fmpt_profile_read(self.ptr, int(kernel_class), ctypes.byref(n),
+                                      ctypes.byref(ms)), self.ptr)
+        return n.value, ms.value
+
     def set_stream(self, stream_ptr):
         check(lib().fmpt_set_stream(self.ptr, ctypes.c_void_p(stream_ptr)), self.ptr)
 

@@ -71,6 +71,20 @@ void* fmpt_get_stream(fmpt_handle* h);
 uint64_t fmpt_launch_count(fmpt_handle* h);
 int fmpt_version(void);
 
+/* Device-side timers: while enabled, every launch of the classes below is
+ * bracketed by CUDA events on the handle's stream.  fmpt_profile_read
+ * synchronises, returns the launch count and summed device milliseconds of
+ * one class and clears it.  Classes: */
+enum fmpt_kernel_class {
+  FMPT_K_TC_GEMM = 0,     /* tcgen05 tensor-core GEMM (mixed precision) */
+  FMPT_K_F64_GEMM = 1,    /* FP64 / complex FP64 CUDA-core GEMM         */
+  FMPT_K_MPO_STEP = 2,    /* block-sparse MPO contraction step          */
+  FMPT_K_CONVERT = 3,     /* operand layout / precision conversion      */
+  FMPT_K_COUNT = 4
+};
+int fmpt_profile_enable(fmpt_handle* h, int on);
+int fmpt_profile_read(fmpt_handle* h, int kernel_class, int64_t* launches, double* total_ms);
+
 /* ------------------------------------------------------------ memory */
 int fmpt_malloc(fmpt_handle* h, size_t bytes, void** dptr);
 int fmpt_free(fmpt_handle* h, void* dptr);

