@@ -57,6 +57,8 @@ SIGNATURES = {
                                c_int, c_int, c_int, c_int, c_int, c_int, c_int]),
     "fmpt_ac_prime": (c_int, [c_void_p, c_int, c_int, dptr, hptr, dptr, dptr, dptr,
                               c_int, c_int, c_int, c_int, c_int]),
+    "fmpt_ac2_prime_noalloc": (c_int, [c_void_p, c_int, dptr, hptr, hptr, dptr, dptr, dptr,
+                                       c_int, c_int, c_int, c_int, c_int, c_int, c_int]),
     "fmpt_c_prime": (c_int, [c_void_p, c_int, c_int, dptr, dptr, dptr, dptr, c_int, c_int, c_int]),
     "fmpt_updateleft": (c_int, [c_void_p, c_int, c_int, dptr, dptr, hptr, dptr, dptr,
                                 c_int, c_int, c_int, c_int, c_int]),

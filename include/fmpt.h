@@ -176,6 +176,29 @@ int fmpt_lanczos_ground(fmpt_op* op, const double* x0, int kmax, double btol, in
 int fmpt_exponentiate(fmpt_op* op, double t_re, double t_im, const double* x, double* xout,
                       int krylovdim, double tol, int* info);
 
+/* ------------------------------------------ allocation-free H_eff * x
+ * No counterpart in the reference.  The plain FP64 two-site H_eff*x of
+ * fmpt_ac2_prime (same arguments, same result) for callers that cannot
+ * allocate device memory while they run: work recorded under stream
+ * capture, applications whose own allocator owns the device memory, fixed
+ * memory budgets.  Instead of pool memory it uses one file-scope device
+ * array of FMPT_NOALLOC_SCRATCH_BYTES, held by every GPU that loads the
+ * library until the process exits; it calls no cudaMalloc/cudaFree and no
+ * allocating library routine.
+ *   - Scratch need: 8*(Dl*wl*P*Dr + Dl*P*wr*Dr) bytes (x2 for C128), P = d1*d2,
+ *     plus a small block table; larger problems return FMPT_ERR_SHAPE with
+ *     the sizes in fmpt_last_error (use fmpt_ac2_prime for them).
+ *   - The first call on a device resolves the array's device address
+ *     (cudaGetSymbolAddress, with that device current); make that first call
+ *     before any stream capture.
+ *   - All calls share the array: calls that overlap on the GPU race on it.
+ *     Issue them on one stream (or serialise them).
+ *   - FP64 forms only (dtype F64 or C128); precision is always FMPT_PREC_FP64. */
+#define FMPT_NOALLOC_SCRATCH_BYTES (64u * 1024u * 1024u)
+int fmpt_ac2_prime_noalloc(fmpt_handle* h, int dtype, const double* x, const double* W1_host,
+                           const double* W2_host, const double* hleft, const double* hright,
+                           double* y, int Dl, int d1, int d2, int Dr, int wl, int wm, int wr);
+
 /* ------------------------------------------------- dense factorisations
  * Truncated SVD of M (m x n, column-major) with MPSTruncation semantics
  * (auxiliary/truncation.jl:27-47, stable_svd.jl:12-18): drop sigma below
