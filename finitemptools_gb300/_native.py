@@ -78,6 +78,8 @@ SIGNATURES = {
                                   P(c_int)]),
     "fmpt_svd_trunc": (c_int, [c_void_p, c_int, dptr, c_int, c_int, c_int, c_double, dptr, dptr,
                                dptr, P(c_int), P(c_double)]),
+    "fmpt_dm_split": (c_int, [c_void_p, c_int, dptr, c_int, c_int, c_int, c_double, c_int,
+                              dptr, dptr, dptr, P(c_int), P(c_double)]),
     "fmpt_qr": (c_int, [c_void_p, c_int, dptr, c_int, c_int, dptr, dptr]),
     "fmpt_lq": (c_int, [c_void_p, c_int, dptr, c_int, c_int, dptr, dptr]),
 }

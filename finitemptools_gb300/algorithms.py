@@ -10,7 +10,7 @@ environments and the Krylov vectors on the GPU; only scalars come back.
 
 import numpy as np
 
-from .auxiliary import (MPSTruncation, default_truncation, dot, gemm, leftorth, norm,
+from .auxiliary import (MPSTruncation, default_truncation, dm_split, dot, gemm, leftorth, norm,
                         rightorth, scal, scale_cols, scale_rows, stable_tsvd)
 from .derivatives import HeffOp
 from .device import DeviceTensor
@@ -39,12 +39,13 @@ class DMRG2:
 
     def __init__(self, maxiter=Defaults.maxiter, tol=Defaults.tol, eig_maxiter=10,
                  eig_tol=Defaults.dmrg_eig_tol, verbosity=Defaults.verbosity, trunc=None,
-                 precision="fp64", reorth=False):
+                 precision="fp64", reorth=False, svd="gesvd"):
         self.maxiter, self.tol = maxiter, tol
         self.eig_maxiter, self.eig_tol = eig_maxiter, eig_tol
         self.verbosity = verbosity
         self.trunc = trunc if trunc is not None else default_truncation()
         self.precision, self.reorth = precision, reorth
+        self.svd = svd          # "gesvd" (reference semantics) or "dm" (density matrix)
 
 
 class DMRG1:
@@ -87,10 +88,18 @@ def _dmrg2_bond_left(m, site, alg):
                 precision=alg.precision, dtype=x2.dtype)
     E, vecs, info, k = op.lanczos(x2, alg.eig_maxiter, alg.eig_tol, alg.reorth)
     del op
-    u, s, vt, err = stable_tsvd(vecs, Dl * d1, d2 * Dr, alg.trunc)
-    kk = s.shape[0]
-    scal(1.0 / norm(s), s)                                      # normalize!(s)
-    svt = scale_rows(vt, kk, d2 * Dr, s)                        # s * v (in place)
+    if alg.svd == "dm":
+        # U orthonormal from M M^H; s*v = U^H M, normalised with s
+        u, s, svt, err = dm_split(vecs, Dl * d1, d2 * Dr, alg.trunc, 0)
+        kk = s.shape[0]
+        nrm = norm(s)
+        scal(1.0 / nrm, s)
+        scal(1.0 / nrm, svt)
+    else:
+        u, s, vt, err = stable_tsvd(vecs, Dl * d1, d2 * Dr, alg.trunc)
+        kk = s.shape[0]
+        scal(1.0 / norm(s), s)                                  # normalize!(s)
+        svt = scale_rows(vt, kk, d2 * Dr, s)                    # s * v (in place)
     usv = gemm(u, svt, (Dl, d1, d2, Dr), Dl * d1, d2 * Dr, kk)
     delta = abs(1 - abs(dot(usv, x2)))   # sum x2 * conj(u s v)  (dmrg.jl:109-110)
     mps[site] = u.view_as((Dl, d1, kk))
@@ -135,15 +144,27 @@ def _dmrg2_bond_right(m, site, alg):
                 precision=alg.precision, dtype=x2.dtype)
     E, vecs, info, k = op.lanczos(x2, alg.eig_maxiter, alg.eig_tol, alg.reorth)
     del op
-    u, s, vt, err = stable_tsvd(vecs, Dl * d1, d2 * Dr, alg.trunc)
-    kk = s.shape[0]
-    scal(1.0 / norm(s), s)
-    # fidelity first (needs u, s, v before they are absorbed)
-    svt = scale_rows(vt.copy(), kk, d2 * Dr, s)
-    usv = gemm(u, svt, (Dl, d1, d2, Dr), Dl * d1, d2 * Dr, kk)
-    delta = abs(1 - abs(dot(usv, x2)))
-    del svt, usv
-    mps[site] = scale_cols(u, Dl * d1, kk, s).view_as((Dl, d1, kk))
+    if alg.svd == "dm":
+        # v^H orthonormal from M^H M; u*s = M V, normalised with s
+        us, s, vt, err = dm_split(vecs, Dl * d1, d2 * Dr, alg.trunc, 1)
+        kk = s.shape[0]
+        nrm = norm(s)
+        scal(1.0 / nrm, s)
+        scal(1.0 / nrm, us)
+        usv = gemm(us, vt, (Dl, d1, d2, Dr), Dl * d1, d2 * Dr, kk)
+        delta = abs(1 - abs(dot(usv, x2)))
+        del usv
+    else:
+        u, s, vt, err = stable_tsvd(vecs, Dl * d1, d2 * Dr, alg.trunc)
+        kk = s.shape[0]
+        scal(1.0 / norm(s), s)
+        # fidelity first (needs u, s, v before they are absorbed)
+        svt = scale_rows(vt.copy(), kk, d2 * Dr, s)
+        usv = gemm(u, svt, (Dl, d1, d2, Dr), Dl * d1, d2 * Dr, kk)
+        delta = abs(1 - abs(dot(usv, x2)))
+        del svt, usv
+        us = scale_cols(u, Dl * d1, kk, s)
+    mps[site] = us.view_as((Dl, d1, kk))
     mps[site + 1] = vt.view_as((kk, d2, Dr))
     mps.s[site + 1] = s
     updateright_(m, site + 1)

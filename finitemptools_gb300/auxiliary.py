@@ -13,7 +13,7 @@ from ._native import C128, TRANS, lib
 from .device import DeviceTensor
 
 __all__ = ["MPSTruncation", "DefaultSVDCutoff", "default_truncation", "gemm", "matmul",
-           "dot", "norm", "scal", "axpy", "stable_tsvd", "leftorth", "rightorth",
+           "dot", "norm", "scal", "axpy", "stable_tsvd", "dm_split", "leftorth", "rightorth",
            "scale_rows", "scale_cols"]
 
 DefaultSVDCutoff = 1.0e-8       # auxiliary/truncation.jl:49
@@ -125,6 +125,24 @@ def stable_tsvd(M, m, n, trunc=None):
     S.view_as((k,))
     Vt.view_as((k, n))
     return U, S, Vt, err.value
+
+
+def dm_split(M, m, n, trunc, side):
+    """Truncated split through the reduced density matrix (White's DMRG
+    truncation, FP64 on the device).  side 0: returns (U [m,k] orthonormal,
+    S [k], SV = U^H M [k,n], err); side 1: (US = M V [m,k], S [k], V^H [k,n]
+    orthonormal, err).  Same truncation rule as stable_tsvd."""
+    h = M.h
+    r = min(m, n)
+    Aout = DeviceTensor((m, r), M.dtype, h)
+    S = DeviceTensor((r,), np.float64, h)
+    Bout = DeviceTensor((r, n), M.dtype, h)
+    k = ctypes.c_int()
+    err = ctypes.c_double()
+    h.check(lib().fmpt_dm_split(h.ptr, M.code, M.ptr, m, n, trunc.D, trunc.eps, int(side),
+                                Aout.ptr, S.ptr, Bout.ptr, ctypes.byref(k), ctypes.byref(err)))
+    k = k.value
+    return Aout.view_as((m, k)), S.view_as((k,)), Bout.view_as((k, n)), err.value
 
 
 def leftorth(M, m, n):

@@ -208,6 +208,110 @@ int fmpt_svd_trunc(fmpt_handle* h, int dtype, const double* M, int m, int n, int
   return FMPT_OK;
 }
 
+int fmpt_dm_split(fmpt_handle* h, int dtype, const double* M, int m, int n, int maxD,
+                  double eps, int side, double* Aout, double* S, double* Bout, int* kout,
+                  double* errout) {
+  if (!h || !M || !Aout || !S || !Bout || !kout) return FMPT_ERR_ARG;
+  if (m < 1 || n < 1 || maxD < 1) return set_error(h, FMPT_ERR_SHAPE, "dm_split: bad extents");
+  if (side != 0 && side != 1) return set_error(h, FMPT_ERR_ARG, "dm_split: side must be 0 or 1");
+  const int cp = dtype == FMPT_C128;
+  const bool left = side == 0;
+  const int r = left ? m : n;
+  const int64_t planeM = (int64_t)m * n;
+  // rho = M M^H (left) or M^H M (right), split planes, FP64 GEMM
+  DevBuf rho, W, rhoI, work, dinfo;
+  FMPT_TRY(rho.alloc(h, (size_t)r * r * sizeof(double) * (cp ? 2 : 1)));
+  {
+    GemmArgs g{};
+    g.cplx = cp; g.alpha[0] = 1.0; g.batch = 1;
+    g.m = r; g.n = r; g.k = left ? n : m;
+    g.A = M; g.lda = m; g.planeA = planeM;
+    g.B = M; g.ldb = m; g.planeB = planeM;
+    g.C = rho.d(); g.ldc = r; g.planeC = (int64_t)r * r;
+    if (left) { g.ta = FMPT_N; g.tb = FMPT_C; } else { g.ta = FMPT_C; g.tb = FMPT_N; }
+    FMPT_TRY(gemm_f64(h, g));
+  }
+  FMPT_TRY(W.alloc(h, (size_t)r * sizeof(double)));
+  FMPT_TRY(dinfo.alloc(h, sizeof(int)));
+  double* A = rho.d();
+  if (cp) {
+    FMPT_TRY(rhoI.alloc(h, (size_t)r * r * 2 * sizeof(double)));
+    FMPT_TRY(copy_mat(h, 1, r, r, rho.d(), r, (int64_t)r * r, 0, 0, rhoI.d(), r, -1));
+    A = rhoI.d();
+  }
+  int lwork = 0;
+  if (cp)
+    FMPT_SOLVER(h, cusolverDnZheevd_bufferSize(h->solver, CUSOLVER_EIG_MODE_VECTOR,
+                                               CUBLAS_FILL_MODE_LOWER, r, (cuDoubleComplex*)A, r,
+                                               W.d(), &lwork));
+  else
+    FMPT_SOLVER(h, cusolverDnDsyevd_bufferSize(h->solver, CUSOLVER_EIG_MODE_VECTOR,
+                                               CUBLAS_FILL_MODE_LOWER, r, A, r, W.d(), &lwork));
+  FMPT_TRY(work.alloc(h, (size_t)std::max(lwork, 1) * sizeof(double) * (cp ? 2 : 1)));
+  if (cp)
+    FMPT_SOLVER(h, cusolverDnZheevd(h->solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, r,
+                                    (cuDoubleComplex*)A, r, W.d(), (cuDoubleComplex*)work.p, lwork,
+                                    (int*)dinfo.p));
+  else
+    FMPT_SOLVER(h, cusolverDnDsyevd(h->solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, r,
+                                    A, r, W.d(), work.d(), lwork, (int*)dinfo.p));
+  int info = 0;
+  FMPT_TRY(read_info(h, (const int*)dinfo.p, &info));
+  if (info != 0) return set_error(h, FMPT_ERR_CUSOLVER, "syevd/heevd info %d", info);
+  // sigma (descending) on the host; the rank is at most min(m, n)
+  std::vector<double> lam(r), s(r);
+  FMPT_CUDA(h, cudaMemcpyAsync(lam.data(), W.d(), r * sizeof(double), cudaMemcpyDeviceToHost,
+                               h->stream));
+  FMPT_CUDA(h, cudaStreamSynchronize(h->stream));
+  const int rank_max = std::min(m, n);
+  for (int i = 0; i < r; i++) s[i] = i < rank_max ? std::sqrt(std::max(lam[r - 1 - i], 0.0)) : 0.0;
+  double nrm = 0.0;
+  for (double v : s) nrm += v * v;
+  nrm = std::sqrt(nrm);
+  int keep = 0;
+  for (double v : s) keep += (v >= eps * nrm && v > 0.0) ? 1 : 0;
+  double e1 = 0.0, e2 = 0.0;
+  for (int i = keep; i < r; i++) e1 += s[i] * s[i];
+  int k = keep;
+  if (keep > maxD) {
+    for (int i = maxD; i < keep; i++) e2 += s[i] * s[i];
+    k = maxD;
+  }
+  if (k < 1) return set_error(h, FMPT_ERR_NONFINITE, "dm_split: zero matrix");
+  *kout = k;
+  if (errout) *errout = std::sqrt(e1 + e2);
+  FMPT_CUDA(h, cudaMemcpyAsync(S, s.data(), k * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  // Q (r x k, split planes): eigenvectors of the k largest eigenvalues, descending;
+  // one copy with a negative column stride starting at the last column
+  DevBuf Q;
+  FMPT_TRY(Q.alloc(h, (size_t)r * k * sizeof(double) * (cp ? 2 : 1)));
+  FMPT_TRY(copy_mat(h, cp, r, k, A + (size_t)(r - 1) * r * (cp ? 2 : 1), -(int64_t)r,
+                    cp ? -1 : 0, 0, 0, Q.d(), r, (int64_t)r * k));
+  GemmArgs g{};
+  g.cplx = cp; g.alpha[0] = 1.0; g.batch = 1;
+  if (left) {
+    // A = Q (m x k);  B = Q^H M (k x n)
+    FMPT_CUDA(h, cudaMemcpyAsync(Aout, Q.d(), (size_t)m * k * sizeof(double) * (cp ? 2 : 1),
+                                 cudaMemcpyDeviceToDevice, h->stream));
+    g.ta = FMPT_C; g.tb = FMPT_N; g.m = k; g.n = n; g.k = m;
+    g.A = Q.d(); g.lda = m; g.planeA = (int64_t)m * k;
+    g.B = M; g.ldb = m; g.planeB = planeM;
+    g.C = Bout; g.ldc = k; g.planeC = (int64_t)k * n;
+    FMPT_TRY(gemm_f64(h, g));
+  } else {
+    // B = Q^H (k x n);  A = M Q (m x k)
+    FMPT_TRY(copy_mat(h, cp, k, n, Q.d(), n, (int64_t)n * k, 1, cp, Bout, k, (int64_t)k * n));
+    g.ta = FMPT_N; g.tb = FMPT_N; g.m = m; g.n = k; g.k = n;
+    g.A = M; g.lda = m; g.planeA = planeM;
+    g.B = Q.d(); g.ldb = n; g.planeB = (int64_t)n * k;
+    g.C = Aout; g.ldc = m; g.planeC = (int64_t)m * k;
+    FMPT_TRY(gemm_f64(h, g));
+  }
+  // the host vector s must stay alive until its async copy finishes
+  FMPT_CUDA(h, cudaStreamSynchronize(h->stream));
+  return FMPT_OK;
+}
+
 int fmpt_qr(fmpt_handle* h, int dtype, const double* M, int m, int n, double* Q, double* R) {
   if (!h || !M || !Q || !R) return FMPT_ERR_ARG;
   if (m < 1 || n < 1) return set_error(h, FMPT_ERR_SHAPE, "qr: bad extents");

@@ -207,6 +207,20 @@ int fmpt_ac2_prime_noalloc(fmpt_handle* h, int dtype, const double* x, const dou
  * (2-norm of the dropped sigma) are HOST outputs. */
 int fmpt_svd_trunc(fmpt_handle* h, int dtype, const double* M, int m, int n, int maxD,
                    double eps, double* U, double* S, double* Vt, int* k, double* err);
+/* The truncated two-site split through the reduced density matrix (White's
+ * DMRG truncation), for the mixed-precision sweeps.  side 0 (left-to-right
+ * sweep): rho = M M^H, A = its k leading eigenvectors (orthonormal columns,
+ * m x k) and B = A^H M (= s*v, k x n).  side 1 (right-to-left): rho = M^H M,
+ * B = the k leading eigenvectors as orthonormal rows (k x n) and A = M B^H
+ * (= u*s, m x k).  Everything in FP64 on the device (GEMM + cuSOLVER
+ * syevd/heevd); S gets sqrt of the kept eigenvalues, truncated with the
+ * MPSTruncation rule of fmpt_svd_trunc.  No factor is divided by s, so the
+ * isometric side stays exactly isometric; singular values below
+ * ~1e-8*sigma_max are resolved only to the FP64 noise of rho (they are
+ * squared).  ~9x faster than gesvd at 2048^2.  No counterpart in the
+ * reference (stable_tsvd! always runs an SVD). */
+int fmpt_dm_split(fmpt_handle* h, int dtype, const double* M, int m, int n, int maxD,
+                  double eps, int side, double* A, double* S, double* B, int* k, double* err);
 /* Thin QR (leftorth!, QR()): M (m x n) = Q (m x r) R (r x n), r = min(m, n). */
 int fmpt_qr(fmpt_handle* h, int dtype, const double* M, int m, int n, double* Q, double* R);
 /* Thin LQ (rightorth, LQ()): M (m x n) = L (m x r) Q (r x n). */

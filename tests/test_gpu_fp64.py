@@ -313,3 +313,29 @@ def test_bad_shapes_raise():
     E = DT.from_numpy(np.ones((3, 5, 3)))
     with pytest.raises(ValueError):
         fm.ac2_prime(x, W, W, E, E)
+
+
+@pytest.mark.parametrize("cplx", [False, True])
+@pytest.mark.parametrize("m,n,side", [(40, 24, 0), (40, 24, 1), (24, 40, 0), (64, 64, 1)])
+def test_dm_split(cplx, m, n, side):
+    """Density-matrix split: the isometric factor is exactly isometric and
+    the product is the rank-k truncation of M (singular values >= 1e-6)."""
+    from finitemptools_gb300.auxiliary import dm_split
+    rng = np.random.default_rng(m + n + side)
+    U0, _ = np.linalg.qr(rnd(rng, (m, m), cplx))
+    V0, _ = np.linalg.qr(rnd(rng, (n, n), cplx))
+    r = min(m, n)
+    s0 = np.logspace(0, -6, r)
+    M = (U0[:, :r] * s0) @ V0[:, :r].conj().T
+    k_max = r - 3
+    A, S, B, err = dm_split(DT.from_numpy(M), m, n, fm.MPSTruncation(k_max, 1e-9), side)
+    An, Sn, Bn = A.numpy(), S.numpy(), B.numpy()
+    assert Sn.shape[0] == k_max
+    assert np.allclose(Sn, s0[:k_max], rtol=1e-8)
+    if side == 0:
+        assert np.allclose(An.conj().T @ An, np.eye(k_max), atol=1e-13)
+    else:
+        assert np.allclose(Bn @ Bn.conj().T, np.eye(k_max), atol=1e-13)
+    Mk = (U0[:, :k_max] * s0[:k_max]) @ V0[:, :k_max].conj().T
+    assert rel(An @ Bn, Mk) < 1e-10
+    assert abs(err - np.linalg.norm(s0[k_max:])) < 1e-10

@@ -105,3 +105,31 @@ def test_mixed_lanczos_energy_close_to_fp64():
         hv = op64(v)
         rq = fm.auxiliary.dot(v, hv) / fm.auxiliary.dot(v, v)
         assert abs(rq - e64) < max(bound ** 2, 1e-10) * 100 * abs(e64), (prec, rq, e64)
+
+
+def _dmrg(L, mpo, D, sweeps, prec, svd, reorth, seed=20):
+    rng = np.random.default_rng(seed)
+    st = O.randommps(L, 2, 8, rng)
+    st, _ = O.canonicalize(st, normalize=True)
+    env = fm.environments(FiniteMPO(mpo, L), fm.FiniteMPS.from_numpy(st))
+    alg = fm.DMRG2(eig_maxiter=30, eig_tol=1e-12, trunc=fm.MPSTruncation(D, 1e-10),
+                   precision=prec, reorth=reorth, svd=svd)
+    for _ in range(sweeps):
+        Es, delta = fm.sweep_(env, alg)
+    return Es, fm.expectation(env.mps, FiniteMPO(mpo, L))
+
+
+def test_mixed_dmrg2_energy_within_1e8_of_fp64():
+    """The spec bar on the XXZ chain (L=20, D=64, 4 sweeps): the state
+    found with 3xTF32 contractions, FP64 Lanczos reorthogonalisation and the
+    FP64 density-matrix split has an FP64 energy within 1e-8 (relative) of
+    the plain FP64 sweep; the density-matrix split alone changes nothing at
+    1e-10."""
+    h = heisenberg_xxz_mpo(1.0, 1.0, 0.0)
+    Es64, E64 = _dmrg(20, h, 64, 4, "fp64", "gesvd", False)
+    Esdm, Edm = _dmrg(20, h, 64, 4, "fp64", "dm", False)
+    Es3, E3 = _dmrg(20, h, 64, 4, "tf32x3", "dm", True)
+    assert abs(Edm - E64) < 1e-10 * abs(E64)
+    assert abs(E3 - E64) < 1e-8 * abs(E64)
+    # the mixed Ritz values carry the first-order operator error only
+    assert abs(Es3[-1] - E64) < 1e-5 * abs(E64)
