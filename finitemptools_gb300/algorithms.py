@@ -39,13 +39,15 @@ class DMRG2:
 
     def __init__(self, maxiter=Defaults.maxiter, tol=Defaults.tol, eig_maxiter=10,
                  eig_tol=Defaults.dmrg_eig_tol, verbosity=Defaults.verbosity, trunc=None,
-                 precision="fp64", reorth=False, svd="gesvd"):
+                 precision="fp64", reorth=False, svd="gesvd", env_precision=None):
         self.maxiter, self.tol = maxiter, tol
         self.eig_maxiter, self.eig_tol = eig_maxiter, eig_tol
         self.verbosity = verbosity
         self.trunc = trunc if trunc is not None else default_truncation()
         self.precision, self.reorth = precision, reorth
         self.svd = svd          # "gesvd" (reference semantics) or "dm" (density matrix)
+        # arithmetic of the environment updates (defaults to the contractions')
+        self.env_precision = env_precision or precision
 
 
 class DMRG1:
@@ -114,6 +116,7 @@ def leftsweep_(m, alg):
     """leftsweep!(m, alg) for DMRG2 (dmrg.jl:89-115) and DMRG1 (:27-52)."""
     if isinstance(alg, DMRG1):
         return _dmrg1_leftsweep(m, alg)
+    m.precision = alg.env_precision
     Es, delta = [], 0.0
     for site in range(1, len(m.mps) - 1):
         E, dl = _dmrg2_bond_left(m, site, alg)
@@ -126,6 +129,7 @@ def rightsweep_(m, alg):
     """rightsweep!(m, alg) for DMRG2 (dmrg.jl:117-144) and DMRG1 (:54-76)."""
     if isinstance(alg, DMRG1):
         return _dmrg1_rightsweep(m, alg)
+    m.precision = alg.env_precision
     Es, delta = [], 0.0
     for site in range(len(m.mps) - 1, 0, -1):
         E, dl = _dmrg2_bond_right(m, site, alg)

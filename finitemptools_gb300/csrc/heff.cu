@@ -393,6 +393,10 @@ int fmpt_updateleft(fmpt_handle* h, int dtype, int precision, const double* hold
     return set_error(h, FMPT_ERR_SHAPE, "updateleft: non-positive dimension");
   if (!W && wl != wr) return set_error(h, FMPT_ERR_SHAPE, "overlap update needs wl == wr");
   const int cp = dtype == FMPT_C128;
+  if (precision != FMPT_PREC_FP64) {
+    if (cp) return set_error(h, FMPT_ERR_UNSUPPORTED, "mixed precision: complex environments");
+    return env_update_tc(h, false, precision, hold, A, W, B, hnew, Dl, d, Dr, wl, wr);
+  }
   MidSchedule s;
   FMPT_TRY(schedule_env(h, cp, W, d, wl, wr, false, s));
   const int64_t nT = (int64_t)Dl * wl * d * Dr, nU = (int64_t)Dl * d * wr * Dr;
@@ -425,6 +429,10 @@ int fmpt_updateright(fmpt_handle* h, int dtype, int precision, const double* hol
     return set_error(h, FMPT_ERR_SHAPE, "updateright: non-positive dimension");
   if (!W && wl != wr) return set_error(h, FMPT_ERR_SHAPE, "overlap update needs wl == wr");
   const int cp = dtype == FMPT_C128;
+  if (precision != FMPT_PREC_FP64) {
+    if (cp) return set_error(h, FMPT_ERR_UNSUPPORTED, "mixed precision: complex environments");
+    return env_update_tc(h, true, precision, hold, A, W, B, hnew, Dl, d, Dr, wl, wr);
+  }
   MidSchedule s;
   FMPT_TRY(schedule_env(h, cp, W, d, wl, wr, true, s));
   const int64_t nT = (int64_t)Dl * d * Dr * wr, nU = (int64_t)wl * Dl * d * Dr;

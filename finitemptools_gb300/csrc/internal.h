@@ -150,6 +150,10 @@ int op_apply_fp64(fmpt_op* op, const double* x, double* y);
 int op_tc_prepare(fmpt_op* op);
 int op_tc_apply(fmpt_op* op, const double* x, double* y);
 int op_tc_check(fmpt_op* op);   // reads the device timeout flag (synchronises)
+// mixed-precision environment update (real data), FP64 output in the reference layout
+int env_update_tc(fmpt_handle* h, bool right, int precision, const double* hold, const double* A,
+                  const double* W, const double* B, double* hnew, int Dl, int d, int Dr, int wl,
+                  int wr);
 void op_tc_free(fmpt_op* op);
 
 // K-major tensor-core operand: TF32 (float storage) or BF16 plane, optional

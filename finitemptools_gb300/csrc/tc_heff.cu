@@ -165,6 +165,47 @@ __global__ void __launch_bounds__(256) mid_tc_p4(const float4* __restrict__ T1, 
   }
 }
 
+// Strided MPO step for the environment updates (any layout, P = d <= 4,
+// MPO bonds <= 8): out[o1,o2,wo,q] = sum_{(wi,wo) in mask} sum_s c[wi,wo][q,s] in[o1,o2,wi,s]
+template <int MODE, int P>
+__global__ void __launch_bounds__(256) mid_tc_mask(const float* __restrict__ T, int64_t i1,
+                                                   int64_t i2, int64_t iw, int64_t is, int n1,
+                                                   int n2, int nw_in, int nw_out, uint64_t mask,
+                                                   const float* __restrict__ cdev, void* hi,
+                                                   void* lo, int64_t o1s, int64_t o2s,
+                                                   int64_t ows, int64_t oqs) {
+  __shared__ float c[64][P * P];                  // [wi*8 + wo][q*P + s]
+  for (int i = threadIdx.x; i < 64 * P * P; i += blockDim.x) c[i / (P * P)][i % (P * P)] = cdev[i];
+  __syncthreads();
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)n1 * n2) return;
+  const int o1 = (int)(t % n1), o2 = (int)(t / n1);
+  const float* ib = T + o1 * i1 + o2 * i2;
+  float v[8][P];
+#pragma unroll
+  for (int wi = 0; wi < 8; wi++)
+#pragma unroll
+    for (int q = 0; q < P; q++) v[wi][q] = wi < nw_in ? ib[wi * iw + q * is] : 0.f;
+  const int64_t ob = o1 * o1s + o2 * o2s;
+#pragma unroll
+  for (int wo = 0; wo < 8; wo++) {
+    if (wo >= nw_out) break;
+    float acc[P];
+#pragma unroll
+    for (int q = 0; q < P; q++) acc[q] = 0.f;
+#pragma unroll
+    for (int wi = 0; wi < 8; wi++) {
+      if (!((mask >> (wi * 8 + wo)) & 1ull)) continue;
+#pragma unroll
+      for (int q = 0; q < P; q++)
+#pragma unroll
+        for (int s2 = 0; s2 < P; s2++) acc[q] = fmaf(c[wi * 8 + wo][q * P + s2], v[wi][s2], acc[q]);
+    }
+#pragma unroll
+    for (int q = 0; q < P; q++) put<MODE>(hi, lo, ob + wo * ows + q * oqs, (double)acc[q]);
+  }
+}
+
 struct TcState {
   int mode = 0, P = 1, es = 4;
   int Kp = 0, Drp = 0;
@@ -329,6 +370,213 @@ int op_tc_apply(fmpt_op* op, const double* x, double* y) {
   FMPT_TRY(tc_gemm(h, st->mode, P * Dl, Dr, (int)st->K2, 1, A2, B2, y, 1, (int64_t)P * Dl, 0,
                    st->err));
   return FMPT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Mixed-precision environment updates (mpo/transfer.jl:26-34), real data.
+//   updateleft : T1[(s,b),(a',w)] = sum_a Bg[a,(s,b)] Lg[a,(a',w)]          (GEMM 1)
+//                U [(a',s'),(w2,b)] = MPO step over (w, s)                    (bitmask)
+//                hnew[b',(w2,b)]  = sum_(a',s') Ag[(a',s'),b'] U[...]        (GEMM 2, FP64 out)
+//   updateright: T1[(a,s),(b',w2)] = sum_b Bt[b,(a,s)] Rt[b,(b',w2)]          (GEMM 1)
+//                U [(s',b'),(w,a)] = MPO step over (w2, s)
+//                hnew[a',(w,a)]   = sum_(s',b') At[(s',b'),a'] U[...]        (GEMM 2, FP64 out)
+namespace {
+
+int mask_and_coef(fmpt_handle* h, const MidSchedule& ms, int P, uint64_t* mask, DevBuf& cbuf) {
+  if (ms.nw_in > 8 || ms.nw_out > 8 || (P != 2 && P != 4))
+    return set_error(h, FMPT_ERR_UNSUPPORTED,
+                     "mixed-precision environment update needs MPO bonds <= 8 and d = 2 or 4");
+  std::vector<float> cf((size_t)64 * P * P, 0.f);
+  uint64_t m = 0;
+  for (int wo = 0; wo < ms.nw_out; wo++)
+    for (int e = ms.wout_start[wo]; e < ms.wout_start[wo + 1]; e++) {
+      const int wi = ms.blk_win[e];
+      m |= 1ull << (wi * 8 + wo);
+      for (int q = 0; q < P * P; q++)
+        cf[(size_t)(wi * 8 + wo) * P * P + q] += (float)ms.coef[(size_t)e * P * P + q];
+    }
+  FMPT_TRY(cbuf.alloc(h, cf.size() * sizeof(float)));
+  FMPT_CUDA(h, cudaMemcpyAsync(cbuf.p, cf.data(), cf.size() * sizeof(float),
+                               cudaMemcpyHostToDevice, h->stream));
+  FMPT_CUDA(h, cudaStreamSynchronize(h->stream));   // cf must outlive the copy
+  *mask = m;
+  return FMPT_OK;
+}
+
+template <int MODE>
+int launch_mask(fmpt_handle* h, int P, const float* T, int64_t i1, int64_t i2, int64_t iw,
+                int64_t is, int n1, int n2, int nw_in, int nw_out, uint64_t mask, const float* c,
+                void* hi, void* lo, int64_t o1, int64_t o2, int64_t ow, int64_t oq) {
+  const int64_t nt = (int64_t)n1 * n2;
+  const unsigned blocks = (unsigned)((nt + 255) / 256);
+  ProfScope prof(h, FMPT_K_MPO_STEP);
+  if (P <= 2)
+    mid_tc_mask<MODE, 2><<<blocks, 256, 0, h->stream>>>(T, i1, i2, iw, is, n1, n2, nw_in, nw_out,
+                                                         mask, c, hi, lo, o1, o2, ow, oq);
+  else
+    mid_tc_mask<MODE, 4><<<blocks, 256, 0, h->stream>>>(T, i1, i2, iw, is, n1, n2, nw_in, nw_out,
+                                                         mask, c, hi, lo, o1, o2, ow, oq);
+  FMPT_LAUNCHED(h);
+  return FMPT_OK;
+}
+
+int conv_state_any(fmpt_handle* h, int mode, const double* x, int K, int Kp, int64_t M, void* hi,
+                   void* lo) {
+  const int64_t n = (int64_t)Kp * M;
+  ProfScope prof(h, FMPT_K_CONVERT);
+  if (mode == M_TF32)
+    conv_state<M_TF32><<<grid1(h, n), 256, 0, h->stream>>>(x, K, Kp, M, hi, lo);
+  else if (mode == M_TF32X3)
+    conv_state<M_TF32X3><<<grid1(h, n), 256, 0, h->stream>>>(x, K, Kp, M, hi, lo);
+  else
+    conv_state<M_BF16><<<grid1(h, n), 256, 0, h->stream>>>(x, K, Kp, M, hi, lo);
+  FMPT_LAUNCHED(h);
+  return FMPT_OK;
+}
+
+struct Planes {
+  DevBuf p[2];
+  void* hi() const { return p[0].p; }
+  void* lo() const { return p[1].p; }
+  int alloc(fmpt_handle* h, int mode, size_t n) {
+    const size_t es = mode == M_BF16 ? 2 : 4;
+    FMPT_TRY(p[0].alloc(h, n * es));
+    if (mode == M_TF32X3) FMPT_TRY(p[1].alloc(h, n * es));
+    return FMPT_OK;
+  }
+  int zero(fmpt_handle* h) {
+    for (auto& b : p)
+      if (b.p) FMPT_CUDA(h, cudaMemsetAsync(b.p, 0, b.bytes, h->stream));
+    return FMPT_OK;
+  }
+};
+
+int env_left_tc(fmpt_handle* h, int precision, const double* hold, const double* A,
+                const double* W, const double* B, double* hnew, int Dl, int d, int Dr, int wl,
+                int wr) {
+  const int mode = tc_mode_of(precision);
+  MidSchedule ms;
+  FMPT_TRY(schedule_env(h, 0, W, d, wl, wr, false, ms));
+  uint64_t mask = 0;
+  DevBuf cbuf;
+  int st = mask_and_coef(h, ms, d, &mask, cbuf);
+  mid_free(h, ms);
+  FMPT_TRY(st);
+  const int Kp = round_up8(Dl), K2 = round_up8(Dl * d);
+  Planes Bg, Lg, Ag, U;
+  DevBuf T1;
+  FMPT_TRY(Bg.alloc(h, mode, (size_t)Kp * d * Dr));
+  FMPT_TRY(Lg.alloc(h, mode, (size_t)Kp * Dl * wl));
+  FMPT_TRY(Ag.alloc(h, mode, (size_t)K2 * Dr));
+  FMPT_TRY(U.alloc(h, mode, (size_t)K2 * wr * Dr));
+  FMPT_TRY(U.zero(h));                                         // K padding
+  FMPT_TRY(T1.alloc(h, (size_t)d * Dr * wl * Dl * sizeof(float)));
+  FMPT_TRY(conv_state_any(h, mode, B, Dl, Kp, (int64_t)d * Dr, Bg.hi(), Bg.lo()));
+  FMPT_TRY(transpose_any(h, mode, hold, (int64_t)Dl * wl, Dl, Dl, Dl, Kp, wl, Lg.hi(), Lg.lo(), Kp,
+                         (int64_t)Kp * Dl));
+  FMPT_TRY(conv_state_any(h, mode, A, Dl * d, K2, Dr, Ag.hi(), Ag.lo()));
+  int* err = nullptr;
+  FMPT_CUDA(h, cudaMallocAsync((void**)&err, sizeof(int), h->stream));
+  FMPT_CUDA(h, cudaMemsetAsync(err, 0, sizeof(int), h->stream));
+  TcOperand A1{Bg.hi(), Bg.lo(), Kp, 0}, B1{Lg.hi(), Lg.lo(), Kp, 0};
+  st = tc_gemm(h, mode, d * Dr, wl * Dl, Kp, 1, A1, B1, T1.p, 0, (int64_t)d * Dr, 0, err);
+  // in : T1[(s + d b) + d Dr (a' + Dl w)]  (o1 = b, o2 = a')
+  // out: U[(a' + Dl s') + K2 (w2 + wr b)]
+  if (st == FMPT_OK) {
+    const float* t1 = (const float*)T1.p;
+    const float* c = (const float*)cbuf.p;
+    const int64_t i1 = d, i2 = (int64_t)d * Dr, iw = (int64_t)d * Dr * Dl, is = 1;
+    const int64_t o1 = (int64_t)K2 * wr, o2 = 1, ow = K2, oq = Dl;
+    if (mode == M_TF32)
+      st = launch_mask<M_TF32>(h, d, t1, i1, i2, iw, is, Dr, Dl, wl, wr, mask, c, U.hi(), U.lo(), o1, o2, ow, oq);
+    else if (mode == M_TF32X3)
+      st = launch_mask<M_TF32X3>(h, d, t1, i1, i2, iw, is, Dr, Dl, wl, wr, mask, c, U.hi(), U.lo(), o1, o2, ow, oq);
+    else
+      st = launch_mask<M_BF16>(h, d, t1, i1, i2, iw, is, Dr, Dl, wl, wr, mask, c, U.hi(), U.lo(), o1, o2, ow, oq);
+  }
+  if (st == FMPT_OK) {
+    TcOperand A2{Ag.hi(), Ag.lo(), K2, 0}, B2{U.hi(), U.lo(), K2, 0};
+    st = tc_gemm(h, mode, Dr, wr * Dr, K2, 1, A2, B2, hnew, 1, Dr, 0, err);
+  }
+  int e = 0;
+  if (st == FMPT_OK) {
+    FMPT_CUDA(h, cudaMemcpyAsync(&e, err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    FMPT_CUDA(h, cudaStreamSynchronize(h->stream));
+  }
+  cudaFreeAsync(err, h->stream);
+  FMPT_TRY(st);
+  if (e) return set_error(h, FMPT_ERR_TIMEOUT, "tensor-core GEMM wait timed out");
+  return FMPT_OK;
+}
+
+int env_right_tc(fmpt_handle* h, int precision, const double* hold, const double* A,
+                 const double* W, const double* B, double* hnew, int Dl, int d, int Dr, int wl,
+                 int wr) {
+  const int mode = tc_mode_of(precision);
+  MidSchedule ms;
+  FMPT_TRY(schedule_env(h, 0, W, d, wl, wr, true, ms));
+  uint64_t mask = 0;
+  DevBuf cbuf;
+  int st = mask_and_coef(h, ms, d, &mask, cbuf);
+  mid_free(h, ms);
+  FMPT_TRY(st);
+  const int Kb = round_up8(Dr), Kq = round_up8(d * Dr);
+  Planes Bt, Rt, At, U;
+  DevBuf T1;
+  FMPT_TRY(Bt.alloc(h, mode, (size_t)Kb * Dl * d));
+  FMPT_TRY(Rt.alloc(h, mode, (size_t)Kb * Dr * wr));
+  FMPT_TRY(At.alloc(h, mode, (size_t)Kq * Dl));
+  FMPT_TRY(U.alloc(h, mode, (size_t)Kq * wl * Dl));
+  FMPT_TRY(U.zero(h));
+  FMPT_TRY(T1.alloc(h, (size_t)Dl * d * Dr * wr * sizeof(float)));
+  // Bt[b + Kb (a + Dl s)] = B[(a + Dl s) + Dl d b]
+  FMPT_TRY(transpose_any(h, mode, B, (int64_t)Dl * d, 0, Dl * d, Dr, Kb, 1, Bt.hi(), Bt.lo(), Kb, 0));
+  // Rt[b + Kb (b' + Dr w2)] = hold[b' + Dr w2 + Dr wr b]
+  FMPT_TRY(transpose_any(h, mode, hold, (int64_t)Dr * wr, Dr, Dr, Dr, Kb, wr, Rt.hi(), Rt.lo(), Kb,
+                         (int64_t)Kb * Dr));
+  // At[(s' + d b') + Kq a'] = A[a' + Dl (s' + d b')]   (rows a', columns (s', b'))
+  FMPT_TRY(transpose_any(h, mode, A, Dl, 0, Dl, d * Dr, Kq, 1, At.hi(), At.lo(), Kq, 0));
+  int* err = nullptr;
+  FMPT_CUDA(h, cudaMallocAsync((void**)&err, sizeof(int), h->stream));
+  FMPT_CUDA(h, cudaMemsetAsync(err, 0, sizeof(int), h->stream));
+  TcOperand A1{Bt.hi(), Bt.lo(), Kb, 0}, B1{Rt.hi(), Rt.lo(), Kb, 0};
+  st = tc_gemm(h, mode, Dl * d, Dr * wr, Kb, 1, A1, B1, T1.p, 0, (int64_t)Dl * d, 0, err);
+  // in : T1[(a + Dl s) + Dl d (b' + Dr w2)]   (o1 = a, o2 = b', w = w2)
+  // out: U[(s' + d b') + Kq (w + wl a)]
+  if (st == FMPT_OK) {
+    const float* t1 = (const float*)T1.p;
+    const float* c = (const float*)cbuf.p;
+    const int64_t i1 = 1, i2 = (int64_t)Dl * d, iw = (int64_t)Dl * d * Dr, is = Dl;
+    const int64_t o1 = (int64_t)Kq * wl, o2 = d, ow = Kq, oq = 1;
+    if (mode == M_TF32)
+      st = launch_mask<M_TF32>(h, d, t1, i1, i2, iw, is, Dl, Dr, wr, wl, mask, c, U.hi(), U.lo(), o1, o2, ow, oq);
+    else if (mode == M_TF32X3)
+      st = launch_mask<M_TF32X3>(h, d, t1, i1, i2, iw, is, Dl, Dr, wr, wl, mask, c, U.hi(), U.lo(), o1, o2, ow, oq);
+    else
+      st = launch_mask<M_BF16>(h, d, t1, i1, i2, iw, is, Dl, Dr, wr, wl, mask, c, U.hi(), U.lo(), o1, o2, ow, oq);
+  }
+  if (st == FMPT_OK) {
+    TcOperand A2{At.hi(), At.lo(), Kq, 0}, B2{U.hi(), U.lo(), Kq, 0};
+    st = tc_gemm(h, mode, Dl, wl * Dl, Kq, 1, A2, B2, hnew, 1, Dl, 0, err);
+  }
+  int e = 0;
+  if (st == FMPT_OK) {
+    FMPT_CUDA(h, cudaMemcpyAsync(&e, err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    FMPT_CUDA(h, cudaStreamSynchronize(h->stream));
+  }
+  cudaFreeAsync(err, h->stream);
+  FMPT_TRY(st);
+  if (e) return set_error(h, FMPT_ERR_TIMEOUT, "tensor-core GEMM wait timed out");
+  return FMPT_OK;
+}
+
+}  // namespace
+
+int env_update_tc(fmpt_handle* h, bool right, int precision, const double* hold,
+                  const double* A, const double* W, const double* B, double* hnew, int Dl, int d,
+                  int Dr, int wl, int wr) {
+  return right ? env_right_tc(h, precision, hold, A, W, B, hnew, Dl, d, Dr, wl, wr)
+               : env_left_tc(h, precision, hold, A, W, B, hnew, Dl, d, Dr, wl, wr);
 }
 
 int op_tc_check(fmpt_op* op) {

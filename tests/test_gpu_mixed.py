@@ -133,3 +133,20 @@ def test_mixed_dmrg2_energy_within_1e8_of_fp64():
     assert abs(E3 - E64) < 1e-8 * abs(E64)
     # the mixed Ritz values carry the first-order operator error only
     assert abs(Es3[-1] - E64) < 1e-5 * abs(E64)
+
+
+@pytest.mark.parametrize("prec", ["tf32x3", "tf32", "bf16"])
+@pytest.mark.parametrize("Dl,Dr,wl,wr,d", [(1, 2, 1, 8, 2), (13, 21, 5, 5, 2), (64, 48, 8, 8, 2),
+                                           (24, 24, 4, 3, 4), (128, 128, 8, 8, 2)])
+def test_env_updates_mixed(prec, Dl, Dr, wl, wr, d):
+    rng = np.random.default_rng(Dl * 7 + Dr + wl)
+    W = rng.standard_normal((wl, d, wr, d)) * (rng.random((wl, 1, wr, 1)) < 0.6)
+    A = rng.standard_normal((Dl, d, Dr))
+    B = rng.standard_normal((Dl, d, Dr))
+    Lh = rng.standard_normal((Dl, wl, Dl))
+    Rh = rng.standard_normal((Dr, wr, Dr))
+    K = 2 * max(Dl * d, Dr * d)      # the two GEMMs' summed lengths (K1 + K2 <= 2 max)
+    gl = fm.updateleft(DT.from_numpy(Lh), DT.from_numpy(A), W, DT.from_numpy(B), prec).numpy()
+    assert rel(gl, O.updateleft(Lh, A, W, B)) < tol(prec, K)
+    gr = fm.updateright(DT.from_numpy(Rh), DT.from_numpy(A), W, DT.from_numpy(B), prec).numpy()
+    assert rel(gr, O.updateright(Rh, A, W, B)) < tol(prec, K)
