@@ -168,25 +168,35 @@ struct Cfg {
   static constexpr int TMEM_COLS = BN <= 32 ? 32 : BN <= 64 ? 64 : BN <= 128 ? 128 : 256;
   static_assert(BN % 16 == 0 && BN >= 16 && BN <= 256, "N tile");
   static_assert(SMEM <= 227 * 1024, "shared memory");
+  static_assert(2 * TMEM_COLS <= 512, "two accumulator buffers must fit in TMEM");
+  static_assert((2 * STAGES + 5) * 8 + 8 <= 256, "barrier area");
 };
 
 template <int MODE, int BN, int STAGES, int OUT>
 __global__ void __launch_bounds__(NTHREADS, 1)
     gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
                 const __grid_constant__ CUtensorMap mapA2, const __grid_constant__ CUtensorMap mapB2,
-                int K, EpiArgs ep) {
+                int K, int tiles_m, int tiles_n, int batch, EpiArgs ep) {
+  // Persistent: CTA b processes tiles b, b + gridDim.x, ...  (M-tile index fastest, so
+  // CTAs running at the same time share B tiles in L2).  The accumulator is double
+  // buffered in TMEM: the epilogue of one tile drains buffer t&1 while the MMA warp
+  // fills the other one with the next tile.
   using C_ = Cfg<MODE, BN, STAGES, OUT>;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                              ~uintptr_t(1023));
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * C_::STAGE_BYTES);
-  // bars[0..S): full, [S..2S): empty, [2S]: accumulator ready, [2S+1]: drain
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 2);
+  // bars: [0,S) full  [S,2S) empty  [2S,2S+2) accumulator full  [2S+2,2S+4) accumulator
+  // empty  [2S+4] drain
+  uint64_t* acc_full = bars + 2 * STAGES;
+  uint64_t* acc_empty = bars + 2 * STAGES + 2;
+  uint64_t* drain = bars + 2 * STAGES + 4;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 5);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-  const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN, z = blockIdx.z;
   const int nk = (K + C_::KELEMS - 1) / C_::KELEMS;
+  const int num_tiles = tiles_m * tiles_n * batch;
 
   auto stageA = [&](int s, int part) { return smem + s * C_::STAGE_BYTES + part * (C_::A_BYTES + C_::B_BYTES); };
   auto stageB = [&](int s, int part) { return stageA(s, part) + C_::A_BYTES; };
@@ -196,8 +206,11 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       mbar_init(smem_u32(&bars[s]), 1);
       mbar_init(smem_u32(&bars[STAGES + s]), 1);
     }
-    mbar_init(smem_u32(&bars[2 * STAGES]), 1);
-    mbar_init(smem_u32(&bars[2 * STAGES + 1]), 1);
+    for (int b = 0; b < 2; b++) {
+      mbar_init(smem_u32(&acc_full[b]), 1);
+      mbar_init(smem_u32(&acc_empty[b]), 4);          // one arrival per epilogue warp
+    }
+    mbar_init(smem_u32(drain), 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&mapA)) : "memory");
@@ -206,7 +219,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(tmem_slot)),
-                 "r"(C_::TMEM_COLS)
+                 "r"(2 * C_::TMEM_COLS)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -217,28 +230,32 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 
   if (warp == 0) {
     if (lane == 0) {
-      int issued_stage_last = -1;
-      for (int kb = 0; kb < nk; kb++) {
-        const int s = kb % STAGES;
-        const uint32_t ph = (kb / STAGES) & 1;
-        if (!mbar_wait(smem_u32(&bars[STAGES + s]), ph ^ 1, abort_flag, ep.err)) break;
-        const uint32_t full = smem_u32(&bars[s]);
-        mbar_expect_tx(full, C_::STAGE_BYTES);
-        const int kc = kb * C_::KELEMS;
-        tma_load_3d(smem_u32(stageA(s, 0)), &mapA, full, kc, m0, z);
-        tma_load_3d(smem_u32(stageB(s, 0)), &mapB, full, kc, n0, z);
-        if (MODE == TF32X3) {
-          tma_load_3d(smem_u32(stageA(s, 1)), &mapA2, full, kc, m0, z);
-          tma_load_3d(smem_u32(stageB(s, 1)), &mapB2, full, kc, n0, z);
+      int it = 0, last = -1;
+      for (int tile = blockIdx.x; tile < num_tiles && !*abort_flag; tile += gridDim.x) {
+        const int mt = tile % tiles_m, nt = (tile / tiles_m) % tiles_n, z = tile / (tiles_m * tiles_n);
+        const int m0 = mt * BM, n0 = nt * BN;
+        for (int kb = 0; kb < nk; kb++, it++) {
+          const int s = it % STAGES;
+          const uint32_t ph = (it / STAGES) & 1;
+          if (!mbar_wait(smem_u32(&bars[STAGES + s]), ph ^ 1, abort_flag, ep.err)) break;
+          const uint32_t full = smem_u32(&bars[s]);
+          mbar_expect_tx(full, C_::STAGE_BYTES);
+          const int kc = kb * C_::KELEMS;
+          tma_load_3d(smem_u32(stageA(s, 0)), &mapA, full, kc, m0, z);
+          tma_load_3d(smem_u32(stageB(s, 0)), &mapB, full, kc, n0, z);
+          if (MODE == TF32X3) {
+            tma_load_3d(smem_u32(stageA(s, 1)), &mapA2, full, kc, m0, z);
+            tma_load_3d(smem_u32(stageB(s, 1)), &mapB2, full, kc, n0, z);
+          }
+          last = it;
         }
-        issued_stage_last = kb;
       }
       if (*abort_flag) {
         // drain: every load this thread issued must land before the CTA exits
-        for (int kb = max(0, issued_stage_last - STAGES + 1); kb <= issued_stage_last; kb++) {
-          const uint32_t bar = smem_u32(&bars[kb % STAGES]);
+        for (int j = max(0, last - STAGES + 1); j <= last; j++) {
+          const uint32_t bar = smem_u32(&bars[j % STAGES]);
           const unsigned long long t0 = globaltimer();
-          while (!mbar_try(bar, (kb / STAGES) & 1) && globaltimer() - t0 < WAIT_NS) {
+          while (!mbar_try(bar, (j / STAGES) & 1) && globaltimer() - t0 < WAIT_NS) {
           }
         }
       }
@@ -246,35 +263,49 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   } else if (warp == 1) {
     if (lane == 0) {
       constexpr uint32_t idesc = make_idesc(MODE, BM, BN);
-      for (int kb = 0; kb < nk; kb++) {
-        const int s = kb % STAGES;
-        const uint32_t ph = (kb / STAGES) & 1;
-        if (!mbar_wait(smem_u32(&bars[s]), ph, abort_flag, ep.err)) break;
+      int it = 0, local = 0;
+      for (int tile = blockIdx.x; tile < num_tiles && !*abort_flag; tile += gridDim.x, local++) {
+        const int buf = local & 1;
+        const uint32_t use = (uint32_t)(local >> 1);
+        if (!mbar_wait(smem_u32(&acc_empty[buf]), (use & 1) ^ 1, abort_flag, ep.err)) break;
         tc_fence_after();
-        const uint32_t a0 = smem_u32(stageA(s, 0)), b0 = smem_u32(stageB(s, 0));
+        const uint32_t tacc = tmem + buf * C_::TMEM_COLS;
+        for (int kb = 0; kb < nk; kb++, it++) {
+          const int s = it % STAGES;
+          const uint32_t ph = (it / STAGES) & 1;
+          if (!mbar_wait(smem_u32(&bars[s]), ph, abort_flag, ep.err)) break;
+          tc_fence_after();
+          const uint32_t a0 = smem_u32(stageA(s, 0)), b0 = smem_u32(stageB(s, 0));
 #pragma unroll
-        for (int ks = 0; ks < 4; ks++) {                     // 4 x 32 bytes of K per stage
-          const uint32_t acc = (kb > 0 || ks > 0) ? 1u : 0u;
-          const uint64_t ad = smem_desc(a0 + ks * 32), bd = smem_desc(b0 + ks * 32);
-          mma<MODE>(tmem, ad, bd, idesc, acc);
-          if (MODE == TF32X3) {
-            const uint32_t a1 = smem_u32(stageA(s, 1)), b1 = smem_u32(stageB(s, 1));
-            mma<MODE>(tmem, ad, smem_desc(b1 + ks * 32), idesc, 1u);
-            mma<MODE>(tmem, smem_desc(a1 + ks * 32), bd, idesc, 1u);
+          for (int ks = 0; ks < 4; ks++) {                     // 4 x 32 bytes of K per stage
+            const uint32_t acc = (kb > 0 || ks > 0) ? 1u : 0u;
+            const uint64_t ad = smem_desc(a0 + ks * 32), bd = smem_desc(b0 + ks * 32);
+            mma<MODE>(tacc, ad, bd, idesc, acc);
+            if (MODE == TF32X3) {
+              const uint32_t a1 = smem_u32(stageA(s, 1)), b1 = smem_u32(stageB(s, 1));
+              mma<MODE>(tacc, ad, smem_desc(b1 + ks * 32), idesc, 1u);
+              mma<MODE>(tacc, smem_desc(a1 + ks * 32), bd, idesc, 1u);
+            }
           }
+          mma_commit(smem_u32(&bars[STAGES + s]));             // frees the stage when done
         }
-        mma_commit(smem_u32(&bars[STAGES + s]));             // frees the stage when done
+        mma_commit(smem_u32(&acc_full[buf]));                  // this tile's accumulator is ready
       }
-      mma_commit(smem_u32(&bars[2 * STAGES]));               // accumulator ready
     }
   } else {
     // epilogue warps 2..5: TMEM lane quarter = warp % 4
     const int q = warp & 3;
-    const bool ok = mbar_wait(smem_u32(&bars[2 * STAGES]), 0, abort_flag, ep.err);
-    tc_fence_after();
-    if (ok && !*abort_flag) {
-      const int row = m0 + 32 * q + lane;
-      const uint32_t tbase = tmem + ((uint32_t)(32 * q) << 16);
+    int local = 0;
+    for (int tile = blockIdx.x; tile < num_tiles; tile += gridDim.x, local++) {
+      const int buf = local & 1;
+      const uint32_t use = (uint32_t)(local >> 1);
+      const bool ok = mbar_wait(smem_u32(&acc_full[buf]), use & 1, abort_flag, ep.err);
+      if (!ok || *abort_flag) break;
+      tc_fence_after();
+      const int mt = tile % tiles_m, nt = (tile / tiles_m) % tiles_n, z = tile / (tiles_m * tiles_n);
+      const int row = mt * BM + 32 * q + lane;
+      const int n0 = nt * BN;
+      const uint32_t tbase = tmem + buf * C_::TMEM_COLS + ((uint32_t)(32 * q) << 16);
 #pragma unroll 1
       for (int c0 = 0; c0 < BN; c0 += 16) {
         uint32_t r[16];
@@ -294,6 +325,13 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           }
         }
       }
+      // the accumulator buffer may be refilled once all four warps have read it
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) {
+        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&acc_empty[buf]))
+                     : "memory");
+      }
     }
   }
   tc_fence_before();
@@ -302,14 +340,14 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     tc_fence_after();
     if (lane == 0) {
       // all MMAs issued by this CTA have retired before TMEM is released
-      mma_commit(smem_u32(&bars[2 * STAGES + 1]));
+      mma_commit(smem_u32(drain));
       const unsigned long long t0 = globaltimer();
-      while (!mbar_try(smem_u32(&bars[2 * STAGES + 1]), 0) && globaltimer() - t0 < WAIT_NS) {
+      while (!mbar_try(smem_u32(drain), 0) && globaltimer() - t0 < WAIT_NS) {
       }
     }
     __syncwarp();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
-                 "r"(C_::TMEM_COLS)
+                 "r"(2 * C_::TMEM_COLS)
                  : "memory");
   }
 }
@@ -374,8 +412,11 @@ int tc_gemm(fmpt_handle* h, int mode, int M, int N, int K, int batch, const TcOp
     mb2 = mb;
   }
   EpiArgs ep{C, ldc, strideC, M, N, err_dev};
-  dim3 grid((M + BM - 1) / BM, (N + BN - 1) / BN, batch);
-  if (grid.y > 65535 || grid.z > 65535) return set_error(h, FMPT_ERR_SHAPE, "tc_gemm grid");
+  const int tiles_m = (M + BM - 1) / BM, tiles_n = (N + BN - 1) / BN;
+  const int64_t tiles = (int64_t)tiles_m * tiles_n * batch;
+  if (tiles > INT32_MAX) return set_error(h, FMPT_ERR_SHAPE, "tc_gemm: too many tiles");
+  const int sms = h->sm_count > 0 ? h->sm_count : 1;
+  dim3 grid((unsigned)std::min<int64_t>(tiles, sms), 1, 1);
   ProfScope prof(h, FMPT_K_TC_GEMM);
 #define LAUNCH(MODE_, BN_, ST_, OUT_)                                                         \
   do {                                                                                        \
@@ -386,7 +427,7 @@ int tc_gemm(fmpt_handle* h, int mode, int M, int N, int K, int batch, const TcOp
       FMPT_CUDA(h, cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, SM_)); \
       attr_done = true;                                                                       \
     }                                                                                         \
-    kfn<<<grid, NTHREADS, SM_, h->stream>>>(ma, mb, ma2, mb2, K, ep);                         \
+    kfn<<<grid, NTHREADS, SM_, h->stream>>>(ma, mb, ma2, mb2, K, tiles_m, tiles_n, batch, ep); \
   } while (0)
   if (mode == TF32) {
     if (out_f64) LAUNCH(TF32, 256, 4, 1); else LAUNCH(TF32, 256, 4, 0);
