@@ -186,6 +186,96 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def dmrg_section(h, fm, budget_s=150.0):
+    """DMRG sweep seconds, plain FP64 vs the mixed form (3xTF32 contractions and
+    environment updates, FP64 Lanczos reorthogonalisation, FP64 density-matrix
+    split), each energy evaluated in FP64 as <psi|H|psi> of the final state.
+      xxz_L20: XXZ L=20, Delta=1, D=64, cutoff 1e-10, 4 sweeps from a seeded D=8
+               right-canonical state; the exact energy is the ED fixture.
+      j1j2_L100_D1024: J1-J2 L=100, J1=1, J2=0.3, cutoff 1e-9, ramp 64 -> 256 -> 1024 in
+               the mixed form, then one timed mixed sweep at D=1024; the FP64 sweep
+               time is extrapolated from three centre bonds timed in both forms.
+               (At J2=0.5 the ground state is an exact dimer product and keeps D<=3,
+               so the D=1024 stage runs at J2=0.3.)"""
+    import time as _t
+    from finitemptools_gb300 import algorithms as A
+    out = {}
+    t_start = _t.perf_counter()
+    with open(os.path.join(ROOT, "tests", "golden", "exact_energies.json")) as f:
+        e_ed = json.load(f)["xxz_L20_J1_Jzz1_hz0"]
+
+    def run(L, mpo, stages, prec, svd, reorth, eps, D0, seed):
+        rng = np.random.default_rng(seed)
+        psi = fm.randommps(L, 2, D0, rng, handle=h)
+        fm.canonicalize_(psi, normalize=True)
+        env = fm.environments(fm.FiniteMPO(mpo, L), psi)
+        times = []
+        for D, n in stages:
+            alg = fm.DMRG2(eig_maxiter=30, eig_tol=1e-12, trunc=fm.MPSTruncation(D, eps),
+                           precision=prec, reorth=reorth, svd=svd)
+            for _ in range(n):
+                h.synchronize()
+                t0 = _t.perf_counter()
+                fm.sweep_(env, alg)
+                h.synchronize()
+                times.append(_t.perf_counter() - t0)
+        return env, times
+
+    hx = fm.heisenberg_xxz_mpo(1.0, 1.0, 0.0)
+    env64, t64 = run(20, hx, [(64, 4)], "fp64", "gesvd", False, 1e-10, 8, 20)
+    envmx, tmx = run(20, hx, [(64, 4)], "tf32x3", "dm", True, 1e-10, 8, 20)
+    E64 = float(fm.expectation(env64.mps, fm.FiniteMPO(hx, 20)))
+    Emx = float(fm.expectation(envmx.mps, fm.FiniteMPO(hx, 20)))
+    out["xxz_L20_D64"] = {"sweep_s_fp64": t64, "sweep_s_mixed": tmx, "E_fp64": E64,
+                          "E_mixed_fp64_eval": Emx, "dE_rel_mixed_vs_fp64": abs(Emx - E64) / abs(E64),
+                          "E_ed": e_ed, "dE_rel_fp64_vs_ed": abs(E64 - e_ed) / abs(e_ed)}
+    if _t.perf_counter() - t_start > budget_s:
+        return out
+    hj = fm.j1j2_heisenberg_mpo(1.0, 0.3)
+    env, tramp = run(100, hj, [(64, 1), (256, 1), (1024, 1)], "tf32x3", "dm", True, 1e-9, 16, 5)
+    alg_mx = fm.DMRG2(eig_maxiter=30, eig_tol=1e-12, trunc=fm.MPSTruncation(1024, 1e-9),
+                      precision="tf32x3", reorth=True, svd="dm")
+    h.synchronize()
+    t0 = _t.perf_counter()
+    fm.sweep_(env, alg_mx)
+    h.synchronize()
+    t_mixed = _t.perf_counter() - t0
+    E = float(fm.expectation(env.mps, fm.FiniteMPO(hj, 100)))
+    Dmax = fm.bond_dimension(env.mps)
+    # the centre bond (left-sweep bond body) in both forms on the same tensors: advance the
+    # mixed left sweep to site 49 so that its left environment is current, then time the
+    # bond three times per form, restoring the two site tensors and the environment after
+    # every call
+    alg_64 = fm.DMRG2(eig_maxiter=30, eig_tol=1e-12, trunc=fm.MPSTruncation(1024, 1e-9))
+    env.precision = alg_mx.env_precision
+    for site in range(1, 49):
+        A._dmrg2_bond_left(env, site, alg_mx)
+    site = 49
+    bonds = []
+    for rep in range(3):
+        tb = {}
+        for name, alg in (("mixed", alg_mx), ("fp64", alg_64)):
+            saved = [env.mps[site].copy(), env.mps[site + 1].copy()]
+            saved_env = env.hstorage[site + 1]
+            env.precision = alg.env_precision
+            h.synchronize()
+            t0 = _t.perf_counter()
+            A._dmrg2_bond_left(env, site, alg)
+            h.synchronize()
+            tb[name] = _t.perf_counter() - t0
+            env.mps[site], env.mps[site + 1] = saved
+            env.hstorage[site + 1] = saved_env
+        bonds.append({"site": site, "D": list(env.mps[site].shape), "s_mixed": tb["mixed"],
+                      "s_fp64": tb["fp64"]})
+    ratio = sum(b["s_fp64"] for b in bonds) / sum(b["s_mixed"] for b in bonds)
+    out["j1j2_L100_J2_0.3_D1024"] = {
+        "ramp_sweeps_s_mixed": tramp, "sweep_s_mixed": t_mixed, "Dmax": Dmax,
+        "E_mixed_fp64_eval": E, "centre_bonds": bonds, "bond_speedup_fp64_over_mixed": ratio,
+        "sweep_s_fp64_extrapolated": t_mixed * ratio,
+        "note": "FP64 sweep time = timed mixed sweep x (FP64 / mixed time of the centre bond)"}
+    return out
+
+
 def config_dict(args, prec):
     return {"workload": "two-site H_eff*x (ac2_prime), Heisenberg Schur MPO w=5, "
                         "x[D,2,2,D], L/R[D,5,D] iid N(0,1) symmetrised",
@@ -205,6 +295,7 @@ def main():
     ap.add_argument("--precision", default="bf16", choices=["fp64", "tf32x3", "tf32", "bf16"])
     ap.add_argument("--no-table", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-dmrg", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -380,6 +471,10 @@ def main():
         for r in table:
             r["speedup_vs_fp64"] = fp64[r["D"]] / r["ms"]
 
+    dmrg = None
+    if rank == 0 and not args.no_dmrg:
+        dmrg = dmrg_section(h, fm)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(D)
@@ -391,7 +486,7 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": prec, "data": "synthetic",
             "config": config_dict(args, prec), "clocks": clocks, "e2e": e2e,
             "gpu_launches": n_launch, "roofline": roof, "cpu_baseline": cpu,
-            "per_dtype": table,
+            "per_dtype": table, "dmrg": dmrg,
         }
         print(json.dumps(line), flush=True)
     if pg:

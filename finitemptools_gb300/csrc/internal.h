@@ -165,7 +165,7 @@ struct TcOperand {
   int64_t bstride;
 };
 // C[m, n] (+ batch) = sum_k A[m, k] B[n, k] on tcgen05; mode 0 TF32, 1 3xTF32, 2 BF16;
-// C is FP32 (out_f64 = 0) or FP64, column-major with ldc.
+// C is FP32 (out_f64 = 0), FP64 (1) or, in BF16 mode, BF16 (2); column-major with ldc.
 int tc_gemm(fmpt_handle* h, int mode, int M, int N, int K, int batch, const TcOperand& A,
             const TcOperand& B, void* C, int out_f64, int64_t ldc, int64_t strideC, int* err_dev);
 }  // namespace fmpt

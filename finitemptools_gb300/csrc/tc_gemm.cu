@@ -319,6 +319,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
               const float v = __uint_as_float(r[j]);
               if (OUT == 1)
                 static_cast<double*>(ep.C)[idx] = (double)v;
+              else if (OUT == 2)
+                static_cast<__nv_bfloat16*>(ep.C)[idx] = __float2bfloat16_rn(v);
               else
                 static_cast<float*>(ep.C)[idx] = v;
             }
@@ -434,7 +436,9 @@ int tc_gemm(fmpt_handle* h, int mode, int M, int N, int K, int batch, const TcOp
   } else if (mode == TF32X3) {
     if (out_f64) LAUNCH(TF32X3, 128, 3, 1); else LAUNCH(TF32X3, 128, 3, 0);
   } else {
-    if (out_f64) LAUNCH(BF16, 256, 4, 1); else LAUNCH(BF16, 256, 4, 0);
+    if (out_f64 == 1) LAUNCH(BF16, 256, 4, 1);
+    else if (out_f64 == 2) LAUNCH(BF16, 256, 4, 2);
+    else LAUNCH(BF16, 256, 4, 0);
   }
 #undef LAUNCH
   FMPT_LAUNCHED(h);

@@ -126,8 +126,15 @@ __global__ void mid_tc(const float* __restrict__ T1, int P, int Dl, int Dr, int 
 // w <= 8: the nonzero (w, w') block pattern is a bitmask, every loop is
 // unrolled with static indices (registers only), T1 is read once as float4
 // and the block coefficients sit in shared memory.
-template <int MODE>
-__global__ void __launch_bounds__(256) mid_tc_p4(const float4* __restrict__ T1, int Dl, int Dr,
+__device__ __forceinline__ float4 load4(const float4* p) { return *p; }
+__device__ __forceinline__ float4 load4(const uint2* p) {
+  const uint2 u = *p;   // four BF16 values
+  return make_float4(__uint_as_float(u.x << 16), __uint_as_float(u.x & 0xffff0000u),
+                     __uint_as_float(u.y << 16), __uint_as_float(u.y & 0xffff0000u));
+}
+
+template <int MODE, typename V4>
+__global__ void __launch_bounds__(256) mid_tc_p4(const V4* __restrict__ T1, int Dl, int Dr,
                                                  int Drp, int64_t K2, int nw_in, int nw_out,
                                                  uint64_t mask, const float* __restrict__ cdev,
                                                  void* hi, void* lo) {
@@ -138,11 +145,11 @@ __global__ void __launch_bounds__(256) mid_tc_p4(const float4* __restrict__ T1, 
   if (t >= (int64_t)Dl * Dr) return;
   const int b = (int)(t % Dr), ap = (int)(t / Dr);
   const int64_t in_w = (int64_t)Dr * Dl;          // float4 stride between w planes
-  const float4* ib = T1 + b + (int64_t)Dr * ap;
+  const V4* ib = T1 + b + (int64_t)Dr * ap;
   float4 v[8];
 #pragma unroll
   for (int wi = 0; wi < 8; wi++)
-    v[wi] = wi < nw_in ? ib[in_w * wi] : make_float4(0.f, 0.f, 0.f, 0.f);
+    v[wi] = wi < nw_in ? load4(ib + in_w * wi) : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
   for (int wo = 0; wo < 8; wo++) {
     if (wo >= nw_out) break;
@@ -279,7 +286,6 @@ int op_tc_prepare(fmpt_op* op) {
     FMPT_TRY(st->T3[p].alloc(h, (size_t)st->K2 * P * Dl * es));
     FMPT_CUDA(h, cudaMemsetAsync(st->T3[p].p, 0, st->T3[p].bytes, h->stream));  // K padding
   }
-  FMPT_TRY(st->T1.alloc(h, (size_t)P * Dr * wl * Dl * sizeof(float)));
   {
     const MidSchedule& ms = op->sched;
     if (P == 4 && ms.nw_in <= 8 && ms.nw_out <= 8) {
@@ -299,6 +305,10 @@ int op_tc_prepare(fmpt_op* op) {
       st->fast_mid = true;
     }
   }
+  // T1 is BF16 when the BF16 fast MPO step reads it (its values are rounded to BF16 for
+  // GEMM 2 anyway), FP32 otherwise; the GEMM-1 output type in op_tc_apply matches this.
+  const bool t1_bf16 = st->mode == M_BF16 && st->fast_mid;
+  FMPT_TRY(st->T1.alloc(h, (size_t)P * Dr * wl * Dl * (t1_bf16 ? 2 : sizeof(float))));
   FMPT_CUDA(h, cudaMallocAsync((void**)&st->err, sizeof(int), h->stream));
   FMPT_CUDA(h, cudaMemsetAsync(st->err, 0, sizeof(int), h->stream));
   void* lo_L = split > 1 ? st->Lg[1].p : nullptr;
@@ -334,8 +344,9 @@ int op_tc_apply(fmpt_op* op, const double* x, double* y) {
   // GEMM 1: T1[(s b), (a' w)] = sum_a xg[a, (s b)] Lg[a, (a' w)]
   TcOperand A1{st->xg[0].p, xlo, st->Kp, 0};
   TcOperand B1{st->Lg[0].p, split > 1 ? st->Lg[1].p : nullptr, st->Kp, 0};
-  FMPT_TRY(tc_gemm(h, st->mode, P * Dr, wl * Dl, st->Kp, 1, A1, B1, st->T1.p, 0, (int64_t)P * Dr,
-                   0, st->err));
+  const bool t1_bf16 = st->mode == M_BF16 && st->fast_mid;
+  FMPT_TRY(tc_gemm(h, st->mode, P * Dr, wl * Dl, st->Kp, 1, A1, B1, st->T1.p, t1_bf16 ? 2 : 0,
+                   (int64_t)P * Dr, 0, st->err));
   // MPO step
   {
     const int64_t nt = (int64_t)Dl * Dr;
@@ -350,7 +361,7 @@ int op_tc_apply(fmpt_op* op, const double* x, double* y) {
       else if (st->mode == M_TF32X3)
         mid_tc_p4<M_TF32X3><<<blocks, 256, 0, h->stream>>>(t1, Dl, Dr, st->Drp, st->K2, s.nw_in, s.nw_out, st->mask, cf, st->T3[0].p, tlo);
       else
-        mid_tc_p4<M_BF16><<<blocks, 256, 0, h->stream>>>(t1, Dl, Dr, st->Drp, st->K2, s.nw_in, s.nw_out, st->mask, cf, st->T3[0].p, tlo);
+        mid_tc_p4<M_BF16><<<blocks, 256, 0, h->stream>>>((const uint2*)st->T1.p, Dl, Dr, st->Drp, st->K2, s.nw_in, s.nw_out, st->mask, cf, st->T3[0].p, tlo);
     } else
 #define MIDTC(MODE_, MP_)                                                                    \
   mid_tc<MODE_, MP_><<<blocks, 256, 0, h->stream>>>((const float*)st->T1.p,                \
