@@ -268,11 +268,49 @@ def dmrg_section(h, fm, budget_s=150.0):
         bonds.append({"site": site, "D": list(env.mps[site].shape), "s_mixed": tb["mixed"],
                       "s_fp64": tb["fp64"]})
     ratio = sum(b["s_fp64"] for b in bonds) / sum(b["s_mixed"] for b in bonds)
+    del env
     out["j1j2_L100_J2_0.3_D1024"] = {
         "ramp_sweeps_s_mixed": tramp, "sweep_s_mixed": t_mixed, "Dmax": Dmax,
         "E_mixed_fp64_eval": E, "centre_bonds": bonds, "bond_speedup_fp64_over_mixed": ratio,
         "sweep_s_fp64_extrapolated": t_mixed * ratio,
         "note": "FP64 sweep time = timed mixed sweep x (FP64 / mixed time of the centre bond)"}
+    if _t.perf_counter() - t_start > budget_s:
+        return out
+    # XX chain (Delta = 0), L=200, D=256, against the free-fermion closed form
+    hxx = fm.heisenberg_xxz_mpo(1.0, 0.0, 0.0)
+    envx, tx = run(200, hxx, [(64, 2), (256, 3)], "tf32x3", "dm", True, 1e-9, 16, 7)
+    Exx = float(fm.expectation(envx.mps, fm.FiniteMPO(hxx, 200)))
+    with open(os.path.join(ROOT, "tests", "golden", "exact_energies.json")) as f:
+        e_ff = json.load(f)["xx_L200_free_fermion"]
+    out["xx_L200_D256"] = {"sweep_s_mixed": tx, "E_mixed_fp64_eval": Exx, "E_free_fermion": e_ff,
+                           "dE_rel_vs_free_fermion": abs(Exx - e_ff) / abs(e_ff),
+                           "Dmax": fm.bond_dimension(envx.mps)}
+    del envx
+    if _t.perf_counter() - t_start > budget_s:
+        return out
+    # one-site TDVP trajectory: TFI L=40, h_i = 1 + 0.1 N(0,1), complex128, D=64,
+    # dt=0.05 (stepsize -0.05i), Krylov dimension 20; <Z_20> after the timed steps
+    L = 40
+    rng = np.random.default_rng(40)
+    hs = 1.0 + 0.1 * rng.standard_normal(L)
+    htfi = fm.tfi_mpo(hs)
+    psi = fm.randommps(L, 2, 64, rng, dtype=np.complex128, handle=h)
+    fm.canonicalize_(psi, normalize=True)
+    envt = fm.environments(fm.FiniteMPO(htfi, L), psi)
+    alg = fm.TDVP1(stepsize=-0.05j, D=64, exptol=1e-8, krylovdim=20)
+    fm.sweep_(envt, alg)                                 # first step (bond growth, warm-up)
+    nsteps = 10
+    h.synchronize()
+    t0 = _t.perf_counter()
+    for _ in range(nsteps):
+        fm.sweep_(envt, alg)
+    h.synchronize()
+    tstep = (_t.perf_counter() - t0) / nsteps
+    Z = np.diag([-1.0, 1.0])
+    out["tdvp1_tfi_L40_D64"] = {"s_per_step_fp64_complex": tstep, "steps_timed": nsteps,
+                                "Z20_after_%d_steps" % (nsteps + 1):
+                                    float(np.real(fm.expectation_local(envt.mps, 20, Z))),
+                                "note": "100 steps extrapolate to %.1f s" % (100 * tstep)}
     return out
 
 

@@ -94,6 +94,7 @@ struct GemmArgs {
   double* C; int64_t ldc; int64_t planeC;
   int batch;                // batched over blockIdx.z with the strides below
   int64_t strideA, strideB, strideC;
+  int nosplit;              // 1: never split K (no workspace allocation)
 };
 int gemm_f64(fmpt_handle* h, const GemmArgs& g);
 

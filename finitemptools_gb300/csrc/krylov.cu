@@ -63,7 +63,7 @@ __global__ void normalize_from_parts(int64_t n, const double* __restrict__ v, do
                                      const double* __restrict__ part, int G, double* nrm) {
   double s = sqrt(sum_parts(part, G));
   if (blockIdx.x == 0 && threadIdx.x == 0) *nrm = s;
-  double inv = 1.0 / s;
+  double inv = s > 0.0 ? 1.0 / s : 0.0;
   for (int64_t i = (int64_t)blockIdx.x * KT + threadIdx.x; i < n; i += (int64_t)gridDim.x * KT)
     x[i] = v[i] * inv;
 }
@@ -200,15 +200,36 @@ __global__ void combine_basis(int cplx, int64_t n, int j, const double* __restri
   }
 }
 
-// scale vector by 1/sqrt(sum parts) and store that norm
-__global__ void normalize_inplace(int64_t n_real, double* __restrict__ z,
-                                  const double* __restrict__ part, int G, double* nrm_out) {
-  double s = sqrt(sum_parts(part, G));
-  if (blockIdx.x == 0 && threadIdx.x == 0) *nrm_out = s;
-  if (s == 0.0) return;
+// Arnoldi step closure on the device: s = ||z|| after orthogonalisation; the
+// norm before it is sqrt(s^2 + sum_i |H[i][j]|^2).  If s is below 1e-12 of
+// that (the Krylov space is exhausted: happy breakdown) the next basis vector
+// and H[j+1][j] are zero, otherwise V_{j+1} = z / s and H[j+1][j] = s.
+__global__ void arnoldi_normalize(int64_t n_real, const double* __restrict__ z,
+                                  const double* __restrict__ part, int G,
+                                  double* __restrict__ Hcol, int j, double* __restrict__ vnext) {
+  const double s = sqrt(sum_parts(part, G));
+  double ref = s * s;
+  for (int i = 0; i <= j; i++) ref += Hcol[2 * i] * Hcol[2 * i] + Hcol[2 * i + 1] * Hcol[2 * i + 1];
+  const bool breakdown = !(s > 1e-12 * sqrt(ref));
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    Hcol[2 * (j + 1)] = breakdown ? 0.0 : s;
+    Hcol[2 * (j + 1) + 1] = 0.0;
+  }
+  const double inv = breakdown ? 0.0 : 1.0 / s;
   for (int64_t e = (int64_t)blockIdx.x * KT + threadIdx.x; e < n_real;
        e += (int64_t)gridDim.x * KT)
-    z[e] = z[e] / s;
+    vnext[e] = z[e] * inv;
+}
+
+// acc *= v (device scalars)
+__global__ void mul_scalar(double* acc, const double* v) { *acc *= *v; }
+
+// x *= *a (device scalar)
+__global__ void scale_by(int64_t n, double* __restrict__ x, const double* a) {
+  const double f = *a;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x)
+    x[e] *= f;
 }
 
 // Lowest eigenpair of the symmetric tridiagonal (alpha[0..k-1], beta[0..k-2])
@@ -491,18 +512,21 @@ int fmpt_exponentiate(fmpt_op* op, double t_re, double t_im, const double* x, do
   const int64_t n = op->n;                     // elements (complex for C128)
   const int64_t nr = n * (cp ? 2 : 1);         // real view
   const int G = grid_for(h, nr);
-  const int M = krylovdim;
-  DevBuf Vb, zb, part, partM, coef, hcol, Hd, Ed, nrm;
+  // the Krylov space cannot be larger than the vector space
+  const int M = (int)std::min<int64_t>(krylovdim, n);
+  const int ldh = M + 1;
+  DevBuf Vb, zb, part, partM, coef, Hdev, Hd, Ed, nrm, acc;
   FMPT_TRY(Vb.alloc(h, (size_t)(M + 1) * nr * sizeof(double)));
   FMPT_TRY(zb.alloc(h, (size_t)nr * sizeof(double)));
   FMPT_TRY(part.alloc(h, (size_t)G * sizeof(double)));
   FMPT_TRY(partM.alloc(h, (size_t)G * (M + 1) * 2 * sizeof(double)));
   FMPT_TRY(coef.alloc(h, (size_t)(M + 1) * 2 * sizeof(double)));
-  FMPT_TRY(hcol.alloc(h, (size_t)(M + 1) * 2 * sizeof(double)));
+  FMPT_TRY(Hdev.alloc(h, (size_t)ldh * M * 2 * sizeof(double)));
   FMPT_TRY(Hd.alloc(h, (size_t)32 * 32 * 2 * sizeof(double)));
   FMPT_TRY(Ed.alloc(h, (size_t)32 * 32 * 2 * sizeof(double)));
   FMPT_TRY(nrm.alloc(h, 2 * sizeof(double)));
-  FMPT_TRY(ensure_pinned(h, (size_t)(M + 2) * 2 + 4));
+  FMPT_TRY(acc.alloc(h, 2 * sizeof(double)));
+  FMPT_TRY(ensure_pinned(h, (size_t)ldh * M * 2 + 8));
   double* V = Vb.d();
   auto V_ = [&](int i) { return V + (int64_t)i * nr; };
   const double tabs = std::hypot(t_re, t_im);
@@ -513,70 +537,52 @@ int fmpt_exponentiate(fmpt_op* op, double t_re, double t_im, const double* x, do
     return FMPT_OK;
   }
   const double sg_r = t_re / tabs, sg_i = t_im / tabs;
-  // w = x / ||x||
+  // w = x / ||x||, acc = ||x|| (the running norm stays on the device)
   rdot_partial<<<G, KT, 0, h->stream>>>(nr, x, x, part.d());
   FMPT_LAUNCHED(h);
-  normalize_from_parts<<<G, KT, 0, h->stream>>>(nr, x, V_(0), part.d(), G, nrm.d());
+  normalize_from_parts<<<G, KT, 0, h->stream>>>(nr, x, V_(0), part.d(), G, acc.d());
   FMPT_LAUNCHED(h);
-  FMPT_CUDA(h, cudaMemcpyAsync(h->pinned, nrm.d(), sizeof(double), cudaMemcpyDeviceToHost,
-                               h->stream));
-  FMPT_CUDA(h, cudaStreamSynchronize(h->stream));
-  double scale = h->pinned[0];
-  if (scale == 0.0) {
-    FMPT_CUDA(h, cudaMemsetAsync(xout, 0, nr * sizeof(double), h->stream));
-    if (info) *info = 0;
-    return FMPT_OK;
-  }
   double tau_done = 0.0, dtau = tabs;
   int steps = 0;
-  std::vector<double> Hh((size_t)(M + 1) * M * 2);     // Hessenberg, column-major (re, im)
+  std::vector<double> Hh((size_t)ldh * M * 2);
+  std::vector<double> Hs;
   while (tau_done < tabs * (1.0 - 1e-15)) {
     if (++steps > 1000) return set_error(h, FMPT_ERR_NOCONV, "exponentiate: too many steps");
-    std::fill(Hh.begin(), Hh.end(), 0.0);
-    int m = M;
-    bool happy = false;
-    double hmax = 0.0;
+    // ---- Arnoldi (two-pass classical Gram-Schmidt) entirely on the device
+    FMPT_CUDA(h, cudaMemsetAsync(Hdev.p, 0, Hdev.bytes, h->stream));
     for (int j = 0; j < M; j++) {
+      double* Hcol = Hdev.d() + (size_t)2 * ldh * j;
       FMPT_TRY(fmpt_op_apply(op, V_(j), zb.d()));
-      // two passes of classical Gram-Schmidt; hcol accumulates the coefficients
-      FMPT_CUDA(h, cudaMemsetAsync(hcol.d(), 0, (size_t)(M + 1) * 2 * sizeof(double), h->stream));
       for (int pass = 0; pass < 2; pass++) {
         multidot_partial<<<G, KT, 0, h->stream>>>(cp, n, j + 1, V, nr, zb.d(), partM.d());
         FMPT_LAUNCHED(h);
-        multidot_finalize<<<1, KT, 0, h->stream>>>(j + 1, G, partM.d(), coef.d(), hcol.d());
+        multidot_finalize<<<1, KT, 0, h->stream>>>(j + 1, G, partM.d(), coef.d(), Hcol);
         FMPT_LAUNCHED(h);
         multi_axpy_sub<<<G, KT, 0, h->stream>>>(cp, n, j + 1, V, nr, coef.d(), zb.d(), part.d());
         FMPT_LAUNCHED(h);
       }
-      normalize_inplace<<<G, KT, 0, h->stream>>>(nr, zb.d(), part.d(), G, nrm.d());
+      arnoldi_normalize<<<G, KT, 0, h->stream>>>(nr, zb.d(), part.d(), G, Hcol, j, V_(j + 1));
       FMPT_LAUNCHED(h);
-      FMPT_CUDA(h, cudaMemcpyAsync(h->pinned, hcol.d(), (size_t)(j + 1) * 2 * sizeof(double),
-                                   cudaMemcpyDeviceToHost, h->stream));
-      FMPT_CUDA(h, cudaMemcpyAsync(h->pinned + 2 * (M + 1), nrm.d(), sizeof(double),
-                                   cudaMemcpyDeviceToHost, h->stream));
-      FMPT_CUDA(h, cudaStreamSynchronize(h->stream));
-      for (int i = 0; i <= j; i++) {
-        Hh[2 * (i + (size_t)(M + 1) * j)] = h->pinned[2 * i];
-        Hh[2 * (i + (size_t)(M + 1) * j) + 1] = h->pinned[2 * i + 1];
-        hmax = std::max(hmax, std::hypot(h->pinned[2 * i], h->pinned[2 * i + 1]));
-      }
-      const double hn = h->pinned[2 * (M + 1)];
-      if (!std::isfinite(hn)) return set_error(h, FMPT_ERR_NONFINITE, "exponentiate: NaN");
-      Hh[2 * (j + 1 + (size_t)(M + 1) * j)] = hn;
-      if (hn < 1e-14 * std::max(1.0, hmax)) { m = j + 1; happy = true; break; }
-      if (j + 1 < M + 1)
-        FMPT_CUDA(h, cudaMemcpyAsync(V_(j + 1), zb.d(), nr * sizeof(double),
-                                     cudaMemcpyDeviceToDevice, h->stream));
     }
+    FMPT_CUDA(h, cudaMemcpyAsync(h->pinned, Hdev.p, Hdev.bytes, cudaMemcpyDeviceToHost,
+                                 h->stream));
+    FMPT_CUDA(h, cudaStreamSynchronize(h->stream));
+    std::copy(h->pinned, h->pinned + Hh.size(), Hh.begin());
+    for (double v : Hh)
+      if (!std::isfinite(v)) return set_error(h, FMPT_ERR_NONFINITE, "exponentiate: NaN");
+    // happy breakdown: the first zero subdiagonal closes the Krylov space
+    int m = M;
+    bool happy = M == n;
+    for (int j = 0; j < M; j++)
+      if (Hh[2 * (j + 1 + (size_t)ldh * j)] == 0.0) { m = j + 1; happy = true; break; }
     dtau = happy ? (tabs - tau_done) : std::min(dtau, tabs - tau_done);
-    std::vector<double> Hs((size_t)m * m * 2);
+    Hs.assign((size_t)m * m * 2, 0.0);
     double err = 0.0;
     for (int tries = 0; tries < 200; tries++) {
-      // Hs = (sign(t) * dtau) * H[0:m, 0:m]
       const double fr = sg_r * dtau, fi = sg_i * dtau;
       for (int c = 0; c < m; c++)
         for (int r = 0; r < m; r++) {
-          double hr = Hh[2 * (r + (size_t)(M + 1) * c)], hi = Hh[2 * (r + (size_t)(M + 1) * c) + 1];
+          const double hr = Hh[2 * (r + (size_t)ldh * c)], hi = Hh[2 * (r + (size_t)ldh * c) + 1];
           Hs[2 * (r + (size_t)m * c)] = fr * hr - fi * hi;
           Hs[2 * (r + (size_t)m * c) + 1] = fr * hi + fi * hr;
         }
@@ -584,35 +590,34 @@ int fmpt_exponentiate(fmpt_op* op, double t_re, double t_im, const double* x, do
                                    cudaMemcpyHostToDevice, h->stream));
       small_expm<<<1, dim3(32, 32), 0, h->stream>>>(m, Hd.d(), Ed.d());
       FMPT_LAUNCHED(h);
-      // first column of exp -> host (error estimate uses its last entry)
-      FMPT_CUDA(h, cudaMemcpyAsync(h->pinned, Ed.d(), (size_t)m * 2 * sizeof(double),
+      if (happy) break;
+      // error estimate |h_{m+1,m} dtau [exp(dtau H)]_{m,1}| needs the last entry only
+      FMPT_CUDA(h, cudaMemcpyAsync(h->pinned, Ed.d() + 2 * (m - 1), 2 * sizeof(double),
                                    cudaMemcpyDeviceToHost, h->stream));
       FMPT_CUDA(h, cudaStreamSynchronize(h->stream));
-      if (happy) { err = 0.0; break; }
-      const double hlast = Hh[2 * (m + (size_t)(M + 1) * (m - 1))];
-      err = std::abs(hlast * dtau) * std::hypot(h->pinned[2 * (m - 1)], h->pinned[2 * (m - 1) + 1]);
+      const double hlast = Hh[2 * (m + (size_t)ldh * (m - 1))];
+      err = std::abs(hlast * dtau) * std::hypot(h->pinned[0], h->pinned[1]);
       if (err <= 0.9 * tol * dtau) break;
       dtau *= 0.5;
     }
-    // w = sum_i E[i, 0] V_i (first column stays on the device in Ed)
+    // w = sum_i E[i, 0] V_i, renormalised into V_0; acc *= ||w||
     combine_basis<<<G, KT, 0, h->stream>>>(cp, n, m, V, nr, Ed.d(), 2, 1.0, 0, zb.d());
     FMPT_LAUNCHED(h);
     rdot_partial<<<G, KT, 0, h->stream>>>(nr, zb.d(), zb.d(), part.d());
     FMPT_LAUNCHED(h);
     normalize_from_parts<<<G, KT, 0, h->stream>>>(nr, zb.d(), V_(0), part.d(), G, nrm.d());
     FMPT_LAUNCHED(h);
-    FMPT_CUDA(h, cudaMemcpyAsync(h->pinned, nrm.d(), sizeof(double), cudaMemcpyDeviceToHost,
-                                 h->stream));
-    FMPT_CUDA(h, cudaStreamSynchronize(h->stream));
-    scale *= h->pinned[0];
+    mul_scalar<<<1, 1, 0, h->stream>>>(acc.d(), nrm.d());
+    FMPT_LAUNCHED(h);
     tau_done += dtau;
     if (!happy && tau_done < tabs) dtau = std::min(2.0 * dtau, tabs - tau_done);
   }
-  // xout = scale * V_0
+  // xout = acc * V_0
   FMPT_CUDA(h, cudaMemcpyAsync(xout, V_(0), nr * sizeof(double), cudaMemcpyDeviceToDevice,
                                h->stream));
-  double sc[2] = {scale, 0.0};
-  FMPT_TRY(fmpt_scal(h, FMPT_F64, nr, sc, xout));
+  scale_by<<<G, KT, 0, h->stream>>>(nr, xout, acc.d());
+  FMPT_LAUNCHED(h);
+  if (op->precision != FMPT_PREC_FP64) FMPT_TRY(op_tc_check(op));
   if (info) *info = steps;
   return FMPT_OK;
 }

@@ -154,6 +154,7 @@ extern "C" int fmpt_ac2_prime_noalloc(fmpt_handle* h, int dtype, const double* x
   const int64_t nx = (int64_t)Dl * P * Dr;
   GemmArgs g{};
   g.cplx = cp; g.alpha[0] = 1.0; g.batch = 1;
+  g.nosplit = 1;            // a split-K workspace would be an allocation
   // 1. T1[(a' w), (s b)] = L[(a' w), a] x[a, (s b)]
   g.ta = FMPT_N; g.tb = FMPT_N; g.m = Dl * wl; g.n = P * Dr; g.k = Dl;
   g.A = hleft; g.lda = (int64_t)Dl * wl; g.planeA = (int64_t)Dl * wl * Dl;
