@@ -20,5 +20,8 @@ from .envs import (ExpectationCache, environments, init_hstorage_, updateleft_, 
 from .mps import (FiniteMPS, bond_dimension, canonicalize_, increase_bond_,  # noqa: F401
                   prodmps, randommps)
 from .transfer import updateleft, updateright  # noqa: F401
+from .u1 import (U1ExpectationCache, U1FiniteMPS, U1HeffOp, U1Space,  # noqa: F401
+                 mpo_channel_charges, u1_environments, u1_expectation, u1_randommps, u1_split,
+                 u1_twosite, u1_updateleft, u1_updateright)
 from .utilities import (FiniteMPO, MPOHamiltonian, SchurMPOTensor,  # noqa: F401
                         heisenberg_xxz_mpo, j1j2_heisenberg_mpo, spin_half_matrices, tfi_mpo)

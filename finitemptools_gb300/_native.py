@@ -23,6 +23,15 @@ F64, C128 = 0, 1
 PREC = {"fp64": 0, "tf32x3": 1, "tf32": 2, "bf16": 3}
 TRANS = {"N": 0, "T": 1, "C": 2, "R": 3}
 
+
+class U1SpaceC(ctypes.Structure):
+    """struct fmpt_u1_space: a charge-sorted sector table (nsect, charge*, dim*)."""
+    _fields_ = [("nsect", c_int), ("charge", P(c_int)), ("dim", P(c_int))]
+
+
+SP = P(U1SpaceC)
+ip = P(c_int)
+
 STATUS = {0: "ok", -1: "invalid argument", -2: "dimension mismatch", -3: "CUDA error",
           -4: "cuSOLVER error", -5: "device wait timed out", -6: "non-finite value",
           -7: "out of device memory", -8: "unsupported", -9: "not converged"}
@@ -82,6 +91,20 @@ SIGNATURES = {
                               dptr, dptr, dptr, P(c_int), P(c_double)]),
     "fmpt_qr": (c_int, [c_void_p, c_int, dptr, c_int, c_int, dptr, dptr]),
     "fmpt_lq": (c_int, [c_void_p, c_int, dptr, c_int, c_int, dptr, dptr]),
+    "fmpt_u1_twosite_size": (c_int, [c_void_p, SP, SP, c_int, ip, c_int, ip, P(c_int64)]),
+    "fmpt_u1_pack2": (c_int, [c_void_p, c_int, dptr, dptr, SP, SP, c_int, ip, c_int, ip, c_int]),
+    "fmpt_u1_op_ac2": (c_int, [c_void_p, c_int, hptr, hptr, dptr, dptr, SP, SP, c_int, ip, c_int,
+                               ip, c_int, ip, c_int, ip, c_int, ip, P(c_void_p)]),
+    "fmpt_op_flops": (c_int, [c_void_p, P(c_double)]),
+    "fmpt_u1_twosite": (c_int, [c_void_p, c_int, dptr, dptr, dptr, SP, SP, SP, c_int, ip, c_int,
+                                ip]),
+    "fmpt_u1_updateleft": (c_int, [c_void_p, c_int, dptr, dptr, hptr, dptr, dptr, SP, SP, c_int,
+                                   ip, c_int, ip, c_int, ip]),
+    "fmpt_u1_updateright": (c_int, [c_void_p, c_int, dptr, dptr, hptr, dptr, dptr, SP, SP, c_int,
+                                    ip, c_int, ip, c_int, ip]),
+    "fmpt_u1_split": (c_int, [c_void_p, c_int, dptr, SP, SP, c_int, ip, c_int, ip, c_int,
+                              c_double, c_int, dptr, dptr, dptr, c_int, ip, ip, ip,
+                              P(c_double)]),
 }
 
 

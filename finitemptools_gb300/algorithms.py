@@ -16,6 +16,7 @@ from .derivatives import HeffOp
 from .device import DeviceTensor
 from .envs import ExpectationCache, environments, increase_bond_env_, updateleft_, updateright_
 from .transfer import updateleft, updateright
+from .u1 import U1ExpectationCache, U1FiniteMPS, u1_expectation, u1_leftsweep_, u1_rightsweep_
 from .utilities import MPOHamiltonian
 
 __all__ = ["Defaults", "DMRG1", "DMRG2", "TDVP1", "leftsweep_", "rightsweep_", "sweep_",
@@ -114,6 +115,10 @@ def _dmrg2_bond_left(m, site, alg):
 
 def leftsweep_(m, alg):
     """leftsweep!(m, alg) for DMRG2 (dmrg.jl:89-115) and DMRG1 (:27-52)."""
+    if isinstance(m, U1ExpectationCache):
+        if not isinstance(alg, DMRG2):
+            raise NotImplementedError("U(1) tensors: DMRG2 sweeps only")
+        return u1_leftsweep_(m, alg)
     if isinstance(alg, DMRG1):
         return _dmrg1_leftsweep(m, alg)
     m.precision = alg.env_precision
@@ -127,6 +132,10 @@ def leftsweep_(m, alg):
 
 def rightsweep_(m, alg):
     """rightsweep!(m, alg) for DMRG2 (dmrg.jl:117-144) and DMRG1 (:54-76)."""
+    if isinstance(m, U1ExpectationCache):
+        if not isinstance(alg, DMRG2):
+            raise NotImplementedError("U(1) tensors: DMRG2 sweeps only")
+        return u1_rightsweep_(m, alg)
     if isinstance(alg, DMRG1):
         return _dmrg1_rightsweep(m, alg)
     m.precision = alg.env_precision
@@ -320,6 +329,8 @@ def compute_(env, alg):
 def ground_state_(state, h, alg=None):
     """ground_state!(state, h, alg) (dmrg.jl:240)."""
     alg = alg if alg is not None else DMRG2()
+    if isinstance(state, U1FiniteMPS):
+        return compute_(U1ExpectationCache(h, state), alg)
     return compute_(environments(h, state, alg.precision), alg)
 
 
@@ -327,6 +338,10 @@ def ground_state_(state, h, alg=None):
 def expectation(psiA, h, psiB=None, precision="fp64"):
     """expectation(psiA, h::FiniteMPO | MPOHamiltonian, psiB): a chain of
     updateright from r_RR, closed with l_LL."""
+    if isinstance(psiA, U1FiniteMPS):
+        if psiB is not None and psiB is not psiA:
+            raise NotImplementedError("U(1) expectation: <psi|H|psi> only")
+        return u1_expectation(psiA, h)
     psiB = psiA if psiB is None else psiB
     L = len(psiA)
     if isinstance(h, MPOHamiltonian):

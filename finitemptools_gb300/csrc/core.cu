@@ -284,6 +284,7 @@ int fmpt_destroy(fmpt_handle* h) {
     for (auto& pr : v) { h->ev_pool.push_back(pr.first); h->ev_pool.push_back(pr.second); }
   for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
   if (h->solver) cusolverDnDestroy(h->solver);
+  if (h->gstatus) cudaFree(h->gstatus);
   if (h->pinned) cudaFreeHost(h->pinned);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
   delete h;
@@ -295,7 +296,7 @@ const char* fmpt_last_error(fmpt_handle* h) { return h ? h->err.c_str() : "null 
 int fmpt_synchronize(fmpt_handle* h) {
   if (!h) return FMPT_ERR_ARG;
   FMPT_CUDA(h, cudaStreamSynchronize(h->stream));
-  return FMPT_OK;
+  return fmpt::gp_check_status(h);   // a timed-out grouped launch reports here
 }
 
 int fmpt_set_stream(fmpt_handle* h, void* s) {

@@ -1,0 +1,411 @@
+// Grouped persistent FP64 engine for block-sparse (U(1) charge-sector)
+// contractions.
+//
+// A GroupedProgram is a short sequence of phases; each phase is a list of
+// uneven block problems:
+//   GEMM phase:  C_p = sum_{j in segs(p)} coef_j * op(A_j) op(B_j)     (overwrite)
+//   SUM  phase:  C_p = sum_{j in segs(p)} coef_j * A_j                 (overwrite)
+// where every operand is a strided sub-matrix (offset + leading dimension) of
+// one of a few operand slots (device base pointers given at run time).  The
+// whole program runs as ONE cooperative launch: CTAs pull 32x32 output tiles
+// of the current phase from a device work counter (atomicAdd, largest blocks
+// first) and meet at a grid barrier between phases.  The barrier spin is
+// bounded (2 s on %globaltimer); on timeout a CTA sets the launch's abort
+// flag and the handle's status word, and every CTA returns.
+//
+// Each output tile sums its segments in the order they were added, so the
+// result does not depend on scheduling.  FP64 is FMA-pipe bound on GB300
+// (about 2 DFMA per clock per SM), so the kernel's job is to keep every SM's
+// FP64 pipe fed across thousands of 1..400-wide blocks.
+#include <algorithm>
+#include <mutex>
+#include <numeric>
+#include <vector>
+
+#include "internal.h"
+
+namespace fmpt {
+namespace {
+
+constexpr int GT = 32, GK = 8, GNT = 256;
+constexpr uint64_t kBarrierTimeoutNs = 2000000000ull;
+
+struct GKArgs {
+  GPhaseDesc ph[GP_MAX_PHASES];
+  int nphase;
+  double* slot[GP_SLOTS];
+  const GProblem* probs;
+  const GSegment* segs;
+  const int* tile_prob;
+  const int* tile_mn;
+  int* ctl;        // [0, GP_MAX_PHASES) tile counters, then barrier count, then abort flag
+  int* status;     // handle status word (1 = a bounded wait gave up)
+};
+
+__device__ __forceinline__ int64_t op_index(int t, int r, int c, int64_t ld) {
+  return (t == FMPT_N || t == FMPT_R) ? (int64_t)r + (int64_t)c * ld
+                                      : (int64_t)c + (int64_t)r * ld;
+}
+
+__device__ __forceinline__ int ld_acquire(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Grid barrier for a cooperative launch; false when the launch aborts.
+__device__ bool grid_barrier(const GKArgs& a, int target, int* s_flag) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int* bar = a.ctl + GP_MAX_PHASES;
+    int* abort_flag = bar + 1;
+    __threadfence();
+    atomicAdd(bar, 1);
+    int ok = 1;
+    const uint64_t t0 = global_ns();
+    while (ld_acquire(bar) < target) {
+      if (ld_acquire(abort_flag)) { ok = 0; break; }
+      if (global_ns() - t0 > kBarrierTimeoutNs) {
+        atomicExch(abort_flag, 1);
+        atomicExch(a.status, 1);
+        ok = 0;
+        break;
+      }
+      __nanosleep(128);
+    }
+    __threadfence();
+    *s_flag = ok;
+  }
+  __syncthreads();
+  return *s_flag != 0;
+}
+
+__device__ __forceinline__ void gemm_tile(const GKArgs& a, const GPhaseDesc& ph, int t,
+                                          double (*As)[GT + 1], double (*Bs)[GT + 1]) {
+  const GProblem P = a.probs[a.tile_prob[t]];
+  const int mn = a.tile_mn[t];
+  const int m0 = (mn & 0xffff) * GT, n0 = ((unsigned)mn >> 16) * GT;
+  const int tid = threadIdx.x;
+  const int tx = tid % 16, ty = tid / 16;
+  const bool a_mfast = (ph.ta == FMPT_N || ph.ta == FMPT_R);
+  const bool b_kfast = (ph.tb == FMPT_N || ph.tb == FMPT_R);
+  const double* Ab = a.slot[ph.a_slot];
+  const double* Bb = a.slot[ph.b_slot];
+  double acc00 = 0.0, acc01 = 0.0, acc10 = 0.0, acc11 = 0.0;
+  for (int sg = P.seg0; sg < P.seg1; sg++) {
+    const GSegment S = a.segs[sg];
+    const double* A = Ab + S.a_off;
+    const double* B = Bb + S.b_off;
+    for (int k0 = 0; k0 < S.k; k0 += GK) {
+      {
+        int mm, kk;
+        if (a_mfast) { mm = tid % GT; kk = tid / GT; } else { kk = tid % GK; mm = tid / GK; }
+        const int gm = m0 + mm, gk = k0 + kk;
+        double v = 0.0;
+        if (gm < P.m && gk < S.k) v = S.coef * __ldg(A + op_index(ph.ta, gm, gk, S.lda));
+        As[kk][mm] = v;
+      }
+      {
+        int nn, kk;
+        if (b_kfast) { kk = tid % GK; nn = tid / GK; } else { nn = tid % GT; kk = tid / GT; }
+        const int gn = n0 + nn, gk = k0 + kk;
+        double v = 0.0;
+        if (gn < P.n && gk < S.k) v = __ldg(B + op_index(ph.tb, gk, gn, S.ldb));
+        Bs[kk][nn] = v;
+      }
+      __syncthreads();
+#pragma unroll
+      for (int kk = 0; kk < GK; kk++) {
+        const double a0 = As[kk][tx], a1 = As[kk][tx + 16];
+        const double b0 = Bs[kk][ty], b1 = Bs[kk][ty + 16];
+        acc00 = fma(a0, b0, acc00);
+        acc01 = fma(a0, b1, acc01);
+        acc10 = fma(a1, b0, acc10);
+        acc11 = fma(a1, b1, acc11);
+      }
+      __syncthreads();
+    }
+  }
+  double* C = a.slot[ph.c_slot] + P.c_off;
+  const int r0 = m0 + tx, r1 = m0 + tx + 16, c0 = n0 + ty, c1 = n0 + ty + 16;
+  if (r0 < P.m && c0 < P.n) C[r0 + c0 * P.ldc] = acc00;
+  if (r0 < P.m && c1 < P.n) C[r0 + c1 * P.ldc] = acc01;
+  if (r1 < P.m && c0 < P.n) C[r1 + c0 * P.ldc] = acc10;
+  if (r1 < P.m && c1 < P.n) C[r1 + c1 * P.ldc] = acc11;
+}
+
+__device__ __forceinline__ void sum_tile(const GKArgs& a, const GPhaseDesc& ph, int t) {
+  const GProblem P = a.probs[a.tile_prob[t]];
+  const int mn = a.tile_mn[t];
+  const int m0 = (mn & 0xffff) * GT, n0 = ((unsigned)mn >> 16) * GT;
+  const int r = m0 + (threadIdx.x % GT);
+  if (r >= P.m) return;
+  const double* Ab = a.slot[ph.a_slot];
+  double* C = a.slot[ph.c_slot] + P.c_off;
+#pragma unroll
+  for (int j = 0; j < GT / (GNT / GT); j++) {
+    const int c = n0 + threadIdx.x / GT + j * (GNT / GT);
+    if (c >= P.n) break;
+    double s = 0.0;
+    for (int sg = P.seg0; sg < P.seg1; sg++) {
+      const GSegment S = a.segs[sg];
+      s = fma(S.coef, __ldg(Ab + S.a_off + r + (int64_t)c * S.lda), s);
+    }
+    C[r + (int64_t)c * P.ldc] = s;
+  }
+}
+
+__global__ void __launch_bounds__(GNT) grouped_kernel(const GKArgs a) {
+  __shared__ double As[GK][GT + 1];
+  __shared__ double Bs[GK][GT + 1];
+  __shared__ int s_tile, s_flag;
+  for (int p = 0; p < a.nphase; p++) {
+    if (p > 0 && !grid_barrier(a, p * (int)gridDim.x, &s_flag)) return;
+    const GPhaseDesc ph = a.ph[p];
+    const int ntiles = ph.tile1 - ph.tile0;
+    while (true) {
+      __syncthreads();
+      if (threadIdx.x == 0) s_tile = atomicAdd(a.ctl + p, 1);
+      __syncthreads();
+      const int t = s_tile;
+      if (t >= ntiles) break;
+      if (ph.type == GP_GEMM)
+        gemm_tile(a, ph, ph.tile0 + t, As, Bs);
+      else
+        sum_tile(a, ph, ph.tile0 + t);
+    }
+  }
+}
+
+int g_occupancy = 0;
+std::mutex g_occ_mu;
+
+int kernel_occupancy(fmpt_handle* h) {
+  std::lock_guard<std::mutex> lock(g_occ_mu);
+  if (g_occupancy == 0) {
+    int occ = 0;
+    FMPT_CUDA(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, grouped_kernel, GNT, 0));
+    g_occupancy = std::max(1, std::min(occ, 8));
+  }
+  return g_occupancy;
+}
+
+}  // namespace
+
+void gp_phase(GroupedProgram& g, int type, int ta, int tb, int a_slot, int b_slot, int c_slot) {
+  GPhaseDesc d{};
+  d.type = type; d.ta = ta; d.tb = tb;
+  d.a_slot = a_slot; d.b_slot = b_slot; d.c_slot = c_slot;
+  g.phases.push_back(d);
+  g.phase_prob0.push_back((int)g.probs.size());
+}
+
+int gp_problem(GroupedProgram& g, int64_t c_off, int64_t ldc, int m, int n) {
+  GProblem p{};
+  p.c_off = c_off; p.ldc = ldc; p.m = m; p.n = n;
+  p.seg0 = p.seg1 = (int)g.segs.size();
+  g.probs.push_back(p);
+  return (int)g.probs.size() - 1;
+}
+
+void gp_segment(GroupedProgram& g, int64_t a_off, int64_t lda, int64_t b_off, int64_t ldb, int k,
+                double coef) {
+  GSegment s{};
+  s.a_off = a_off; s.lda = lda; s.b_off = b_off; s.ldb = ldb; s.coef = coef; s.k = k;
+  g.segs.push_back(s);
+  GProblem& p = g.probs.back();
+  p.seg1 = (int)g.segs.size();
+  if (g.phases.back().type == GP_GEMM)
+    g.flops += 2.0 * p.m * (double)p.n * k;
+  else
+    g.sum_elems += (double)p.m * p.n;
+}
+
+void gp_slot(GroupedProgram& g, int slot, int64_t elems) {
+  if (slot >= 0 && slot < GP_SLOTS) g.slot_elems[slot] = elems;
+}
+
+namespace {
+
+// Largest element index of op(X) (rows x cols, leading dimension ld) at offset off.
+int64_t footprint(int t, int64_t off, int rows, int cols, int64_t ld) {
+  const bool n = (t == FMPT_N || t == FMPT_R);
+  return n ? off + (rows - 1) + (int64_t)(cols - 1) * ld : off + (cols - 1) + (int64_t)(rows - 1) * ld;
+}
+
+int check_span(fmpt_handle* h, const GroupedProgram& g, int slot, int t, int64_t off, int rows,
+               int cols, int64_t ld, const char* what, int prob) {
+  if (rows <= 0 || cols <= 0) return FMPT_OK;
+  if (slot < 0 || slot >= GP_SLOTS || g.slot_elems[slot] < 0)
+    return set_error(h, FMPT_ERR_ARG, "grouped: slot %d of %s has no declared extent", slot, what);
+  const int64_t lead = (t == FMPT_N || t == FMPT_R) ? rows : cols;
+  if (off < 0 || ld < lead || footprint(t, off, rows, cols, ld) >= g.slot_elems[slot])
+    return set_error(h, FMPT_ERR_SHAPE,
+                     "grouped: %s of block %d (offset %lld, %d x %d, ld %lld) outside its operand "
+                     "(%lld elements)", what, prob, (long long)off, rows, cols, (long long)ld,
+                     (long long)g.slot_elems[slot]);
+  return FMPT_OK;
+}
+
+int validate(fmpt_handle* h, const GroupedProgram& g) {
+  for (size_t ph = 0; ph < g.phases.size(); ph++) {
+    const GPhaseDesc& d = g.phases[ph];
+    for (int i = g.phase_prob0[ph]; i < g.phase_prob0[ph + 1]; i++) {
+      const GProblem& p = g.probs[i];
+      if (p.m < 0 || p.n < 0 || p.seg0 < 0 || p.seg1 > (int)g.segs.size() || p.seg0 > p.seg1)
+        return set_error(h, FMPT_ERR_SHAPE, "grouped: malformed block %d", i);
+      FMPT_TRY(check_span(h, g, d.c_slot, FMPT_N, p.c_off, p.m, p.n, p.ldc, "output", i));
+      for (int s = p.seg0; s < p.seg1; s++) {
+        const GSegment& sg = g.segs[s];
+        if (d.type == GP_GEMM) {
+          if (sg.k < 0) return set_error(h, FMPT_ERR_SHAPE, "grouped: negative k in block %d", i);
+          if (sg.k == 0) continue;
+          FMPT_TRY(check_span(h, g, d.a_slot, d.ta, sg.a_off, p.m, sg.k, sg.lda, "A operand", i));
+          FMPT_TRY(check_span(h, g, d.b_slot, d.tb, sg.b_off, sg.k, p.n, sg.ldb, "B operand", i));
+        } else {
+          FMPT_TRY(check_span(h, g, d.a_slot, FMPT_N, sg.a_off, p.m, p.n, sg.lda, "summand", i));
+        }
+      }
+    }
+  }
+  return FMPT_OK;
+}
+
+}  // namespace
+
+int gp_finalize(fmpt_handle* h, GroupedProgram& g) {
+  if ((int)g.phases.size() > GP_MAX_PHASES)
+    return set_error(h, FMPT_ERR_UNSUPPORTED, "grouped: more than %d phases", GP_MAX_PHASES);
+  g.phase_prob0.push_back((int)g.probs.size());
+  FMPT_TRY(validate(h, g));
+  g.tile_prob.clear();
+  g.tile_mn.clear();
+  int max_tiles = 0;
+  for (size_t ph = 0; ph < g.phases.size(); ph++) {
+    const int p0 = g.phase_prob0[ph], p1 = g.phase_prob0[ph + 1];
+    // largest work per tile first, so the long tiles do not straggle at the end
+    std::vector<int64_t> cost(p1 - p0, 0);
+    for (int i = p0; i < p1; i++) {
+      const GProblem& p = g.probs[i];
+      for (int s = p.seg0; s < p.seg1; s++)
+        cost[i - p0] += g.phases[ph].type == GP_GEMM ? g.segs[s].k : 1;
+    }
+    std::vector<int> order(p1 - p0);
+    std::iota(order.begin(), order.end(), p0);
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int x, int y) { return cost[x - p0] > cost[y - p0]; });
+    g.phases[ph].tile0 = (int)g.tile_prob.size();
+    for (int i : order) {
+      const GProblem& p = g.probs[i];
+      if (p.m <= 0 || p.n <= 0) continue;
+      const int tm = (p.m + GT - 1) / GT, tn = (p.n + GT - 1) / GT;
+      if (tm > 0xffff || tn > 0x7fff)
+        return set_error(h, FMPT_ERR_SHAPE, "grouped: block %d x %d too large", p.m, p.n);
+      for (int b = 0; b < tn; b++)
+        for (int a = 0; a < tm; a++) {
+          g.tile_prob.push_back(i);
+          g.tile_mn.push_back(a | (b << 16));
+        }
+    }
+    g.phases[ph].tile1 = (int)g.tile_prob.size();
+    max_tiles = std::max(max_tiles, g.phases[ph].tile1 - g.phases[ph].tile0);
+  }
+  // one device allocation: problems | segments | tile_prob | tile_mn | control words
+  auto up256 = [](size_t b) { return (b + 255) / 256 * 256; };
+  const size_t bp = up256(g.probs.size() * sizeof(GProblem));
+  const size_t bs = up256(g.segs.size() * sizeof(GSegment));
+  const size_t bt = up256(g.tile_prob.size() * sizeof(int));
+  const size_t ctl_bytes = 256;
+  FMPT_TRY(g.dev.alloc(h, bp + bs + 2 * bt + ctl_bytes));
+  char* base = static_cast<char*>(g.dev.p);
+  g.d_probs = reinterpret_cast<GProblem*>(base);
+  g.d_segs = reinterpret_cast<GSegment*>(base + bp);
+  g.d_tile_prob = reinterpret_cast<int*>(base + bp + bs);
+  g.d_tile_mn = reinterpret_cast<int*>(base + bp + bs + bt);
+  g.d_ctl = reinterpret_cast<int*>(base + bp + bs + 2 * bt);
+  // pageable-source copies return once the source is staged
+  if (!g.probs.empty())
+    FMPT_CUDA(h, cudaMemcpyAsync(g.d_probs, g.probs.data(), g.probs.size() * sizeof(GProblem),
+                                 cudaMemcpyHostToDevice, h->stream));
+  if (!g.segs.empty())
+    FMPT_CUDA(h, cudaMemcpyAsync(g.d_segs, g.segs.data(), g.segs.size() * sizeof(GSegment),
+                                 cudaMemcpyHostToDevice, h->stream));
+  if (!g.tile_prob.empty()) {
+    FMPT_CUDA(h, cudaMemcpyAsync(g.d_tile_prob, g.tile_prob.data(),
+                                 g.tile_prob.size() * sizeof(int), cudaMemcpyHostToDevice,
+                                 h->stream));
+    FMPT_CUDA(h, cudaMemcpyAsync(g.d_tile_mn, g.tile_mn.data(), g.tile_mn.size() * sizeof(int),
+                                 cudaMemcpyHostToDevice, h->stream));
+  }
+  const int occ = kernel_occupancy(h);
+  if (occ <= 0) return set_error(h, FMPT_ERR_CUDA, "grouped: occupancy query failed");
+  const int sms = h->sm_count > 0 ? h->sm_count : 1;
+  g.grid = std::max(1, std::min(max_tiles, occ * sms));
+  g.ready = true;
+  return FMPT_OK;
+}
+
+int gp_status_word(fmpt_handle* h, int** out) {
+  if (!h->gstatus) {
+    FMPT_CUDA(h, cudaMalloc(&h->gstatus, sizeof(int)));
+    FMPT_CUDA(h, cudaMemsetAsync(h->gstatus, 0, sizeof(int), h->stream));
+  }
+  *out = h->gstatus;
+  return FMPT_OK;
+}
+
+int gp_check_status(fmpt_handle* h) {
+  if (!h->gstatus) return FMPT_OK;
+  FMPT_TRY(ensure_pinned(h, 1));
+  int* pin = reinterpret_cast<int*>(h->pinned);
+  FMPT_CUDA(h, cudaMemcpyAsync(pin, h->gstatus, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  FMPT_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (*pin != 0) {
+    FMPT_CUDA(h, cudaMemsetAsync(h->gstatus, 0, sizeof(int), h->stream));
+    return set_error(h, FMPT_ERR_TIMEOUT,
+                     "grouped block-sparse launch: a grid barrier timed out (results invalid)");
+  }
+  return FMPT_OK;
+}
+
+int gp_run(fmpt_handle* h, const GroupedProgram& g, double* const* slots, int nslots) {
+  if (!g.ready) return set_error(h, FMPT_ERR_ARG, "grouped: program not finalised");
+  if (g.tile_prob.empty()) return FMPT_OK;
+  GKArgs a{};
+  a.nphase = (int)g.phases.size();
+  for (int p = 0; p < a.nphase; p++) a.ph[p] = g.phases[p];
+  for (int s = 0; s < GP_SLOTS; s++) a.slot[s] = s < nslots ? slots[s] : nullptr;
+  for (int p = 0; p < a.nphase; p++) {
+    const GPhaseDesc& d = g.phases[p];
+    if (d.tile1 == d.tile0) continue;
+    if (!a.slot[d.a_slot] || !a.slot[d.c_slot] || (d.type == GP_GEMM && !a.slot[d.b_slot]))
+      return set_error(h, FMPT_ERR_ARG, "grouped: operand slot of phase %d is null", p);
+  }
+  a.probs = g.d_probs; a.segs = g.d_segs;
+  a.tile_prob = g.d_tile_prob; a.tile_mn = g.d_tile_mn;
+  a.ctl = g.d_ctl;
+  FMPT_TRY(gp_status_word(h, &a.status));
+  FMPT_CUDA(h, cudaMemsetAsync(g.d_ctl, 0, (GP_MAX_PHASES + 2) * sizeof(int), h->stream));
+  ProfScope prof(h, FMPT_K_GROUPED);
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3(g.grid);
+  cfg.blockDim = dim3(GNT);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = h->stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  FMPT_CUDA(h, cudaLaunchKernelEx(&cfg, grouped_kernel, a));
+  FMPT_LAUNCHED(h);
+  return FMPT_OK;
+}
+
+}  // namespace fmpt

@@ -340,6 +340,7 @@ int fmpt_op_c(fmpt_handle* h, int dtype, int precision, const double* hleft,
 int fmpt_op_apply(fmpt_op* op, const double* x, double* y) {
   if (!op) return FMPT_ERR_ARG;
   if (!x || !y) return set_error(op->h, FMPT_ERR_ARG, "op_apply: null vector");
+  if (op->u1) return op_u1_apply(op, x, y);
   if (op->precision != FMPT_PREC_FP64) return op_tc_apply(op, x, y);
   return op_apply_fp64(op, x, y);
 }
@@ -350,6 +351,7 @@ int fmpt_op_destroy(fmpt_op* op) {
   if (!op) return FMPT_OK;
   mid_free(op->h, op->sched);
   op_tc_free(op);
+  op_u1_free(op);
   delete op;
   return FMPT_OK;
 }

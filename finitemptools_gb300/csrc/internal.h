@@ -26,6 +26,9 @@ struct fmpt_handle {
   bool prof = false;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof_ev[FMPT_K_COUNT];
   std::vector<cudaEvent_t> ev_pool;
+  // status word of the grouped block-sparse launches (1 = a grid barrier timed
+  // out); allocated on first use, read and cleared by gp_check_status
+  int* gstatus = nullptr;
 };
 
 namespace fmpt {
@@ -125,6 +128,59 @@ int schedule_ac(fmpt_handle* h, int cplx, const double* W, int d, int wl, int wr
 int schedule_env(fmpt_handle* h, int cplx, const double* W, int d, int wl, int wr, bool right,
                  MidSchedule& s);
 
+// -------- grouped persistent block-sparse engine (grouped.cu)
+constexpr int GP_MAX_PHASES = 4, GP_SLOTS = 8;
+enum { GP_GEMM = 0, GP_SUM = 1 };
+// One output block: C (m x n, column-major with ldc) at c_off in the phase's C slot.
+struct GProblem {
+  int64_t c_off, ldc;
+  int m, n, seg0, seg1;
+};
+// One term of a block: coef * op(A) op(B) (GEMM, inner extent k) or coef * A (SUM).
+struct GSegment {
+  int64_t a_off, lda, b_off, ldb;
+  double coef;
+  int k, pad;
+};
+struct GPhaseDesc {
+  int type, ta, tb, a_slot, b_slot, c_slot, tile0, tile1;
+};
+struct GroupedProgram {
+  std::vector<GPhaseDesc> phases;
+  std::vector<int> phase_prob0;
+  std::vector<GProblem> probs;
+  std::vector<GSegment> segs;
+  std::vector<int> tile_prob, tile_mn;
+  double flops = 0.0;       // 2 m n k over the GEMM segments
+  double sum_elems = 0.0;   // output elements x terms of the SUM phases
+  int64_t slot_elems[GP_SLOTS] = {-1, -1, -1, -1, -1, -1, -1, -1};  // operand extents
+  DevBuf dev;
+  GProblem* d_probs = nullptr;
+  GSegment* d_segs = nullptr;
+  int* d_tile_prob = nullptr;
+  int* d_tile_mn = nullptr;
+  int* d_ctl = nullptr;
+  int grid = 0;
+  bool ready = false;
+};
+// Builder: a phase, then its problems, each followed by its segments.
+void gp_phase(GroupedProgram& g, int type, int ta, int tb, int a_slot, int b_slot, int c_slot);
+int gp_problem(GroupedProgram& g, int64_t c_off, int64_t ldc, int m, int n);
+void gp_segment(GroupedProgram& g, int64_t a_off, int64_t lda, int64_t b_off, int64_t ldb, int k,
+                double coef);
+// Declares how many doubles operand slot `slot` holds; gp_finalize checks every
+// block footprint against it (host side, before anything reaches the GPU).
+void gp_slot(GroupedProgram& g, int slot, int64_t elems);
+int gp_finalize(fmpt_handle* h, GroupedProgram& g);   // bounds check + tiles + upload
+int gp_run(fmpt_handle* h, const GroupedProgram& g, double* const* slots, int nslots);
+int gp_check_status(fmpt_handle* h);                  // synchronises; FMPT_ERR_TIMEOUT if set
+
+// -------- dense helpers shared with the sector code (linalg.cu)
+int copy_mat(fmpt_handle* h, int cplx, int rows, int cols, const double* src, int64_t s_ld,
+             int64_t s_plane, int trans, int conj, double* dst, int64_t d_ld, int64_t d_plane);
+int svd_tall(fmpt_handle* h, int cplx, int m, int n, double* Awork, double* S, double* U,
+             double* VT);
+
 // -------- vector kernels (krylov.cu)
 int vec_dot_dev(fmpt_handle* h, int cplx, int64_t n, const double* x, const double* y,
                 double* out_dev /* re, im */);
@@ -144,6 +200,7 @@ struct fmpt_op {
   fmpt::MidSchedule sched;
   int64_t n = 0;          // vector length (complex elements for C128)
   void* tc = nullptr;     // tensor-core state (mixed precision), owned
+  void* u1 = nullptr;     // U(1) block-sparse state (grouped program + scratch), owned
 };
 
 namespace fmpt {
@@ -156,6 +213,8 @@ int env_update_tc(fmpt_handle* h, bool right, int precision, const double* hold,
                   const double* W, const double* B, double* hnew, int Dl, int d, int Dr, int wl,
                   int wr);
 void op_tc_free(fmpt_op* op);
+int op_u1_apply(fmpt_op* op, const double* x, double* y);
+void op_u1_free(fmpt_op* op);
 
 // K-major tensor-core operand: TF32 (float storage) or BF16 plane, optional
 // TF32 low plane (3xTF32), row stride and batch stride in elements.

@@ -494,6 +494,7 @@ int fmpt_lanczos_ground(fmpt_op* op, const double* x0, int kmax, double btol, in
   FMPT_CUDA(h, cudaStreamSynchronize(h->stream));
   *eigval = h->pinned[0];
   if (op->precision != FMPT_PREC_FP64) FMPT_TRY(op_tc_check(op));
+  if (op->u1) FMPT_TRY(gp_check_status(op->h));
   if (info) *info = inf;
   if (niter) *niter = k;
   return FMPT_OK;
@@ -618,6 +619,7 @@ int fmpt_exponentiate(fmpt_op* op, double t_re, double t_im, const double* x, do
   scale_by<<<G, KT, 0, h->stream>>>(nr, xout, acc.d());
   FMPT_LAUNCHED(h);
   if (op->precision != FMPT_PREC_FP64) FMPT_TRY(op_tc_check(op));
+  if (op->u1) FMPT_TRY(gp_check_status(op->h));
   if (info) *info = steps;
   return FMPT_OK;
 }

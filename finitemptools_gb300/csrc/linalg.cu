@@ -58,6 +58,8 @@ __global__ void zero_lower(int cplx, int rows, int cols, double* M, int64_t ld, 
   }
 }
 
+}  // namespace
+
 int copy_mat(fmpt_handle* h, int cplx, int rows, int cols, const double* src, int64_t s_ld,
              int64_t s_plane, int trans, int conj, double* dst, int64_t d_ld, int64_t d_plane) {
   int64_t tot = (int64_t)rows * cols;
@@ -77,7 +79,7 @@ int copy_mat(fmpt_handle* h, int cplx, int rows, int cols, const double* src, in
                        __FILE__, __LINE__, #expr, (int)_s);                          \
   } while (0)
 
-int read_info(fmpt_handle* h, const int* dinfo, int* out) {
+static int read_info(fmpt_handle* h, const int* dinfo, int* out) {
   FMPT_TRY(ensure_pinned(h, 1));
   FMPT_CUDA(h, cudaMemcpyAsync(h->pinned, dinfo, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
   FMPT_CUDA(h, cudaStreamSynchronize(h->stream));
@@ -150,7 +152,6 @@ int svd_tall(fmpt_handle* h, int cplx, int m, int n, double* Awork, double* S, d
   return copy_mat(h, cplx, n, n, V.d(), n, cplx ? -1 : 0, 1, cplx, VT, n, cplx ? -1 : 0);
 }
 
-}  // namespace
 }  // namespace fmpt
 
 using namespace fmpt;

@@ -80,7 +80,8 @@ enum fmpt_kernel_class {
   FMPT_K_F64_GEMM = 1,    /* FP64 / complex FP64 CUDA-core GEMM         */
   FMPT_K_MPO_STEP = 2,    /* block-sparse MPO contraction step          */
   FMPT_K_CONVERT = 3,     /* operand layout / precision conversion      */
-  FMPT_K_COUNT = 4
+  FMPT_K_GROUPED = 4,     /* grouped block-sparse (U(1)) persistent launch */
+  FMPT_K_COUNT = 5
 };
 int fmpt_profile_enable(fmpt_handle* h, int on);
 int fmpt_profile_read(fmpt_handle* h, int kernel_class, int64_t* launches, double* total_ms);
@@ -225,6 +226,89 @@ int fmpt_dm_split(fmpt_handle* h, int dtype, const double* M, int m, int n, int 
 int fmpt_qr(fmpt_handle* h, int dtype, const double* M, int m, int n, double* Q, double* R);
 /* Thin LQ (rightorth, LQ()): M (m x n) = L (m x r) Q (r x n). */
 int fmpt_lq(fmpt_handle* h, int dtype, const double* M, int m, int n, double* Lout, double* Q);
+
+/* ------------------------------------------------- U(1) block-sparse path
+ * Charge-conserving (U(1), e.g. Sz) tensors, as TensorKit holds them for
+ * U1Space legs (the reference's symmetric path: heisenberg_xxz_chain,
+ * utilities/models.jl:47, with the charge labels of abelian_matrix_from_dense,
+ * auxiliary/abelianmatrix.jl:112-124: physical basis state i has charge i).
+ *
+ * A virtual leg is a table of sectors (charge, dimension), charges strictly
+ * increasing; its basis is charge-sorted, sector by sector.  MPS tensors
+ * A[a, s, b] and environments L[a', w, a] are stored DENSE in these sorted
+ * bases (the reference's index order and column-major layout) with exact
+ * zeros outside the allowed blocks:
+ *   A[a, s, b]    nonzero only if q(a) + qp(s)  == q(b)
+ *   L[a', w, a]   nonzero only if q(a') == q(a) + qw(w)   (same rule for R[b', w, b])
+ *   W[wl, s', wr, s] must satisfy qw(wl) + qp(s') == qw(wr) + qp(s)
+ * qp are the physical charges, qw the charges of the MPO bond channels (the
+ * charge the operator string to the left of the bond has added).  The
+ * two-site vector x[a, s1, s2, b] is PACKED: only its allowed blocks
+ * (ia, s, ib), s = s1 + d1*s2, each column-major dim(ia) x dim(ib), in the
+ * order ia fastest, then s, then ib.  All of these run FP64 (real only) on the
+ * grouped persistent engine: one cooperative launch per contraction, CTAs
+ * pulling 32x32 tiles of the uneven blocks from a device work counter, a
+ * bounded grid barrier between the three steps (L*x, MPO step, *R). */
+typedef struct fmpt_u1_space {
+  int nsect;            /* number of sectors                     */
+  const int* charge;    /* nsect charges, strictly increasing   */
+  const int* dim;       /* nsect dimensions, each >= 1           */
+} fmpt_u1_space;
+
+/* Length (elements) of the packed two-site vector (host-only; h may be NULL). */
+int fmpt_u1_twosite_size(fmpt_handle* h, const fmpt_u1_space* Vl, const fmpt_u1_space* Vr,
+                         int d1, const int* qp1, int d2, const int* qp2, int64_t* n);
+/* dense charge-sorted x[a, s1, s2, b] <-> packed (direction 0: pack, 1: unpack;
+ * unpack writes the zeros too). */
+int fmpt_u1_pack2(fmpt_handle* h, int dtype, const double* src, double* dst,
+                  const fmpt_u1_space* Vl, const fmpt_u1_space* Vr, int d1, const int* qp1,
+                  int d2, const int* qp2, int direction);
+/* Block-sparse two-site H_eff operator (ac2_prime, derivatives.jl:20-22, on
+ * U1Space tensors) for the Krylov solvers: fmpt_op_apply maps packed x to
+ * packed y, fmpt_op_size is the packed length.  W1/W2 are HOST MPO tensors;
+ * qwl/qwm/qwr the channel charges of their bonds; hleft [Dl, wl, Dl] and
+ * hright [Dr, wr, Dr] device environments that must outlive the operator. */
+int fmpt_u1_op_ac2(fmpt_handle* h, int dtype, const double* W1_host, const double* W2_host,
+                   const double* hleft, const double* hright, const fmpt_u1_space* Vl,
+                   const fmpt_u1_space* Vr, int d1, const int* qp1, int d2, const int* qp2,
+                   int wl, const int* qwl, int wm, const int* qwm, int wr, const int* qwr,
+                   fmpt_op** out);
+/* Algorithmic FLOPs of one fmpt_op_apply (dense: the pairwise-order count
+ * 4 w d^2 D^3-type formula of the operator's shape; U(1): the block-sparse
+ * GEMM and MPO-step work of its block lists). */
+int fmpt_op_flops(fmpt_op* op, double* flops);
+/* x[a, s1, s2, b] (packed) = sum_m A[a, s1, m] B[m, s2, b]  (dmrg.jl:98). */
+int fmpt_u1_twosite(fmpt_handle* h, int dtype, const double* A, const double* B, double* x,
+                    const fmpt_u1_space* Vl, const fmpt_u1_space* Vm, const fmpt_u1_space* Vr,
+                    int d1, const int* qp1, int d2, const int* qp2);
+/* Environment updates (mpo/transfer.jl:26-34) on U(1) tensors: hold is
+ * [Dl, wl, Dl] (left) or [Dr, wr, Dr] (right); A, B are [Dl, d, Dr]; the
+ * output is written in full (zeros outside the allowed blocks). */
+int fmpt_u1_updateleft(fmpt_handle* h, int dtype, const double* hold, const double* A,
+                       const double* W_host, const double* B, double* hnew,
+                       const fmpt_u1_space* Vl, const fmpt_u1_space* Vr, int d, const int* qp,
+                       int wl, const int* qwl, int wr, const int* qwr);
+int fmpt_u1_updateright(fmpt_handle* h, int dtype, const double* hold, const double* A,
+                        const double* W_host, const double* B, double* hnew,
+                        const fmpt_u1_space* Vl, const fmpt_u1_space* Vr, int d, const int* qp,
+                        int wl, const int* qwl, int wr, const int* qwr);
+/* Truncated two-site split of a packed x (stable_tsvd! + MPSTruncation,
+ * stable_svd.jl:12-18, truncation.jl:27-47, with TensorKit's cross-sector
+ * rule): each charge sector qc of the new bond, rows (s1, a) with
+ * q(a) + qp1(s1) == qc and columns (s2, b) with q(b) - qp2(s2) == qc, is
+ * factorised by an FP64 SVD on the device; then sigma below eps*||sigma||_2
+ * (over all sectors) is dropped and at most maxD values are kept, largest
+ * first (ties: lower charge first).  The kept sigma are normalised to unit
+ * 2-norm (normalize!(s) of DMRG2) and returned in S; side 0 gives A = u
+ * (left isometry) and B = s*v, side 1 gives A = u*s and B = v (right
+ * isometry).  A is [Dl, d1, Dm'] and B [Dm', d2, Dr] in the new sorted basis,
+ * written in full; size them for Dm' <= min(maxD, Dl*d1, d2*Dr).  HOST
+ * outputs: the new leg (nsect_out sectors into charge_out/dim_out, capacity
+ * cap) and err (2-norm of the dropped sigma before normalisation). */
+int fmpt_u1_split(fmpt_handle* h, int dtype, const double* x, const fmpt_u1_space* Vl,
+                  const fmpt_u1_space* Vr, int d1, const int* qp1, int d2, const int* qp2,
+                  int maxD, double eps, int side, double* A, double* S, double* B, int cap,
+                  int* nsect_out, int* charge_out, int* dim_out, double* err);
 
 #ifdef __cplusplus
 }

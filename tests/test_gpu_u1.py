@@ -1,0 +1,221 @@
+"""Parity of the U(1) block-sparse device path (grouped persistent engine)
+against the oracle's block-sparse restatement, the dense FP64 device path and
+exact diagonalisation.
+
+Bar: the plain FP64 bar of the dense path -- H_eff*x and environment updates
+within 1e-12 relative of the oracle (they reach ~1e-15), exact zeros outside
+the allowed charge blocks, split factors within 1e-12, sweep energies within
+1e-10 of exact diagonalisation in the Sz sector.
+"""
+
+import numpy as np
+import pytest
+
+import oracle as O
+from oracle import u1 as OU
+from oracle.ed import xxz_ground_energy
+import finitemptools_gb300 as fm
+from finitemptools_gb300 import DeviceTensor as DT
+from finitemptools_gb300.u1 import (U1FiniteMPS, U1Space, u1_pack2, u1_right_canonicalize_,
+                                    u1_unpack2)
+from finitemptools_gb300.utilities import heisenberg_xxz_mpo, j1j2_heisenberg_mpo
+
+pytestmark = pytest.mark.gpu
+QP = (0, 1)
+
+
+def rel(a, b):
+    return np.linalg.norm(np.asarray(a) - np.asarray(b)) / max(np.linalg.norm(b), 1e-300)
+
+
+def sp(leg):
+    return U1Space(leg.items())
+
+
+def _bond(L, N, D, site, seed, mpo=None):
+    rng = np.random.default_rng(seed)
+    Ws = (mpo or heisenberg_xxz_mpo(1.0, 0.7, 0.3)).site_tensors(L)
+    qw = OU.channel_charges(Ws, list(QP))
+    mps, legs = OU.random_u1_state(L, N, D, list(QP), rng)
+    w = Ws[0].shape[0]
+    Vl, Vr = legs[site - 1], legs[site + 1]
+    Lm = rng.standard_normal((Vl.dim, w, Vl.dim)) * OU.allowed_env(Vl, qw[site - 1])
+    Rm = rng.standard_normal((Vr.dim, w, Vr.dim)) * OU.allowed_env(Vr, qw[site + 1])
+    return Ws, qw, mps, legs, Lm, Rm
+
+
+@pytest.mark.parametrize("L,N,D,site", [(6, 3, 4, 3), (10, 5, 20, 5), (12, 4, 33, 2),
+                                        (16, 8, 96, 8), (24, 12, 300, 12)])
+def test_u1_ac2_apply(L, N, D, site):
+    Ws, qw, mps, legs, Lm, Rm = _bond(L, N, D, site, L + D)
+    Vl, Vr = legs[site - 1], legs[site + 1]
+    W1, W2 = Ws[site - 1], Ws[site]
+    X = np.tensordot(mps[site - 1], mps[site], axes=([2], [0]))
+    ref = O.ac2_prime(X, W1, W2, Lm, Rm)
+    dL, dR = DT.from_numpy(Lm), DT.from_numpy(Rm)
+    op = fm.U1HeffOp(dL, dR, W1, W2, sp(Vl), sp(Vr), QP, QP, qw[site - 1], qw[site],
+                     qw[site + 1])
+    x = DT.from_numpy(OU.pack2(X, Vl, Vr, list(QP), list(QP)))
+    assert op.n == x.size
+    y = op(x).numpy()
+    assert rel(y, OU.pack2(ref, Vl, Vr, list(QP), list(QP))) < 1e-13
+    # the dense FP64 device path on the same charge-sorted tensors
+    yd = fm.ac2_prime(DT.from_numpy(X), W1, W2, dL, dR).numpy()
+    assert rel(y, OU.pack2(yd, Vl, Vr, list(QP), list(QP))) < 1e-13
+    # repeated application is bit-identical (fixed summation order)
+    assert np.array_equal(op(x).numpy(), y)
+    assert op.flops() > 0
+
+
+def test_u1_pack_roundtrip():
+    Ws, qw, mps, legs, Lm, Rm = _bond(12, 6, 40, 6, 2)
+    Vl, Vr = legs[5], legs[7]
+    X = np.tensordot(mps[5], mps[6], axes=([2], [0]))
+    xp = u1_pack2(DT.from_numpy(X), sp(Vl), sp(Vr), QP, QP)
+    assert np.array_equal(xp.numpy(), OU.pack2(X, Vl, Vr, list(QP), list(QP)))
+    Xb = u1_unpack2(xp, sp(Vl), sp(Vr), QP, QP).numpy()
+    assert np.array_equal(Xb, X)
+
+
+@pytest.mark.parametrize("L,N,D,site", [(8, 4, 6, 4), (12, 6, 40, 6), (20, 10, 150, 9)])
+def test_u1_twosite_and_envs(L, N, D, site):
+    Ws, qw, mps, legs, Lm, Rm = _bond(L, N, D, site, 3 * L + D)
+    Vl, Vm, Vr = legs[site - 1], legs[site], legs[site + 1]
+    A, B = mps[site - 1], mps[site]
+    x = fm.u1_twosite(DT.from_numpy(A), DT.from_numpy(B), sp(Vl), sp(Vm), sp(Vr), QP, QP)
+    ref = OU.pack2(np.tensordot(A, B, axes=([2], [0])), Vl, Vr, list(QP), list(QP))
+    assert rel(x.numpy(), ref) < 1e-14
+    # updateleft over site `site` (legs Vl -> Vm), both kets different tensors
+    rng = np.random.default_rng(L)
+    Bk = A + 0.5 * rng.standard_normal(A.shape) * OU.allowed3(Vl, Vm, list(QP))
+    W = Ws[site - 1]
+    refL = O.updateleft(Lm, A, W, Bk)
+    gL = fm.u1_updateleft(DT.from_numpy(Lm), DT.from_numpy(A), W, DT.from_numpy(Bk), sp(Vl),
+                          sp(Vm), QP, qw[site - 1], qw[site]).numpy()
+    assert rel(gL, refL) < 1e-13
+    assert np.all(gL[~OU.allowed_env(Vm, qw[site])] == 0.0)
+    # updateright over site `site + 1` (legs Vm -> Vr)
+    W = Ws[site]
+    Bk = B + 0.5 * rng.standard_normal(B.shape) * OU.allowed3(Vm, Vr, list(QP))
+    refR = O.updateright(Rm, B, W, Bk)
+    gR = fm.u1_updateright(DT.from_numpy(Rm), DT.from_numpy(B), W, DT.from_numpy(Bk), sp(Vm),
+                           sp(Vr), QP, qw[site], qw[site + 1]).numpy()
+    assert rel(gR, refR) < 1e-13
+    assert np.all(gR[~OU.allowed_env(Vm, qw[site])] == 0.0)
+
+
+@pytest.mark.parametrize("side", [0, 1])
+@pytest.mark.parametrize("maxD,eps", [(100000, 0.0), (17, 0.0), (40, 1e-3)])
+def test_u1_split(side, maxD, eps):
+    Ws, qw, mps, legs, Lm, Rm = _bond(14, 7, 48, 7, 11)
+    Vl, Vr = legs[6], legs[8]
+    X = np.tensordot(mps[6], mps[7], axes=([2], [0]))
+    tr = O.MPSTruncation(maxD, eps)
+    xp = DT.from_numpy(OU.pack2(X, Vl, Vr, list(QP), list(QP)))
+    A, S, B, Vm, err = fm.u1_split(xp, sp(Vl), sp(Vr), QP, QP, fm.MPSTruncation(maxD, eps), side)
+    Ao, So, Bo, Vmo, erro = OU.u1_split(X, Vl, Vr, list(QP), list(QP), tr, side)
+    assert Vm.charges == tuple(Vmo.charges) and Vm.dims == tuple(Vmo.dims)
+    assert np.abs(S.numpy() - So).max() < 1e-12
+    assert abs(err - erro) <= 1e-10 * max(erro, 1e-3)
+    An, Bn = A.numpy(), B.numpy()
+    prod = np.tensordot(An, Bn, axes=([2], [0]))
+    assert rel(prod, np.tensordot(Ao, Bo, axes=([2], [0]))) < 1e-12
+    k = Vm.dim
+    if side == 0:
+        G = An.reshape(-1, k, order="F")
+        assert np.abs(G.T @ G - np.eye(k)).max() < 1e-12
+    else:
+        G = Bn.reshape(k, -1, order="F")
+        assert np.abs(G @ G.T - np.eye(k)).max() < 1e-12
+    assert np.all(An[~OU.allowed3(Vl, Vmo, list(QP))] == 0.0)
+    assert np.all(Bn[~OU.allowed3(Vmo, Vr, list(QP))] == 0.0)
+
+
+def _states(L, N, D, seed):
+    mps, legs = OU.random_u1_state(L, N, D, list(QP), np.random.default_rng(seed))
+    psi = U1FiniteMPS([DT.from_numpy(A) for A in mps], [sp(l) for l in legs], QP)
+    return mps, legs, psi
+
+
+def test_u1_lanczos_matches_oracle():
+    L, N = 10, 5
+    Ws = heisenberg_xxz_mpo().site_tensors(L)
+    mps, legs, psi = _states(L, N, 16, 4)
+    env_o = OU.U1OracleEnv(Ws, mps, legs, list(QP), schur=True)
+    env_o.right_canonicalize()
+    u1_right_canonicalize_(psi)
+    for i in range(1, L + 1):
+        assert rel(psi[i].numpy(), env_o.mps[i - 1]) < 1e-11 or \
+            rel(np.abs(psi[i].numpy()), np.abs(env_o.mps[i - 1])) < 1e-11
+    m = fm.U1ExpectationCache(heisenberg_xxz_mpo(), psi)
+    site = 1
+    Vl, Vm, Vr = psi.spaces[1], psi.spaces[2], psi.spaces[3]
+    x2 = fm.u1_twosite(psi[1], psi[2], Vl, Vm, Vr, QP, QP)
+    op = fm.U1HeffOp(m.hstorage[1], m.hstorage[3], m.mpo[1], m.mpo[2], Vl, Vr, QP, QP,
+                     m.qw[1], m.qw[2], m.qw[3])
+    E, vec, info, k = op.lanczos(x2, 30, 1e-12)
+    W1, W2 = Ws[0], Ws[1]
+    Lh, Rh = env_o.hstorage[0], env_o.hstorage[2]
+    X = np.tensordot(env_o.mps[0], env_o.mps[1], axes=([2], [0]))
+
+    def f(v):
+        return O.ac2_prime(v.reshape(X.shape, order="F"), W1, W2, Lh, Rh).ravel(order="F")
+
+    Eo, vo, _, ko = O.simple_lanczos_solver(f, X.ravel(order="F"), 30, 1e-12)
+    assert abs(E - Eo) < 1e-10 * abs(Eo)
+    assert k == ko
+
+
+@pytest.mark.parametrize("L,N,D,model", [(12, 6, 48, "xxz"), (12, 4, 48, "xxz"),
+                                         (10, 5, 40, "j1j2")])
+def test_u1_dmrg2_vs_ed_and_oracle(L, N, D, model):
+    mpo = heisenberg_xxz_mpo() if model == "xxz" else j1j2_heisenberg_mpo(1.0, 0.5)
+    Ws = mpo.site_tensors(L)
+    mps, legs, psi = _states(L, N, 8, 7)
+    env_o = OU.U1OracleEnv(Ws, mps, legs, list(QP), schur=True)
+    env_o.right_canonicalize()
+    u1_right_canonicalize_(psi)
+    alg = fm.DMRG2(eig_maxiter=30, eig_tol=1e-12, trunc=fm.MPSTruncation(D, 1e-12), verbosity=0)
+    m = fm.U1ExpectationCache(mpo, psi)
+    tr = O.MPSTruncation(D, 1e-12)
+    for sweep in range(3):
+        Eg, dg = fm.sweep_(m, alg)
+        Eo, do = OU.u1_dmrg2_sweep(env_o, tr, 30, 1e-12)
+        assert np.abs(np.asarray(Eg) - np.asarray(Eo)).max() < 1e-9 * abs(Eo[-1])
+    if model == "xxz":
+        e_ed = xxz_ground_energy(L, nup=N)
+    else:
+        from oracle.ed import j1j2_ground_energy
+        e_ed = j1j2_ground_energy(L, 1.0, 0.5, nup=N)
+    assert abs(Eg[-1] - e_ed) < 1e-10 * abs(e_ed)
+    assert abs(fm.expectation(psi, mpo) - Eg[-1]) < 1e-10 * abs(e_ed)
+    assert psi.total_charge == N
+
+
+def test_u1_dmrg2_matches_dense_path():
+    """Same chain, dense FP64 path vs U(1) path: same ground energy."""
+    L, N = 12, 6
+    mpo = heisenberg_xxz_mpo()
+    mps, legs, psi = _states(L, N, 8, 9)
+    u1_right_canonicalize_(psi)
+    dense = fm.FiniteMPS([DT.from_numpy(A.numpy()) for A in psi.data])
+    alg = fm.DMRG2(eig_maxiter=30, eig_tol=1e-12, trunc=fm.MPSTruncation(64, 1e-12), verbosity=0)
+    m1 = fm.U1ExpectationCache(mpo, psi)
+    m2 = fm.environments(mpo, dense)
+    for _ in range(3):
+        E1, _ = fm.sweep_(m1, alg)
+        E2, _ = fm.sweep_(m2, alg)
+    assert abs(E1[-1] - E2[-1]) < 1e-10 * abs(E2[-1])
+    assert abs(E1[-1] - xxz_ground_energy(L, nup=N)) < 1e-10 * abs(E1[-1])
+
+
+def test_u1_rejects_bad_input():
+    Ws, qw, mps, legs, Lm, Rm = _bond(8, 4, 6, 4, 1)
+    Vl, Vr = legs[3], legs[5]
+    dL, dR = DT.from_numpy(Lm), DT.from_numpy(Rm)
+    bad = Ws[3].copy()
+    bad[0, 0, 1, 0] = 1.0        # S+ channel on a charge-diagonal entry
+    with pytest.raises(fm.FMPTError):
+        fm.U1HeffOp(dL, dR, bad, Ws[4], sp(Vl), sp(Vr), QP, QP, qw[3], qw[4], qw[5])
+    with pytest.raises(fm.FMPTError):   # wrong channel charges
+        fm.U1HeffOp(dL, dR, Ws[3], Ws[4], sp(Vl), sp(Vr), QP, QP, qw[3], [0, 0, 0, 0, 0], qw[5])
