@@ -103,7 +103,7 @@ SIGNATURES = {
     "fmpt_u1_updateright": (c_int, [c_void_p, c_int, dptr, dptr, hptr, dptr, dptr, SP, SP, c_int,
                                     ip, c_int, ip, c_int, ip]),
     "fmpt_u1_split": (c_int, [c_void_p, c_int, dptr, SP, SP, c_int, ip, c_int, ip, c_int,
-                              c_double, c_int, dptr, dptr, dptr, c_int, ip, ip, ip,
+                              c_double, c_int, c_int, dptr, dptr, dptr, c_int, ip, ip, ip,
                               P(c_double)]),
 }
 

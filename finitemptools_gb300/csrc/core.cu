@@ -63,6 +63,45 @@ int ensure_pinned(fmpt_handle* h, size_t n) {
   return FMPT_OK;
 }
 
+int ensure_aux(fmpt_handle* h, int n) {
+  if (h->aux_event.empty()) {
+    cudaEvent_t e;
+    FMPT_CUDA(h, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    h->aux_event.push_back(e);
+  }
+  while ((int)h->aux_stream.size() < n) {
+    cudaStream_t st;
+    FMPT_CUDA(h, cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    cusolverDnHandle_t sv;
+    if (cusolverDnCreate(&sv) != CUSOLVER_STATUS_SUCCESS) {
+      cudaStreamDestroy(st);
+      return set_error(h, FMPT_ERR_CUSOLVER, "aux stream: cusolverDnCreate failed");
+    }
+    cusolverDnSetStream(sv, st);
+    cudaEvent_t e;
+    FMPT_CUDA(h, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    h->aux_stream.push_back(st);
+    h->aux_solver.push_back(sv);
+    h->aux_event.push_back(e);
+  }
+  return FMPT_OK;
+}
+
+int aux_fork(fmpt_handle* h, int n) {
+  FMPT_TRY(ensure_aux(h, n));
+  FMPT_CUDA(h, cudaEventRecord(h->aux_event[0], h->stream));
+  for (int i = 0; i < n; i++) FMPT_CUDA(h, cudaStreamWaitEvent(h->aux_stream[i], h->aux_event[0], 0));
+  return FMPT_OK;
+}
+
+int aux_join(fmpt_handle* h, int n) {
+  for (int i = 0; i < n; i++) {
+    FMPT_CUDA(h, cudaEventRecord(h->aux_event[1 + i], h->aux_stream[i]));
+    FMPT_CUDA(h, cudaStreamWaitEvent(h->stream, h->aux_event[1 + i], 0));
+  }
+  return FMPT_OK;
+}
+
 namespace {
 
 constexpr int RT = 256;       // threads per reduction block
@@ -284,6 +323,9 @@ int fmpt_destroy(fmpt_handle* h) {
     for (auto& pr : v) { h->ev_pool.push_back(pr.first); h->ev_pool.push_back(pr.second); }
   for (cudaEvent_t e : h->ev_pool) cudaEventDestroy(e);
   if (h->solver) cusolverDnDestroy(h->solver);
+  for (auto sv : h->aux_solver) cusolverDnDestroy(sv);
+  for (auto st : h->aux_stream) cudaStreamDestroy(st);
+  for (auto ev : h->aux_event) cudaEventDestroy(ev);
   if (h->gstatus) cudaFree(h->gstatus);
   if (h->pinned) cudaFreeHost(h->pinned);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);

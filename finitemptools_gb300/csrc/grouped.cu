@@ -4,7 +4,7 @@
 // A GroupedProgram is a short sequence of phases; each phase is a list of
 // uneven block problems:
 //   GEMM phase:  C_p = sum_{j in segs(p)} coef_j * op(A_j) op(B_j)     (overwrite)
-//   SUM  phase:  C_p = sum_{j in segs(p)} coef_j * A_j                 (overwrite)
+//   SUM  phase:  C_p = sum_{j in segs(p)} coef_j * op(A_j)             (overwrite)
 // where every operand is a strided sub-matrix (offset + leading dimension) of
 // one of a few operand slots (device base pointers given at run time).  The
 // whole program runs as ONE cooperative launch: CTAs pull 32x32 output tiles
@@ -155,7 +155,7 @@ __device__ __forceinline__ void sum_tile(const GKArgs& a, const GPhaseDesc& ph, 
     double s = 0.0;
     for (int sg = P.seg0; sg < P.seg1; sg++) {
       const GSegment S = a.segs[sg];
-      s = fma(S.coef, __ldg(Ab + S.a_off + r + (int64_t)c * S.lda), s);
+      s = fma(S.coef, __ldg(Ab + S.a_off + op_index(ph.ta, r, c, S.lda)), s);
     }
     C[r + (int64_t)c * P.ldc] = s;
   }
@@ -269,7 +269,7 @@ int validate(fmpt_handle* h, const GroupedProgram& g) {
           FMPT_TRY(check_span(h, g, d.a_slot, d.ta, sg.a_off, p.m, sg.k, sg.lda, "A operand", i));
           FMPT_TRY(check_span(h, g, d.b_slot, d.tb, sg.b_off, sg.k, p.n, sg.ldb, "B operand", i));
         } else {
-          FMPT_TRY(check_span(h, g, d.a_slot, FMPT_N, sg.a_off, p.m, p.n, sg.lda, "summand", i));
+          FMPT_TRY(check_span(h, g, d.a_slot, d.ta, sg.a_off, p.m, p.n, sg.lda, "summand", i));
         }
       }
     }

@@ -29,6 +29,11 @@ struct fmpt_handle {
   // status word of the grouped block-sparse launches (1 = a grid barrier timed
   // out); allocated on first use, read and cleared by gp_check_status
   int* gstatus = nullptr;
+  // auxiliary streams with their own cuSOLVER handles for independent
+  // factorisations (created on first use): fork/join through events on `stream`
+  std::vector<cudaStream_t> aux_stream;
+  std::vector<cusolverDnHandle_t> aux_solver;
+  std::vector<cudaEvent_t> aux_event;   // [0] fork, [1 + i] join of aux stream i
 };
 
 namespace fmpt {
@@ -75,6 +80,11 @@ struct DevBuf {
 };
 
 int ensure_pinned(fmpt_handle* h, size_t n_doubles);
+// At least n auxiliary streams/solvers; aux_fork makes them wait for the work
+// queued so far on h->stream, aux_join makes h->stream wait for them.
+int ensure_aux(fmpt_handle* h, int n);
+int aux_fork(fmpt_handle* h, int n);
+int aux_join(fmpt_handle* h, int n);
 
 // Scoped device timer for one launch of a kernel class (no-op unless profiling).
 struct ProfScope {

@@ -264,8 +264,14 @@ int fmpt_dm_split(fmpt_handle* h, int dtype, const double* M, int m, int n, int 
   FMPT_CUDA(h, cudaMemcpyAsync(lam.data(), W.d(), r * sizeof(double), cudaMemcpyDeviceToHost,
                                h->stream));
   FMPT_CUDA(h, cudaStreamSynchronize(h->stream));
+  // eigenvalues below the eigensolver's noise floor (~ r eps lambda_max) are
+  // exact zeros: their square roots (~1e-8 sigma_max) would be junk directions
   const int rank_max = std::min(m, n);
-  for (int i = 0; i < r; i++) s[i] = i < rank_max ? std::sqrt(std::max(lam[r - 1 - i], 0.0)) : 0.0;
+  const double floor_ = 4.0 * r * 2.220446049250313e-16 * std::max(lam[r - 1], 0.0);
+  for (int i = 0; i < r; i++) {
+    const double l = lam[r - 1 - i];
+    s[i] = (i < rank_max && l > floor_) ? std::sqrt(l) : 0.0;
+  }
   double nrm = 0.0;
   for (double v : s) nrm += v * v;
   nrm = std::sqrt(nrm);

@@ -13,6 +13,7 @@
 // W[wl, s', wr, s] conserves qw(wl) + qp(s') == qw(wr) + qp(s).
 #include <algorithm>
 #include <cmath>
+#include <map>
 #include <vector>
 
 #include "internal.h"
@@ -183,6 +184,185 @@ struct ScratchPair {
 
 int alloc_scratch(fmpt_handle* h, DevBuf& b, int64_t n) {
   return b.alloc(h, (size_t)std::max<int64_t>(n, 1) * sizeof(double));
+}
+
+
+// One charge sector of the new bond in a two-site split.
+struct SplitSeg {
+  int s, i;
+  int64_t off;
+};
+struct SplitSector {
+  int q = 0;
+  std::vector<SplitSeg> rows, cols;   // (s1, ia) row blocks, (s2, ib) column blocks
+  int r = 0, c = 0, kq = 0, keep = 0;
+  int64_t moff = 0, uoff = 0, voff = 0, soff = 0;
+  // density-matrix form: Gram extent n, padded extent npad, offset of the
+  // (padded) Gram / eigenvector matrix
+  int n = 0, npad = 0;
+  int64_t goff = 0;
+};
+
+// Pads every Gram matrix of a batch to its class size: the padded diagonal
+// gets -trace (so the padded eigenvalues sort below the nonnegative spectrum
+// and their eigenvectors stay on the padded coordinates).  One CTA per matrix.
+__global__ void pad_gram_kernel(const int64_t* __restrict__ goff, const int* __restrict__ nn,
+                                const int* __restrict__ np, double* __restrict__ G) {
+  __shared__ double red[256];
+  double* g = G + goff[blockIdx.x];
+  const int n = nn[blockIdx.x], npad = np[blockIdx.x];
+  double t = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) t += g[i + (int64_t)i * npad];
+  red[threadIdx.x] = t;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  const double pad = red[0] > 0.0 ? -red[0] : -1.0;
+  for (int i = n + threadIdx.x; i < npad; i += blockDim.x) g[i + (int64_t)i * npad] = pad;
+}
+
+#define FMPT_SOLVER_U1(h, expr)                                                      \
+  do {                                                                               \
+    cusolverStatus_t _s = (expr);                                                    \
+    if (_s != CUSOLVER_STATUS_SUCCESS)                                               \
+      return set_error((h), FMPT_ERR_CUSOLVER, "%s:%d %s -> cusolver status %d",     \
+                       __FILE__, __LINE__, #expr, (int)_s);                          \
+  } while (0)
+
+// Density-matrix form of the sector factorisation: Gram matrix of every
+// sector (side 0: M M^T, side 1: M^T M) in one grouped launch, padded to
+// multiples of 32, then one batched symmetric eigensolve (cuSOLVER
+// Xsyev, FP64) per padded size.  On return Gw holds the eigenvectors
+// (ascending eigenvalues), sv the singular values sqrt(max(lambda, 0)),
+// largest first, min(r, c) per sector.
+int density_eigen(fmpt_handle* h, int side, std::vector<SplitSector>& sec, const double* Mw,
+                  int64_t mtot, DevBuf& Gw, std::vector<double>& sv) {
+  std::map<int, std::vector<int>> classes;   // padded size -> sectors
+  for (size_t si = 0; si < sec.size(); si++) {
+    SplitSector& S_ = sec[si];
+    S_.n = side == 0 ? S_.r : S_.c;
+    S_.npad = std::max(32, (S_.n + 31) / 32 * 32);
+    classes[S_.npad].push_back((int)si);
+  }
+  int64_t gtot = 0, wtot = 0;
+  std::vector<int64_t> woff(sec.size(), 0);
+  for (auto& kv : classes)
+    for (int si : kv.second) {
+      sec[si].goff = gtot;
+      gtot += (int64_t)kv.first * kv.first;
+      woff[si] = wtot;
+      wtot += kv.first;
+    }
+  DevBuf Ww, info, tab;
+  FMPT_TRY(alloc_scratch(h, Gw, gtot));
+  FMPT_TRY(alloc_scratch(h, Ww, wtot));
+  FMPT_TRY(info.alloc(h, sizeof(int) * sec.size()));
+  FMPT_CUDA(h, cudaMemsetAsync(Gw.p, 0, (size_t)gtot * sizeof(double), h->stream));
+  {  // all Gram matrices in one grouped launch
+    GroupedProgram g;
+    if (side == 0)
+      gp_phase(g, GP_GEMM, FMPT_N, FMPT_T, 0, 0, 1);
+    else
+      gp_phase(g, GP_GEMM, FMPT_T, FMPT_N, 0, 0, 1);
+    for (const SplitSector& S_ : sec) {
+      gp_problem(g, S_.goff, S_.npad, S_.n, S_.n);
+      gp_segment(g, S_.moff, S_.r, S_.moff, S_.r, side == 0 ? S_.c : S_.r, 1.0);
+    }
+    gp_slot(g, 0, mtot);
+    gp_slot(g, 1, gtot);
+    FMPT_TRY(gp_finalize(h, g));
+    double* slots[2] = {const_cast<double*>(Mw), Gw.d()};
+    FMPT_TRY(gp_run(h, g, slots, 2));
+  }
+  {  // padding
+    const size_t ns = sec.size();
+    std::vector<int64_t> go(ns);
+    std::vector<int> nn(ns), np(ns);
+    for (size_t i = 0; i < ns; i++) { go[i] = sec[i].goff; nn[i] = sec[i].n; np[i] = sec[i].npad; }
+    FMPT_TRY(tab.alloc(h, ns * (sizeof(int64_t) + 2 * sizeof(int)) + 64));
+    char* t = static_cast<char*>(tab.p);
+    FMPT_CUDA(h, cudaMemcpyAsync(t, go.data(), ns * sizeof(int64_t), cudaMemcpyHostToDevice,
+                                 h->stream));
+    FMPT_CUDA(h, cudaMemcpyAsync(t + ns * sizeof(int64_t), nn.data(), ns * sizeof(int),
+                                 cudaMemcpyHostToDevice, h->stream));
+    FMPT_CUDA(h, cudaMemcpyAsync(t + ns * (sizeof(int64_t) + sizeof(int)), np.data(),
+                                 ns * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+    pad_gram_kernel<<<(unsigned)ns, 256, 0, h->stream>>>(
+        reinterpret_cast<const int64_t*>(t), reinterpret_cast<const int*>(t + ns * sizeof(int64_t)),
+        reinterpret_cast<const int*>(t + ns * (sizeof(int64_t) + sizeof(int))), Gw.d());
+    FMPT_LAUNCHED(h);
+  }
+  // one batched eigensolve per padded size, the sizes concurrently on
+  // auxiliary streams (each call is latency bound for n <= a few hundred)
+  const int nclass = (int)classes.size();
+  const int nstream = std::min(nclass, 6);
+  std::vector<size_t> dbytes(nclass, 0), hbytes(nclass, 0), doff(nclass, 0);
+  cusolverDnParams_t params;
+  FMPT_SOLVER_U1(h, cusolverDnCreateParams(&params));
+  int st = ensure_aux(h, nstream);
+  size_t dtot = 0;
+  int ci = 0;
+  for (auto& kv : classes) {
+    if (st != FMPT_OK) break;
+    const int64_t npad = kv.first, batch = (int64_t)kv.second.size();
+    cusolverStatus_t cs = cusolverDnXsyevBatched_bufferSize(
+        h->aux_solver[ci % nstream], params, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER,
+        npad, CUDA_R_64F, Gw.d() + sec[kv.second[0]].goff, npad, CUDA_R_64F,
+        Ww.d() + woff[kv.second[0]], CUDA_R_64F, &dbytes[ci], &hbytes[ci], batch);
+    if (cs != CUSOLVER_STATUS_SUCCESS)
+      st = set_error(h, FMPT_ERR_CUSOLVER, "syevBatched buffer size: status %d", (int)cs);
+    doff[ci] = dtot;
+    dtot += (dbytes[ci] + 255) / 256 * 256;
+    ci++;
+  }
+  DevBuf dwork;
+  if (st == FMPT_OK) st = dwork.alloc(h, std::max<size_t>(dtot, 256));
+  std::vector<std::vector<char>> hwork(nclass);
+  if (st == FMPT_OK) st = aux_fork(h, nstream);
+  ci = 0;
+  int idx0 = 0;
+  for (auto& kv : classes) {
+    if (st != FMPT_OK) break;
+    const int64_t npad = kv.first, batch = (int64_t)kv.second.size();
+    hwork[ci].resize(std::max<size_t>(hbytes[ci], 1));
+    cusolverStatus_t cs = cusolverDnXsyevBatched(
+        h->aux_solver[ci % nstream], params, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER,
+        npad, CUDA_R_64F, Gw.d() + sec[kv.second[0]].goff, npad, CUDA_R_64F,
+        Ww.d() + woff[kv.second[0]], CUDA_R_64F, static_cast<char*>(dwork.p) + doff[ci],
+        dbytes[ci], hwork[ci].data(), hbytes[ci], static_cast<int*>(info.p) + idx0, batch);
+    if (cs != CUSOLVER_STATUS_SUCCESS)
+      st = set_error(h, FMPT_ERR_CUSOLVER, "syevBatched: status %d", (int)cs);
+    idx0 += (int)batch;
+    ci++;
+  }
+  // join even after a failed call, so no auxiliary work outlives the scratch
+  const int jst = ensure_aux(h, nstream) == FMPT_OK ? aux_join(h, nstream) : FMPT_ERR_CUDA;
+  cusolverDnDestroyParams(params);
+  FMPT_TRY(st);
+  FMPT_TRY(jst);
+  std::vector<double> lam(wtot);
+  std::vector<int> inf(sec.size());
+  FMPT_CUDA(h, cudaMemcpyAsync(lam.data(), Ww.p, wtot * sizeof(double), cudaMemcpyDeviceToHost,
+                               h->stream));
+  FMPT_CUDA(h, cudaMemcpyAsync(inf.data(), info.p, sec.size() * sizeof(int),
+                               cudaMemcpyDeviceToHost, h->stream));
+  FMPT_CUDA(h, cudaStreamSynchronize(h->stream));
+  for (int v : inf)
+    if (v != 0) return set_error(h, FMPT_ERR_CUSOLVER, "syevBatched: info %d", v);
+  // eigenvalues below the eigensolver's noise floor (~ n eps lambda_max) are
+  // exact zeros: their square roots (~1e-8 sigma_max) would be junk directions
+  for (size_t si = 0; si < sec.size(); si++) {
+    const SplitSector& S_ = sec[si];
+    const double lmax = std::max(lam[woff[si] + S_.npad - 1], 0.0);
+    const double floor_ = 4.0 * S_.n * 2.220446049250313e-16 * lmax;
+    for (int i = 0; i < S_.kq; i++) {
+      const double l = lam[woff[si] + S_.npad - 1 - i];
+      sv[S_.soff + i] = l > floor_ ? std::sqrt(l) : 0.0;
+    }
+  }
+  return FMPT_OK;
 }
 
 }  // namespace
@@ -615,13 +795,15 @@ int fmpt_u1_updateright(fmpt_handle* h, int dtype, const double* hold, const dou
 
 int fmpt_u1_split(fmpt_handle* h, int dtype, const double* x, const fmpt_u1_space* Vl,
                   const fmpt_u1_space* Vr, int d1, const int* qp1, int d2, const int* qp2,
-                  int maxD, double eps, int side, double* A, double* S, double* B, int cap,
-                  int* nsect_out, int* charge_out, int* dim_out, double* err) {
+                  int maxD, double eps, int side, int method, double* A, double* S, double* B,
+                  int cap, int* nsect_out, int* charge_out, int* dim_out, double* err) {
   FMPT_TRY(check_real(h, dtype));
   if (!x || !A || !S || !B || !nsect_out || !charge_out || !dim_out)
     return set_error(h, FMPT_ERR_ARG, "u1_split: null pointer");
   if (maxD < 1) return set_error(h, FMPT_ERR_SHAPE, "u1_split: maxD must be >= 1");
   if (side != 0 && side != 1) return set_error(h, FMPT_ERR_ARG, "u1_split: side must be 0 or 1");
+  if (method != 0 && method != 1)
+    return set_error(h, FMPT_ERR_ARG, "u1_split: method must be 0 (SVD) or 1 (density matrix)");
   Leg L, R;
   FMPT_TRY(read_leg(h, Vl, L, "left leg"));
   FMPT_TRY(read_leg(h, Vr, R, "right leg"));
@@ -632,22 +814,15 @@ int fmpt_u1_split(fmpt_handle* h, int dtype, const double* x, const fmpt_u1_spac
   const int nl = L.n(), nr = R.n();
   const int64_t Dl = L.total, Dr = R.total;
   // sectors of the new bond: rows (s1, ia) and columns (s2, ib) of each charge
-  struct Seg { int s, i; int64_t off; };
-  struct Sector {
-    int q;
-    std::vector<Seg> rows, cols;
-    int r = 0, c = 0, kq = 0, keep = 0;
-    int64_t moff = 0, uoff = 0, voff = 0, soff = 0;
-  };
   std::vector<int> cand;
   for (int s1 = 0; s1 < d1; s1++)
     for (int ia = 0; ia < nl; ia++) cand.push_back(L.q[ia] + qp1[s1]);
   std::sort(cand.begin(), cand.end());
   cand.erase(std::unique(cand.begin(), cand.end()), cand.end());
-  std::vector<Sector> sec;
+  std::vector<SplitSector> sec;
   int64_t mtot = 0, utot = 0, vtot = 0, stot = 0, wmax = 0;
   for (int qc : cand) {
-    Sector S_;
+    SplitSector S_;
     S_.q = qc;
     for (int s1 = 0; s1 < d1; s1++)
       for (int ia = 0; ia < nl; ia++)
@@ -658,25 +833,23 @@ int fmpt_u1_split(fmpt_handle* h, int dtype, const double* x, const fmpt_u1_spac
     if (S_.r == 0 || S_.c == 0) continue;
     S_.kq = std::min(S_.r, S_.c);
     S_.moff = mtot; mtot += (int64_t)S_.r * S_.c;
-    S_.uoff = utot; utot += (int64_t)S_.r * S_.kq;
-    S_.voff = vtot; vtot += (int64_t)S_.kq * S_.c;
     S_.soff = stot; stot += S_.kq;
-    if (S_.r < S_.c) wmax = std::max(wmax, (int64_t)S_.r * S_.c);
+    if (method == 0) {
+      S_.uoff = utot; utot += (int64_t)S_.r * S_.kq;
+      S_.voff = vtot; vtot += (int64_t)S_.kq * S_.c;
+      if (S_.r < S_.c) wmax = std::max(wmax, (int64_t)S_.r * S_.c);
+    }
     sec.push_back(std::move(S_));
   }
   if (sec.empty()) return set_error(h, FMPT_ERR_SHAPE, "u1_split: no allowed charge sector");
   DevBuf Mw, Uw, Vw, Sw, Tw;
   FMPT_TRY(alloc_scratch(h, Mw, mtot));
-  FMPT_TRY(alloc_scratch(h, Uw, utot));
-  FMPT_TRY(alloc_scratch(h, Vw, vtot));
-  FMPT_TRY(alloc_scratch(h, Sw, stot));
-  FMPT_TRY(alloc_scratch(h, Tw, wmax));
   {  // gather every sector matrix in one launch
     GroupedProgram g;
     gp_phase(g, GP_SUM, FMPT_N, FMPT_N, 0, 0, 1);
-    for (const Sector& S_ : sec)
-      for (const Seg& rs : S_.rows)
-        for (const Seg& cs : S_.cols) {
+    for (const SplitSector& S_ : sec)
+      for (const SplitSeg& rs : S_.rows)
+        for (const SplitSeg& cs : S_.cols) {
           const int64_t xo = pk.at(rs.i, rs.s + d1 * cs.s, cs.i);
           if (xo < 0) return set_error(h, FMPT_ERR_ARG, "u1_split: inconsistent sector table");
           gp_problem(g, S_.moff + rs.off + cs.off * S_.r, S_.r, L.dim[rs.i], R.dim[cs.i]);
@@ -688,29 +861,38 @@ int fmpt_u1_split(fmpt_handle* h, int dtype, const double* x, const fmpt_u1_spac
     double* slots[2] = {const_cast<double*>(x), Mw.d()};
     FMPT_TRY(gp_run(h, g, slots, 2));
   }
-  // per-sector FP64 SVD on the device
-  for (const Sector& S_ : sec) {
-    double* Mq = Mw.d() + S_.moff;
-    double* Uq = Uw.d() + S_.uoff;
-    double* Vq = Vw.d() + S_.voff;
-    double* Sq = Sw.d() + S_.soff;
-    if (S_.r >= S_.c) {
-      FMPT_TRY(svd_tall(h, 0, S_.r, S_.c, Mq, Sq, Uq, Vq));
-    } else {
-      // M^T (c x r) = U' S VT'  ->  M = VT'^T S U'^T
-      DevBuf U2, V2;
-      FMPT_TRY(alloc_scratch(h, U2, (int64_t)S_.c * S_.r));
-      FMPT_TRY(alloc_scratch(h, V2, (int64_t)S_.r * S_.r));
-      FMPT_TRY(copy_mat(h, 0, S_.c, S_.r, Mq, S_.r, 0, 1, 0, Tw.d(), S_.c, 0));
-      FMPT_TRY(svd_tall(h, 0, S_.c, S_.r, Tw.d(), Sq, U2.d(), V2.d()));
-      FMPT_TRY(copy_mat(h, 0, S_.r, S_.r, V2.d(), S_.r, 0, 1, 0, Uq, S_.r, 0));
-      FMPT_TRY(copy_mat(h, 0, S_.r, S_.c, U2.d(), S_.c, 0, 1, 0, Vq, S_.kq, 0));
+  std::vector<double> sv(stot, 0.0);
+  DevBuf Gw;   // density-matrix form: Gram matrices, then their eigenvectors
+  if (method == 0) {
+    // per-sector FP64 SVD on the device
+    FMPT_TRY(alloc_scratch(h, Uw, utot));
+    FMPT_TRY(alloc_scratch(h, Vw, vtot));
+    FMPT_TRY(alloc_scratch(h, Sw, stot));
+    FMPT_TRY(alloc_scratch(h, Tw, wmax));
+    for (const SplitSector& S_ : sec) {
+      double* Mq = Mw.d() + S_.moff;
+      double* Uq = Uw.d() + S_.uoff;
+      double* Vq = Vw.d() + S_.voff;
+      double* Sq = Sw.d() + S_.soff;
+      if (S_.r >= S_.c) {
+        FMPT_TRY(svd_tall(h, 0, S_.r, S_.c, Mq, Sq, Uq, Vq));
+      } else {
+        // M^T (c x r) = U' S VT'  ->  M = VT'^T S U'^T
+        DevBuf U2, V2;
+        FMPT_TRY(alloc_scratch(h, U2, (int64_t)S_.c * S_.r));
+        FMPT_TRY(alloc_scratch(h, V2, (int64_t)S_.r * S_.r));
+        FMPT_TRY(copy_mat(h, 0, S_.c, S_.r, Mq, S_.r, 0, 1, 0, Tw.d(), S_.c, 0));
+        FMPT_TRY(svd_tall(h, 0, S_.c, S_.r, Tw.d(), Sq, U2.d(), V2.d()));
+        FMPT_TRY(copy_mat(h, 0, S_.r, S_.r, V2.d(), S_.r, 0, 1, 0, Uq, S_.r, 0));
+        FMPT_TRY(copy_mat(h, 0, S_.r, S_.c, U2.d(), S_.c, 0, 1, 0, Vq, S_.kq, 0));
+      }
     }
+    FMPT_CUDA(h, cudaMemcpyAsync(sv.data(), Sw.d(), stot * sizeof(double),
+                                 cudaMemcpyDeviceToHost, h->stream));
+    FMPT_CUDA(h, cudaStreamSynchronize(h->stream));
+  } else {
+    FMPT_TRY(density_eigen(h, side, sec, Mw.d(), mtot, Gw, sv));
   }
-  std::vector<double> sv(stot);
-  FMPT_CUDA(h, cudaMemcpyAsync(sv.data(), Sw.d(), stot * sizeof(double), cudaMemcpyDeviceToHost,
-                               h->stream));
-  FMPT_CUDA(h, cudaStreamSynchronize(h->stream));
   FMPT_TRY(gp_check_status(h));
   // truncation across sectors (MPSTruncation: cutoff relative to the norm, then dimension)
   double nrm2 = 0.0;
@@ -721,7 +903,7 @@ int fmpt_u1_split(fmpt_handle* h, int dtype, const double* x, const fmpt_u1_spac
   for (int si = 0; si < (int)sec.size(); si++)
     for (int i = 0; i < sec[si].kq; i++) {
       const double v = sv[sec[si].soff + i];
-      if (v >= eps * nrm) kept.push_back({v, si, i});
+      if (v >= eps * nrm && (method == 0 || v > 0.0)) kept.push_back({v, si, i});
     }
   std::stable_sort(kept.begin(), kept.end(), [](const Val& a, const Val& b) {
     if (a.v != b.v) return a.v > b.v;
@@ -731,7 +913,7 @@ int fmpt_u1_split(fmpt_handle* h, int dtype, const double* x, const fmpt_u1_spac
   if ((int)kept.size() > maxD) kept.resize(maxD);
   for (const Val& v : kept) sec[v.sec].keep = std::max(sec[v.sec].keep, v.idx + 1);
   double kept2 = 0.0, drop2 = 0.0;
-  for (const Sector& S_ : sec)
+  for (const SplitSector& S_ : sec)
     for (int i = 0; i < S_.kq; i++) {
       const double v2 = sv[S_.soff + i] * sv[S_.soff + i];
       if (i < S_.keep) kept2 += v2; else drop2 += v2;
@@ -753,52 +935,117 @@ int fmpt_u1_split(fmpt_handle* h, int dtype, const double* x, const fmpt_u1_spac
     ns++;
   }
   *nsect_out = ns;
-  // normalised sigma, zero past the kept prefix; scale the factor that carries s
   std::vector<double> sn(stot, 0.0), skept;
-  for (const Sector& S_ : sec)
+  for (const SplitSector& S_ : sec)
     for (int i = 0; i < S_.keep; i++) {
       sn[S_.soff + i] = sv[S_.soff + i] / knorm;
       skept.push_back(sn[S_.soff + i]);
     }
-  FMPT_CUDA(h, cudaMemcpyAsync(Sw.d(), sn.data(), stot * sizeof(double), cudaMemcpyHostToDevice,
-                               h->stream));
   FMPT_CUDA(h, cudaMemcpyAsync(S, skept.data(), skept.size() * sizeof(double),
                                cudaMemcpyHostToDevice, h->stream));
-  for (const Sector& S_ : sec) {
-    if (S_.keep == 0) continue;
-    if (side == 0)
-      FMPT_TRY(fmpt_scale_dim(h, FMPT_F64, 0, S_.kq, S_.c, Sw.d() + S_.soff, Vw.d() + S_.voff));
-    else
-      FMPT_TRY(fmpt_scale_dim(h, FMPT_F64, 1, S_.r, S_.kq, Sw.d() + S_.soff, Uw.d() + S_.uoff));
-  }
-  // scatter the kept columns of U into A[a, s1, m] and rows of V into B[m, s2, b]
   FMPT_CUDA(h, cudaMemsetAsync(A, 0, (size_t)Dl * d1 * Dm * sizeof(double), h->stream));
   FMPT_CUDA(h, cudaMemsetAsync(B, 0, (size_t)Dm * d2 * Dr * sizeof(double), h->stream));
   GroupedProgram g;
-  gp_phase(g, GP_SUM, FMPT_N, FMPT_N, 0, 0, 2);
-  for (size_t si = 0; si < sec.size(); si++) {
-    const Sector& S_ = sec[si];
-    if (S_.keep == 0) continue;
-    for (const Seg& rs : S_.rows) {
-      gp_problem(g, L.off[rs.i] + Dl * rs.s + Dl * d1 * moff2[si], Dl * d1, L.dim[rs.i], S_.keep);
-      gp_segment(g, S_.uoff + rs.off, S_.r, 0, 0, 0, 1.0);
+  if (method == 0) {
+    // normalised sigma (zero past the kept prefix) into the factor that carries s
+    FMPT_CUDA(h, cudaMemcpyAsync(Sw.d(), sn.data(), stot * sizeof(double),
+                                 cudaMemcpyHostToDevice, h->stream));
+    for (const SplitSector& S_ : sec) {
+      if (S_.keep == 0) continue;
+      if (side == 0)
+        FMPT_TRY(fmpt_scale_dim(h, FMPT_F64, 0, S_.kq, S_.c, Sw.d() + S_.soff, Vw.d() + S_.voff));
+      else
+        FMPT_TRY(fmpt_scale_dim(h, FMPT_F64, 1, S_.r, S_.kq, Sw.d() + S_.soff, Uw.d() + S_.uoff));
     }
-  }
-  gp_phase(g, GP_SUM, FMPT_N, FMPT_N, 1, 1, 3);
-  for (size_t si = 0; si < sec.size(); si++) {
-    const Sector& S_ = sec[si];
-    if (S_.keep == 0) continue;
-    for (const Seg& cs : S_.cols) {
-      gp_problem(g, moff2[si] + Dm * cs.s + Dm * d2 * R.off[cs.i], Dm * d2, S_.keep, R.dim[cs.i]);
-      gp_segment(g, S_.voff + cs.off * S_.kq, S_.kq, 0, 0, 0, 1.0);
+    // scatter the kept columns of U into A[a, s1, m] and rows of V into B[m, s2, b]
+    gp_phase(g, GP_SUM, FMPT_N, FMPT_N, 0, 0, 2);
+    for (size_t si = 0; si < sec.size(); si++) {
+      const SplitSector& S_ = sec[si];
+      if (S_.keep == 0) continue;
+      for (const SplitSeg& rs : S_.rows) {
+        gp_problem(g, L.off[rs.i] + Dl * rs.s + Dl * d1 * moff2[si], Dl * d1, L.dim[rs.i], S_.keep);
+        gp_segment(g, S_.uoff + rs.off, S_.r, 0, 0, 0, 1.0);
+      }
     }
+    gp_phase(g, GP_SUM, FMPT_N, FMPT_N, 1, 1, 3);
+    for (size_t si = 0; si < sec.size(); si++) {
+      const SplitSector& S_ = sec[si];
+      if (S_.keep == 0) continue;
+      for (const SplitSeg& cs : S_.cols) {
+        gp_problem(g, moff2[si] + Dm * cs.s + Dm * d2 * R.off[cs.i], Dm * d2, S_.keep, R.dim[cs.i]);
+        gp_segment(g, S_.voff + cs.off * S_.kq, S_.kq, 0, 0, 0, 1.0);
+      }
+    }
+    gp_slot(g, 0, utot);
+    gp_slot(g, 1, vtot);
+  } else {
+    // Q: the kept eigenvectors (largest first), n x keep per sector, contiguous
+    int64_t qtot = 0;
+    std::vector<int64_t> qoff(sec.size(), 0);
+    for (size_t si = 0; si < sec.size(); si++) {
+      qoff[si] = qtot;
+      qtot += (int64_t)sec[si].n * sec[si].keep;
+    }
+    FMPT_TRY(alloc_scratch(h, Uw, qtot));
+    for (size_t si = 0; si < sec.size(); si++) {
+      const SplitSector& S_ = sec[si];
+      if (S_.keep == 0) continue;
+      FMPT_TRY(copy_mat(h, 0, S_.n, S_.keep, Gw.d() + S_.goff + (int64_t)(S_.npad - 1) * S_.npad,
+                        -(int64_t)S_.npad, 0, 0, 0, Uw.d() + qoff[si], S_.n, 0));
+    }
+    const double inv = 1.0 / knorm;
+    if (side == 0) {
+      // A = U (isometric); B = U^T M / ||s_kept|| (= normalised s * v)
+      gp_phase(g, GP_SUM, FMPT_N, FMPT_N, 0, 0, 2);
+      for (size_t si = 0; si < sec.size(); si++) {
+        const SplitSector& S_ = sec[si];
+        if (S_.keep == 0) continue;
+        for (const SplitSeg& rs : S_.rows) {
+          gp_problem(g, L.off[rs.i] + Dl * rs.s + Dl * d1 * moff2[si], Dl * d1, L.dim[rs.i],
+                     S_.keep);
+          gp_segment(g, qoff[si] + rs.off, S_.r, 0, 0, 0, 1.0);
+        }
+      }
+      gp_phase(g, GP_GEMM, FMPT_T, FMPT_N, 0, 1, 3);
+      for (size_t si = 0; si < sec.size(); si++) {
+        const SplitSector& S_ = sec[si];
+        if (S_.keep == 0) continue;
+        for (const SplitSeg& cs : S_.cols) {
+          gp_problem(g, moff2[si] + Dm * cs.s + Dm * d2 * R.off[cs.i], Dm * d2, S_.keep,
+                     R.dim[cs.i]);
+          gp_segment(g, qoff[si], S_.r, S_.moff + cs.off * S_.r, S_.r, S_.r, inv);
+        }
+      }
+    } else {
+      // B = V^T (isometric rows); A = M V / ||s_kept|| (= u * normalised s)
+      gp_phase(g, GP_SUM, FMPT_T, FMPT_N, 0, 0, 3);
+      for (size_t si = 0; si < sec.size(); si++) {
+        const SplitSector& S_ = sec[si];
+        if (S_.keep == 0) continue;
+        for (const SplitSeg& cs : S_.cols) {
+          gp_problem(g, moff2[si] + Dm * cs.s + Dm * d2 * R.off[cs.i], Dm * d2, S_.keep,
+                     R.dim[cs.i]);
+          gp_segment(g, qoff[si] + cs.off, S_.c, 0, 0, 0, 1.0);
+        }
+      }
+      gp_phase(g, GP_GEMM, FMPT_N, FMPT_N, 1, 0, 2);
+      for (size_t si = 0; si < sec.size(); si++) {
+        const SplitSector& S_ = sec[si];
+        if (S_.keep == 0) continue;
+        for (const SplitSeg& rs : S_.rows) {
+          gp_problem(g, L.off[rs.i] + Dl * rs.s + Dl * d1 * moff2[si], Dl * d1, L.dim[rs.i],
+                     S_.keep);
+          gp_segment(g, S_.moff + rs.off, S_.r, qoff[si], S_.c, S_.c, inv);
+        }
+      }
+    }
+    gp_slot(g, 0, qtot);
+    gp_slot(g, 1, mtot);
   }
-  gp_slot(g, 0, utot);
-  gp_slot(g, 1, vtot);
   gp_slot(g, 2, Dl * d1 * Dm);
   gp_slot(g, 3, Dm * d2 * Dr);
   FMPT_TRY(gp_finalize(h, g));
-  double* slots[4] = {Uw.d(), Vw.d(), A, B};
+  double* slots[4] = {Uw.d(), method == 0 ? Vw.d() : Mw.d(), A, B};
   FMPT_TRY(gp_run(h, g, slots, 4));
   // host vectors above were staged by the (pageable) copies; the scratch
   // buffers are stream-ordered, so nothing else needs to wait here

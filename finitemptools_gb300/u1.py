@@ -228,7 +228,7 @@ def random_u1_tensors(L, N, D, qphys=(0, 1), rng=None):
     return tensors, spaces
 
 
-def u1_randommps(L, N, D, qphys=(0, 1), rng=None, handle=None, canonical=True):
+def u1_randommps(L, N, D, qphys=(0, 1), rng=None, handle=None, canonical=True, method="dm"):
     """randommps with U1Space legs and total charge N, right-canonicalised and
     normalised (canonicalize!(normalize=true), mps/orth.jl:40-49) by exact
     two-site splits from the right."""
@@ -236,19 +236,20 @@ def u1_randommps(L, N, D, qphys=(0, 1), rng=None, handle=None, canonical=True):
     tensors, spaces = random_u1_tensors(L, N, D, qphys, rng)
     psi = U1FiniteMPS([DeviceTensor.from_numpy(A, handle) for A in tensors], spaces, qphys)
     if canonical:
-        u1_right_canonicalize_(psi)
+        u1_right_canonicalize_(psi, method)
     return psi
 
 
-def u1_right_canonicalize_(psi):
-    """Right-canonical form through exact two-site splits (side 1), sweeping
-    from the right; the last split normalises the state."""
+def u1_right_canonicalize_(psi, method="dm"):
+    """Right-canonical form through two-site splits (side 1) that keep every
+    nonzero singular value, sweeping from the right; the last split
+    normalises the state.  ``method`` as in u1_split."""
     L = len(psi)
     for i in range(L - 1, 0, -1):
         Vl, Vm, Vr = psi.spaces[i], psi.spaces[i + 1], psi.spaces[i + 2]
         x = u1_twosite(psi[i], psi[i + 1], Vl, Vm, Vr, psi.qphys, psi.qphys)
         trunc = MPSTruncation(Vm.dim, 1e-14)
-        A, S, B, Vnew, _ = u1_split(x, Vl, Vr, psi.qphys, psi.qphys, trunc, side=1)
+        A, S, B, Vnew, _ = u1_split(x, Vl, Vr, psi.qphys, psi.qphys, trunc, 1, method)
         psi.set_site(i + 1, B, left=Vnew)
         psi.set_site(i, A)
         psi.s[i + 1] = S
@@ -303,10 +304,13 @@ def u1_unpack2(x, Vl, Vr, qp1, qp2):
     return X
 
 
-def u1_split(x, Vl, Vr, qp1, qp2, trunc, side):
+def u1_split(x, Vl, Vr, qp1, qp2, trunc, side, method="gesvd"):
     """Truncated, normalised two-site split (stable_tsvd! + normalize!(s) of
-    DMRG2 with TensorKit's cross-sector truncation).  Returns
-    (A [Dl, d1, Dm], S [Dm], B [Dm, d2, Dr], Vm, err)."""
+    DMRG2 with TensorKit's cross-sector truncation).  ``method`` "gesvd": an
+    SVD per sector; "dm": the density-matrix form (batched eigensolves, see
+    include/fmpt.h).  Returns (A [Dl, d1, Dm], S [Dm], B [Dm, d2, Dr], Vm, err)."""
+    if method not in ("gesvd", "dm"):
+        raise ValueError("method must be 'gesvd' or 'dm'")
     h = x.h
     d1, q1 = _phys(qp1)
     d2, q2 = _phys(qp2)
@@ -320,7 +324,8 @@ def u1_split(x, Vl, Vr, qp1, qp2, trunc, side):
     do = (ctypes.c_int * cap)()
     err = ctypes.c_double()
     h.check(lib().fmpt_u1_split(h.ptr, F64, x.ptr, Vl.ref, Vr.ref, d1, q1, d2, q2, int(trunc.D),
-                                float(trunc.eps), int(side), A.ptr, S.ptr, B.ptr, cap,
+                                float(trunc.eps), int(side), 0 if method == "gesvd" else 1,
+                                A.ptr, S.ptr, B.ptr, cap,
                                 ctypes.byref(ns), qo, do, ctypes.byref(err)))
     Vm = U1Space([(qo[i], do[i]) for i in range(ns.value)])
     A.view_as((Vl.dim, d1, Vm.dim))
@@ -487,7 +492,7 @@ def _u1_bond(m, site, alg, side):
                   m.qw[site], m.qw[site + 1], m.qw[site + 2])
     E, vecs, info, k = op.lanczos(x2, alg.eig_maxiter, alg.eig_tol, alg.reorth)
     del op
-    A, S, B, Vnew, err = u1_split(vecs, Vl, Vr, qp, qp, alg.trunc, side)
+    A, S, B, Vnew, err = u1_split(vecs, Vl, Vr, qp, qp, alg.trunc, side, alg.svd)
     usv = u1_twosite(A, B, Vl, Vnew, Vr, qp, qp)
     delta = abs(1 - abs(dot(usv, x2)))      # dmrg.jl:109-110
     del usv
@@ -505,8 +510,10 @@ def _u1_bond(m, site, alg, side):
 
 
 def _check_alg(alg):
-    if getattr(alg, "precision", "fp64") != "fp64" or getattr(alg, "svd", "gesvd") != "gesvd":
-        raise ValueError("the U(1) path runs the FP64 contractions and the sector SVD only")
+    if getattr(alg, "precision", "fp64") != "fp64":
+        raise ValueError("the U(1) path runs its contractions in FP64")
+    if getattr(alg, "svd", "gesvd") not in ("gesvd", "dm"):
+        raise ValueError("U(1) split: svd must be 'gesvd' or 'dm'")
 
 
 def u1_leftsweep_(m, alg):

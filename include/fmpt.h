@@ -304,11 +304,18 @@ int fmpt_u1_updateright(fmpt_handle* h, int dtype, const double* hold, const dou
  * isometry).  A is [Dl, d1, Dm'] and B [Dm', d2, Dr] in the new sorted basis,
  * written in full; size them for Dm' <= min(maxD, Dl*d1, d2*Dr).  HOST
  * outputs: the new leg (nsect_out sectors into charge_out/dim_out, capacity
- * cap) and err (2-norm of the dropped sigma before normalisation). */
+ * cap) and err (2-norm of the dropped sigma before normalisation).
+ * method 0: an SVD per sector (gesvd, gesvdj fallback: the reference's
+ * stable_tsvd!).  method 1: the density-matrix form of fmpt_dm_split for
+ * every sector at once -- all Gram matrices in one grouped launch, one
+ * batched FP64 eigensolve per padded size; the isometric side is the exact
+ * eigenvector set and the other factor a product with x (no division by
+ * sigma); sigma below ~1e-8*sigma_max is resolved only to the FP64 noise of
+ * the Gram matrix.  No counterpart in the reference. */
 int fmpt_u1_split(fmpt_handle* h, int dtype, const double* x, const fmpt_u1_space* Vl,
                   const fmpt_u1_space* Vr, int d1, const int* qp1, int d2, const int* qp2,
-                  int maxD, double eps, int side, double* A, double* S, double* B, int cap,
-                  int* nsect_out, int* charge_out, int* dim_out, double* err);
+                  int maxD, double eps, int side, int method, double* A, double* S, double* B,
+                  int cap, int* nsect_out, int* charge_out, int* dim_out, double* err);
 
 #ifdef __cplusplus
 }

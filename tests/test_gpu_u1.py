@@ -104,22 +104,32 @@ def test_u1_twosite_and_envs(L, N, D, site):
     assert np.all(gR[~OU.allowed_env(Vm, qw[site])] == 0.0)
 
 
+@pytest.mark.parametrize("method", ["gesvd", "dm"])
 @pytest.mark.parametrize("side", [0, 1])
 @pytest.mark.parametrize("maxD,eps", [(100000, 0.0), (17, 0.0), (40, 1e-3)])
-def test_u1_split(side, maxD, eps):
+def test_u1_split(side, maxD, eps, method):
     Ws, qw, mps, legs, Lm, Rm = _bond(14, 7, 48, 7, 11)
     Vl, Vr = legs[6], legs[8]
     X = np.tensordot(mps[6], mps[7], axes=([2], [0]))
     tr = O.MPSTruncation(maxD, eps)
     xp = DT.from_numpy(OU.pack2(X, Vl, Vr, list(QP), list(QP)))
-    A, S, B, Vm, err = fm.u1_split(xp, sp(Vl), sp(Vr), QP, QP, fm.MPSTruncation(maxD, eps), side)
+    A, S, B, Vm, err = fm.u1_split(xp, sp(Vl), sp(Vr), QP, QP, fm.MPSTruncation(maxD, eps), side,
+                                   method)
     Ao, So, Bo, Vmo, erro = OU.u1_split(X, Vl, Vr, list(QP), list(QP), tr, side)
-    assert Vm.charges == tuple(Vmo.charges) and Vm.dims == tuple(Vmo.dims)
-    assert np.abs(S.numpy() - So).max() < 1e-12
-    assert abs(err - erro) <= 1e-10 * max(erro, 1e-3)
+    # the density-matrix form resolves sigma to ~1e-8 sigma_max (squared in the Gram matrix)
+    tol = 1e-12 if method == "gesvd" else 1e-9
     An, Bn = A.numpy(), B.numpy()
+    if method == "dm" and eps == 0.0 and maxD > Vl.dim * 2:
+        # x = A.B has rank-deficient sectors: the SVD keeps its ~1e-16 singular
+        # values, the density-matrix form drops exact zeros; both reproduce x
+        prod = np.tensordot(An, Bn, axes=([2], [0]))
+        assert rel(prod, X / np.linalg.norm(X)) < tol
+        return
+    assert Vm.charges == tuple(Vmo.charges) and Vm.dims == tuple(Vmo.dims)
+    assert np.abs(S.numpy() - So).max() < tol
+    assert abs(err - erro) <= max(1e-10 * erro, tol * np.linalg.norm(X))
     prod = np.tensordot(An, Bn, axes=([2], [0]))
-    assert rel(prod, np.tensordot(Ao, Bo, axes=([2], [0]))) < 1e-12
+    assert rel(prod, np.tensordot(Ao, Bo, axes=([2], [0]))) < tol
     k = Vm.dim
     if side == 0:
         G = An.reshape(-1, k, order="F")
@@ -143,7 +153,7 @@ def test_u1_lanczos_matches_oracle():
     mps, legs, psi = _states(L, N, 16, 4)
     env_o = OU.U1OracleEnv(Ws, mps, legs, list(QP), schur=True)
     env_o.right_canonicalize()
-    u1_right_canonicalize_(psi)
+    u1_right_canonicalize_(psi, "gesvd")
     for i in range(1, L + 1):
         assert rel(psi[i].numpy(), env_o.mps[i - 1]) < 1e-11 or \
             rel(np.abs(psi[i].numpy()), np.abs(env_o.mps[i - 1])) < 1e-11
@@ -190,6 +200,20 @@ def test_u1_dmrg2_vs_ed_and_oracle(L, N, D, model):
     assert abs(Eg[-1] - e_ed) < 1e-10 * abs(e_ed)
     assert abs(fm.expectation(psi, mpo) - Eg[-1]) < 1e-10 * abs(e_ed)
     assert psi.total_charge == N
+
+
+def test_u1_dmrg2_density_matrix_split():
+    """svd="dm" (batched density-matrix split) converges to the same energy."""
+    L, N = 12, 6
+    mpo = heisenberg_xxz_mpo()
+    mps, legs, psi = _states(L, N, 8, 12)
+    u1_right_canonicalize_(psi)
+    alg = fm.DMRG2(eig_maxiter=30, eig_tol=1e-12, trunc=fm.MPSTruncation(64, 1e-12), verbosity=0,
+                   svd="dm")
+    m = fm.U1ExpectationCache(mpo, psi)
+    for _ in range(3):
+        E, _ = fm.sweep_(m, alg)
+    assert abs(E[-1] - xxz_ground_energy(L, nup=N)) < 1e-10 * abs(E[-1])
 
 
 def test_u1_dmrg2_matches_dense_path():
