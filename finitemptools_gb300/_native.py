@@ -43,6 +43,8 @@ SIGNATURES = {
     "fmpt_status_string": (c_char_p, [c_int]),
     "fmpt_last_error": (c_char_p, [c_void_p]),
     "fmpt_synchronize": (c_int, [c_void_p]),
+    "fmpt_set_graphs": (c_int, [c_void_p, c_int]),
+    "fmpt_graph_launch_count": (c_uint64, [c_void_p]),
     "fmpt_set_stream": (c_int, [c_void_p, c_void_p]),
     "fmpt_get_stream": (c_void_p, [c_void_p]),
     "fmpt_launch_count": (c_uint64, [c_void_p]),

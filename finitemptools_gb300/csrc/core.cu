@@ -39,6 +39,9 @@ static cudaEvent_t pool_event(fmpt_handle* h) {
 
 ProfScope::ProfScope(fmpt_handle* hh, int c) : h(hh), cls(c) {
   if (!h || !h->prof) return;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(h->stream, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone)
+    return;   // no timers inside a graph capture
   b = pool_event(h);
   e = pool_event(h);
   cudaEventRecord(b, h->stream);
@@ -326,6 +329,7 @@ int fmpt_destroy(fmpt_handle* h) {
   for (auto sv : h->aux_solver) cusolverDnDestroy(sv);
   for (auto st : h->aux_stream) cudaStreamDestroy(st);
   for (auto ev : h->aux_event) cudaEventDestroy(ev);
+  if (h->lanczos_exec) cudaGraphExecDestroy(h->lanczos_exec);
   if (h->gstatus) cudaFree(h->gstatus);
   if (h->pinned) cudaFreeHost(h->pinned);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
@@ -334,6 +338,14 @@ int fmpt_destroy(fmpt_handle* h) {
 }
 
 const char* fmpt_last_error(fmpt_handle* h) { return h ? h->err.c_str() : "null handle"; }
+
+uint64_t fmpt_graph_launch_count(fmpt_handle* h) { return h ? h->graph_launches : 0; }
+
+int fmpt_set_graphs(fmpt_handle* h, int on) {
+  if (!h) return FMPT_ERR_ARG;
+  h->graphs = on != 0;
+  return FMPT_OK;
+}
 
 int fmpt_synchronize(fmpt_handle* h) {
   if (!h) return FMPT_ERR_ARG;

@@ -40,6 +40,7 @@ struct GKArgs {
   const int* tile_mn;
   int* ctl;        // [0, GP_MAX_PHASES) tile counters, then barrier count, then abort flag
   int* status;     // handle status word (1 = a bounded wait gave up)
+  const int* gate; // nonzero at launch: return at once (nullptr: always run)
 };
 
 __device__ __forceinline__ int64_t op_index(int t, int r, int c, int64_t ld) {
@@ -165,6 +166,7 @@ __global__ void __launch_bounds__(GNT) grouped_kernel(const GKArgs a) {
   __shared__ double As[GK][GT + 1];
   __shared__ double Bs[GK][GT + 1];
   __shared__ int s_tile, s_flag;
+  if (a.gate && *a.gate) return;   // uniform for the whole grid: set before the launch
   for (int p = 0; p < a.nphase; p++) {
     if (p > 0 && !grid_barrier(a, p * (int)gridDim.x, &s_flag)) return;
     const GPhaseDesc ph = a.ph[p];
@@ -362,11 +364,12 @@ int gp_status_word(fmpt_handle* h, int** out) {
 
 int gp_check_status(fmpt_handle* h) {
   if (!h->gstatus) return FMPT_OK;
-  FMPT_TRY(ensure_pinned(h, 1));
-  int* pin = reinterpret_cast<int*>(h->pinned);
-  FMPT_CUDA(h, cudaMemcpyAsync(pin, h->gstatus, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  // a local word (not the shared pinned staging buffer, which callers may
+  // still be reading from)
+  int v = 0;
+  FMPT_CUDA(h, cudaMemcpyAsync(&v, h->gstatus, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
   FMPT_CUDA(h, cudaStreamSynchronize(h->stream));
-  if (*pin != 0) {
+  if (v != 0) {
     FMPT_CUDA(h, cudaMemsetAsync(h->gstatus, 0, sizeof(int), h->stream));
     return set_error(h, FMPT_ERR_TIMEOUT,
                      "grouped block-sparse launch: a grid barrier timed out (results invalid)");
@@ -374,7 +377,14 @@ int gp_check_status(fmpt_handle* h) {
   return FMPT_OK;
 }
 
-int gp_run(fmpt_handle* h, const GroupedProgram& g, double* const* slots, int nslots) {
+int gp_prepare(fmpt_handle* h) {
+  int* st = nullptr;
+  FMPT_TRY(gp_status_word(h, &st));
+  return kernel_occupancy(h) > 0 ? FMPT_OK : FMPT_ERR_CUDA;
+}
+
+int gp_run(fmpt_handle* h, const GroupedProgram& g, double* const* slots, int nslots,
+           const int* gate) {
   if (!g.ready) return set_error(h, FMPT_ERR_ARG, "grouped: program not finalised");
   if (g.tile_prob.empty()) return FMPT_OK;
   GKArgs a{};
@@ -390,6 +400,7 @@ int gp_run(fmpt_handle* h, const GroupedProgram& g, double* const* slots, int ns
   a.probs = g.d_probs; a.segs = g.d_segs;
   a.tile_prob = g.d_tile_prob; a.tile_mn = g.d_tile_mn;
   a.ctl = g.d_ctl;
+  a.gate = gate;
   FMPT_TRY(gp_status_word(h, &a.status));
   FMPT_CUDA(h, cudaMemsetAsync(g.d_ctl, 0, (GP_MAX_PHASES + 2) * sizeof(int), h->stream));
   ProfScope prof(h, FMPT_K_GROUPED);

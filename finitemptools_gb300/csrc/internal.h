@@ -34,6 +34,10 @@ struct fmpt_handle {
   std::vector<cudaStream_t> aux_stream;
   std::vector<cusolverDnHandle_t> aux_solver;
   std::vector<cudaEvent_t> aux_event;   // [0] fork, [1 + i] join of aux stream i
+  // CUDA graphs for the Krylov solvers of block-sparse operators (fmpt_set_graphs)
+  bool graphs = true;
+  cudaGraphExec_t lanczos_exec = nullptr;   // reused through cudaGraphExecUpdate
+  uint64_t graph_launches = 0;
 };
 
 namespace fmpt {
@@ -182,7 +186,11 @@ void gp_segment(GroupedProgram& g, int64_t a_off, int64_t lda, int64_t b_off, in
 // block footprint against it (host side, before anything reaches the GPU).
 void gp_slot(GroupedProgram& g, int slot, int64_t elems);
 int gp_finalize(fmpt_handle* h, GroupedProgram& g);   // bounds check + tiles + upload
-int gp_run(fmpt_handle* h, const GroupedProgram& g, double* const* slots, int nslots);
+// gate: optional device flag; when it is nonzero at launch time every CTA
+// returns at once (a solver step after convergence inside a CUDA graph)
+int gp_run(fmpt_handle* h, const GroupedProgram& g, double* const* slots, int nslots,
+           const int* gate = nullptr);
+int gp_prepare(fmpt_handle* h);   // allocations gp_run needs, done before a stream capture
 int gp_check_status(fmpt_handle* h);                  // synchronises; FMPT_ERR_TIMEOUT if set
 
 // -------- dense helpers shared with the sector code (linalg.cu)
@@ -223,7 +231,7 @@ int env_update_tc(fmpt_handle* h, bool right, int precision, const double* hold,
                   const double* W, const double* B, double* hnew, int Dl, int d, int Dr, int wl,
                   int wr);
 void op_tc_free(fmpt_op* op);
-int op_u1_apply(fmpt_op* op, const double* x, double* y);
+int op_u1_apply(fmpt_op* op, const double* x, double* y, const int* gate = nullptr);
 void op_u1_free(fmpt_op* op);
 
 // K-major tensor-core operand: TF32 (float storage) or BF16 plane, optional

@@ -50,7 +50,8 @@ __device__ double sum_parts(const double* part, int G) {
 
 // part[b] = sum x*y over a grid-stride slice (real view of length n)
 __global__ void rdot_partial(int64_t n, const double* __restrict__ x, const double* __restrict__ y,
-                             double* __restrict__ part) {
+                             double* __restrict__ part, const int* gate = nullptr) {
+  if (gate && *gate) return;
   double s = 0.0;
   for (int64_t i = (int64_t)blockIdx.x * KT + threadIdx.x; i < n; i += (int64_t)gridDim.x * KT)
     s = fma(x[i], y[i], s);
@@ -72,7 +73,8 @@ __global__ void normalize_from_parts(int64_t n, const double* __restrict__ v, do
 __global__ void lanczos_axpy(int64_t n, double* __restrict__ y, const double* __restrict__ q,
                              const double* __restrict__ qm1, const double* __restrict__ part_a,
                              int G, const double* b_old, double* alpha_out,
-                             double* __restrict__ part_b) {
+                             double* __restrict__ part_b, const int* gate = nullptr) {
+  if (gate && *gate) return;
   const double a = sum_parts(part_a, G);
   const double b = (qm1 != nullptr) ? *b_old : 0.0;
   if (blockIdx.x == 0 && threadIdx.x == 0) *alpha_out = a;
@@ -104,7 +106,8 @@ __global__ void lanczos_scale(int64_t n, double* __restrict__ y, const double* _
 // partial dots h_i = <V_i, z> ; part layout [G][j][2]
 __global__ void multidot_partial(int cplx, int64_t n, int j, const double* __restrict__ V,
                                  int64_t vstride, const double* __restrict__ z,
-                                 double* __restrict__ part) {
+                                 double* __restrict__ part, const int* gate = nullptr) {
+  if (gate && *gate) return;
   for (int i = 0; i < j; i++) {
     const double* v = V + (int64_t)i * vstride;
     double sr = 0.0, si = 0.0;
@@ -129,7 +132,9 @@ __global__ void multidot_partial(int cplx, int64_t n, int j, const double* __res
 
 // coef[i] (re, im) = sum over G partials; written by one block
 __global__ void multidot_finalize(int j, int G, const double* __restrict__ part,
-                                  double* __restrict__ coef, double* __restrict__ accum) {
+                                  double* __restrict__ coef, double* __restrict__ accum,
+                                  const int* gate = nullptr) {
+  if (gate && *gate) return;
   for (int i = 0; i < j; i++) {
     double sr = 0.0, si = 0.0;
     for (int g = threadIdx.x; g < G; g += KT) {
@@ -149,7 +154,9 @@ __global__ void multidot_finalize(int j, int G, const double* __restrict__ part,
 // z -= sum_i coef_i V_i ; part = partial |z|^2
 __global__ void multi_axpy_sub(int cplx, int64_t n, int j, const double* __restrict__ V,
                                int64_t vstride, const double* __restrict__ coef,
-                               double* __restrict__ z, double* __restrict__ part) {
+                               double* __restrict__ z, double* __restrict__ part,
+                               const int* gate = nullptr) {
+  if (gate && *gate) return;
   double s = 0.0;
   for (int64_t e = (int64_t)blockIdx.x * KT + threadIdx.x; e < n; e += (int64_t)gridDim.x * KT) {
     double zr = z[e], zi = cplx ? z[n + e] : 0.0;
@@ -177,7 +184,9 @@ __global__ void multi_axpy_sub(int cplx, int64_t n, int j, const double* __restr
 // out = sum_i c_i V_i (c complex when cplx, real otherwise); scale multiplies
 __global__ void combine_basis(int cplx, int64_t n, int j, const double* __restrict__ V,
                               int64_t vstride, const double* __restrict__ c, int cstride,
-                              double scale, int last_first, double* __restrict__ out) {
+                              double scale, int last_first, double* __restrict__ out,
+                              const int* j_dev = nullptr) {
+  if (j_dev) j = *j_dev;
   for (int64_t e = (int64_t)blockIdx.x * KT + threadIdx.x; e < n; e += (int64_t)gridDim.x * KT) {
     double r = 0.0, im = 0.0;
     // lanczos_linear_transformation_single (simple_lanczos.jl:70-78) adds the
@@ -235,10 +244,9 @@ __global__ void scale_by(int64_t n, double* __restrict__ x, const double* a) {
 // Lowest eigenpair of the symmetric tridiagonal (alpha[0..k-1], beta[0..k-2])
 // by Sturm-sequence bisection and inverse iteration with a partially pivoted
 // tridiagonal solve (the LAPACK dgtsv elimination).  One thread: k <= 128.
-__global__ void tridiag_lowest(int k, const double* __restrict__ alpha,
-                               const double* __restrict__ beta, double* eval_out,
-                               double* __restrict__ evec_out) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+__device__ void tridiag_lowest_body(int k, const double* __restrict__ alpha,
+                                    const double* __restrict__ beta, double* eval_out,
+                                    double* __restrict__ evec_out) {
   double lo = alpha[0], hi = alpha[0];
   for (int i = 0; i < k; i++) {
     double r = (i > 0 ? fabs(beta[i - 1]) : 0.0) + (i < k - 1 ? fabs(beta[i]) : 0.0);
@@ -312,6 +320,45 @@ __global__ void tridiag_lowest(int k, const double* __restrict__ alpha,
   for (int i = 0; i < k; i++) evec_out[i] = x[i];
 }
 
+__global__ void tridiag_lowest(int k, const double* __restrict__ alpha,
+                               const double* __restrict__ beta, double* eval_out,
+                               double* __restrict__ evec_out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  tridiag_lowest_body(k, alpha, beta, eval_out, evec_out);
+}
+
+// the same with the Krylov dimension read from the device (graph-driven solve)
+__global__ void tridiag_lowest_dev(const int* __restrict__ k, const double* __restrict__ alpha,
+                                   const double* __restrict__ beta, double* eval_out,
+                                   double* __restrict__ evec_out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  tridiag_lowest_body(*k, alpha, beta, eval_out, evec_out);
+}
+
+// Graph-driven Lanczos step closure.  ctl: [0] stop (converged or failed),
+// [1] Krylov dimension k, [2] beta was not finite, [3] converged (beta < btol).
+// Step j has produced alpha_j and the partial norms of the new residual y:
+// beta_j = ||y||; k = j + 1; stop when beta_j < btol (or is not finite),
+// otherwise V_{j+1} = y / beta_j.
+__global__ void lanczos_close(int64_t n, const double* __restrict__ y,
+                              const double* __restrict__ part_b, int G, double* beta_out,
+                              int* ctl, double btol, int j, double* __restrict__ vnext) {
+  if (ctl[0]) return;
+  const double b = sqrt(sum_parts(part_b, G));
+  const bool bad = !isfinite(b);
+  const bool conv = !bad && b < btol;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    *beta_out = b;
+    ctl[1] = j + 1;
+    if (bad) ctl[2] = 1;
+    if (conv) ctl[3] = 1;
+    if (bad || conv) ctl[0] = 1;
+  }
+  if (bad || conv) return;
+  for (int64_t i = (int64_t)blockIdx.x * KT + threadIdx.x; i < n; i += (int64_t)gridDim.x * KT)
+    vnext[i] = y[i] / b;
+}
+
 // E = exp(H) for a small complex matrix (m <= 32, column-major, re/im pairs)
 // by Taylor scaling and squaring (Moler & Van Loan, method 3): scale so that
 // the 1-norm is <= 1/2, sum 20 Taylor terms, square back.
@@ -379,6 +426,124 @@ int grid_for(fmpt_handle* h, int64_t n) {
   return (int)std::max<int64_t>(1, std::min(g, cap));
 }
 
+// Lanczos on a block-sparse operator as ONE CUDA graph: every step of the
+// reference recurrence (simple_lanczos.jl:27-68) for j = 0..kmax-1 is
+// captured; the step closure (lanczos_close) raises a device stop flag when
+// beta < btol, and every later node of the graph -- the grouped H_eff launch
+// included -- reads it and returns at once.  One host synchronisation per
+// solve.  Any capture or instantiation failure sets *fallback and leaves the
+// stream as it was, so the caller runs the host-driven loop instead.
+int lanczos_graph(fmpt_op* op, const double* x0, int kmax, double btol, int reorth,
+                  double* eigval, double* xout, int* info, int* niter, bool* fallback) {
+  fmpt_handle* h = op->h;
+  *fallback = true;
+  cudaStreamCaptureStatus cap0 = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(h->stream, &cap0) != cudaSuccess ||
+      cap0 != cudaStreamCaptureStatusNone) {
+    cudaGetLastError();
+    return FMPT_OK;   // the caller is capturing already: no nested capture
+  }
+  const int64_t n = op->n;   // real data
+  const int G = grid_for(h, n);
+  DevBuf Vb, Yb, scal, partA, partB, partM, coef, ctlb;
+  FMPT_TRY(Vb.alloc(h, (size_t)(kmax + 1) * n * sizeof(double)));
+  FMPT_TRY(Yb.alloc(h, (size_t)n * sizeof(double)));
+  FMPT_TRY(scal.alloc(h, (size_t)(3 * kmax + 8) * sizeof(double)));
+  FMPT_TRY(partA.alloc(h, (size_t)G * sizeof(double)));
+  FMPT_TRY(partB.alloc(h, (size_t)G * sizeof(double)));
+  FMPT_TRY(partM.alloc(h, (size_t)G * (kmax + 1) * 2 * sizeof(double)));
+  FMPT_TRY(coef.alloc(h, (size_t)(kmax + 1) * 2 * sizeof(double)));
+  FMPT_TRY(ctlb.alloc(h, 4 * sizeof(int)));
+  FMPT_TRY(gp_prepare(h));
+  FMPT_TRY(ensure_pinned(h, 4));
+  double* V = Vb.d();
+  double* y = Yb.d();
+  double* s_vm = scal.d();
+  double* s_alpha = scal.d() + 1;
+  double* s_beta = scal.d() + 1 + kmax;
+  double* s_eval = scal.d() + 1 + 2 * kmax;
+  double* s_evec = scal.d() + 2 + 2 * kmax;
+  int* ctl = static_cast<int*>(ctlb.p);
+  auto V_ = [&](int i) { return V + (int64_t)i * n; };
+  cudaStream_t st = h->stream;
+  auto record = [&]() -> int {
+    FMPT_CUDA(h, cudaMemsetAsync(ctl, 0, 4 * sizeof(int), st));
+    rdot_partial<<<G, KT, 0, st>>>(n, x0, x0, partA.d());
+    FMPT_LAUNCHED(h);
+    normalize_from_parts<<<G, KT, 0, st>>>(n, x0, V_(0), partA.d(), G, s_vm);
+    FMPT_LAUNCHED(h);
+    for (int j = 0; j < kmax; j++) {
+      FMPT_TRY(op_u1_apply(op, V_(j), y, ctl));
+      rdot_partial<<<G, KT, 0, st>>>(n, V_(j), y, partA.d(), ctl);
+      FMPT_LAUNCHED(h);
+      lanczos_axpy<<<G, KT, 0, st>>>(n, y, V_(j), j ? V_(j - 1) : nullptr, partA.d(), G,
+                                     j ? s_beta + (j - 1) : nullptr, s_alpha + j, partB.d(), ctl);
+      FMPT_LAUNCHED(h);
+      if (reorth) {
+        multidot_partial<<<G, KT, 0, st>>>(0, n, j + 1, V, n, y, partM.d(), ctl);
+        FMPT_LAUNCHED(h);
+        multidot_finalize<<<1, KT, 0, st>>>(j + 1, G, partM.d(), coef.d(), nullptr, ctl);
+        FMPT_LAUNCHED(h);
+        multi_axpy_sub<<<G, KT, 0, st>>>(0, n, j + 1, V, n, coef.d(), y, partB.d(), ctl);
+        FMPT_LAUNCHED(h);
+      }
+      lanczos_close<<<G, KT, 0, st>>>(n, y, partB.d(), G, s_beta + j, ctl, btol, j, V_(j + 1));
+      FMPT_LAUNCHED(h);
+    }
+    tridiag_lowest_dev<<<1, 1, 0, st>>>(ctl + 1, s_alpha, s_beta, s_eval, s_evec);
+    FMPT_LAUNCHED(h);
+    combine_basis<<<G, KT, 0, st>>>(0, n, 0, V, n, s_evec, 1, 1.0, 1, xout, ctl + 1);
+    FMPT_LAUNCHED(h);
+    FMPT_CUDA(h, cudaMemcpyAsync(h->pinned, s_eval, sizeof(double), cudaMemcpyDeviceToHost, st));
+    FMPT_CUDA(h, cudaMemcpyAsync(h->pinned + 1, ctl, 4 * sizeof(int), cudaMemcpyDeviceToHost, st));
+    return FMPT_OK;
+  };
+  if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaGetLastError();
+    return FMPT_OK;
+  }
+  const int rst = record();
+  cudaGraph_t graph = nullptr;
+  const cudaError_t ce = cudaStreamEndCapture(st, &graph);
+  if (rst != FMPT_OK || ce != cudaSuccess || !graph) {
+    if (graph) cudaGraphDestroy(graph);
+    cudaGetLastError();
+    return FMPT_OK;
+  }
+  bool ready = false;
+  if (h->lanczos_exec) {
+    cudaGraphExecUpdateResultInfo ri;
+    if (cudaGraphExecUpdate(h->lanczos_exec, graph, &ri) == cudaSuccess) {
+      ready = true;
+    } else {
+      cudaGetLastError();
+      cudaGraphExecDestroy(h->lanczos_exec);
+      h->lanczos_exec = nullptr;
+    }
+  }
+  if (!ready && cudaGraphInstantiate(&h->lanczos_exec, graph, 0) != cudaSuccess) {
+    cudaGetLastError();
+    h->lanczos_exec = nullptr;
+    cudaGraphDestroy(graph);
+    return FMPT_OK;
+  }
+  cudaGraphDestroy(graph);
+  *fallback = false;
+  FMPT_CUDA(h, cudaGraphLaunch(h->lanczos_exec, st));
+  h->graph_launches++;
+  FMPT_CUDA(h, cudaStreamSynchronize(st));
+  // read the staged results before anything else reuses the pinned buffer
+  const int* c = reinterpret_cast<const int*>(h->pinned + 1);
+  const int k = c[1], bad = c[2], conv = c[3];
+  const double ev = h->pinned[0];
+  FMPT_TRY(gp_check_status(h));
+  if (bad) return set_error(h, FMPT_ERR_NONFINITE, "lanczos: beta is not finite");
+  *eigval = ev;
+  if (info) *info = conv ? 0 : -1;
+  if (niter) *niter = k;
+  return FMPT_OK;
+}
+
 }  // namespace
 }  // namespace fmpt
 
@@ -392,6 +557,11 @@ int fmpt_lanczos_ground(fmpt_op* op, const double* x0, int kmax, double btol, in
   fmpt_handle* h = op->h;
   if (!x0 || !xout || !eigval) return set_error(h, FMPT_ERR_ARG, "lanczos: null pointer");
   if (kmax < 1 || kmax > 128) return set_error(h, FMPT_ERR_ARG, "lanczos: kmax must be 1..128");
+  if (op->u1 && h->graphs) {
+    bool fallback = false;
+    const int st = lanczos_graph(op, x0, kmax, btol, reorth, eigval, xout, info, niter, &fallback);
+    if (!fallback) return st;
+  }
   const int cp = op->dtype == FMPT_C128;
   const int64_t n = op->n * (cp ? 2 : 1);   // real view of the vector
   const int G = grid_for(h, n);

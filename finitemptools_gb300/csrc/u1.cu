@@ -367,11 +367,11 @@ int density_eigen(fmpt_handle* h, int side, std::vector<SplitSector>& sec, const
 
 }  // namespace
 
-int op_u1_apply(fmpt_op* op, const double* x, double* y) {
+int op_u1_apply(fmpt_op* op, const double* x, double* y, const int* gate) {
   U1OpState* st = static_cast<U1OpState*>(op->u1);
   double* slots[6] = {const_cast<double*>(op->hleft), const_cast<double*>(op->hright),
                       const_cast<double*>(x), y, st->T1.d(), st->T3.d()};
-  return gp_run(op->h, st->prog, slots, 6);
+  return gp_run(op->h, st->prog, slots, 6, gate);
 }
 
 void op_u1_free(fmpt_op* op) {

@@ -28,6 +28,13 @@ class Handle:
     def synchronize(self):
         check(lib().fmpt_synchronize(self.ptr), self.ptr)
 
+    def set_graphs(self, on=True):
+        """CUDA-graph Krylov solves for block-sparse operators (default on)."""
+        self.check(lib().fmpt_set_graphs(self.ptr, 1 if on else 0))
+
+    def graph_count(self):
+        return int(lib().fmpt_graph_launch_count(self.ptr))
+
     def launch_count(self):
         return int(lib().fmpt_launch_count(self.ptr))
 

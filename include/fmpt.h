@@ -63,6 +63,16 @@ int fmpt_destroy(fmpt_handle* h);
 const char* fmpt_status_string(int status);
 const char* fmpt_last_error(fmpt_handle* h);
 int fmpt_synchronize(fmpt_handle* h);
+/* CUDA graphs for the Krylov solvers (default on): fmpt_lanczos_ground on a
+ * block-sparse (U(1)) operator captures all its iterations into one graph --
+ * after convergence a device flag turns the remaining steps into no-ops -- and
+ * launches it once, with one host synchronisation per solve instead of one
+ * per iteration.  The instantiated graph is reused across solves through
+ * cudaGraphExecUpdate.  Off: the host-driven loop.  No counterpart in the
+ * reference. */
+int fmpt_set_graphs(fmpt_handle* h, int on);
+/* Number of CUDA graph launches of this handle's solvers. */
+uint64_t fmpt_graph_launch_count(fmpt_handle* h);
 /* Run subsequent work of this handle on an external cudaStream_t (NULL: the
  * handle's own stream). */
 int fmpt_set_stream(fmpt_handle* h, void* cuda_stream);

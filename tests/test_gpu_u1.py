@@ -176,6 +176,37 @@ def test_u1_lanczos_matches_oracle():
     assert k == ko
 
 
+@pytest.mark.parametrize("kmax", [3, 30])
+def test_u1_lanczos_graph_equals_host_loop(kmax):
+    """The graph-captured solve runs the same kernels in the same order as the
+    host-driven loop: identical results, including early convergence (on a
+    4-site chain the two-site space has a few states, so kmax 30 exhausts the
+    Krylov space before kmax)."""
+    L, N = 4, 2
+    mps, legs, psi = _states(L, N, 8, 21)
+    u1_right_canonicalize_(psi)
+    m = fm.U1ExpectationCache(heisenberg_xxz_mpo(), psi)
+    Vl, Vm, Vr = psi.spaces[2], psi.spaces[3], psi.spaces[4]
+    x2 = fm.u1_twosite(psi[2], psi[3], Vl, Vm, Vr, QP, QP)
+    op = fm.U1HeffOp(m.hstorage[2], m.hstorage[4], m.mpo[2], m.mpo[3], Vl, Vr, QP, QP,
+                     m.qw[2], m.qw[3], m.qw[4])
+    assert op.n < 30
+    h = psi.handle
+    g0 = h.graph_count()
+    h.set_graphs(True)
+    E1, v1, i1, k1 = op.lanczos(x2, kmax, 1e-12)
+    assert h.graph_count() == g0 + 1
+    E1b, v1b, _, _ = op.lanczos(x2, kmax, 1e-12)      # reused executable graph
+    assert h.graph_count() == g0 + 2
+    h.set_graphs(False)
+    E2, v2, i2, k2 = op.lanczos(x2, kmax, 1e-12)
+    h.set_graphs(True)
+    assert (E1, i1, k1) == (E2, i2, k2) and E1b == E1
+    assert np.array_equal(v1.numpy(), v2.numpy()) and np.array_equal(v1b.numpy(), v1.numpy())
+    if kmax == 30:
+        assert i1 == 0 and k1 < 30
+
+
 @pytest.mark.parametrize("L,N,D,model", [(12, 6, 48, "xxz"), (12, 4, 48, "xxz"),
                                          (10, 5, 40, "j1j2")])
 def test_u1_dmrg2_vs_ed_and_oracle(L, N, D, model):
