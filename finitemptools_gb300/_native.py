@@ -45,6 +45,9 @@ SIGNATURES = {
     "fmpt_synchronize": (c_int, [c_void_p]),
     "fmpt_set_graphs": (c_int, [c_void_p, c_int]),
     "fmpt_graph_launch_count": (c_uint64, [c_void_p]),
+    "fmpt_set_tuning": (c_int, [c_void_p, c_int]),
+    "fmpt_tuning_info": (c_int, [c_void_p, P(c_int), P(c_int64)]),
+    "fmpt_op_tile": (c_int, [c_void_p]),
     "fmpt_set_stream": (c_int, [c_void_p, c_void_p]),
     "fmpt_get_stream": (c_void_p, [c_void_p]),
     "fmpt_launch_count": (c_uint64, [c_void_p]),

@@ -341,6 +341,20 @@ const char* fmpt_last_error(fmpt_handle* h) { return h ? h->err.c_str() : "null 
 
 uint64_t fmpt_graph_launch_count(fmpt_handle* h) { return h ? h->graph_launches : 0; }
 
+int fmpt_set_tuning(fmpt_handle* h, int mode) {
+  if (!h) return FMPT_ERR_ARG;
+  if (mode < 0 || mode > 2) return fmpt::set_error(h, FMPT_ERR_ARG, "tuning mode must be 0, 1 or 2");
+  h->tune_mode = mode;
+  return FMPT_OK;
+}
+
+int fmpt_tuning_info(fmpt_handle* h, int* entries, int64_t* timed) {
+  if (!h) return FMPT_ERR_ARG;
+  if (entries) *entries = (int)h->tune_cache.size();
+  if (timed) *timed = (int64_t)h->tune_runs;
+  return FMPT_OK;
+}
+
 int fmpt_set_graphs(fmpt_handle* h, int on) {
   if (!h) return FMPT_ERR_ARG;
   h->graphs = on != 0;

@@ -18,6 +18,7 @@
 // (about 2 DFMA per clock per SM), so the kernel's job is to keep every SM's
 // FP64 pipe fed across thousands of 1..400-wide blocks.
 #include <algorithm>
+#include <cmath>
 #include <mutex>
 #include <numeric>
 #include <vector>
@@ -27,7 +28,8 @@
 namespace fmpt {
 namespace {
 
-constexpr int GT = 32, GK = 8, GNT = 256;
+constexpr int GK = 8, GNT = 256;
+constexpr int kTile[GP_VARIANTS] = {32, 64};   // tile edge of each kernel variant
 constexpr uint64_t kBarrierTimeoutNs = 2000000000ull;
 
 struct GKArgs {
@@ -87,8 +89,14 @@ __device__ bool grid_barrier(const GKArgs& a, int target, int* s_flag) {
   return *s_flag != 0;
 }
 
+// One GTxGT output tile of a GEMM problem: 256 threads on a 16x16 grid, each
+// owning (GT/16)^2 outputs at rows tx + 16 i, columns ty + 16 j.  Every output
+// sums its segments and k in the same order for any GT, so the tile shape
+// never changes the result.
+template <int GT>
 __device__ __forceinline__ void gemm_tile(const GKArgs& a, const GPhaseDesc& ph, int t,
                                           double (*As)[GT + 1], double (*Bs)[GT + 1]) {
+  constexpr int TPR = GT / 16;
   const GProblem P = a.probs[a.tile_prob[t]];
   const int mn = a.tile_mn[t];
   const int m0 = (mn & 0xffff) * GT, n0 = ((unsigned)mn >> 16) * GT;
@@ -98,23 +106,29 @@ __device__ __forceinline__ void gemm_tile(const GKArgs& a, const GPhaseDesc& ph,
   const bool b_kfast = (ph.tb == FMPT_N || ph.tb == FMPT_R);
   const double* Ab = a.slot[ph.a_slot];
   const double* Bb = a.slot[ph.b_slot];
-  double acc00 = 0.0, acc01 = 0.0, acc10 = 0.0, acc11 = 0.0;
+  double acc[TPR][TPR];
+#pragma unroll
+  for (int i = 0; i < TPR; i++)
+#pragma unroll
+    for (int j = 0; j < TPR; j++) acc[i][j] = 0.0;
   for (int sg = P.seg0; sg < P.seg1; sg++) {
     const GSegment S = a.segs[sg];
     const double* A = Ab + S.a_off;
     const double* B = Bb + S.b_off;
     for (int k0 = 0; k0 < S.k; k0 += GK) {
-      {
+#pragma unroll
+      for (int e = tid; e < GT * GK; e += GNT) {
         int mm, kk;
-        if (a_mfast) { mm = tid % GT; kk = tid / GT; } else { kk = tid % GK; mm = tid / GK; }
+        if (a_mfast) { mm = e % GT; kk = e / GT; } else { kk = e % GK; mm = e / GK; }
         const int gm = m0 + mm, gk = k0 + kk;
         double v = 0.0;
         if (gm < P.m && gk < S.k) v = S.coef * __ldg(A + op_index(ph.ta, gm, gk, S.lda));
         As[kk][mm] = v;
       }
-      {
+#pragma unroll
+      for (int e = tid; e < GT * GK; e += GNT) {
         int nn, kk;
-        if (b_kfast) { kk = tid % GK; nn = tid / GK; } else { nn = tid % GT; kk = tid / GT; }
+        if (b_kfast) { kk = e % GK; nn = e / GK; } else { nn = e % GT; kk = e / GT; }
         const int gn = n0 + nn, gk = k0 + kk;
         double v = 0.0;
         if (gn < P.n && gk < S.k) v = __ldg(B + op_index(ph.tb, gk, gn, S.ldb));
@@ -123,24 +137,31 @@ __device__ __forceinline__ void gemm_tile(const GKArgs& a, const GPhaseDesc& ph,
       __syncthreads();
 #pragma unroll
       for (int kk = 0; kk < GK; kk++) {
-        const double a0 = As[kk][tx], a1 = As[kk][tx + 16];
-        const double b0 = Bs[kk][ty], b1 = Bs[kk][ty + 16];
-        acc00 = fma(a0, b0, acc00);
-        acc01 = fma(a0, b1, acc01);
-        acc10 = fma(a1, b0, acc10);
-        acc11 = fma(a1, b1, acc11);
+        double av[TPR], bv[TPR];
+#pragma unroll
+        for (int i = 0; i < TPR; i++) { av[i] = As[kk][tx + 16 * i]; bv[i] = Bs[kk][ty + 16 * i]; }
+#pragma unroll
+        for (int i = 0; i < TPR; i++)
+#pragma unroll
+          for (int j = 0; j < TPR; j++) acc[i][j] = fma(av[i], bv[j], acc[i][j]);
       }
       __syncthreads();
     }
   }
   double* C = a.slot[ph.c_slot] + P.c_off;
-  const int r0 = m0 + tx, r1 = m0 + tx + 16, c0 = n0 + ty, c1 = n0 + ty + 16;
-  if (r0 < P.m && c0 < P.n) C[r0 + c0 * P.ldc] = acc00;
-  if (r0 < P.m && c1 < P.n) C[r0 + c1 * P.ldc] = acc01;
-  if (r1 < P.m && c0 < P.n) C[r1 + c0 * P.ldc] = acc10;
-  if (r1 < P.m && c1 < P.n) C[r1 + c1 * P.ldc] = acc11;
+#pragma unroll
+  for (int i = 0; i < TPR; i++) {
+    const int r = m0 + tx + 16 * i;
+    if (r >= P.m) continue;
+#pragma unroll
+    for (int j = 0; j < TPR; j++) {
+      const int c = n0 + ty + 16 * j;
+      if (c < P.n) C[r + (int64_t)c * P.ldc] = acc[i][j];
+    }
+  }
 }
 
+template <int GT>
 __device__ __forceinline__ void sum_tile(const GKArgs& a, const GPhaseDesc& ph, int t) {
   const GProblem P = a.probs[a.tile_prob[t]];
   const int mn = a.tile_mn[t];
@@ -149,9 +170,10 @@ __device__ __forceinline__ void sum_tile(const GKArgs& a, const GPhaseDesc& ph, 
   if (r >= P.m) return;
   const double* Ab = a.slot[ph.a_slot];
   double* C = a.slot[ph.c_slot] + P.c_off;
-#pragma unroll
-  for (int j = 0; j < GT / (GNT / GT); j++) {
-    const int c = n0 + threadIdx.x / GT + j * (GNT / GT);
+  constexpr int CSTEP = GNT / GT;
+#pragma unroll 4
+  for (int j = 0; j < GT / CSTEP; j++) {
+    const int c = n0 + threadIdx.x / GT + j * CSTEP;
     if (c >= P.n) break;
     double s = 0.0;
     for (int sg = P.seg0; sg < P.seg1; sg++) {
@@ -162,6 +184,7 @@ __device__ __forceinline__ void sum_tile(const GKArgs& a, const GPhaseDesc& ph, 
   }
 }
 
+template <int GT>
 __global__ void __launch_bounds__(GNT) grouped_kernel(const GKArgs a) {
   __shared__ double As[GK][GT + 1];
   __shared__ double Bs[GK][GT + 1];
@@ -178,24 +201,27 @@ __global__ void __launch_bounds__(GNT) grouped_kernel(const GKArgs a) {
       const int t = s_tile;
       if (t >= ntiles) break;
       if (ph.type == GP_GEMM)
-        gemm_tile(a, ph, ph.tile0 + t, As, Bs);
+        gemm_tile<GT>(a, ph, ph.tile0 + t, As, Bs);
       else
-        sum_tile(a, ph, ph.tile0 + t);
+        sum_tile<GT>(a, ph, ph.tile0 + t);
     }
   }
 }
 
-int g_occupancy = 0;
+int g_occupancy[GP_VARIANTS] = {0, 0};
 std::mutex g_occ_mu;
 
-int kernel_occupancy(fmpt_handle* h) {
+int kernel_occupancy(fmpt_handle* h, int v) {
   std::lock_guard<std::mutex> lock(g_occ_mu);
-  if (g_occupancy == 0) {
+  if (g_occupancy[v] == 0) {
     int occ = 0;
-    FMPT_CUDA(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, grouped_kernel, GNT, 0));
-    g_occupancy = std::max(1, std::min(occ, 8));
+    if (v == 0)
+      FMPT_CUDA(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, grouped_kernel<32>, GNT, 0));
+    else
+      FMPT_CUDA(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, grouped_kernel<64>, GNT, 0));
+    g_occupancy[v] = std::max(1, std::min(occ, 8));
   }
-  return g_occupancy;
+  return g_occupancy[v];
 }
 
 }  // namespace
@@ -288,35 +314,44 @@ int gp_finalize(fmpt_handle* h, GroupedProgram& g) {
   FMPT_TRY(validate(h, g));
   g.tile_prob.clear();
   g.tile_mn.clear();
-  int max_tiles = 0;
+  int max_tiles[GP_VARIANTS] = {0, 0};
+  for (int v = 0; v < GP_VARIANTS; v++) {
+    const int GT = kTile[v];
+    g.vtile0[v].assign(g.phases.size(), 0);
+    g.vtile1[v].assign(g.phases.size(), 0);
+    for (size_t ph = 0; ph < g.phases.size(); ph++) {
+      const int p0 = g.phase_prob0[ph], p1 = g.phase_prob0[ph + 1];
+      // largest work per tile first, so the long tiles do not straggle at the end
+      std::vector<int64_t> cost(p1 - p0, 0);
+      for (int i = p0; i < p1; i++) {
+        const GProblem& p = g.probs[i];
+        for (int s = p.seg0; s < p.seg1; s++)
+          cost[i - p0] += g.phases[ph].type == GP_GEMM ? g.segs[s].k : 1;
+      }
+      std::vector<int> order(p1 - p0);
+      std::iota(order.begin(), order.end(), p0);
+      std::stable_sort(order.begin(), order.end(),
+                       [&](int x, int y) { return cost[x - p0] > cost[y - p0]; });
+      g.vtile0[v][ph] = (int)g.tile_prob.size();
+      for (int i : order) {
+        const GProblem& p = g.probs[i];
+        if (p.m <= 0 || p.n <= 0) continue;
+        const int tm = (p.m + GT - 1) / GT, tn = (p.n + GT - 1) / GT;
+        if (tm > 0xffff || tn > 0x7fff)
+          return set_error(h, FMPT_ERR_SHAPE, "grouped: block %d x %d too large", p.m, p.n);
+        for (int b = 0; b < tn; b++)
+          for (int a = 0; a < tm; a++) {
+            g.tile_prob.push_back(i);
+            g.tile_mn.push_back(a | (b << 16));
+          }
+      }
+      g.vtile1[v][ph] = (int)g.tile_prob.size();
+      max_tiles[v] = std::max(max_tiles[v], g.vtile1[v][ph] - g.vtile0[v][ph]);
+    }
+  }
   for (size_t ph = 0; ph < g.phases.size(); ph++) {
-    const int p0 = g.phase_prob0[ph], p1 = g.phase_prob0[ph + 1];
-    // largest work per tile first, so the long tiles do not straggle at the end
-    std::vector<int64_t> cost(p1 - p0, 0);
-    for (int i = p0; i < p1; i++) {
-      const GProblem& p = g.probs[i];
-      for (int s = p.seg0; s < p.seg1; s++)
-        cost[i - p0] += g.phases[ph].type == GP_GEMM ? g.segs[s].k : 1;
-    }
-    std::vector<int> order(p1 - p0);
-    std::iota(order.begin(), order.end(), p0);
-    std::stable_sort(order.begin(), order.end(),
-                     [&](int x, int y) { return cost[x - p0] > cost[y - p0]; });
-    g.phases[ph].tile0 = (int)g.tile_prob.size();
-    for (int i : order) {
-      const GProblem& p = g.probs[i];
-      if (p.m <= 0 || p.n <= 0) continue;
-      const int tm = (p.m + GT - 1) / GT, tn = (p.n + GT - 1) / GT;
-      if (tm > 0xffff || tn > 0x7fff)
-        return set_error(h, FMPT_ERR_SHAPE, "grouped: block %d x %d too large", p.m, p.n);
-      for (int b = 0; b < tn; b++)
-        for (int a = 0; a < tm; a++) {
-          g.tile_prob.push_back(i);
-          g.tile_mn.push_back(a | (b << 16));
-        }
-    }
-    g.phases[ph].tile1 = (int)g.tile_prob.size();
-    max_tiles = std::max(max_tiles, g.phases[ph].tile1 - g.phases[ph].tile0);
+    g.phases[ph].tile0 = g.vtile0[0][ph];
+    g.phases[ph].tile1 = g.vtile1[0][ph];
   }
   // one device allocation: problems | segments | tile_prob | tile_mn | control words
   auto up256 = [](size_t b) { return (b + 255) / 256 * 256; };
@@ -345,11 +380,60 @@ int gp_finalize(fmpt_handle* h, GroupedProgram& g) {
     FMPT_CUDA(h, cudaMemcpyAsync(g.d_tile_mn, g.tile_mn.data(), g.tile_mn.size() * sizeof(int),
                                  cudaMemcpyHostToDevice, h->stream));
   }
-  const int occ = kernel_occupancy(h);
-  if (occ <= 0) return set_error(h, FMPT_ERR_CUDA, "grouped: occupancy query failed");
   const int sms = h->sm_count > 0 ? h->sm_count : 1;
-  g.grid = std::max(1, std::min(max_tiles, occ * sms));
+  for (int v = 0; v < GP_VARIANTS; v++) {
+    const int occ = kernel_occupancy(h, v);
+    if (occ <= 0) return set_error(h, FMPT_ERR_CUDA, "grouped: occupancy query failed");
+    g.vgrid[v] = std::max(1, std::min(max_tiles[v], occ * sms));
+  }
   g.ready = true;
+  return FMPT_OK;
+}
+
+int gp_autotune(fmpt_handle* h, GroupedProgram& g, double* const* slots, int nslots, int kind) {
+  if (h->tune_mode == 1 || h->tune_mode == 2) {
+    g.variant = h->tune_mode - 1;
+    return FMPT_OK;
+  }
+  g.variant = 0;
+  // small programs: the 32x32 tile balances better and timing costs more than it saves
+  if (g.flops < 2.0e7 || g.tile_prob.empty()) return FMPT_OK;
+  const int key = kind * 1000 + (int)std::floor(std::log2(g.flops) * 2.0);
+  auto it = h->tune_cache.find(key);
+  if (it != h->tune_cache.end()) {
+    g.variant = it->second;
+    return FMPT_OK;
+  }
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(h->stream, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone) {
+    cudaGetLastError();
+    return FMPT_OK;   // no timing inside a capture: keep the default
+  }
+  cudaEvent_t e0, e1;
+  FMPT_CUDA(h, cudaEventCreate(&e0));
+  if (cudaEventCreate(&e1) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return set_error(h, FMPT_ERR_CUDA, "autotune: event creation failed");
+  }
+  int best = 0, st = FMPT_OK;
+  float best_ms = 0.f;
+  for (int v = 0; v < GP_VARIANTS && st == FMPT_OK; v++) {
+    st = gp_run(h, g, slots, nslots, nullptr, v);          // warm-up
+    if (st == FMPT_OK && cudaEventRecord(e0, h->stream) != cudaSuccess) st = FMPT_ERR_CUDA;
+    for (int r = 0; r < 3 && st == FMPT_OK; r++) st = gp_run(h, g, slots, nslots, nullptr, v);
+    if (st == FMPT_OK && cudaEventRecord(e1, h->stream) != cudaSuccess) st = FMPT_ERR_CUDA;
+    float ms = 0.f;
+    if (st == FMPT_OK &&
+        (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess))
+      st = FMPT_ERR_CUDA;
+    if (st == FMPT_OK && (v == 0 || ms < best_ms)) { best = v; best_ms = ms; }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st != FMPT_OK) return st == FMPT_ERR_CUDA ? set_error(h, st, "autotune: timing failed") : st;
+  h->tune_cache[key] = best;
+  h->tune_runs++;
+  g.variant = best;
   return FMPT_OK;
 }
 
@@ -380,19 +464,27 @@ int gp_check_status(fmpt_handle* h) {
 int gp_prepare(fmpt_handle* h) {
   int* st = nullptr;
   FMPT_TRY(gp_status_word(h, &st));
-  return kernel_occupancy(h) > 0 ? FMPT_OK : FMPT_ERR_CUDA;
+  for (int v = 0; v < GP_VARIANTS; v++)
+    if (kernel_occupancy(h, v) <= 0) return FMPT_ERR_CUDA;
+  return FMPT_OK;
 }
 
 int gp_run(fmpt_handle* h, const GroupedProgram& g, double* const* slots, int nslots,
-           const int* gate) {
+           const int* gate, int variant) {
   if (!g.ready) return set_error(h, FMPT_ERR_ARG, "grouped: program not finalised");
   if (g.tile_prob.empty()) return FMPT_OK;
+  const int v = variant < 0 ? g.variant : variant;
+  if (v < 0 || v >= GP_VARIANTS) return set_error(h, FMPT_ERR_ARG, "grouped: variant %d", v);
   GKArgs a{};
   a.nphase = (int)g.phases.size();
-  for (int p = 0; p < a.nphase; p++) a.ph[p] = g.phases[p];
+  for (int p = 0; p < a.nphase; p++) {
+    a.ph[p] = g.phases[p];
+    a.ph[p].tile0 = g.vtile0[v][p];
+    a.ph[p].tile1 = g.vtile1[v][p];
+  }
   for (int s = 0; s < GP_SLOTS; s++) a.slot[s] = s < nslots ? slots[s] : nullptr;
   for (int p = 0; p < a.nphase; p++) {
-    const GPhaseDesc& d = g.phases[p];
+    const GPhaseDesc& d = a.ph[p];
     if (d.tile1 == d.tile0) continue;
     if (!a.slot[d.a_slot] || !a.slot[d.c_slot] || (d.type == GP_GEMM && !a.slot[d.b_slot]))
       return set_error(h, FMPT_ERR_ARG, "grouped: operand slot of phase %d is null", p);
@@ -405,7 +497,7 @@ int gp_run(fmpt_handle* h, const GroupedProgram& g, double* const* slots, int ns
   FMPT_CUDA(h, cudaMemsetAsync(g.d_ctl, 0, (GP_MAX_PHASES + 2) * sizeof(int), h->stream));
   ProfScope prof(h, FMPT_K_GROUPED);
   cudaLaunchConfig_t cfg{};
-  cfg.gridDim = dim3(g.grid);
+  cfg.gridDim = dim3(g.vgrid[v]);
   cfg.blockDim = dim3(GNT);
   cfg.dynamicSmemBytes = 0;
   cfg.stream = h->stream;
@@ -414,7 +506,10 @@ int gp_run(fmpt_handle* h, const GroupedProgram& g, double* const* slots, int ns
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  FMPT_CUDA(h, cudaLaunchKernelEx(&cfg, grouped_kernel, a));
+  if (v == 0)
+    FMPT_CUDA(h, cudaLaunchKernelEx(&cfg, grouped_kernel<32>, a));
+  else
+    FMPT_CUDA(h, cudaLaunchKernelEx(&cfg, grouped_kernel<64>, a));
   FMPT_LAUNCHED(h);
   return FMPT_OK;
 }

@@ -6,6 +6,7 @@
 
 #include <cstdint>
 #include <cstdio>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -38,6 +39,11 @@ struct fmpt_handle {
   bool graphs = true;
   cudaGraphExec_t lanczos_exec = nullptr;   // reused through cudaGraphExecUpdate
   uint64_t graph_launches = 0;
+  // grouped-kernel tile autotuner (fmpt_set_tuning): 0 measure, 1 force the
+  // 32x32 tile, 2 force 64x64; cache: (program kind, work bucket) -> variant
+  int tune_mode = 0;
+  std::map<int, int> tune_cache;
+  uint64_t tune_runs = 0;
 };
 
 namespace fmpt {
@@ -144,6 +150,7 @@ int schedule_env(fmpt_handle* h, int cplx, const double* W, int d, int wl, int w
 
 // -------- grouped persistent block-sparse engine (grouped.cu)
 constexpr int GP_MAX_PHASES = 4, GP_SLOTS = 8;
+constexpr int GP_VARIANTS = 2;   // kernel variants: 32x32 and 64x64 output tiles
 enum { GP_GEMM = 0, GP_SUM = 1 };
 // One output block: C (m x n, column-major with ldc) at c_off in the phase's C slot.
 struct GProblem {
@@ -164,7 +171,10 @@ struct GroupedProgram {
   std::vector<int> phase_prob0;
   std::vector<GProblem> probs;
   std::vector<GSegment> segs;
-  std::vector<int> tile_prob, tile_mn;
+  std::vector<int> tile_prob, tile_mn;           // the tiles of every variant, one after another
+  std::vector<int> vtile0[GP_VARIANTS], vtile1[GP_VARIANTS];   // per variant and phase
+  int vgrid[GP_VARIANTS] = {0, 0};
+  int variant = 0;                                // the one gp_run launches by default
   double flops = 0.0;       // 2 m n k over the GEMM segments
   double sum_elems = 0.0;   // output elements x terms of the SUM phases
   int64_t slot_elems[GP_SLOTS] = {-1, -1, -1, -1, -1, -1, -1, -1};  // operand extents
@@ -174,7 +184,6 @@ struct GroupedProgram {
   int* d_tile_prob = nullptr;
   int* d_tile_mn = nullptr;
   int* d_ctl = nullptr;
-  int grid = 0;
   bool ready = false;
 };
 // Builder: a phase, then its problems, each followed by its segments.
@@ -189,8 +198,13 @@ int gp_finalize(fmpt_handle* h, GroupedProgram& g);   // bounds check + tiles + 
 // gate: optional device flag; when it is nonzero at launch time every CTA
 // returns at once (a solver step after convergence inside a CUDA graph)
 int gp_run(fmpt_handle* h, const GroupedProgram& g, double* const* slots, int nslots,
-           const int* gate = nullptr);
+           const int* gate = nullptr, int variant = -1);
 int gp_prepare(fmpt_handle* h);   // allocations gp_run needs, done before a stream capture
+// Picks g.variant: the handle's cached choice for (kind, work bucket), else
+// (tune mode 0) times every variant on these slots -- the program must be
+// safe to run repeatedly on them -- and caches the fastest.
+enum { GP_KIND_HEFF = 1, GP_KIND_ENV = 2, GP_KIND_OTHER = 3 };
+int gp_autotune(fmpt_handle* h, GroupedProgram& g, double* const* slots, int nslots, int kind);
 int gp_check_status(fmpt_handle* h);                  // synchronises; FMPT_ERR_TIMEOUT if set
 
 // -------- dense helpers shared with the sector code (linalg.cu)

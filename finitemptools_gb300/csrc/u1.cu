@@ -547,12 +547,32 @@ int fmpt_u1_op_ac2(fmpt_handle* h, int dtype, const double* W1, const double* W2
   int s = gp_finalize(h, g);
   if (s == FMPT_OK) s = alloc_scratch(h, st->T1, t1n);
   if (s == FMPT_OK) s = alloc_scratch(h, st->T3, t3n);
+  if (s == FMPT_OK) {
+    // tile variant: timed on scratch vectors the first time this work size is seen
+    DevBuf xs, ys;
+    const bool tune = h->tune_mode == 0 && g.flops >= 2.0e7;
+    if (tune) s = alloc_scratch(h, xs, pk.n);
+    if (s == FMPT_OK && tune) s = alloc_scratch(h, ys, pk.n);
+    if (s == FMPT_OK && tune)
+      s = cudaMemsetAsync(xs.p, 0, (size_t)pk.n * sizeof(double), h->stream) == cudaSuccess
+              ? FMPT_OK : set_error(h, FMPT_ERR_CUDA, "u1_op_ac2: memset failed");
+    if (s == FMPT_OK) {
+      double* slots[6] = {const_cast<double*>(hleft), const_cast<double*>(hright), xs.d(), ys.d(),
+                          st->T1.d(), st->T3.d()};
+      s = gp_autotune(h, g, slots, 6, GP_KIND_HEFF);
+    }
+  }
   if (s != FMPT_OK) {
     fmpt_op_destroy(op);
     return s;
   }
   *out = op;
   return FMPT_OK;
+}
+
+int fmpt_op_tile(fmpt_op* op) {
+  if (!op || !op->u1) return 0;
+  return static_cast<U1OpState*>(op->u1)->prog.variant == 0 ? 32 : 64;
 }
 
 int fmpt_op_flops(fmpt_op* op, double* flops) {
@@ -776,6 +796,7 @@ static int u1_env(fmpt_handle* h, bool right, int dtype, const double* hold, con
   FMPT_CUDA(h, cudaMemsetAsync(hnew, 0, (size_t)out_elems * sizeof(double), h->stream));
   double* slots[6] = {const_cast<double*>(hold), const_cast<double*>(A), const_cast<double*>(B),
                       hnew, sc.T1.d(), sc.T3.d()};
+  FMPT_TRY(gp_autotune(h, g, slots, 6, GP_KIND_ENV));   // reruns write the same values
   return gp_run(h, g, slots, 6);
 }
 

@@ -35,6 +35,15 @@ class Handle:
     def graph_count(self):
         return int(lib().fmpt_graph_launch_count(self.ptr))
 
+    def set_tuning(self, mode=0):
+        """Grouped-kernel tile choice: 0 autotune (default), 1 force 32x32, 2 force 64x64."""
+        self.check(lib().fmpt_set_tuning(self.ptr, int(mode)))
+
+    def tuning_info(self):
+        n, t = ctypes.c_int(), ctypes.c_int64()
+        self.check(lib().fmpt_tuning_info(self.ptr, ctypes.byref(n), ctypes.byref(t)))
+        return n.value, t.value
+
     def launch_count(self):
         return int(lib().fmpt_launch_count(self.ptr))
 

@@ -381,6 +381,10 @@ class U1HeffOp:
         self.n = int(lib().fmpt_op_size(op))
         self.shape = (self.n,)
 
+    def tile(self):
+        """Output tile edge the grouped kernel runs this operator with (autotuned)."""
+        return int(lib().fmpt_op_tile(self.ptr))
+
     def flops(self):
         f = ctypes.c_double()
         self.h.check(lib().fmpt_op_flops(self.ptr, ctypes.byref(f)))

@@ -73,6 +73,18 @@ int fmpt_synchronize(fmpt_handle* h);
 int fmpt_set_graphs(fmpt_handle* h, int on);
 /* Number of CUDA graph launches of this handle's solvers. */
 uint64_t fmpt_graph_launch_count(fmpt_handle* h);
+/* Tile autotuner of the grouped block-sparse kernel.  mode 0 (default): the
+ * first time a block-sparse operator or environment update of a new work size
+ * (kind, half-octave of FLOPs) is built, every kernel variant (32x32 and 64x64
+ * output tiles) is timed on it and the fastest is cached in the handle;
+ * mode 1 / 2 force the 32x32 / 64x64 tile.  All variants sum every output in
+ * the same order: the choice never changes results.  No counterpart in the
+ * reference. */
+int fmpt_set_tuning(fmpt_handle* h, int mode);
+/* Number of cached tuning decisions and of timed tunings so far. */
+int fmpt_tuning_info(fmpt_handle* h, int* entries, int64_t* timed);
+/* Output tile edge (32 or 64) a block-sparse operator runs with (0: dense op). */
+int fmpt_op_tile(fmpt_op* op);
 /* Run subsequent work of this handle on an external cudaStream_t (NULL: the
  * handle's own stream). */
 int fmpt_set_stream(fmpt_handle* h, void* cuda_stream);

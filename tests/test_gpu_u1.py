@@ -67,6 +67,42 @@ def test_u1_ac2_apply(L, N, D, site):
     assert op.flops() > 0
 
 
+@pytest.mark.parametrize("L,N,D,site", [(10, 5, 20, 5), (16, 8, 96, 8), (24, 12, 300, 12)])
+def test_u1_tile_variants_identical(L, N, D, site):
+    """Both grouped-kernel tile variants (32x32, 64x64) sum every output in the
+    same order: forced either way, H_eff*x and the environment update agree
+    bit for bit; the autotuner caches a decision for large programs."""
+    Ws, qw, mps, legs, Lm, Rm = _bond(L, N, D, site, 5 * L + D)
+    Vl, Vm, Vr = legs[site - 1], legs[site], legs[site + 1]
+    W1, W2 = Ws[site - 1], Ws[site]
+    X = np.tensordot(mps[site - 1], mps[site], axes=([2], [0]))
+    dL, dR = DT.from_numpy(Lm), DT.from_numpy(Rm)
+    x = DT.from_numpy(OU.pack2(X, Vl, Vr, list(QP), list(QP)))
+    A = DT.from_numpy(mps[site - 1])
+    h = dL.h
+    ys, es = [], []
+    try:
+        for mode, tile in ((1, 32), (2, 64)):
+            h.set_tuning(mode)
+            op = fm.U1HeffOp(dL, dR, W1, W2, sp(Vl), sp(Vr), QP, QP, qw[site - 1], qw[site],
+                             qw[site + 1])
+            assert op.tile() == tile
+            ys.append(op(x).numpy())
+            es.append(fm.u1_updateleft(dL, A, W1, A, sp(Vl), sp(Vm), QP, qw[site - 1],
+                                       qw[site]).numpy())
+        h.set_tuning(0)
+        op = fm.U1HeffOp(dL, dR, W1, W2, sp(Vl), sp(Vr), QP, QP, qw[site - 1], qw[site],
+                         qw[site + 1])
+        y_auto = op(x).numpy()
+        if op.flops() >= 2e7:
+            assert h.tuning_info()[0] >= 1
+    finally:
+        h.set_tuning(0)
+    assert np.array_equal(ys[0], ys[1]) and np.array_equal(y_auto, ys[0])
+    assert np.array_equal(es[0], es[1])
+    assert rel(ys[0], OU.pack2(O.ac2_prime(X, W1, W2, Lm, Rm), Vl, Vr, list(QP), list(QP))) < 1e-13
+
+
 def test_u1_pack_roundtrip():
     Ws, qw, mps, legs, Lm, Rm = _bond(12, 6, 40, 6, 2)
     Vl, Vr = legs[5], legs[7]
