@@ -314,6 +314,124 @@ def dmrg_section(h, fm, budget_s=150.0):
     return out
 
 
+def u1_section(h, fm, budget_s=150.0):
+    """U(1) block-sparse DMRG2 (charge = number of up spins, total Sz = 0): the
+    grouped persistent FP64 engine, graph-captured Lanczos, autotuned tiles and
+    the batched density-matrix sector split.
+      xxz_L20: parity with exact diagonalisation (same fixture as the dense path).
+      heisenberg_L64: D ramp 64 -> 256 -> 1024 (cutoff 1e-14, 10 Lanczos vectors),
+               two timed sweeps at D=1024; the centre bond's H_eff*x in the
+               block-sparse form vs the dense FP64 form on the same (charge-sorted)
+               tensors, and vs the oracle's block-by-block numpy restatement on the
+               host cores (the reference's symmetric CPU path cannot run here)."""
+    import time as _t
+    from finitemptools_gb300 import DeviceTensor as DT
+    from finitemptools_gb300.u1 import (U1ExpectationCache, U1HeffOp, u1_pack2, u1_randommps,
+                                        u1_twosite, u1_unpack2)
+    out = {}
+    t_start = _t.perf_counter()
+    with open(os.path.join(ROOT, "tests", "golden", "exact_energies.json")) as f:
+        e_ed = json.load(f)["xxz_L20_J1_Jzz1_hz0"]
+    hx = fm.heisenberg_xxz_mpo(1.0, 1.0, 0.0)
+
+    def sweeps(m, D, n, eps, kmax):
+        alg = fm.DMRG2(eig_maxiter=kmax, eig_tol=1e-12, trunc=fm.MPSTruncation(D, eps), svd="dm",
+                       verbosity=0)
+        ts, Es = [], []
+        for _ in range(n):
+            h.synchronize()
+            t0 = _t.perf_counter()
+            E, _ = fm.sweep_(m, alg)
+            h.synchronize()
+            ts.append(_t.perf_counter() - t0)
+            Es.append(E[-1])
+        return ts, Es
+
+    psi = u1_randommps(20, 10, 8, rng=20, handle=h)
+    m = U1ExpectationCache(hx, psi)
+    t20, _ = sweeps(m, 64, 4, 1e-10, 30)
+    E20 = float(fm.expectation(psi, hx))
+    out["xxz_L20_Sz0_D64"] = {"sweep_s": t20, "E": E20, "E_ed": e_ed,
+                              "dE_rel_vs_ed": abs(E20 - e_ed) / abs(e_ed)}
+    del m, psi
+    if _t.perf_counter() - t_start > budget_s:
+        return out
+    L, N = 64, 32
+    psi = u1_randommps(L, N, 16, rng=64, handle=h)
+    m = U1ExpectationCache(hx, psi)
+    # cutoff 1e-14: the bond dimension, not the cutoff, limits the state (at 1e-10
+    # the L=64 ground state stops growing near D=200)
+    tramp, _ = sweeps(m, 64, 1, 1e-14, 10)
+    t2, _ = sweeps(m, 256, 1, 1e-14, 10)
+    tramp += t2
+    t1024, E1024 = sweeps(m, 1024, 2, 1e-14, 10)
+    E = float(fm.expectation(psi, hx))
+    site = L // 2
+    Vl, Vm, Vr = psi.spaces[site], psi.spaces[site + 1], psi.spaces[site + 2]
+    qp = psi.qphys
+    x = u1_twosite(psi[site], psi[site + 1], Vl, Vm, Vr, qp, qp)
+    op = U1HeffOp(m.hstorage[site], m.hstorage[site + 2], m.mpo[site], m.mpo[site + 1], Vl, Vr,
+                  qp, qp, m.qw[site], m.qw[site + 1], m.qw[site + 2])
+    y = DT((op.n,), np.float64, h)
+    h.profile(True)
+    for _ in range(3):
+        op(x, y)
+    h.profile_read(4)
+    for _ in range(10):
+        op(x, y)
+    n_g, ms_g = h.profile_read(4)
+    h.profile(False)
+    ms_u1 = ms_g / max(n_g, 1)
+    X = u1_unpack2(x, Vl, Vr, qp, qp)
+    dop = fm.HeffOp("ac2", m.hstorage[site], m.hstorage[site + 2], W1=m.mpo[site],
+                    W2=m.mpo[site + 1])
+    Y = DT(X.shape, np.float64, h)
+    dop(X, Y)
+    h.synchronize()
+    t0 = _t.perf_counter()
+    for _ in range(3):
+        dop(X, Y)
+    h.synchronize()
+    ms_dense = (_t.perf_counter() - t0) / 3 * 1e3
+    yd = u1_pack2(Y, Vl, Vr, qp, qp).numpy()
+    yu = y.numpy()
+    lz = {}
+    for g in (False, True):
+        h.set_graphs(g)
+        op.lanczos(x, 10, 1e-12)
+        h.synchronize()
+        t0 = _t.perf_counter()
+        op.lanczos(x, 10, 1e-12)
+        h.synchronize()
+        lz["graph" if g else "host_loop"] = (_t.perf_counter() - t0) * 1e3
+    h.set_graphs(True)
+    cpu_ms = None
+    try:   # the oracle's block-by-block restatement on the host cores (baseline leg)
+        from oracle.u1 import Leg, ac2_prime_blocks
+        Lh, Rh, Xh = m.hstorage[site].numpy(), m.hstorage[site + 2].numpy(), X.numpy()
+        vl, vr = Leg(zip(Vl.charges, Vl.dims)), Leg(zip(Vr.charges, Vr.dims))
+        t0 = _t.perf_counter()
+        ac2_prime_blocks(Xh, m.mpo[site], m.mpo[site + 1], Lh, Rh, vl, vr, list(qp), list(qp),
+                         m.qw[site], m.qw[site + 2])
+        cpu_ms = (_t.perf_counter() - t0) * 1e3
+    except Exception as e:     # noqa: BLE001 -- the baseline is optional in the report
+        cpu_ms = "unavailable: %s" % e
+    out["heisenberg_L64_Sz0_D1024"] = {
+        "ramp_sweeps_s": tramp, "sweep_s_D1024": t1024, "E_last_sweeps": E1024, "E": E,
+        "bond_dims_max": max(psi.bond_dimensions()),
+        "centre_leg_sectors": len(Vm.charges), "centre_block_dims": list(Vm.dims),
+        "heff_block_sparse_ms": ms_u1, "heff_block_sparse_flops": op.flops(),
+        "heff_block_sparse_gflops": op.flops() / (ms_u1 * 1e-3) / 1e9,
+        "heff_tile": op.tile(), "heff_dense_fp64_ms": ms_dense,
+        "heff_speedup_vs_dense_fp64": ms_dense / ms_u1,
+        "heff_rel_diff_vs_dense": float(np.linalg.norm(yu - yd) / np.linalg.norm(yd)),
+        "lanczos10_ms": lz, "heff_cpu_oracle_blocks_ms": cpu_ms,
+        "tuning_entries_timed": h.tuning_info(),
+        "note": "sweeps: DMRG2 svd=dm (batched density-matrix sector split), eig_maxiter 10, "
+                "cutoff 1e-14"}
+    return out
+
+
 def config_dict(args, prec):
     return {"workload": "two-site H_eff*x (ac2_prime), Heisenberg Schur MPO w=5, "
                         "x[D,2,2,D], L/R[D,5,D] iid N(0,1) symmetrised",
@@ -334,6 +452,7 @@ def main():
     ap.add_argument("--no-table", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-dmrg", action="store_true")
+    ap.add_argument("--no-u1", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -512,6 +631,9 @@ def main():
     dmrg = None
     if rank == 0 and not args.no_dmrg:
         dmrg = dmrg_section(h, fm)
+    u1 = None
+    if rank == 0 and not args.no_u1:
+        u1 = u1_section(h, fm)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -524,7 +646,7 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": prec, "data": "synthetic",
             "config": config_dict(args, prec), "clocks": clocks, "e2e": e2e,
             "gpu_launches": n_launch, "roofline": roof, "cpu_baseline": cpu,
-            "per_dtype": table, "dmrg": dmrg,
+            "per_dtype": table, "dmrg": dmrg, "u1": u1,
         }
         print(json.dumps(line), flush=True)
     if pg:
