@@ -432,6 +432,51 @@ def u1_section(h, fm, budget_s=150.0):
     return out
 
 
+def u1_heff_case(args):
+    """The block-sparse two-site H_eff*x alone: legs of the centre bond of an L=64,
+    total-Sz=0 chain with bond dimension D (sector dimensions from the product-state
+    counts), iid N(0,1) allowed blocks of L, R and x (seeded), Heisenberg MPO, the
+    32x32 tile forced (no tuning launches).  Warm-up applications, then timed ones;
+    the only grouped launches of the process are these, which is what an ncu capture
+    with -k regex:grouped_kernel -s <warmup> needs."""
+    import finitemptools_gb300 as fm
+    from finitemptools_gb300 import DeviceTensor as DT
+    from finitemptools_gb300.u1 import U1HeffOp, mpo_channel_charges, random_u1_tensors
+    h = fm.default_handle()
+    h.set_tuning(1)
+    L, N, D = 64, 32, args.u1_heff
+    _, spaces = random_u1_tensors(L, N, D, (0, 1), 1)
+    site = L // 2
+    Vl, Vr = spaces[site - 1], spaces[site + 1]
+    Ws = fm.heisenberg_xxz_mpo().site_tensors(L)
+    qw = mpo_channel_charges(Ws, (0, 1))
+    rng = np.random.default_rng(64)
+
+    def env(V, q):
+        bq = V.basis_charges()
+        mask = bq[:, None, None] == bq[None, None, :] + np.asarray(q)[None, :, None]
+        return DT.from_numpy(rng.standard_normal((V.dim, len(q), V.dim)) * mask, h)
+
+    Lm, Rm = env(Vl, qw[site]), env(Vr, qw[site + 2])
+    op = U1HeffOp(Lm, Rm, Ws[site - 1], Ws[site], Vl, Vr, (0, 1), (0, 1), qw[site], qw[site + 1],
+                  qw[site + 2])
+    x = DT.from_numpy(rng.standard_normal(op.n), h)
+    y = DT((op.n,), np.float64, h)
+    for _ in range(args.warmup):
+        op(x, y)
+    h.synchronize()
+    h.profile(True)
+    for _ in range(args.steps):
+        op(x, y)
+    n, ms = h.profile_read(4)
+    h.profile(False)
+    ms = ms / max(n, 1)
+    print(json.dumps({"case": "u1_heff", "L": L, "D": D, "left_leg": list(Vl.dims),
+                      "right_leg": list(Vr.dims), "n_packed": op.n, "flops": op.flops(),
+                      "ms": ms, "gflops": op.flops() / (ms * 1e-3) / 1e9, "tile": op.tile(),
+                      "launches": n}), flush=True)
+
+
 def config_dict(args, prec):
     return {"workload": "two-site H_eff*x (ac2_prime), Heisenberg Schur MPO w=5, "
                         "x[D,2,2,D], L/R[D,5,D] iid N(0,1) symmetrised",
@@ -453,10 +498,15 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-dmrg", action="store_true")
     ap.add_argument("--no-u1", action="store_true")
+    ap.add_argument("--u1-heff", type=int, default=0, metavar="D",
+                    help="only time the block-sparse H_eff*x of an L=64, Sz=0 centre bond "
+                         "with bond dimension D (profiling case) and exit")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return run_reference(args)
+    if args.u1_heff:
+        return u1_heff_case(args)
 
     import torch
     import finitemptools_gb300 as fm
