@@ -96,6 +96,12 @@ SIGNATURES = {
                               dptr, dptr, dptr, P(c_int), P(c_double)]),
     "fmpt_qr": (c_int, [c_void_p, c_int, dptr, c_int, c_int, dptr, dptr]),
     "fmpt_lq": (c_int, [c_void_p, c_int, dptr, c_int, c_int, dptr, dptr]),
+    "fmpt_expm_nodes": (c_int, [c_void_p, c_double, c_double, dptr, c_int, c_int, P(c_double),
+                                dptr, P(c_double)]),
+    "fmpt_wgrad": (c_int, [c_void_p, c_int, dptr, dptr, dptr, dptr, dptr, c_int, c_int, c_int,
+                           c_int, c_int]),
+    "fmpt_swap13": (c_int, [c_void_p, c_int, dptr, dptr, c_int, c_int, c_int, c_int]),
+    "fmpt_qr_adjoint": (c_int, [c_void_p, c_int, dptr, dptr, dptr, dptr, dptr, c_int, c_int]),
     "fmpt_u1_twosite_size": (c_int, [c_void_p, SP, SP, c_int, ip, c_int, ip, P(c_int64)]),
     "fmpt_u1_pack2": (c_int, [c_void_p, c_int, dptr, dptr, SP, SP, c_int, ip, c_int, ip, c_int]),
     "fmpt_u1_op_ac2": (c_int, [c_void_p, c_int, hptr, hptr, dptr, dptr, SP, SP, c_int, ip, c_int,

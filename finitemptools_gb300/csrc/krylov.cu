@@ -794,4 +794,105 @@ int fmpt_exponentiate(fmpt_op* op, double t_re, double t_im, const double* x, do
   return FMPT_OK;
 }
 
+// exp(s_j t H) x for several s_j from ONE Krylov space of x (the quadrature
+// nodes of the exponential's adjoint).  Arnoldi as in fmpt_exponentiate;
+// no step-size control: err_est (host) gets max_j |h_{m+1,m} [exp(s_j t H_m)]_{m,1}|,
+// the usual a-posteriori estimate relative to ||x||.
+int fmpt_expm_nodes(fmpt_op* op, double t_re, double t_im, const double* x, int krylovdim,
+                    int nnodes, const double* nodes, double* out, double* err_est) {
+  if (!op) return FMPT_ERR_ARG;
+  fmpt_handle* h = op->h;
+  if (!x || !out || !nodes || nnodes < 1)
+    return set_error(h, FMPT_ERR_ARG, "expm_nodes: null pointer or no nodes");
+  if (krylovdim < 1 || krylovdim > 31)
+    return set_error(h, FMPT_ERR_ARG, "expm_nodes: krylovdim must be 1..31");
+  const int cp = op->dtype == FMPT_C128;
+  if (!cp && t_im != 0.0)
+    return set_error(h, FMPT_ERR_ARG, "expm_nodes: complex time needs dtype C128");
+  const int64_t n = op->n;
+  const int64_t nr = n * (cp ? 2 : 1);
+  const int G = grid_for(h, nr);
+  const int M = (int)std::min<int64_t>(krylovdim, n);
+  const int ldh = M + 1;
+  DevBuf Vb, zb, part, partM, coef, Hdev, Hd, Ed, acc;
+  FMPT_TRY(Vb.alloc(h, (size_t)(M + 1) * nr * sizeof(double)));
+  FMPT_TRY(zb.alloc(h, (size_t)nr * sizeof(double)));
+  FMPT_TRY(part.alloc(h, (size_t)G * sizeof(double)));
+  FMPT_TRY(partM.alloc(h, (size_t)G * (M + 1) * 2 * sizeof(double)));
+  FMPT_TRY(coef.alloc(h, (size_t)(M + 1) * 2 * sizeof(double)));
+  FMPT_TRY(Hdev.alloc(h, (size_t)ldh * M * 2 * sizeof(double)));
+  FMPT_TRY(Hd.alloc(h, (size_t)nnodes * 32 * 32 * 2 * sizeof(double)));
+  FMPT_TRY(Ed.alloc(h, (size_t)nnodes * 32 * 32 * 2 * sizeof(double)));
+  FMPT_TRY(acc.alloc(h, 2 * sizeof(double)));
+  FMPT_TRY(ensure_pinned(h, (size_t)ldh * M * 2 + 2 * nnodes + 8));
+  double* V = Vb.d();
+  auto V_ = [&](int i) { return V + (int64_t)i * nr; };
+  rdot_partial<<<G, KT, 0, h->stream>>>(nr, x, x, part.d());
+  FMPT_LAUNCHED(h);
+  normalize_from_parts<<<G, KT, 0, h->stream>>>(nr, x, V_(0), part.d(), G, acc.d());
+  FMPT_LAUNCHED(h);
+  FMPT_CUDA(h, cudaMemsetAsync(Hdev.p, 0, Hdev.bytes, h->stream));
+  for (int j = 0; j < M; j++) {
+    double* Hcol = Hdev.d() + (size_t)2 * ldh * j;
+    FMPT_TRY(fmpt_op_apply(op, V_(j), zb.d()));
+    for (int pass = 0; pass < 2; pass++) {
+      multidot_partial<<<G, KT, 0, h->stream>>>(cp, n, j + 1, V, nr, zb.d(), partM.d());
+      FMPT_LAUNCHED(h);
+      multidot_finalize<<<1, KT, 0, h->stream>>>(j + 1, G, partM.d(), coef.d(), Hcol);
+      FMPT_LAUNCHED(h);
+      multi_axpy_sub<<<G, KT, 0, h->stream>>>(cp, n, j + 1, V, nr, coef.d(), zb.d(), part.d());
+      FMPT_LAUNCHED(h);
+    }
+    arnoldi_normalize<<<G, KT, 0, h->stream>>>(nr, zb.d(), part.d(), G, Hcol, j, V_(j + 1));
+    FMPT_LAUNCHED(h);
+  }
+  std::vector<double> Hh((size_t)ldh * M * 2);
+  FMPT_CUDA(h, cudaMemcpyAsync(h->pinned, Hdev.p, Hdev.bytes, cudaMemcpyDeviceToHost, h->stream));
+  FMPT_CUDA(h, cudaStreamSynchronize(h->stream));
+  std::copy(h->pinned, h->pinned + Hh.size(), Hh.begin());
+  for (double v : Hh)
+    if (!std::isfinite(v)) return set_error(h, FMPT_ERR_NONFINITE, "expm_nodes: NaN");
+  int m = M;
+  bool happy = M == n;
+  for (int j = 0; j < M; j++)
+    if (Hh[2 * (j + 1 + (size_t)ldh * j)] == 0.0) { m = j + 1; happy = true; break; }
+  std::vector<double> Hs((size_t)nnodes * 32 * 32 * 2, 0.0);
+  for (int q = 0; q < nnodes; q++) {
+    const double fr = nodes[q] * t_re, fi = nodes[q] * t_im;
+    double* Hq = Hs.data() + (size_t)q * 32 * 32 * 2;
+    for (int c = 0; c < m; c++)
+      for (int r = 0; r < m; r++) {
+        const double hr = Hh[2 * (r + (size_t)ldh * c)], hi = Hh[2 * (r + (size_t)ldh * c) + 1];
+        Hq[2 * (r + (size_t)m * c)] = fr * hr - fi * hi;
+        Hq[2 * (r + (size_t)m * c) + 1] = fr * hi + fi * hr;
+      }
+  }
+  FMPT_CUDA(h, cudaMemcpyAsync(Hd.d(), Hs.data(), Hs.size() * sizeof(double),
+                               cudaMemcpyHostToDevice, h->stream));
+  for (int q = 0; q < nnodes; q++) {
+    const double* Hq = Hd.d() + (size_t)q * 32 * 32 * 2;
+    double* Eq = Ed.d() + (size_t)q * 32 * 32 * 2;
+    small_expm<<<1, dim3(32, 32), 0, h->stream>>>(m, Hq, Eq);
+    FMPT_LAUNCHED(h);
+    double* oq = out + (int64_t)q * nr;
+    combine_basis<<<G, KT, 0, h->stream>>>(cp, n, m, V, nr, Eq, 2, 1.0, 0, oq);
+    FMPT_LAUNCHED(h);
+    scale_by<<<G, KT, 0, h->stream>>>(nr, oq, acc.d());
+    FMPT_LAUNCHED(h);
+    FMPT_CUDA(h, cudaMemcpyAsync(h->pinned + 2 * q, Eq + 2 * (m - 1), 2 * sizeof(double),
+                                 cudaMemcpyDeviceToHost, h->stream));
+  }
+  FMPT_CUDA(h, cudaStreamSynchronize(h->stream));
+  double e = 0.0;
+  if (!happy) {
+    const double hlast = std::abs(Hh[2 * (m + (size_t)ldh * (m - 1))]);
+    for (int q = 0; q < nnodes; q++)
+      e = std::max(e, hlast * std::hypot(h->pinned[2 * q], h->pinned[2 * q + 1]));
+  }
+  if (err_est) *err_est = e;
+  if (op->precision != FMPT_PREC_FP64) FMPT_TRY(op_tc_check(op));
+  if (op->u1) FMPT_TRY(gp_check_status(op->h));
+  return FMPT_OK;
+}
+
 }  // extern "C"

@@ -339,6 +339,34 @@ int fmpt_u1_split(fmpt_handle* h, int dtype, const double* x, const fmpt_u1_spac
                   int maxD, double eps, int side, int method, double* A, double* S, double* B,
                   int cap, int* nsect_out, int* charge_out, int* dim_out, double* err);
 
+/* ------------------------------------- adjoint (reverse-mode) building blocks
+ * For the differentiable one-site TDVP (gradients of an observable after a
+ * TDVP trajectory with respect to the MPO couplings).  The reference has no
+ * gradient code (ChainRulesCore is not one of its dependencies); these are the
+ * backward counterparts of ac_prime (derivatives.jl:2-4), updateleft/right
+ * (mpo/transfer.jl:26-34), leftorth!/rightorth (tdvp.jl:33,55) and the Krylov
+ * exponential (tdvp.jl:3-6).  Cotangents follow zbar = dL/dRe z + i dL/dIm z.
+ *
+ * exp(s_j t H) x for nnodes values s_j (HOST array) from one Krylov space of
+ * dimension krylovdim (<= 31) built from x; out holds nnodes vectors of the
+ * operator's size one after another; err_est (HOST) the a-posteriori error
+ * estimate relative to ||x||. */
+int fmpt_expm_nodes(fmpt_op* op, double t_re, double t_im, const double* x, int krylovdim,
+                    int nnodes, const double* nodes, double* out, double* err_est);
+/* MPO-tensor gradient of Re<a, ac_prime(b, W, L, R)>:
+ * out[w, s', w2, s] = conj(sum conj(a[a',s',b']) L[a',w,a] b[a,s,b] R[b',w2,b])
+ * (device output, wl*d*wr*d elements). */
+int fmpt_wgrad(fmpt_handle* h, int dtype, const double* a, const double* Lenv, const double* b,
+               const double* Renv, double* out, int Dl, int d, int Dr, int wl, int wr);
+/* dst[k, j, i] = src[i, j, k], conjugated when conj != 0 (out of place). */
+int fmpt_swap13(fmpt_handle* h, int dtype, const double* src, double* dst, int n0, int n1, int n2,
+                int conj);
+/* Cotangent of M for the thin QR M = Q R (m >= n, real diagonal of R, the
+ * fmpt_qr convention) given the cotangents Qbar (m x n) and Rbar (n x n);
+ * complex (C128) only. */
+int fmpt_qr_adjoint(fmpt_handle* h, int dtype, const double* Q, const double* R, const double* Qbar,
+                    const double* Rbar, double* Mbar, int m, int n);
+
 #ifdef __cplusplus
 }
 #endif
