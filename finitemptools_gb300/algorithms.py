@@ -248,6 +248,13 @@ def _dmrg1_rightsweep(m, alg):
 
 
 # ----------------------------------------------------------------- TDVP1
+def _env_prec(alg, A):
+    """Arithmetic of TDVP1's environment updates: the contractions' precision for
+    real data; FP64 for complex data (the tensor-core environment update is real
+    only, and at the TDVP bond dimensions it is a small share of a step)."""
+    return "fp64" if A.dtype == np.complex128 else alg.precision
+
+
 def _tdvp1_leftsweep(m, alg):
     """_leftsweep!(m, ::TDVP1) (tdvp.jl:19-44)."""
     increase_bond_env_(m, alg.D)
@@ -264,7 +271,7 @@ def _tdvp1_leftsweep(m, alg):
         Q, v = leftorth(tmp, Dl * d, Dr)
         r = Q.shape[1]
         mps[site] = Q.view_as((Dl, d, r))
-        hnew = updateleft(hs[site], mps[site], mpo[site], mps[site], alg.precision)
+        hnew = updateleft(hs[site], mps[site], mpo[site], mps[site], _env_prec(alg, A))
         opc = HeffOp("c", hnew, hs[site + 1], precision=alg.precision, dtype=A.dtype)
         v = opc.exponentiate(-dt / 2, v, alg.exptol / abs(dt / 2), alg.krylovdim)
         del opc
@@ -289,7 +296,7 @@ def _tdvp1_rightsweep(m, alg):
         r = Q.shape[0]
         mps[site + 1] = Q.view_as((r, d, Dr))
         hnew = updateright(hs[site + 2], mps[site + 1], mpo[site + 1], mps[site + 1],
-                           alg.precision)
+                           _env_prec(alg, B))
         opc = HeffOp("c", hs[site + 1], hnew, precision=alg.precision, dtype=B.dtype)
         v = opc.exponentiate(-dt / 2, v, alg.exptol / abs(dt / 2), alg.krylovdim)
         del opc

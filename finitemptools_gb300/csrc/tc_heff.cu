@@ -48,24 +48,26 @@ __device__ __forceinline__ void put(void* hi, void* lo, int64_t i, double v) {
   }
 }
 
-// xg[a + Kp*m] = x[a + Dl*m] (zero for a >= Dl)
+// xg[a + dld*m] = x[a + Dl*m] for a < Kp (zero for a >= Dl); dld >= Kp is the row
+// stride (2*Kp for the real embedding of complex data: real part, then imaginary part)
 template <int MODE>
 __global__ void conv_state(const double* __restrict__ x, int Dl, int Kp, int64_t M, void* hi,
-                           void* lo) {
+                           void* lo, int64_t dld) {
   const int64_t tot = (int64_t)Kp * M;
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < tot;
        t += (int64_t)gridDim.x * blockDim.x) {
     const int a = (int)(t % Kp);
     const int64_t m = t / Kp;
-    put<MODE>(hi, lo, t, a < Dl ? x[a + (int64_t)Dl * m] : 0.0);
+    put<MODE>(hi, lo, a + dld * m, a < Dl ? x[a + (int64_t)Dl * m] : 0.0);
   }
 }
 
 // batched transpose with conversion:
-//   dst[c + dld*r + dz*z] = src[r + sld*c + sz*z]   for r < R, c < Cp (zero for c >= C)
+//   dst[c + dld*r + dz*z] = scale * src[r + sld*c + sz*z]   for r < R, c < Cp (zero for c >= C)
 template <int MODE>
 __global__ void conv_transpose(const double* __restrict__ src, int64_t sld, int64_t sz, int R,
-                               int C, int Cp, void* hi, void* lo, int64_t dld, int64_t dz) {
+                               int C, int Cp, void* hi, void* lo, int64_t dld, int64_t dz,
+                               double scale) {
   __shared__ double tile[32][33];
   const int z = blockIdx.z;
   const int r0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
@@ -77,7 +79,7 @@ __global__ void conv_transpose(const double* __restrict__ src, int64_t sld, int6
   __syncthreads();
   for (int j = ty; j < 32; j += 8) {
     const int c = c0 + tx, r = r0 + j;
-    if (r < R && c < Cp) put<MODE>(hi, lo, (int64_t)c + dld * r + dz * z, tile[tx][j]);
+    if (r < R && c < Cp) put<MODE>(hi, lo, (int64_t)c + dld * r + dz * z, scale * tile[tx][j]);
   }
 }
 
@@ -215,6 +217,8 @@ __global__ void __launch_bounds__(256) mid_tc_mask(const float* __restrict__ T, 
 
 struct TcState {
   int mode = 0, P = 1, es = 4;
+  bool cplx = false;        // complex data: real embedding, every GEMM's K and N doubled
+  MidSchedule rsched;       // real coefficients of a complex operator's MPO step
   int Kp = 0, Drp = 0;
   int64_t K2 = 0;
   DevBuf Lg[2], Rg[2], xg[2], T1, T3[2];
@@ -234,31 +238,77 @@ int grid1(fmpt_handle* h, int64_t n) {
 
 template <int MODE>
 int launch_transpose(fmpt_handle* h, const double* src, int64_t sld, int64_t sz, int R, int C,
-                     int Cp, int Z, void* hi, void* lo, int64_t dld, int64_t dz) {
+                     int Cp, int Z, void* hi, void* lo, int64_t dld, int64_t dz, double scale) {
   dim3 grid((R + 31) / 32, (Cp + 31) / 32, Z);
   ProfScope prof(h, FMPT_K_CONVERT);
-  conv_transpose<MODE><<<grid, dim3(32, 8), 0, h->stream>>>(src, sld, sz, R, C, Cp, hi, lo, dld, dz);
+  conv_transpose<MODE><<<grid, dim3(32, 8), 0, h->stream>>>(src, sld, sz, R, C, Cp, hi, lo, dld, dz,
+                                                           scale);
   FMPT_LAUNCHED(h);
   return FMPT_OK;
 }
 
 int transpose_any(fmpt_handle* h, int mode, const double* src, int64_t sld, int64_t sz, int R,
-                  int C, int Cp, int Z, void* hi, void* lo, int64_t dld, int64_t dz) {
-  if (mode == M_TF32) return launch_transpose<M_TF32>(h, src, sld, sz, R, C, Cp, Z, hi, lo, dld, dz);
-  if (mode == M_TF32X3) return launch_transpose<M_TF32X3>(h, src, sld, sz, R, C, Cp, Z, hi, lo, dld, dz);
-  return launch_transpose<M_BF16>(h, src, sld, sz, R, C, Cp, Z, hi, lo, dld, dz);
+                  int C, int Cp, int Z, void* hi, void* lo, int64_t dld, int64_t dz,
+                  double scale = 1.0) {
+  if (mode == M_TF32)
+    return launch_transpose<M_TF32>(h, src, sld, sz, R, C, Cp, Z, hi, lo, dld, dz, scale);
+  if (mode == M_TF32X3)
+    return launch_transpose<M_TF32X3>(h, src, sld, sz, R, C, Cp, Z, hi, lo, dld, dz, scale);
+  return launch_transpose<M_BF16>(h, src, sld, sz, R, C, Cp, Z, hi, lo, dld, dz, scale);
+}
+
+inline void* offset(void* p, int64_t elems, int es) {
+  return p ? static_cast<char*>(p) + elems * es : nullptr;
+}
+
+// Complex operand in the real embedding, K-major with row length 2*Kc:
+//   rows [0, N):   [ Re | -Im ]      rows [N, 2N):  [ Im | Re ]
+// from a split-plane complex source read by the same batched transpose as the real case
+// (src plane offset `plane`); N rows; dz is the destination offset of batch z.
+int embed_complex(fmpt_handle* h, int mode, const double* src, int64_t plane, int64_t sld,
+                  int64_t sz, int R, int C, int Cp, int Z, int64_t dz, int64_t N, int Kc,
+                  void* hi, void* lo, int es) {
+  const int64_t dld = 2LL * Kc;
+  const double* re = src;
+  const double* im = src + plane;
+  FMPT_TRY(transpose_any(h, mode, re, sld, sz, R, C, Cp, Z, hi, lo, dld, dz, 1.0));
+  FMPT_TRY(transpose_any(h, mode, im, sld, sz, R, C, Cp, Z, offset(hi, Kc, es), offset(lo, Kc, es),
+                         dld, dz, -1.0));
+  FMPT_TRY(transpose_any(h, mode, im, sld, sz, R, C, Cp, Z, offset(hi, N * dld, es),
+                         offset(lo, N * dld, es), dld, dz, 1.0));
+  return transpose_any(h, mode, re, sld, sz, R, C, Cp, Z, offset(hi, N * dld + Kc, es),
+                       offset(lo, N * dld + Kc, es), dld, dz, 1.0);
 }
 
 }  // namespace
 
 int op_tc_prepare(fmpt_op* op) {
   fmpt_handle* h = op->h;
-  if (op->dtype != FMPT_F64)
-    return set_error(h, FMPT_ERR_UNSUPPORTED, "mixed precision: complex operators not built");
   TcState* st = new TcState();
   op->tc = st;
   st->mode = tc_mode_of(op->precision);
   st->es = st->mode == M_BF16 ? 2 : 4;
+  st->cplx = op->dtype == FMPT_C128;
+  if (st->cplx && op->kind != 2) {
+    // the MPO step of the embedding acts on the real and imaginary planes alike: it needs
+    // real coefficients (true for the spin and fermion MPOs of the configs)
+    const MidSchedule& cs = op->sched;
+    MidSchedule& rs = st->rsched;
+    rs.nw_in = cs.nw_in; rs.nw_out = cs.nw_out; rs.p_in = cs.p_in; rs.p_out = cs.p_out;
+    rs.cplx = 0;
+    rs.blk_win = cs.blk_win;
+    rs.wout_start = cs.wout_start;
+    const size_t pp = (size_t)cs.p_in * cs.p_out;
+    for (size_t e = 0; e < cs.blk_win.size(); e++) {
+      for (size_t q = 0; q < pp; q++) {
+        if (cs.coef[e * 2 * pp + pp + q] != 0.0)
+          return set_error(h, FMPT_ERR_UNSUPPORTED,
+                           "mixed precision, complex data: the MPO must be real");
+        rs.coef.push_back(cs.coef[e * 2 * pp + q]);
+      }
+    }
+    FMPT_TRY(mid_upload(h, rs));
+  }
   const int Dl = op->Dl, Dr = op->Dr, wl = op->wl, wr = op->wr;
   if (op->kind == 2) {
     // c_prime: identity MPO step over w (wl == wr), one "physical" index
@@ -279,15 +329,16 @@ int op_tc_prepare(fmpt_op* op) {
   st->K2 = (int64_t)wr * st->Drp;
   const int split = st->mode == M_TF32X3 ? 2 : 1;
   const size_t es = st->es;
+  const int cf = st->cplx ? 2 : 1;   // the real embedding doubles K and N of both GEMMs
   for (int p = 0; p < split; p++) {
-    FMPT_TRY(st->Lg[p].alloc(h, (size_t)st->Kp * Dl * wl * es));
-    FMPT_TRY(st->Rg[p].alloc(h, (size_t)st->K2 * Dr * es));
-    FMPT_TRY(st->xg[p].alloc(h, (size_t)st->Kp * P * Dr * es));
-    FMPT_TRY(st->T3[p].alloc(h, (size_t)st->K2 * P * Dl * es));
+    FMPT_TRY(st->Lg[p].alloc(h, (size_t)cf * st->Kp * Dl * wl * cf * es));
+    FMPT_TRY(st->Rg[p].alloc(h, (size_t)cf * st->K2 * Dr * cf * es));
+    FMPT_TRY(st->xg[p].alloc(h, (size_t)cf * st->Kp * P * Dr * es));
+    FMPT_TRY(st->T3[p].alloc(h, (size_t)cf * st->K2 * P * Dl * es));
     FMPT_CUDA(h, cudaMemsetAsync(st->T3[p].p, 0, st->T3[p].bytes, h->stream));  // K padding
   }
   {
-    const MidSchedule& ms = op->sched;
+    const MidSchedule& ms = st->cplx && op->kind != 2 ? st->rsched : op->sched;
     if (P == 4 && ms.nw_in <= 8 && ms.nw_out <= 8) {
       std::vector<float> cf(64 * 16, 0.f);
       uint64_t mask = 0;
@@ -307,12 +358,23 @@ int op_tc_prepare(fmpt_op* op) {
   }
   // T1 is BF16 when the BF16 fast MPO step reads it (its values are rounded to BF16 for
   // GEMM 2 anyway), FP32 otherwise; the GEMM-1 output type in op_tc_apply matches this.
-  const bool t1_bf16 = st->mode == M_BF16 && st->fast_mid;
-  FMPT_TRY(st->T1.alloc(h, (size_t)P * Dr * wl * Dl * (t1_bf16 ? 2 : sizeof(float))));
+  const bool t1_bf16 = st->mode == M_BF16 && st->fast_mid && !st->cplx;
+  FMPT_TRY(st->T1.alloc(h, (size_t)cf * P * Dr * wl * Dl * (t1_bf16 ? 2 : sizeof(float))));
   FMPT_CUDA(h, cudaMallocAsync((void**)&st->err, sizeof(int), h->stream));
   FMPT_CUDA(h, cudaMemsetAsync(st->err, 0, sizeof(int), h->stream));
   void* lo_L = split > 1 ? st->Lg[1].p : nullptr;
   void* lo_R = split > 1 ? st->Rg[1].p : nullptr;
+  if (st->cplx) {
+    // rows (a' + Dl*w) of [Re L | -Im L] then [Im L | Re L], K = a (twice)
+    FMPT_TRY(embed_complex(h, st->mode, op->hleft, (int64_t)Dl * wl * Dl, (int64_t)Dl * wl, Dl,
+                           Dl, Dl, st->Kp, wl, 2LL * st->Kp * Dl, (int64_t)Dl * wl, st->Kp,
+                           st->Lg[0].p, lo_L, (int)es));
+    // rows b' of [Re R | -Im R] then [Im R | Re R], K = (b + Drp*w2) (twice)
+    FMPT_TRY(embed_complex(h, st->mode, op->hright, (int64_t)Dr * wr * Dr, (int64_t)Dr * wr, Dr,
+                           Dr, Dr, st->Drp, wr, st->Drp, Dr, (int)st->K2, st->Rg[0].p, lo_R,
+                           (int)es));
+    return FMPT_OK;
+  }
   // Lg[a + Kp*(a' + Dl*w)] = L[a' + Dl*w + Dl*wl*a]: per w, (r=a', c=a)
   FMPT_TRY(transpose_any(h, st->mode, op->hleft, (int64_t)Dl * wl, Dl, Dl, Dl, st->Kp, wl,
                          st->Lg[0].p, lo_L, st->Kp, (int64_t)st->Kp * Dl));
@@ -322,10 +384,13 @@ int op_tc_prepare(fmpt_op* op) {
   return FMPT_OK;
 }
 
+int op_tc_apply_complex(fmpt_op* op, TcState* st, const double* x, double* y);
+
 int op_tc_apply(fmpt_op* op, const double* x, double* y) {
   fmpt_handle* h = op->h;
   TcState* st = static_cast<TcState*>(op->tc);
   if (!st) return set_error(h, FMPT_ERR_ARG, "operator has no tensor-core state");
+  if (st->cplx) return op_tc_apply_complex(op, st, x, y);
   const int Dl = op->Dl, Dr = op->Dr, wl = op->wl, P = st->P;
   const int split = st->mode == M_TF32X3 ? 2 : 1;
   void* xlo = split > 1 ? st->xg[1].p : nullptr;
@@ -334,11 +399,11 @@ int op_tc_apply(fmpt_op* op, const double* x, double* y) {
   {
   ProfScope prof(h, FMPT_K_CONVERT);
   if (st->mode == M_TF32)
-    conv_state<M_TF32><<<grid1(h, nx), 256, 0, h->stream>>>(x, Dl, st->Kp, (int64_t)P * Dr, st->xg[0].p, xlo);
+    conv_state<M_TF32><<<grid1(h, nx), 256, 0, h->stream>>>(x, Dl, st->Kp, (int64_t)P * Dr, st->xg[0].p, xlo, st->Kp);
   else if (st->mode == M_TF32X3)
-    conv_state<M_TF32X3><<<grid1(h, nx), 256, 0, h->stream>>>(x, Dl, st->Kp, (int64_t)P * Dr, st->xg[0].p, xlo);
+    conv_state<M_TF32X3><<<grid1(h, nx), 256, 0, h->stream>>>(x, Dl, st->Kp, (int64_t)P * Dr, st->xg[0].p, xlo, st->Kp);
   else
-    conv_state<M_BF16><<<grid1(h, nx), 256, 0, h->stream>>>(x, Dl, st->Kp, (int64_t)P * Dr, st->xg[0].p, xlo);
+    conv_state<M_BF16><<<grid1(h, nx), 256, 0, h->stream>>>(x, Dl, st->Kp, (int64_t)P * Dr, st->xg[0].p, xlo, st->Kp);
   FMPT_LAUNCHED(h);
   }
   // GEMM 1: T1[(s b), (a' w)] = sum_a xg[a, (s b)] Lg[a, (a' w)]
@@ -381,6 +446,79 @@ int op_tc_apply(fmpt_op* op, const double* x, double* y) {
   FMPT_TRY(tc_gemm(h, st->mode, P * Dl, Dr, (int)st->K2, 1, A2, B2, y, 1, (int64_t)P * Dl, 0,
                    st->err));
   return FMPT_OK;
+}
+
+// Complex data in the real embedding (split planes in, split planes out):
+//   GEMM 1  T1[(s b), (a' w)] (+ imaginary plane) = xg'[(s b), 2K] . Lg'[(a' w) x 2, 2K]
+//           with xg' rows [Re x | Im x] and Lg' rows [Re L | -Im L], [Im L | Re L]; the
+//           doubled N makes the second half of the output exactly the imaginary plane
+//   MPO     the real step on each plane, written as T3' rows [Re T3 | Im T3]
+//   GEMM 2  y (both planes) = T3'[(a' s'), 2 K2] . Rg'[b' x 2, 2 K2]
+int op_tc_apply_complex(fmpt_op* op, TcState* st, const double* x, double* y) {
+  fmpt_handle* h = op->h;
+  const int Dl = op->Dl, Dr = op->Dr, wl = op->wl, P = st->P;
+  const int split = st->mode == M_TF32X3 ? 2 : 1;
+  const int es = st->es;
+  void* xlo = split > 1 ? st->xg[1].p : nullptr;
+  void* tlo = split > 1 ? st->T3[1].p : nullptr;
+  const int64_t nplane = (int64_t)Dl * P * Dr;
+  const int64_t nx = (int64_t)st->Kp * P * Dr;
+  {
+    ProfScope prof(h, FMPT_K_CONVERT);
+    for (int part = 0; part < 2; part++) {
+      const double* src = x + part * nplane;
+      void* hi = offset(st->xg[0].p, part * st->Kp, es);
+      void* lo = offset(xlo, part * st->Kp, es);
+      if (st->mode == M_TF32)
+        conv_state<M_TF32><<<grid1(h, nx), 256, 0, h->stream>>>(src, Dl, st->Kp, (int64_t)P * Dr, hi, lo, 2LL * st->Kp);
+      else if (st->mode == M_TF32X3)
+        conv_state<M_TF32X3><<<grid1(h, nx), 256, 0, h->stream>>>(src, Dl, st->Kp, (int64_t)P * Dr, hi, lo, 2LL * st->Kp);
+      else
+        conv_state<M_BF16><<<grid1(h, nx), 256, 0, h->stream>>>(src, Dl, st->Kp, (int64_t)P * Dr, hi, lo, 2LL * st->Kp);
+      FMPT_LAUNCHED(h);
+    }
+  }
+  TcOperand A1{st->xg[0].p, xlo, 2LL * st->Kp, 0};
+  TcOperand B1{st->Lg[0].p, split > 1 ? st->Lg[1].p : nullptr, 2LL * st->Kp, 0};
+  FMPT_TRY(tc_gemm(h, st->mode, P * Dr, 2 * wl * Dl, 2 * st->Kp, 1, A1, B1, st->T1.p, 0,
+                   (int64_t)P * Dr, 0, st->err));
+  {
+    const int64_t nt = (int64_t)Dl * Dr;
+    const unsigned blocks = (unsigned)((nt + 255) / 256);
+    const MidSchedule& s = op->kind == 2 ? op->sched : st->rsched;
+    const int64_t t1plane = (int64_t)P * Dr * wl * Dl;
+    const int64_t K2c = 2 * st->K2;     // row stride of T3'
+    ProfScope prof(h, FMPT_K_MPO_STEP);
+    for (int part = 0; part < 2; part++) {
+      const float* t1 = static_cast<const float*>(st->T1.p) + part * t1plane;
+      void* hi = offset(st->T3[0].p, part * st->K2, es);
+      void* lo = offset(tlo, part * st->K2, es);
+      if (st->fast_mid) {
+        const float* cf = (const float*)st->cfast.p;
+        if (st->mode == M_TF32)
+          mid_tc_p4<M_TF32><<<blocks, 256, 0, h->stream>>>((const float4*)t1, Dl, Dr, st->Drp, K2c, s.nw_in, s.nw_out, st->mask, cf, hi, lo);
+        else if (st->mode == M_TF32X3)
+          mid_tc_p4<M_TF32X3><<<blocks, 256, 0, h->stream>>>((const float4*)t1, Dl, Dr, st->Drp, K2c, s.nw_in, s.nw_out, st->mask, cf, hi, lo);
+        else
+          mid_tc_p4<M_BF16><<<blocks, 256, 0, h->stream>>>((const float4*)t1, Dl, Dr, st->Drp, K2c, s.nw_in, s.nw_out, st->mask, cf, hi, lo);
+      } else {
+#define MIDTCC(MODE_, MP_)                                                                   \
+  mid_tc<MODE_, MP_><<<blocks, 256, 0, h->stream>>>(t1, P, Dl, Dr, st->Drp, K2c, s.nw_out,    \
+                                                    s.d_win, s.d_wstart, s.d_coef, hi, lo)
+        if (P <= 4) {
+          if (st->mode == M_TF32) MIDTCC(M_TF32, 4); else if (st->mode == M_TF32X3) MIDTCC(M_TF32X3, 4); else MIDTCC(M_BF16, 4);
+        } else {
+          if (st->mode == M_TF32) MIDTCC(M_TF32, 16); else if (st->mode == M_TF32X3) MIDTCC(M_TF32X3, 16); else MIDTCC(M_BF16, 16);
+        }
+#undef MIDTCC
+      }
+      FMPT_LAUNCHED(h);
+    }
+  }
+  TcOperand A2{st->T3[0].p, tlo, 2 * st->K2, 0};
+  TcOperand B2{st->Rg[0].p, split > 1 ? st->Rg[1].p : nullptr, 2 * st->K2, 0};
+  return tc_gemm(h, st->mode, P * Dl, 2 * Dr, (int)(2 * st->K2), 1, A2, B2, y, 1, (int64_t)P * Dl,
+                 0, st->err);
 }
 
 // ---------------------------------------------------------------------------
@@ -436,11 +574,11 @@ int conv_state_any(fmpt_handle* h, int mode, const double* x, int K, int Kp, int
   const int64_t n = (int64_t)Kp * M;
   ProfScope prof(h, FMPT_K_CONVERT);
   if (mode == M_TF32)
-    conv_state<M_TF32><<<grid1(h, n), 256, 0, h->stream>>>(x, K, Kp, M, hi, lo);
+    conv_state<M_TF32><<<grid1(h, n), 256, 0, h->stream>>>(x, K, Kp, M, hi, lo, Kp);
   else if (mode == M_TF32X3)
-    conv_state<M_TF32X3><<<grid1(h, n), 256, 0, h->stream>>>(x, K, Kp, M, hi, lo);
+    conv_state<M_TF32X3><<<grid1(h, n), 256, 0, h->stream>>>(x, K, Kp, M, hi, lo, Kp);
   else
-    conv_state<M_BF16><<<grid1(h, n), 256, 0, h->stream>>>(x, K, Kp, M, hi, lo);
+    conv_state<M_BF16><<<grid1(h, n), 256, 0, h->stream>>>(x, K, Kp, M, hi, lo, Kp);
   FMPT_LAUNCHED(h);
   return FMPT_OK;
 }

@@ -150,3 +150,63 @@ def test_env_updates_mixed(prec, Dl, Dr, wl, wr, d):
     assert rel(gl, O.updateleft(Lh, A, W, B)) < tol(prec, K)
     gr = fm.updateright(DT.from_numpy(Rh), DT.from_numpy(A), W, DT.from_numpy(B), prec).numpy()
     assert rel(gr, O.updateright(Rh, A, W, B)) < tol(prec, K)
+
+
+# ------------------------------------------------------------ complex data
+def cherm(rng, D, w):
+    E = rng.standard_normal((D, w, D)) + 1j * rng.standard_normal((D, w, D))
+    return 0.5 * (E + np.conj(E.transpose(2, 1, 0)))
+
+
+@pytest.mark.parametrize("prec", ["tf32x3", "tf32", "bf16"])
+@pytest.mark.parametrize("Dl,Dr", [(7, 13), (64, 64), (100, 37)])
+def test_complex_mixed_forms(prec, Dl, Dr):
+    """Complex data on the tensor cores through the real embedding (split
+    planes): ac2, ac and c against complex FP64, same bounds as the real forms
+    with K doubled (the embedding sums real and imaginary products)."""
+    rng = np.random.default_rng(Dl + 7 * Dr)
+    W = heisenberg_xxz_mpo(1.0, 0.7, 0.2)[1].dense()
+    L, R = cherm(rng, Dl, 5), cherm(rng, Dr, 5)
+    dL, dR = DT.from_numpy(L), DT.from_numpy(R)
+    x2 = rng.standard_normal((Dl, 2, 2, Dr)) + 1j * rng.standard_normal((Dl, 2, 2, Dr))
+    ref = O.ac2_prime(x2, W, W, L, R)
+    y = fm.ac2_prime(DT.from_numpy(x2), W, W, dL, dR, precision=prec).numpy()
+    assert rel(y, ref) < tol(prec, 2 * (Dl + 5 * Dr)), rel(y, ref)
+    x1 = rng.standard_normal((Dl, 2, Dr)) + 1j * rng.standard_normal((Dl, 2, Dr))
+    ref = O.ac_prime(x1, W, L, R)
+    y = fm.ac_prime(DT.from_numpy(x1), W, dL, dR, precision=prec).numpy()
+    assert rel(y, ref) < tol(prec, 2 * (Dl + 5 * Dr)), rel(y, ref)
+    C = rng.standard_normal((Dl, Dr)) + 1j * rng.standard_normal((Dl, Dr))
+    ref = O.c_prime(C, L, R)
+    y = fm.c_prime(DT.from_numpy(C), dL, dR, precision=prec).numpy()
+    assert rel(y, ref) < tol(prec, 2 * (Dl + 5 * Dr)), rel(y, ref)
+
+
+def test_complex_mixed_rejects_complex_mpo():
+    rng = np.random.default_rng(5)
+    W = heisenberg_xxz_mpo()[1].dense().astype(np.complex128)
+    W[0, 0, 1, 1] += 0.1j
+    L, R = cherm(rng, 8, 5), cherm(rng, 8, 5)
+    x = rng.standard_normal((8, 2, 8)) + 0j
+    with pytest.raises(fm.FMPTError):
+        fm.ac_prime(DT.from_numpy(x), W, DT.from_numpy(L), DT.from_numpy(R), precision="tf32x3")
+
+
+def test_tdvp1_complex_mixed_matches_fp64():
+    """Config 5's chosen form: TDVP1 with 3xTF32 complex contractions (FP64
+    Krylov, QR and environment updates) tracks the FP64 trajectory."""
+    rng = np.random.default_rng(40)
+    L = 12
+    hs = 1.0 + 0.1 * rng.standard_normal(L)
+    psi0 = fm.randommps(L, 2, 16, rng, dtype=np.complex128)
+    fm.canonicalize_(psi0, normalize=True)
+    Z = np.diag([-1.0, 1.0])
+    vals = {}
+    for prec in ("fp64", "tf32x3"):
+        psi = fm.FiniteMPS([A.copy() for A in psi0.data])
+        env = fm.environments(fm.tfi_mpo(hs), psi)
+        alg = fm.TDVP1(stepsize=-0.05j, D=16, exptol=1e-8, krylovdim=20, precision=prec)
+        for _ in range(5):
+            fm.sweep_(env, alg)
+        vals[prec] = [float(np.real(fm.expectation_local(env.mps, i, Z))) for i in (3, 6, 9)]
+    assert np.abs(np.array(vals["tf32x3"]) - np.array(vals["fp64"])).max() < 1e-5
