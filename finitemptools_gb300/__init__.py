@@ -8,13 +8,15 @@ call raises ``FMPTError`` when the library or a GPU is missing.
 """
 
 from ._native import FMPTError, lib  # noqa: F401
-from .algorithms import (DMRG1, DMRG2, TDVP1, Defaults, compute_, expectation,  # noqa: F401
+from .algorithms import (DMRG1, DMRG1S, DMRG2, TDVP1, TDVP1S, TDVP2, Defaults,  # noqa: F401
+                         compute_, expectation,  # noqa: F401
                          expectation_local, ground_state_, leftsweep_, rightsweep_, sweep_)
 from .auxiliary import (MPSTruncation, default_truncation, leftorth, rightorth,  # noqa: F401
                         stable_tsvd)
 from .derivatives import HeffOp, ac2_prime, ac_prime, c_prime, exponentiate  # noqa: F401
 from .derivatives import simple_lanczos_solver  # noqa: F401
 from .device import DeviceTensor, Handle, default_handle  # noqa: F401
+from .expansion import OptimalExpansion, default_expansion  # noqa: F401
 from .envs import (ExpectationCache, environments, init_hstorage_, updateleft_,  # noqa: F401
                    updateright_)
 from .mps import (FiniteMPS, bond_dimension, canonicalize_, increase_bond_,  # noqa: F401

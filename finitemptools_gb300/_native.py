@@ -101,6 +101,8 @@ SIGNATURES = {
     "fmpt_wgrad": (c_int, [c_void_p, c_int, dptr, dptr, dptr, dptr, dptr, c_int, c_int, c_int,
                            c_int, c_int]),
     "fmpt_swap13": (c_int, [c_void_p, c_int, dptr, dptr, c_int, c_int, c_int, c_int]),
+    "fmpt_copy2d": (c_int, [c_void_p, c_int, c_int, c_int, dptr, c_int64, c_int64, dptr, c_int64,
+                            c_int64]),
     "fmpt_qr_adjoint": (c_int, [c_void_p, c_int, dptr, dptr, dptr, dptr, dptr, c_int, c_int]),
     "fmpt_u1_twosite_size": (c_int, [c_void_p, SP, SP, c_int, ip, c_int, ip, P(c_int64)]),
     "fmpt_u1_pack2": (c_int, [c_void_p, c_int, dptr, dptr, SP, SP, c_int, ip, c_int, ip, c_int]),

@@ -16,10 +16,13 @@ from .derivatives import HeffOp
 from .device import DeviceTensor
 from .envs import ExpectationCache, environments, increase_bond_env_, updateleft_, updateright_
 from .transfer import updateleft, updateright
+from .expansion import (DMRG1S, TDVP1S, TDVP2, dmrg1s_leftsweep_, dmrg1s_rightsweep_,
+                        tdvp1s_sweep_, tdvp2_sweep_)
 from .u1 import U1ExpectationCache, U1FiniteMPS, u1_expectation, u1_leftsweep_, u1_rightsweep_
 from .utilities import MPOHamiltonian
 
-__all__ = ["Defaults", "DMRG1", "DMRG2", "TDVP1", "leftsweep_", "rightsweep_", "sweep_",
+__all__ = ["Defaults", "DMRG1", "DMRG2", "DMRG1S", "TDVP1", "TDVP2", "TDVP1S", "leftsweep_",
+           "rightsweep_", "sweep_",
            "compute_", "ground_state_", "expectation", "expectation_local"]
 
 
@@ -119,6 +122,8 @@ def leftsweep_(m, alg):
         if not isinstance(alg, DMRG2):
             raise NotImplementedError("U(1) tensors: DMRG2 sweeps only")
         return u1_leftsweep_(m, alg)
+    if isinstance(alg, DMRG1S):
+        return dmrg1s_leftsweep_(m, alg)
     if isinstance(alg, DMRG1):
         return _dmrg1_leftsweep(m, alg)
     m.precision = alg.env_precision
@@ -136,6 +141,8 @@ def rightsweep_(m, alg):
         if not isinstance(alg, DMRG2):
             raise NotImplementedError("U(1) tensors: DMRG2 sweeps only")
         return u1_rightsweep_(m, alg)
+    if isinstance(alg, DMRG1S):
+        return dmrg1s_rightsweep_(m, alg)
     if isinstance(alg, DMRG1):
         return _dmrg1_rightsweep(m, alg)
     m.precision = alg.env_precision
@@ -316,6 +323,12 @@ def sweep_(m, alg):
         _tdvp1_leftsweep(m, alg)
         _tdvp1_rightsweep(m, alg)
         return None
+    if isinstance(alg, TDVP2):
+        tdvp2_sweep_(m, alg)
+        return None
+    if isinstance(alg, TDVP1S):
+        tdvp1s_sweep_(m, alg)
+        return None
     E1, d1 = leftsweep_(m, alg)
     E2, d2 = rightsweep_(m, alg)
     return E1 + E2, max(d1, d2)
@@ -334,8 +347,8 @@ def compute_(env, alg):
 
 
 def ground_state_(state, h, alg=None):
-    """ground_state!(state, h, alg) (dmrg.jl:240)."""
-    alg = alg if alg is not None else DMRG2()
+    """ground_state!(state, h, alg=DMRG1S()) (dmrg.jl:240)."""
+    alg = alg if alg is not None else DMRG1S()
     if isinstance(state, U1FiniteMPS):
         return compute_(U1ExpectationCache(h, state), alg)
     return compute_(environments(h, state, alg.precision), alg)

@@ -136,6 +136,19 @@ GemmArgs cgemm(int ta, int tb, int m, int n, int k, double alpha, double beta, c
   return g;
 }
 
+// dst(i, j) = src(i, j) for an m x n block; complex: split planes at the given offsets
+__global__ void copy2d_kernel(int cplx, int m, int n, const double* __restrict__ src, int64_t lds,
+                              int64_t ps, double* __restrict__ dst, int64_t ldd, int64_t pd) {
+  const int64_t tot = (int64_t)m * n;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < tot;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(t % m);
+    const int64_t j = t / m;
+    dst[i + ldd * j] = src[i + lds * j];
+    if (cplx) dst[pd + i + ldd * j] = src[ps + i + lds * j];
+  }
+}
+
 }  // namespace
 }  // namespace fmpt
 
@@ -171,6 +184,21 @@ int fmpt_wgrad(fmpt_handle* h, int dtype, const double* a, const double* Lenv, c
   const int nout = wl * d * wr * d;
   wgrad_reduce<<<nout, AT, 0, h->stream>>>(cp, Dl, d, Dr, wl, wr, a, (int64_t)Dl * d * Dr, Q.d(),
                                            nQ, out, nout);
+  FMPT_LAUNCHED(h);
+  return FMPT_OK;
+}
+
+int fmpt_copy2d(fmpt_handle* h, int dtype, int m, int n, const double* src, int64_t lds,
+                int64_t plane_src, double* dst, int64_t ldd, int64_t plane_dst) {
+  if (!h) return FMPT_ERR_ARG;
+  if (m < 0 || n < 0) return set_error(h, FMPT_ERR_SHAPE, "copy2d: negative extent");
+  if ((int64_t)m * n == 0) return FMPT_OK;
+  if (!src || !dst) return set_error(h, FMPT_ERR_ARG, "copy2d: null pointer");
+  if (lds < m || ldd < m) return set_error(h, FMPT_ERR_SHAPE, "copy2d: leading dimension < rows");
+  const int64_t tot = (int64_t)m * n;
+  const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((tot + 255) / 256, 8LL * h->sm_count));
+  copy2d_kernel<<<blocks, 256, 0, h->stream>>>(dtype == FMPT_C128, m, n, src, lds, plane_src, dst,
+                                               ldd, plane_dst);
   FMPT_LAUNCHED(h);
   return FMPT_OK;
 }

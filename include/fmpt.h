@@ -358,6 +358,11 @@ int fmpt_expm_nodes(fmpt_op* op, double t_re, double t_im, const double* x, int 
  * (device output, wl*d*wr*d elements). */
 int fmpt_wgrad(fmpt_handle* h, int dtype, const double* a, const double* Lenv, const double* b,
                const double* Renv, double* out, int Dl, int d, int Dr, int wl, int wr);
+/* dst(i, j) = src(i, j) for an m x n column-major block (leading dimensions lds,
+ * ldd; complex split planes at the element offsets plane_src / plane_dst): the
+ * catdomain / catcodomain concatenations of the subspace expansion. */
+int fmpt_copy2d(fmpt_handle* h, int dtype, int m, int n, const double* src, int64_t lds,
+                int64_t plane_src, double* dst, int64_t ldd, int64_t plane_dst);
 /* dst[k, j, i] = src[i, j, k], conjugated when conj != 0 (out of place). */
 int fmpt_swap13(fmpt_handle* h, int dtype, const double* src, double* dst, int n0, int n1, int n2,
                 int conj);
