@@ -192,6 +192,8 @@ def dmrg_section(h, fm, budget_s=150.0):
     split), each energy evaluated in FP64 as <psi|H|psi> of the final state.
       xxz_L20: XXZ L=20, Delta=1, D=64, cutoff 1e-10, 4 sweeps from a seeded D=8
                right-canonical state; the exact energy is the ED fixture.
+      xxz_L20_D64_dmrg1s: the same chain and start with DMRG1S + OptimalExpansion, FP64,
+               6 sweeps.
       j1j2_L100_D1024: J1-J2 L=100, J1=1, J2=0.3, cutoff 1e-9, ramp 64 -> 256 -> 1024 in
                the mixed form, then one timed mixed sweep at D=1024; the FP64 sweep
                time is extrapolated from three centre bonds timed in both forms.
@@ -230,6 +232,26 @@ def dmrg_section(h, fm, budget_s=150.0):
     out["xxz_L20_D64"] = {"sweep_s_fp64": t64, "sweep_s_mixed": tmx, "E_fp64": E64,
                           "E_mixed_fp64_eval": Emx, "dE_rel_mixed_vs_fp64": abs(Emx - E64) / abs(E64),
                           "E_ed": e_ed, "dE_rel_fp64_vs_ed": abs(E64 - e_ed) / abs(e_ed)}
+    # DMRG1S with OptimalExpansion (the reference's default ground-state algorithm), same
+    # chain, start and truncation as the FP64 DMRG2 run above
+    rng = np.random.default_rng(20)
+    psi1 = fm.randommps(20, 2, 8, rng, handle=h)
+    fm.canonicalize_(psi1, normalize=True)
+    env1 = fm.environments(fm.FiniteMPO(hx, 20), psi1)
+    alg1 = fm.DMRG1S(eig_maxiter=30, eig_tol=1e-12, trunc=fm.MPSTruncation(64, 1e-10),
+                     verbosity=0)
+    t1s = []
+    for _ in range(6):
+        h.synchronize()
+        t0 = _t.perf_counter()
+        fm.sweep_(env1, alg1)
+        h.synchronize()
+        t1s.append(_t.perf_counter() - t0)
+    E1 = float(fm.expectation(env1.mps, fm.FiniteMPO(hx, 20)))
+    out["xxz_L20_D64_dmrg1s"] = {"sweep_s_fp64": t1s, "E_fp64": E1, "E_ed": e_ed,
+                                 "dE_rel_vs_ed": abs(E1 - e_ed) / abs(e_ed),
+                                 "Dmax": fm.bond_dimension(env1.mps)}
+    del env1, psi1
     if _t.perf_counter() - t_start > budget_s:
         return out
     hj = fm.j1j2_heisenberg_mpo(1.0, 0.3)
@@ -329,26 +351,34 @@ def dmrg_section(h, fm, budget_s=150.0):
         return out
     # one-site TDVP trajectory: TFI L=40, h_i = 1 + 0.1 N(0,1), complex128, D=64,
     # dt=0.05 (stepsize -0.05i), Krylov dimension 20; <Z_20> after the timed steps
+    # (the same trajectory with the contractions in 3xTF32: complex data on the tensor
+    # cores through the real embedding, FP64 Krylov, QR and environment updates)
     L = 40
-    rng = np.random.default_rng(40)
-    hs = 1.0 + 0.1 * rng.standard_normal(L)
-    htfi = fm.tfi_mpo(hs)
-    psi = fm.randommps(L, 2, 64, rng, dtype=np.complex128, handle=h)
-    fm.canonicalize_(psi, normalize=True)
-    envt = fm.environments(fm.FiniteMPO(htfi, L), psi)
-    alg = fm.TDVP1(stepsize=-0.05j, D=64, exptol=1e-8, krylovdim=20)
-    fm.sweep_(envt, alg)                                 # first step (bond growth, warm-up)
-    nsteps = 10
-    h.synchronize()
-    t0 = _t.perf_counter()
-    for _ in range(nsteps):
-        fm.sweep_(envt, alg)
-    h.synchronize()
-    tstep = (_t.perf_counter() - t0) / nsteps
     Z = np.diag([-1.0, 1.0])
+    nsteps = 10
+    res = {}
+    for prec in ("fp64", "tf32x3"):
+        rng = np.random.default_rng(40)
+        hs = 1.0 + 0.1 * rng.standard_normal(L)
+        htfi = fm.tfi_mpo(hs)
+        psi = fm.randommps(L, 2, 64, rng, dtype=np.complex128, handle=h)
+        fm.canonicalize_(psi, normalize=True)
+        envt = fm.environments(fm.FiniteMPO(htfi, L), psi)
+        alg = fm.TDVP1(stepsize=-0.05j, D=64, exptol=1e-8, krylovdim=20, precision=prec)
+        fm.sweep_(envt, alg)                             # first step (bond growth, warm-up)
+        h.synchronize()
+        t0 = _t.perf_counter()
+        for _ in range(nsteps):
+            fm.sweep_(envt, alg)
+        h.synchronize()
+        res[prec] = ((_t.perf_counter() - t0) / nsteps,
+                     float(np.real(fm.expectation_local(envt.mps, 20, Z))))
+        del envt, psi
+    tstep = res["fp64"][0]
     out["tdvp1_tfi_L40_D64"] = {"s_per_step_fp64_complex": tstep, "steps_timed": nsteps,
-                                "Z20_after_%d_steps" % (nsteps + 1):
-                                    float(np.real(fm.expectation_local(envt.mps, 20, Z))),
+                                "s_per_step_tf32x3_complex": res["tf32x3"][0],
+                                "Z20_after_%d_steps" % (nsteps + 1): res["fp64"][1],
+                                "Z20_tf32x3_minus_fp64": res["tf32x3"][1] - res["fp64"][1],
                                 "note": "100 steps extrapolate to %.1f s" % (100 * tstep)}
     return out
 

@@ -15,6 +15,7 @@ from .auxiliary import (MPSTruncation, default_truncation, dm_split, dot, gemm, 
 from .derivatives import HeffOp
 from .device import DeviceTensor
 from .envs import ExpectationCache, environments, increase_bond_env_, updateleft_, updateright_
+from .excited import project_, projectors1, projectors2
 from .transfer import updateleft, updateright
 from .expansion import (DMRG1S, TDVP1S, TDVP2, dmrg1s_leftsweep_, dmrg1s_rightsweep_,
                         tdvp1s_sweep_, tdvp2_sweep_)
@@ -85,6 +86,24 @@ def _two_site(A, B):
     return gemm(A, B, (Dl, d1, d2, Dr), Dl * d1, d2 * Dr, Dm)
 
 
+def _project_op(op, x, ps):
+    """Projected caches (dmrgexcited.jl:96-102, :124-130): x = _project!(x, ps) in
+    place (the projected tensor is the one the fidelity is measured against)
+    and op composed with _project!.  No-op without projectors."""
+    if ps:
+        project_(x, ps)
+        op.set_projectors(ps)
+
+
+def _start_vector(op, A, ps):
+    """One-site start vector: _project!(copy(mps[site]), p1) for projected caches
+    (dmrgexcited.jl:20-23), with op composed with _project!; A itself otherwise."""
+    if not ps:
+        return A
+    op.set_projectors(ps)
+    return project_(A.copy(), ps)
+
+
 def _dmrg2_bond_left(m, site, alg):
     """leftsweep! bond body (dmrg.jl:95-113): mps[site] = u, mps[site+1] = s*v."""
     mps, mpo, hs = m.mps, m.mpo, m.hstorage
@@ -92,6 +111,7 @@ def _dmrg2_bond_left(m, site, alg):
     Dl, d1, d2, Dr = x2.shape
     op = HeffOp("ac2", hs[site], hs[site + 2], W1=mpo[site], W2=mpo[site + 1],
                 precision=alg.precision, dtype=x2.dtype)
+    _project_op(op, x2, projectors2(m, site))
     E, vecs, info, k = op.lanczos(x2, alg.eig_maxiter, alg.eig_tol, alg.reorth)
     del op
     if alg.svd == "dm":
@@ -162,6 +182,7 @@ def _dmrg2_bond_right(m, site, alg):
     Dl, d1, d2, Dr = x2.shape
     op = HeffOp("ac2", hs[site], hs[site + 2], W1=mpo[site], W2=mpo[site + 1],
                 precision=alg.precision, dtype=x2.dtype)
+    _project_op(op, x2, projectors2(m, site))
     E, vecs, info, k = op.lanczos(x2, alg.eig_maxiter, alg.eig_tol, alg.reorth)
     del op
     if alg.svd == "dm":
@@ -221,7 +242,8 @@ def _dmrg1_leftsweep(m, alg):
         A = mps[site]
         op = HeffOp("ac", hs[site], hs[site + 1], W1=mpo[site], precision=alg.precision,
                     dtype=A.dtype)
-        E, vec, _, _ = op.lanczos(A, alg.eig_maxiter, alg.eig_tol, alg.reorth)
+        x0 = _start_vector(op, A, projectors1(m, site))
+        E, vec, _, _ = op.lanczos(x0, alg.eig_maxiter, alg.eig_tol, alg.reorth)
         Es.append(E)
         delta = max(delta, _galerkin(m, site, alg.precision))
         Dl, d, Dr = A.shape
@@ -241,7 +263,8 @@ def _dmrg1_rightsweep(m, alg):
         A = mps[site]
         op = HeffOp("ac", hs[site], hs[site + 1], W1=mpo[site], precision=alg.precision,
                     dtype=A.dtype)
-        E, vec, _, _ = op.lanczos(A, alg.eig_maxiter, alg.eig_tol, alg.reorth)
+        x0 = _start_vector(op, A, projectors1(m, site))
+        E, vec, _, _ = op.lanczos(x0, alg.eig_maxiter, alg.eig_tol, alg.reorth)
         Es.append(E)
         delta = max(delta, _galerkin(m, site, alg.precision))
         Dl, d, Dr = A.shape

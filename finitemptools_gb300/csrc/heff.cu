@@ -340,9 +340,14 @@ int fmpt_op_c(fmpt_handle* h, int dtype, int precision, const double* hleft,
 int fmpt_op_apply(fmpt_op* op, const double* x, double* y) {
   if (!op) return FMPT_ERR_ARG;
   if (!x || !y) return set_error(op->h, FMPT_ERR_ARG, "op_apply: null vector");
-  if (op->u1) return op_u1_apply(op, x, y);
-  if (op->precision != FMPT_PREC_FP64) return op_tc_apply(op, x, y);
-  return op_apply_fp64(op, x, y);
+  if (op->u1) {
+    FMPT_TRY(op_u1_apply(op, x, y));
+  } else if (op->precision != FMPT_PREC_FP64) {
+    FMPT_TRY(op_tc_apply(op, x, y));
+  } else {
+    FMPT_TRY(op_apply_fp64(op, x, y));
+  }
+  return op_project(op, y);
 }
 
 int64_t fmpt_op_size(fmpt_op* op) { return op ? op->n : -1; }
@@ -352,6 +357,7 @@ int fmpt_op_destroy(fmpt_op* op) {
   mid_free(op->h, op->sched);
   op_tc_free(op);
   op_u1_free(op);
+  if (op->proj_part) cudaFreeAsync(op->proj_part, op->h->stream);
   delete op;
   return FMPT_OK;
 }

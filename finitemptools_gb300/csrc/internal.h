@@ -233,6 +233,11 @@ struct fmpt_op {
   int64_t n = 0;          // vector length (complex elements for C128)
   void* tc = nullptr;     // tensor-core state (mixed precision), owned
   void* u1 = nullptr;     // U(1) block-sparse state (grouped program + scratch), owned
+  // projectors of the excited-state sweeps: after every application
+  // y -= dot(y, p) p for each p in order (device vectors of n elements, not owned)
+  std::vector<const double*> proj;
+  double* proj_part = nullptr;   // 2 * proj_G block partials, owned
+  int proj_G = 0;
 };
 
 namespace fmpt {
@@ -246,6 +251,8 @@ int env_update_tc(fmpt_handle* h, bool right, int precision, const double* hold,
                   int wr);
 void op_tc_free(fmpt_op* op);
 int op_u1_apply(fmpt_op* op, const double* x, double* y, const int* gate = nullptr);
+// the projections of op->proj applied to y in place (no-op without projectors)
+int op_project(fmpt_op* op, double* y, const int* gate = nullptr);
 void op_u1_free(fmpt_op* op);
 
 // K-major tensor-core operand: TF32 (float storage) or BF16 plane, optional

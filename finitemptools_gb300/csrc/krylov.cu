@@ -474,6 +474,7 @@ int lanczos_graph(fmpt_op* op, const double* x0, int kmax, double btol, int reor
     FMPT_LAUNCHED(h);
     for (int j = 0; j < kmax; j++) {
       FMPT_TRY(op_u1_apply(op, V_(j), y, ctl));
+      FMPT_TRY(op_project(op, y, ctl));
       rdot_partial<<<G, KT, 0, st>>>(n, V_(j), y, partA.d(), ctl);
       FMPT_LAUNCHED(h);
       lanczos_axpy<<<G, KT, 0, st>>>(n, y, V_(j), j ? V_(j - 1) : nullptr, partA.d(), G,
@@ -544,12 +545,95 @@ int lanczos_graph(fmpt_op* op, const double* x0, int kmax, double btol, int reor
   return FMPT_OK;
 }
 
+// part[2b], part[2b+1] = Re, Im of a grid-stride slice of dot(y, p) = sum conj(y) p
+// (Julia's dot, as in _project!); split planes at offset n when cplx
+__global__ void proj_dot_partial(int cplx, int64_t n, const double* __restrict__ y,
+                                 const double* __restrict__ p, double* __restrict__ part,
+                                 const int* gate) {
+  if (gate && *gate) return;
+  double sr = 0.0, si = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * KT + threadIdx.x; i < n; i += (int64_t)gridDim.x * KT) {
+    sr = fma(y[i], p[i], sr);
+    if (cplx) {
+      sr = fma(y[n + i], p[n + i], sr);
+      si = fma(y[i], p[n + i], si);
+      si = fma(-y[n + i], p[i], si);
+    }
+  }
+  sr = block_sum(sr);
+  if (cplx) si = block_sum(si);
+  if (threadIdx.x == 0) {
+    part[2 * blockIdx.x] = sr;
+    part[2 * blockIdx.x + 1] = si;
+  }
+}
+
+// c = sum of the G partials (same fixed order in every block); y -= c p
+__global__ void proj_axpy(int cplx, int64_t n, double* __restrict__ y, const double* __restrict__ p,
+                          const double* __restrict__ part, int G, const int* gate) {
+  if (gate && *gate) return;
+  double ar = 0.0, ai = 0.0;
+  for (int i = threadIdx.x; i < G; i += KT) {
+    ar += part[2 * i];
+    ai += part[2 * i + 1];
+  }
+  const double cr = block_sum(ar);
+  const double ci = cplx ? block_sum(ai) : 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * KT + threadIdx.x; i < n; i += (int64_t)gridDim.x * KT) {
+    if (cplx) {
+      const double pr = p[i], pi = p[n + i];
+      y[i] -= cr * pr - ci * pi;
+      y[n + i] -= cr * pi + ci * pr;
+    } else {
+      y[i] -= cr * p[i];
+    }
+  }
+}
+
 }  // namespace
+
+// _project! (algorithms/dmrgexcited.jl:1-6): y = y - dot(y, p) p for every
+// projector in turn, on the handle's stream with the scalars kept on the device
+int op_project(fmpt_op* op, double* y, const int* gate) {
+  if (op->proj.empty()) return FMPT_OK;
+  fmpt_handle* h = op->h;
+  const int cp = op->dtype == FMPT_C128;
+  for (const double* p : op->proj) {
+    proj_dot_partial<<<op->proj_G, KT, 0, h->stream>>>(cp, op->n, y, p, op->proj_part, gate);
+    FMPT_LAUNCHED(h);
+    proj_axpy<<<op->proj_G, KT, 0, h->stream>>>(cp, op->n, y, p, op->proj_part, op->proj_G,
+                                                 gate);
+    FMPT_LAUNCHED(h);
+  }
+  return FMPT_OK;
+}
+
 }  // namespace fmpt
 
 using namespace fmpt;
 
 extern "C" {
+
+int fmpt_op_set_projectors(fmpt_op* op, int nproj, const double* const* p) {
+  if (!op) return FMPT_ERR_ARG;
+  fmpt_handle* h = op->h;
+  if (nproj < 0 || (nproj > 0 && !p))
+    return set_error(h, FMPT_ERR_ARG, "set_projectors: bad projector list");
+  for (int i = 0; i < nproj; i++)
+    if (!p[i]) return set_error(h, FMPT_ERR_ARG, "set_projectors: null projector %d", i);
+  if (nproj > 0 && !op->proj_part) {
+    const int G = grid_for(h, op->n);
+    void* q = nullptr;
+    cudaError_t e = cudaMallocAsync(&q, 2 * (size_t)G * sizeof(double), h->stream);
+    if (e != cudaSuccess)
+      return set_error(h, e == cudaErrorMemoryAllocation ? FMPT_ERR_NOMEM : FMPT_ERR_CUDA,
+                       "set_projectors: %s", cudaGetErrorString(e));
+    op->proj_part = static_cast<double*>(q);
+    op->proj_G = G;
+  }
+  op->proj.assign(p, p + nproj);
+  return FMPT_OK;
+}
 
 int fmpt_lanczos_ground(fmpt_op* op, const double* x0, int kmax, double btol, int reorth,
                         double* eigval, double* xout, int* info, int* niter) {

@@ -106,6 +106,15 @@ class HeffOp:
         self.h.check(lib().fmpt_op_apply(self.ptr, x.ptr, y.ptr))
         return y
 
+    def set_projectors(self, projectors):
+        """Compose the operator with _project! (dmrgexcited.jl:1-6): after every
+        application y -= dot(y, p) p for each device tensor p in order."""
+        for p in projectors:
+            self._check_x(p)
+        self._proj = list(projectors)                     # keep them alive
+        arr = (ctypes.c_void_p * max(1, len(self._proj)))(*[p.ptr for p in self._proj])
+        self.h.check(lib().fmpt_op_set_projectors(self.ptr, len(self._proj), arr))
+
     def lanczos(self, x0, kmax=10, btol=1e-8, reorth=False):
         """simple_lanczos_solver(f, x0, "SR", kmax, btol) -> (eval, evec, info, niter)."""
         self._check_x(x0)

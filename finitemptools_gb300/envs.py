@@ -88,29 +88,47 @@ def init_hstorage_(m, center=1):
     return hs
 
 
-def environments(mpo, mps, precision="fp64"):
-    """environments(mpo, mps) (finiteenv.jl:57)."""
+def environments(mpo, mps, projectors=None, precision="fp64"):
+    """environments(mpo, mps) (finiteenv.jl:57), and environments(mpo, mps,
+    projectors) (:126-127), which returns a ProjectedExpectationCache for
+    excited-state sweeps.  A string in the third position is the precision."""
+    if isinstance(projectors, str):
+        projectors, precision = None, projectors
     if mps.dtype != np.complex128 and any(np.iscomplexobj(W) for W in
                                           (mpo.site_tensors(len(mps)) if isinstance(mpo, MPOHamiltonian) else mpo)):
         raise TypeError("complex MPO needs a complex MPS")
+    if projectors is not None:
+        from .excited import ProjectedExpectationCache
+        return ProjectedExpectationCache(mpo, mps, projectors, precision)
     return ExpectationCache(mpo, mps, precision)
 
 
 def updateleft_(env, site):
-    """updateleft!(env, site) (finiteenv.jl:72-74)."""
+    """updateleft!(env, site) (finiteenv.jl:72-74); a projected cache also
+    updates its overlap storages (:144-149)."""
     env.hstorage[site + 1] = updateleft(env.hstorage[site], env.mps[site], env.mpo[site],
                                         env.mps[site], env.precision)
+    if getattr(env, "cstorages", None):
+        from .excited import cstorage_updateleft_
+        cstorage_updateleft_(env, site)
 
 
 def updateright_(env, site):
-    """updateright!(env, site) (finiteenv.jl:76-78)."""
+    """updateright!(env, site) (finiteenv.jl:76-78); a projected cache also
+    updates its overlap storages (:152-157)."""
     env.hstorage[site] = updateright(env.hstorage[site + 1], env.mps[site], env.mpo[site],
                                      env.mps[site], env.precision)
+    if getattr(env, "cstorages", None):
+        from .excited import cstorage_updateright_
+        cstorage_updateright_(env, site)
 
 
 def increase_bond_env_(env, D):
-    """increase_bond!(m::ExpectationCache; D) (finiteenv.jl:87-93)."""
+    """increase_bond!(m::ExpectationCache; D) (finiteenv.jl:87-93) and
+    (m::ProjectedExpectationCache; D) (:159-168)."""
     if bond_dimension(env.mps) < D:
         increase_bond_(env.mps, D)
         canonicalize_(env.mps, normalize=False)
         init_hstorage_(env, 1)
+        if getattr(env, "cstorages", None):
+            env.reinit_cstorages()

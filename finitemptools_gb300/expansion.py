@@ -23,6 +23,7 @@ from .auxiliary import (MPSTruncation, default_truncation, gemm, leftorth, right
 from .derivatives import HeffOp
 from .device import DeviceTensor
 from .envs import updateleft_, updateright_
+from .excited import projectors1
 
 __all__ = ["OptimalExpansion", "default_expansion", "DMRG1S", "TDVP2", "TDVP1S",
            "right_expansion_", "left_expansion_", "dmrg1s_leftsweep_", "dmrg1s_rightsweep_",
@@ -176,8 +177,9 @@ def left_expansion_(m, site, expan, trunc):
 
 # -------------------------------------------------------------------- DMRG1S
 def dmrg1s_leftsweep_(m, alg):
-    """leftsweep!(m, ::DMRG1S) (dmrg.jl:158-186)."""
-    from .algorithms import _galerkin
+    """leftsweep!(m, ::DMRG1S) (dmrg.jl:158-186); projected caches as in
+    dmrgexcited.jl:153-184."""
+    from .algorithms import _galerkin, _start_vector
     mps, mpo, hs = m.mps, m.mpo, m.hstorage
     Es, delta = [], 0.0
     for site in range(1, len(mps)):
@@ -185,7 +187,8 @@ def dmrg1s_leftsweep_(m, alg):
         A = mps[site]
         op = HeffOp("ac", hs[site], hs[site + 1], W1=mpo[site], precision=alg.precision,
                     dtype=A.dtype)
-        E, vec, _, _ = op.lanczos(A, alg.eig_maxiter, alg.eig_tol, alg.reorth)
+        x0 = _start_vector(op, A, projectors1(m, site))
+        E, vec, _, _ = op.lanczos(x0, alg.eig_maxiter, alg.eig_tol, alg.reorth)
         del op
         Es.append(E)
         delta = max(delta, _galerkin(m, site, alg.precision))
@@ -200,8 +203,9 @@ def dmrg1s_leftsweep_(m, alg):
 
 
 def dmrg1s_rightsweep_(m, alg):
-    """rightsweep!(m, ::DMRG1S) (dmrg.jl:188-215)."""
-    from .algorithms import _galerkin
+    """rightsweep!(m, ::DMRG1S) (dmrg.jl:188-215); projected caches as in
+    dmrgexcited.jl:186-216."""
+    from .algorithms import _galerkin, _start_vector
     mps, mpo, hs = m.mps, m.mpo, m.hstorage
     Es, delta = [], 0.0
     for site in range(len(mps), 1, -1):
@@ -209,7 +213,8 @@ def dmrg1s_rightsweep_(m, alg):
         A = mps[site]
         op = HeffOp("ac", hs[site], hs[site + 1], W1=mpo[site], precision=alg.precision,
                     dtype=A.dtype)
-        E, vec, _, _ = op.lanczos(A, alg.eig_maxiter, alg.eig_tol, alg.reorth)
+        x0 = _start_vector(op, A, projectors1(m, site))
+        E, vec, _, _ = op.lanczos(x0, alg.eig_maxiter, alg.eig_tol, alg.reorth)
         del op
         Es.append(E)
         delta = max(delta, _galerkin(m, site, alg.precision))

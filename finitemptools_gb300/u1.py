@@ -405,6 +405,16 @@ class U1HeffOp:
         self.h.check(lib().fmpt_op_apply(self.ptr, x.ptr, y.ptr))
         return y
 
+    def set_projectors(self, projectors):
+        """Compose with _project! (dmrgexcited.jl:1-6) on packed vectors: after
+        every application y -= dot(y, p) p for each packed device vector p."""
+        for p in projectors:
+            if tuple(p.shape) != self.shape or p.dtype != np.float64:
+                raise ValueError("DimensionMismatch: projector %s vs %s" % (p.shape, self.shape))
+        self._proj = list(projectors)
+        arr = (ctypes.c_void_p * max(1, len(self._proj)))(*[p.ptr for p in self._proj])
+        self.h.check(lib().fmpt_op_set_projectors(self.ptr, len(self._proj), arr))
+
     def lanczos(self, x0, kmax=10, btol=1e-8, reorth=False):
         """simple_lanczos_solver(f, x0, "SR", kmax, btol) on packed vectors."""
         out = DeviceTensor(self.shape, np.float64, self.h)

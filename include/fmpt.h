@@ -182,6 +182,16 @@ int fmpt_op_apply(fmpt_op* op, const double* x, double* y);
 int64_t fmpt_op_size(fmpt_op* op);
 int fmpt_op_destroy(fmpt_op* op);
 
+/* Projected operator of the excited-state sweeps: after every application
+ * (fmpt_op_apply and every solver built on it, the graph-captured Lanczos
+ * included) y = y - dot(y, p) p for p = p[0], ..., p[nproj-1] in order, with
+ * Julia's dot(y, p) = sum conj(y) p.  This is _project! of
+ * algorithms/dmrgexcited.jl:1-6 composed with ac_prime / ac2_prime as in
+ * :21 and :102.  p holds nproj device pointers to vectors of fmpt_op_size(op)
+ * elements (the c_proj / _c2_prime_2 projections); they are referenced, not
+ * copied.  nproj = 0 removes the projectors. */
+int fmpt_op_set_projectors(fmpt_op* op, int nproj, const double* const* p);
+
 /* Lowest eigenpair by the reference's plain Lanczos
  * (auxiliary/simple_lanczos.jl:83-120): three-term recurrence, stop when
  * beta < btol, at most kmax Krylov vectors, lowest Ritz pair of the

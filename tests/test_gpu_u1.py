@@ -243,6 +243,48 @@ def test_u1_lanczos_graph_equals_host_loop(kmax):
         assert i1 == 0 and k1 < 30
 
 
+def test_u1_projected_lanczos_graph_equals_host_loop():
+    """fmpt_op_set_projectors on a block-sparse operator: the projection runs
+    inside the captured graph (gated by the stop flag) and in the host-driven
+    loop with identical results; the projected operator is _project!(H x), and
+    projecting out the lowest eigenvector leaves the second eigenvalue."""
+    L, N = 4, 2
+    mps, legs, psi = _states(L, N, 8, 21)
+    u1_right_canonicalize_(psi)
+    m = fm.U1ExpectationCache(heisenberg_xxz_mpo(), psi)
+    Vl, Vm, Vr = psi.spaces[2], psi.spaces[3], psi.spaces[4]
+    x2 = fm.u1_twosite(psi[2], psi[3], Vl, Vm, Vr, QP, QP)
+    op = fm.U1HeffOp(m.hstorage[2], m.hstorage[4], m.mpo[2], m.mpo[3], Vl, Vr, QP, QP,
+                     m.qw[2], m.qw[3], m.qw[4])
+    n = op.n
+    H = np.empty((n, n))
+    for j in range(n):
+        e = np.zeros(n)
+        e[j] = 1.0
+        H[:, j] = op(DT.from_numpy(e)).numpy()
+    assert np.abs(H - H.T).max() < 1e-12
+    w, V = np.linalg.eigh(H)
+    p0 = DT.from_numpy(V[:, 0])
+    op.set_projectors([p0])
+    xr = np.random.default_rng(3).standard_normal(n)
+    y = op(DT.from_numpy(xr)).numpy()
+    Hx = H @ xr
+    assert np.abs(y - (Hx - np.dot(Hx, V[:, 0]) * V[:, 0])).max() < 1e-12 * np.abs(Hx).max()
+    x0 = x2.copy()
+    fm.project_(x0, [p0])
+    h = psi.handle
+    h.set_graphs(True)
+    g0 = h.graph_count()
+    E1, v1, i1, k1 = op.lanczos(x0, 30, 1e-12)
+    assert h.graph_count() == g0 + 1
+    h.set_graphs(False)
+    E2, v2, i2, k2 = op.lanczos(x0, 30, 1e-12)
+    h.set_graphs(True)
+    assert (E1, i1, k1) == (E2, i2, k2)
+    assert np.array_equal(v1.numpy(), v2.numpy())
+    assert abs(E1 - w[1]) < 1e-10
+
+
 @pytest.mark.parametrize("L,N,D,model", [(12, 6, 48, "xxz"), (12, 4, 48, "xxz"),
                                          (10, 5, 40, "j1j2")])
 def test_u1_dmrg2_vs_ed_and_oracle(L, N, D, model):
