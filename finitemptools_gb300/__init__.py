@@ -17,6 +17,8 @@ from .derivatives import HeffOp, ac2_prime, ac_prime, c_prime, exponentiate  # n
 from .derivatives import simple_lanczos_solver  # noqa: F401
 from .device import DeviceTensor, Handle, default_handle  # noqa: F401
 from .expansion import OptimalExpansion, default_expansion  # noqa: F401
+from .exactdiag import (ExactFiniteMPS, exact_diagonalization, exact_timeevolution,  # noqa: F401
+                        init_h_center, max_bond_dimensions)
 from .excited import (ProjectedExpectationCache, c2_proj, c_proj, init_cstorage_right,  # noqa: F401
                       overlap_updateleft, overlap_updateright, project_)
 from .envs import (ExpectationCache, environments, init_hstorage_, updateleft_,  # noqa: F401

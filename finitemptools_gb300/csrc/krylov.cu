@@ -590,6 +590,213 @@ __global__ void proj_axpy(int cplx, int64_t n, double* __restrict__ y, const dou
   }
 }
 
+// ---- several eigenpairs: thick-restart Lanczos (exact diagonalisation)
+
+// Symmetric eigendecomposition of a small dense matrix by cyclic Jacobi
+// rotations (the two-sided rotation of Golub & Van Loan, Matrix Computations,
+// sec. 8.5): A (column-major m x m) is destroyed, w receives the eigenvalues in
+// ascending order and Z the matching orthonormal columns.
+void jacobi_eigh(int m, std::vector<double>& A, std::vector<double>& w, std::vector<double>& Z) {
+  std::vector<double> R((size_t)m * m, 0.0);
+  for (int i = 0; i < m; i++) R[i + (size_t)i * m] = 1.0;
+  auto a = [&](int i, int j) -> double& { return A[i + (size_t)j * m]; };
+  double fro = 0.0;
+  for (double v : A) fro += v * v;
+  for (int sweep = 0; sweep < 64; sweep++) {
+    double off = 0.0;
+    for (int q = 1; q < m; q++)
+      for (int p = 0; p < q; p++) off += a(p, q) * a(p, q);
+    if (off <= 1e-32 * fro) break;
+    for (int p = 0; p < m - 1; p++)
+      for (int q = p + 1; q < m; q++) {
+        const double apq = a(p, q);
+        if (apq == 0.0) continue;
+        const double theta = (a(q, q) - a(p, p)) / (2.0 * apq);
+        const double t = (theta >= 0.0 ? 1.0 : -1.0) /
+                         (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+        const double c = 1.0 / std::sqrt(t * t + 1.0), sn = t * c;
+        for (int k = 0; k < m; k++) {          // A J
+          const double akp = a(k, p), akq = a(k, q);
+          a(k, p) = c * akp - sn * akq;
+          a(k, q) = sn * akp + c * akq;
+        }
+        for (int k = 0; k < m; k++) {          // J^T (A J)
+          const double apk = a(p, k), aqk = a(q, k);
+          a(p, k) = c * apk - sn * aqk;
+          a(q, k) = sn * apk + c * aqk;
+        }
+        for (int k = 0; k < m; k++) {          // Z J
+          double* zp = &R[k + (size_t)p * m];
+          double* zq = &R[k + (size_t)q * m];
+          const double zkp = *zp, zkq = *zq;
+          *zp = c * zkp - sn * zkq;
+          *zq = sn * zkp + c * zkq;
+        }
+      }
+  }
+  std::vector<int> ord(m);
+  for (int i = 0; i < m; i++) ord[i] = i;
+  std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return a(x, x) < a(y, y); });
+  w.resize(m);
+  Z.assign((size_t)m * m, 0.0);
+  for (int i = 0; i < m; i++) {
+    w[i] = a(ord[i], ord[i]);
+    for (int k = 0; k < m; k++) Z[k + (size_t)i * m] = R[k + (size_t)ord[i] * m];
+  }
+}
+
+// C (nr x c) = V (nr x mm, real view, ld nr) * Y (mm x c, host) on the stream
+int basis_times(fmpt_handle* h, const double* V, int64_t nr, int mm, const std::vector<double>& Y,
+                int c, DevBuf& Yd, double* C) {
+  FMPT_CUDA(h, cudaMemcpyAsync(Yd.d(), Y.data(), (size_t)mm * c * sizeof(double),
+                               cudaMemcpyHostToDevice, h->stream));
+  GemmArgs g{};
+  g.cplx = 0; g.ta = FMPT_N; g.tb = FMPT_N;
+  g.m = (int)nr; g.n = c; g.k = mm;
+  g.alpha[0] = 1.0; g.beta[0] = 0.0;
+  g.A = V; g.lda = nr; g.planeA = 0;
+  g.B = Yd.d(); g.ldb = mm; g.planeB = 0;
+  g.C = C; g.ldc = nr; g.planeC = 0;
+  g.batch = 1;
+  return gemm_f64(h, g);
+}
+
+// Thick-restart Lanczos (Wu & Simon, SIAM J. Matrix Anal. Appl. 22 (2000) 602)
+// with full reorthogonalisation (two classical Gram-Schmidt passes) for the
+// ``num`` eigenvalues of a Hermitian operator at one end of the spectrum
+// (which 0: smallest, 1: largest).  The basis lives on the device; the
+// Rayleigh quotient (at most krylovdim x krylovdim, real symmetric: the
+// Lanczos coefficients of a Hermitian operator are real) is solved on the host.
+// A Ritz pair has converged when its residual norm |beta_m y_m| <= tol.
+int eigsolve_impl(fmpt_op* op, const double* x0, int num, int kdim, int maxiter, double tol,
+                  int which, double* evals, double* evecs, double* resid, int* nconv,
+                  int* napply) {
+  fmpt_handle* h = op->h;
+  const int cp = op->dtype == FMPT_C128;
+  const int64_t n = op->n;
+  const int64_t nr = n * (cp ? 2 : 1);
+  const int m = (int)std::min<int64_t>(kdim, n);
+  if (num > m) return set_error(h, FMPT_ERR_ARG, "eigsolve: num %d exceeds the space", num);
+  if (m < n && m < num + 2)
+    return set_error(h, FMPT_ERR_ARG, "eigsolve: krylovdim must be at least num + 2");
+  const int G = grid_for(h, n);
+  DevBuf Vb, zb, partA, partM, coef, acc, Yd, tmp, snrm;
+  FMPT_TRY(Vb.alloc(h, (size_t)(m + 1) * nr * sizeof(double)));
+  FMPT_TRY(zb.alloc(h, (size_t)nr * sizeof(double)));
+  FMPT_TRY(partA.alloc(h, (size_t)G * sizeof(double)));
+  FMPT_TRY(partM.alloc(h, (size_t)G * (m + 1) * 2 * sizeof(double)));
+  FMPT_TRY(coef.alloc(h, (size_t)(m + 1) * 2 * sizeof(double)));
+  FMPT_TRY(acc.alloc(h, (size_t)(m + 1) * 2 * sizeof(double)));
+  FMPT_TRY(Yd.alloc(h, (size_t)m * m * sizeof(double)));
+  FMPT_TRY(snrm.alloc(h, sizeof(double)));
+  FMPT_TRY(ensure_pinned(h, (size_t)2 * (m + 1) + G + 1));
+  double* V = Vb.d();
+  double* z = zb.d();
+  auto V_ = [&](int i) { return V + (int64_t)i * nr; };
+  cudaStream_t st = h->stream;
+  rdot_partial<<<G, KT, 0, st>>>(nr, x0, x0, partA.d());
+  FMPT_LAUNCHED(h);
+  normalize_from_parts<<<G, KT, 0, st>>>(nr, x0, V_(0), partA.d(), G, snrm.d());
+  FMPT_LAUNCHED(h);
+  FMPT_CUDA(h, cudaMemcpyAsync(h->pinned, snrm.d(), sizeof(double), cudaMemcpyDeviceToHost, st));
+  FMPT_CUDA(h, cudaStreamSynchronize(st));
+  if (!(h->pinned[0] > 0.0) || !std::isfinite(h->pinned[0]))
+    return set_error(h, FMPT_ERR_ARG, "eigsolve: the start vector is zero or not finite");
+  std::vector<double> H((size_t)(m + 1) * (m + 1), 0.0);
+  auto Hx = [&](int i, int j) -> double& { return H[i + (size_t)j * (m + 1)]; };
+  std::vector<double> theta, Y, A;
+  int k = 0, applies = 0;
+  for (int it = 0;; it++) {
+    bool breakdown = false;
+    int j = k;
+    for (; j < m; j++) {
+      FMPT_TRY(fmpt_op_apply(op, V_(j), z));
+      applies++;
+      FMPT_CUDA(h, cudaMemsetAsync(acc.d(), 0, (size_t)2 * (j + 1) * sizeof(double), st));
+      for (int pass = 0; pass < 2; pass++) {
+        multidot_partial<<<G, KT, 0, st>>>(cp, n, j + 1, V, nr, z, partM.d());
+        FMPT_LAUNCHED(h);
+        multidot_finalize<<<1, KT, 0, st>>>(j + 1, G, partM.d(), coef.d(), acc.d());
+        FMPT_LAUNCHED(h);
+        multi_axpy_sub<<<G, KT, 0, st>>>(cp, n, j + 1, V, nr, coef.d(), z, partA.d());
+        FMPT_LAUNCHED(h);
+      }
+      double* hp = h->pinned;
+      FMPT_CUDA(h, cudaMemcpyAsync(hp, acc.d(), (size_t)2 * (j + 1) * sizeof(double),
+                                   cudaMemcpyDeviceToHost, st));
+      FMPT_CUDA(h, cudaMemcpyAsync(hp + 2 * (j + 1), partA.d(), (size_t)G * sizeof(double),
+                                   cudaMemcpyDeviceToHost, st));
+      FMPT_CUDA(h, cudaStreamSynchronize(st));
+      double b2 = 0.0;
+      for (int g = 0; g < G; g++) b2 += hp[2 * (j + 1) + g];
+      double ref = b2;
+      for (int i = 0; i <= j; i++) {
+        Hx(i, j) = Hx(j, i) = hp[2 * i];
+        ref += hp[2 * i] * hp[2 * i] + hp[2 * i + 1] * hp[2 * i + 1];
+      }
+      if (!std::isfinite(b2)) return set_error(h, FMPT_ERR_NONFINITE, "eigsolve: not finite");
+      const double beta = std::sqrt(b2);
+      if (!(beta > 1e-12 * std::sqrt(ref))) {     // invariant subspace: exact Ritz pairs
+        breakdown = true;
+        j++;
+        break;
+      }
+      normalize_from_parts<<<G, KT, 0, st>>>(nr, z, V_(j + 1), partA.d(), G, snrm.d());
+      FMPT_LAUNCHED(h);
+      Hx(j + 1, j) = Hx(j, j + 1) = beta;
+    }
+    const int mm = j;
+    const double beta_last = breakdown ? 0.0 : Hx(mm, mm - 1);
+    A.assign((size_t)mm * mm, 0.0);
+    for (int c = 0; c < mm; c++)
+      for (int r = 0; r < mm; r++) A[r + (size_t)c * mm] = Hx(r, c);
+    jacobi_eigh(mm, A, theta, Y);
+    std::vector<int> idx(mm);
+    for (int i = 0; i < mm; i++) idx[i] = which == 1 ? mm - 1 - i : i;
+    std::vector<double> res(mm);
+    int conv = 0;
+    for (int i = 0; i < mm; i++) res[i] = std::fabs(beta_last * Y[(mm - 1) + (size_t)idx[i] * mm]);
+    while (conv < num && res[conv] <= tol) conv++;
+    if (conv >= num || breakdown || it + 1 >= maxiter) {
+      if (mm < num)
+        return set_error(h, FMPT_ERR_ARG,
+                         "eigsolve: the start vector lies in an invariant subspace of "
+                         "dimension %d < num", mm);
+      std::vector<double> Ys((size_t)mm * num);
+      for (int i = 0; i < num; i++)
+        for (int r = 0; r < mm; r++) Ys[r + (size_t)i * mm] = Y[r + (size_t)idx[i] * mm];
+      FMPT_TRY(basis_times(h, V, nr, mm, Ys, num, Yd, evecs));
+      for (int i = 0; i < num; i++) {
+        evals[i] = theta[idx[i]];
+        if (resid) resid[i] = res[i];
+      }
+      if (nconv) *nconv = breakdown ? num : conv;
+      if (napply) *napply = applies;
+      FMPT_CUDA(h, cudaStreamSynchronize(st));
+      return FMPT_OK;
+    }
+    // keep the ``keep`` best Ritz vectors and the residual direction
+    const int keep = std::min(mm - 1, num + (mm - num) / 2);
+    std::vector<double> Ys((size_t)mm * keep);
+    for (int i = 0; i < keep; i++)
+      for (int r = 0; r < mm; r++) Ys[r + (size_t)i * mm] = Y[r + (size_t)idx[i] * mm];
+    if (!tmp.p) {
+      FMPT_TRY(tmp.alloc(h, (size_t)m * nr * sizeof(double)));
+    }
+    FMPT_TRY(basis_times(h, V, nr, mm, Ys, keep, Yd, tmp.d()));
+    FMPT_CUDA(h, cudaMemcpyAsync(V, tmp.d(), (size_t)keep * nr * sizeof(double),
+                                 cudaMemcpyDeviceToDevice, st));
+    FMPT_CUDA(h, cudaMemcpyAsync(V_(keep), V_(mm), (size_t)nr * sizeof(double),
+                                 cudaMemcpyDeviceToDevice, st));
+    std::fill(H.begin(), H.end(), 0.0);
+    for (int i = 0; i < keep; i++) {
+      Hx(i, i) = theta[idx[i]];
+      Hx(i, keep) = Hx(keep, i) = beta_last * Y[(mm - 1) + (size_t)idx[i] * mm];
+    }
+    k = keep;
+  }
+}
+
 }  // namespace
 
 // _project! (algorithms/dmrgexcited.jl:1-6): y = y - dot(y, p) p for every
@@ -613,6 +820,19 @@ int op_project(fmpt_op* op, double* y, const int* gate) {
 using namespace fmpt;
 
 extern "C" {
+
+int fmpt_eigsolve(fmpt_op* op, const double* x0, int num, int krylovdim, int maxiter, double tol,
+                  int which, double* evals, double* evecs, double* resid, int* nconv,
+                  int* napply) {
+  if (!op) return FMPT_ERR_ARG;
+  fmpt_handle* h = op->h;
+  if (!x0 || !evals || !evecs) return set_error(h, FMPT_ERR_ARG, "eigsolve: null pointer");
+  if (num < 1 || krylovdim < 2 || krylovdim > 256 || maxiter < 1 || !(tol >= 0.0) ||
+      (which != 0 && which != 1))
+    return set_error(h, FMPT_ERR_ARG, "eigsolve: bad num/krylovdim/maxiter/tol/which");
+  return eigsolve_impl(op, x0, num, krylovdim, maxiter, tol, which, evals, evecs, resid, nconv,
+                       napply);
+}
 
 int fmpt_op_set_projectors(fmpt_op* op, int nproj, const double* const* p) {
   if (!op) return FMPT_ERR_ARG;

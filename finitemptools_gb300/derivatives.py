@@ -127,6 +127,30 @@ class HeffOp:
                                                ctypes.byref(info), ctypes.byref(it)))
         return ev.value, out, info.value, it.value
 
+    def eigsolve(self, x0, num=1, which="SR", krylovdim=30, maxiter=100, tol=1e-12):
+        """eigsolve(f, x0, num, which, Lanczos()) (algorithms/exactdiag.jl:28): the
+        num lowest ("SR") or highest ("LR") eigenpairs by thick-restart Lanczos.
+        Returns (values, vectors, info) with info = {converged, residuals, applies}."""
+        self._check_x(x0)
+        if which not in ("SR", "SA", "LR", "LA"):
+            raise ValueError("which must be 'SR' or 'LR'")
+        num = int(num)
+        per = DeviceTensor(self.shape, self.dtype, self.h).nbytes
+        buf = DeviceTensor((per // 8 * num,), np.float64, self.h)
+        vals = (ctypes.c_double * num)()
+        res = (ctypes.c_double * num)()
+        nconv, napply = ctypes.c_int(), ctypes.c_int()
+        self.h.check(lib().fmpt_eigsolve(self.ptr, x0.ptr, num, int(krylovdim), int(maxiter),
+                                         float(tol), 1 if which in ("LR", "LA") else 0, vals,
+                                         buf.ptr, res, ctypes.byref(nconv), ctypes.byref(napply)))
+        vecs = []
+        for i in range(num):
+            v = DeviceTensor(self.shape, self.dtype, self.h)
+            self.h.check(lib().fmpt_memcpy_d2d(self.h.ptr, v.ptr, buf.ptr + i * per, per))
+            vecs.append(v)
+        info = {"converged": nconv.value, "residuals": list(res), "applies": napply.value}
+        return list(vals), vecs, info
+
     def exponentiate(self, t, x, tol=1e-8, krylovdim=30):
         """exp(t * H) x (KrylovKit.exponentiate as used by _exp_evolve)."""
         self._check_x(x)

@@ -201,6 +201,20 @@ int fmpt_op_set_projectors(fmpt_op* op, int nproj, const double* const* p);
 int fmpt_lanczos_ground(fmpt_op* op, const double* x0, int kmax, double btol, int reorth,
                         double* eigval, double* xout, int* info, int* niter);
 
+/* The num lowest (which 0, "SR") or highest (which 1, "LR") eigenpairs of a
+ * Hermitian op: eigsolve(f, x0, num, which, Lanczos()) as
+ * exact_diagonalization calls it (algorithms/exactdiag.jl:28).  KrylovKit's
+ * Lanczos is not vendored; this is a thick-restart Lanczos (Wu & Simon 2000)
+ * with full FP64 reorthogonalisation, a basis of at most krylovdim (2..256)
+ * device vectors and at most maxiter restarts.  A Ritz pair has converged when
+ * its residual norm is <= tol.  evals/resid (num each) and nconv/napply (the
+ * number of converged leading pairs and of operator applications) are HOST
+ * outputs; evecs is a device buffer of num vectors of fmpt_op_size(op)
+ * elements (complex: split planes per vector), one after the other. */
+int fmpt_eigsolve(fmpt_op* op, const double* x0, int num, int krylovdim, int maxiter, double tol,
+                  int which, double* evals, double* evecs, double* resid, int* nconv,
+                  int* napply);
+
 /* xout = exp(t * op) x  (t = t_re + i t_im) by a Krylov projection of at
  * most krylovdim vectors with adaptive time stepping to ``tol`` (the
  * tolerance _exp_evolve hands KrylovKit.exponentiate, algorithms/tdvp.jl:3-6,
