@@ -130,6 +130,11 @@ def canonicalize_(psi, normalize=False):
     """right_canonicalize! (mps/orth.jl:40-49): SVD leftorth! sweep, optional
     normalisation of the last site, SVD rightorth! sweep (no truncation)."""
     L = len(psi)
+    # maybe_init_boundary_s! (finitemps.jl:179-189): identities on the open ends
+    if psi.s[1] is None:
+        psi.s[1] = DeviceTensor.from_numpy(np.ones(psi[1].shape[0]), psi.handle, np.float64)
+    if psi.s[L + 1] is None:
+        psi.s[L + 1] = DeviceTensor.from_numpy(np.ones(psi[L].shape[2]), psi.handle, np.float64)
     for i in range(1, L):                                    # orth.jl:5-20
         A = psi[i]
         Dl, d, Dr = A.shape

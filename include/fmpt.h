@@ -201,6 +201,15 @@ int fmpt_op_set_projectors(fmpt_op* op, int nproj, const double* const* p);
 int fmpt_lanczos_ground(fmpt_op* op, const double* x0, int kmax, double btol, int reorth,
                         double* eigval, double* xout, int* info, int* niter);
 
+/* TEBD gate action (the bondmpo contraction of bond_evolution,
+ * circuit/apply_gates.jl:11-50): y[a, p', b] = sum_p G[p', p] x[a, p, b] for a
+ * device tensor x [Dl, P, Dr] whose middle index fuses the physical indices of
+ * the gate's sites (first site fastest) and a HOST gate matrix G [P, P]
+ * (column-major, outputs first; C128: real plane then imaginary plane).
+ * Out of place. */
+int fmpt_apply_gate(fmpt_handle* h, int dtype, const double* G_host, int P, const double* x,
+                    double* y, int Dl, int Dr);
+
 /* The num lowest (which 0, "SR") or highest (which 1, "LR") eigenpairs of a
  * Hermitian op: eigsolve(f, x0, num, which, Lanczos()) as
  * exact_diagonalization calls it (algorithms/exactdiag.jl:28).  KrylovKit's
