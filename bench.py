@@ -501,6 +501,123 @@ def u1_section(h, fm, budget_s=150.0):
     return out
 
 
+def next_rows_section(h, fm):
+    """The paths beside the hot path, each timed once on synthetic inputs:
+      ed_xxz_L20: exact_diagonalization of the XXZ chain L=20 (Delta=1) through the
+          device ac_prime at the centre (n = 2^20, environments 512 and 1024 wide),
+          num=2, tol 1e-10; E0 against the ED fixture; the host numpy ac_prime of
+          the oracle timed on the same centre (2 applications) for comparison.
+      excited_xxz_L20_D64: projected DMRG2 for the first excited state (ground state
+          from 4 DMRG2 sweeps at D=64 as the projector, 4 projected sweeps), E1
+          against the device ED value above.
+      tebd_bond_D256: one layer of 19 two-site gates exp(-i 0.05 h) (TFI bonds) on
+          a random right-canonical complex MPS, L=20, D=256 kept, in the gesvd and
+          density-matrix forms; the oracle's numpy bond update timed on 2 bonds."""
+    import time as _t
+    import oracle as O
+    from oracle import core as OC
+    from oracle import tebd as OT
+    out = {}
+    with open(os.path.join(ROOT, "tests", "golden", "exact_energies.json")) as f:
+        e_ed = json.load(f)["xxz_L20_J1_Jzz1_hz0"]
+    hx = fm.heisenberg_xxz_mpo(1.0, 1.0, 0.0)
+    # --- exact diagonalisation on the device
+    h.synchronize()
+    t0 = _t.perf_counter()
+    vals, states = fm.exact_diagonalization(hx, len=20, num=2, rng=np.random.default_rng(1),
+                                            tol=1e-10, handle=h)
+    h.synchronize()
+    t_ed = _t.perf_counter() - t0
+    psi = states[0]
+    left, right, Wc = fm.init_h_center(hx, psi)
+    op = fm.HeffOp("ac", left, right, W1=Wc)
+    x = psi[psi.center]
+    op(x)
+    h.synchronize()
+    t0 = _t.perf_counter()
+    for _ in range(5):
+        op(x)
+    h.synchronize()
+    t_apply = (_t.perf_counter() - t0) / 5
+    Ln, Rn, xn = left.numpy(), right.numpy(), x.numpy()
+    t0 = _t.perf_counter()
+    for _ in range(2):
+        OC.ac_prime(xn, np.asarray(Wc), Ln, Rn)
+    t_apply_cpu = (_t.perf_counter() - t0) / 2
+    out["ed_xxz_L20"] = {"s_total": t_ed, "E0": vals[0], "E1": vals[1], "E0_fixture": e_ed,
+                         "dE0_rel": abs(vals[0] - e_ed) / abs(e_ed),
+                         "centre_shape": list(x.shape), "ms_per_apply_gpu_fp64": 1e3 * t_apply,
+                         "ms_per_apply_cpu_numpy": 1e3 * t_apply_cpu,
+                         "apply_speedup": t_apply_cpu / t_apply}
+    del op, left, right, states, psi
+    # --- first excited state by projected DMRG2
+    rng = np.random.default_rng(20)
+    g = fm.randommps(20, 2, 8, rng, handle=h)
+    fm.canonicalize_(g, normalize=True)
+    envg = fm.environments(fm.FiniteMPO(hx, 20), g)
+    alg = fm.DMRG2(eig_maxiter=20, eig_tol=1e-12, trunc=fm.MPSTruncation(64, 1e-10), verbosity=0)
+    for _ in range(4):
+        fm.sweep_(envg, alg)
+    st = fm.randommps(20, 2, 8, np.random.default_rng(21), handle=h)
+    fm.canonicalize_(st, normalize=True)
+    envx = fm.environments(fm.FiniteMPO(hx, 20), st, [envg.mps])
+    tx = []
+    for _ in range(4):
+        h.synchronize()
+        t0 = _t.perf_counter()
+        Es, _ = fm.sweep_(envx, alg)
+        h.synchronize()
+        tx.append(_t.perf_counter() - t0)
+    out["excited_xxz_L20_D64"] = {"sweep_s": tx, "E1_dmrg": Es[-1], "E1_device_ed": vals[1],
+                                  "dE1_rel": abs(Es[-1] - vals[1]) / abs(vals[1])}
+    del envx, envg
+    # --- TEBD bond updates at D=256
+    L, D = 20, 256
+    Z = np.diag([-1.0, 1.0])
+    X = np.array([[0.0, 1.0], [1.0, 0.0]])
+    import scipy.linalg
+    G = scipy.linalg.expm(-0.05j * (-np.kron(Z, Z) - 0.5 * (np.kron(np.eye(2), X) +
+                                                             np.kron(X, np.eye(2)))))
+    mps, sv = O.canonicalize(O.randommps(L, 2, D, np.random.default_rng(256),
+                                         dtype=np.complex128), normalize=True)
+    sv[0], sv[L] = np.ones(1), np.ones(1)
+    layer = fm.QuantumCircuit(fm.QuantumGate((i, i + 1), G) for i in range(1, L))
+    res = {}
+    for name, svd, meth in (("gesvd", "gesvd", "gesvd"), ("gesvdp", "gesvd", "gesvdp"),
+                            ("dm", "dm", "gesvd")):
+        h.set_svd_method(meth)
+        psi_t = fm.FiniteMPS.from_numpy(mps)
+        for i in range(1, L + 2):
+            psi_t.s[i] = fm.DeviceTensor.from_numpy(np.asarray(sv[i - 1], dtype=np.float64))
+        centre = layer[L // 2 - 1]                                   # gate on (L/2, L/2+1)
+        fm.apply_([centre], psi_t, trunc=fm.MPSTruncation(D, 1e-12), svd=svd)   # warm-up
+        h.synchronize()
+        t0 = _t.perf_counter()
+        for _ in range(3):
+            fm.apply_([centre], psi_t, trunc=fm.MPSTruncation(D, 1e-12), svd=svd)
+        h.synchronize()
+        t_c = (_t.perf_counter() - t0) / 3
+        t0 = _t.perf_counter()
+        fm.apply_(layer, psi_t, trunc=fm.MPSTruncation(D, 1e-12), svd=svd)
+        h.synchronize()
+        res[name] = (t_c, (_t.perf_counter() - t0) / len(layer))
+    h.set_svd_method("gesvd")
+    mo, so = [A.copy() for A in mps], list(sv)
+    c = L // 2
+    t0 = _t.perf_counter()
+    for i in (c, c + 1):
+        OT.apply_gate((i, i + 1), G, mo, so, O.MPSTruncation(D, 1e-12))
+    t_cpu = (_t.perf_counter() - t0) / 2
+    out["tebd_bond_D256"] = {
+        "ms_per_centre_gate": {k: 1e3 * v[0] for k, v in res.items()},
+        "ms_per_gate_layer_average": {k: 1e3 * v[1] for k, v in res.items()},
+        "ms_per_centre_gate_cpu_numpy": 1e3 * t_cpu,
+        "centre_speedup_gesvd": t_cpu / res["gesvd"][0],
+        "note": "centre gate: theta 512 x 512 complex; the layer average includes the small "
+                "edge bonds"}
+    return out
+
+
 def tdvp_grad_section(h, fm, nsteps=5):
     """Config 5 (differentiable TDVP1), reduced length: TFI L=40,
     h_i = 1 + 0.1 N(0,1) (seed 40), random normalised complex MPS D=64, dt=0.05
@@ -617,6 +734,7 @@ def main():
     ap.add_argument("--no-dmrg", action="store_true")
     ap.add_argument("--no-u1", action="store_true")
     ap.add_argument("--no-grad", action="store_true")
+    ap.add_argument("--no-next", action="store_true")
     ap.add_argument("--u1-heff", type=int, default=0, metavar="D",
                     help="only time the block-sparse H_eff*x of an L=64, Sz=0 centre bond "
                          "with bond dimension D (profiling case) and exit")
@@ -807,6 +925,10 @@ def main():
     if rank == 0 and not args.no_grad:
         tgrad = tdvp_grad_section(h, fm)
 
+    nxt = None
+    if rank == 0 and not args.no_next:
+        nxt = next_rows_section(h, fm)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(D)
@@ -819,6 +941,7 @@ def main():
             "config": config_dict(args, prec), "clocks": clocks, "e2e": e2e,
             "gpu_launches": n_launch, "roofline": roof, "cpu_baseline": cpu,
             "per_dtype": table, "dmrg": dmrg, "u1": u1, "tdvp_gradient": tgrad,
+            "next_rows": nxt,
         }
         print(json.dumps(line), flush=True)
     if pg:

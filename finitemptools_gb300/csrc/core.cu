@@ -355,6 +355,13 @@ int fmpt_tuning_info(fmpt_handle* h, int* entries, int64_t* timed) {
   return FMPT_OK;
 }
 
+int fmpt_set_svd_method(fmpt_handle* h, int method) {
+  if (!h) return FMPT_ERR_ARG;
+  if (method != 0 && method != 1) return set_error(h, FMPT_ERR_ARG, "svd method must be 0 or 1");
+  h->svd_method = method;
+  return FMPT_OK;
+}
+
 int fmpt_set_graphs(fmpt_handle* h, int on) {
   if (!h) return FMPT_ERR_ARG;
   h->graphs = on != 0;

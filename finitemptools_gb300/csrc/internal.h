@@ -37,6 +37,7 @@ struct fmpt_handle {
   std::vector<cudaEvent_t> aux_event;   // [0] fork, [1 + i] join of aux stream i
   // CUDA graphs for the Krylov solvers of block-sparse operators (fmpt_set_graphs)
   bool graphs = true;
+  int svd_method = 0;          // 0 gesvd (bidiagonalisation), 1 gesvdp (polar decomposition)
   cudaGraphExec_t lanczos_exec = nullptr;   // reused through cudaGraphExecUpdate
   uint64_t graph_launches = 0;
   // grouped-kernel tile autotuner (fmpt_set_tuning): 0 measure, 1 force the

@@ -87,10 +87,62 @@ static int read_info(fmpt_handle* h, const int* dinfo, int* out) {
   return FMPT_OK;
 }
 
+// Thin SVD through the polar decomposition A = U_p H (cuSOLVER Xgesvdp, the
+// QDWH iteration followed by an eigendecomposition of H): mostly level-3 work,
+// where gesvd's bidiagonalisation is level-2 bound.  Returns FMPT_OK and
+// *ok = false when the routine reports failure, so that the caller can fall
+// back.  A is overwritten.
+static int svd_tall_polar(fmpt_handle* h, int cplx, int m, int n, double* Awork, double* S,
+                          double* U, double* VT, bool* ok) {
+  *ok = false;
+  cusolverDnParams_t params = nullptr;
+  FMPT_SOLVER(h, cusolverDnCreateParams(&params));
+  const cudaDataType dt = cplx ? CUDA_C_64F : CUDA_R_64F;
+  DevBuf V, dinfo, wd;
+  int st = V.alloc(h, (size_t)n * n * sizeof(double) * (cplx ? 2 : 1));
+  if (st == FMPT_OK) st = dinfo.alloc(h, sizeof(int));
+  size_t wdev = 0, whost = 0;
+  cusolverStatus_t cs = CUSOLVER_STATUS_SUCCESS;
+  if (st == FMPT_OK)
+    cs = cusolverDnXgesvdp_bufferSize(h->solver, params, CUSOLVER_EIG_MODE_VECTOR, 1, m, n, dt,
+                                      Awork, m, CUDA_R_64F, S, dt, U, m, dt, V.p, n, dt, &wdev,
+                                      &whost);
+  std::vector<char> wh;
+  if (st == FMPT_OK && cs == CUSOLVER_STATUS_SUCCESS) {
+    st = wd.alloc(h, std::max<size_t>(wdev, 16));
+    wh.resize(std::max<size_t>(whost, 16));
+  }
+  double err_sigma = 0.0;
+  if (st == FMPT_OK && cs == CUSOLVER_STATUS_SUCCESS)
+    cs = cusolverDnXgesvdp(h->solver, params, CUSOLVER_EIG_MODE_VECTOR, 1, m, n, dt, Awork, m,
+                           CUDA_R_64F, S, dt, U, m, dt, V.p, n, dt, wd.p, wdev, wh.data(), whost,
+                           (int*)dinfo.p, &err_sigma);
+  cusolverDnDestroyParams(params);
+  FMPT_TRY(st);
+  if (cs != CUSOLVER_STATUS_SUCCESS) return FMPT_OK;
+  int info = 0;
+  FMPT_TRY(read_info(h, (const int*)dinfo.p, &info));
+  if (info != 0 || !std::isfinite(err_sigma)) return FMPT_OK;
+  *ok = true;
+  // VT = V^H (interleaved layout, n x n)
+  return copy_mat(h, cplx, n, n, V.d(), n, cplx ? -1 : 0, 1, cplx, VT, n, cplx ? -1 : 0);
+}
+
 // Full thin SVD of a tall (m >= n) matrix given in solver layout (real, or
 // interleaved complex) in Awork (overwritten).  U: m x n, S: n, VT: n x n.
+// The handle's svd_method selects gesvd (default) or the polar-decomposition
+// SVD; a failure of either falls back to the one-sided Jacobi SVD.
 int svd_tall(fmpt_handle* h, int cplx, int m, int n, double* Awork, double* S, double* U,
              double* VT) {
+  if (h->svd_method == 1) {
+    DevBuf Acopy;
+    const size_t abytes = (size_t)m * n * sizeof(double) * (cplx ? 2 : 1);
+    FMPT_TRY(Acopy.alloc(h, abytes));
+    FMPT_CUDA(h, cudaMemcpyAsync(Acopy.p, Awork, abytes, cudaMemcpyDeviceToDevice, h->stream));
+    bool ok = false;
+    FMPT_TRY(svd_tall_polar(h, cplx, m, n, Acopy.d(), S, U, VT, &ok));
+    if (ok) return FMPT_OK;
+  }
   DevBuf work, rwork, dinfo;
   FMPT_TRY(dinfo.alloc(h, sizeof(int)));
   int lwork = 0;

@@ -28,6 +28,14 @@ class Handle:
     def synchronize(self):
         check(lib().fmpt_synchronize(self.ptr), self.ptr)
 
+    def set_svd_method(self, method="gesvd"):
+        """SVD routine of the truncated splits: "gesvd" (default) or "gesvdp"
+        (polar decomposition)."""
+        codes = {"gesvd": 0, "gesvdp": 1}
+        if method not in codes:
+            raise ValueError("svd method must be 'gesvd' or 'gesvdp'")
+        self.check(lib().fmpt_set_svd_method(self.ptr, codes[method]))
+
     def set_graphs(self, on=True):
         """CUDA-graph Krylov solves for block-sparse operators (default on)."""
         self.check(lib().fmpt_set_graphs(self.ptr, 1 if on else 0))

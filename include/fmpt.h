@@ -63,6 +63,14 @@ int fmpt_destroy(fmpt_handle* h);
 const char* fmpt_status_string(int status);
 const char* fmpt_last_error(fmpt_handle* h);
 int fmpt_synchronize(fmpt_handle* h);
+/* SVD routine of every truncated split on this handle (fmpt_svd_trunc, the
+ * U(1) per-sector SVD, the TEBD bond updates): 0 = cuSOLVER gesvd
+ * (bidiagonalisation; the default, as the reference's LAPACK fallback in
+ * auxiliary/stable_svd.jl:12-18), 1 = cuSOLVER Xgesvdp (polar decomposition,
+ * level-3 bound, faster from a few hundred columns).  Either falls back to the
+ * one-sided Jacobi SVD when it reports failure. */
+int fmpt_set_svd_method(fmpt_handle* h, int method);
+
 /* CUDA graphs for the Krylov solvers (default on): fmpt_lanczos_ground on a
  * block-sparse (U(1)) operator captures all its iterations into one graph --
  * after convergence a device flag turns the remaining steps into no-ops -- and
