@@ -233,25 +233,33 @@ def dmrg_section(h, fm, budget_s=150.0):
                           "E_mixed_fp64_eval": Emx, "dE_rel_mixed_vs_fp64": abs(Emx - E64) / abs(E64),
                           "E_ed": e_ed, "dE_rel_fp64_vs_ed": abs(E64 - e_ed) / abs(e_ed)}
     # DMRG1S with OptimalExpansion (the reference's default ground-state algorithm), same
-    # chain, start and truncation as the FP64 DMRG2 run above
-    rng = np.random.default_rng(20)
-    psi1 = fm.randommps(20, 2, 8, rng, handle=h)
-    fm.canonicalize_(psi1, normalize=True)
-    env1 = fm.environments(fm.FiniteMPO(hx, 20), psi1)
-    alg1 = fm.DMRG1S(eig_maxiter=30, eig_tol=1e-12, trunc=fm.MPSTruncation(64, 1e-10),
-                     verbosity=0)
-    t1s = []
-    for _ in range(6):
-        h.synchronize()
-        t0 = _t.perf_counter()
-        fm.sweep_(env1, alg1)
-        h.synchronize()
-        t1s.append(_t.perf_counter() - t0)
-    E1 = float(fm.expectation(env1.mps, fm.FiniteMPO(hx, 20)))
-    out["xxz_L20_D64_dmrg1s"] = {"sweep_s_fp64": t1s, "E_fp64": E1, "E_ed": e_ed,
-                                 "dE_rel_vs_ed": abs(E1 - e_ed) / abs(e_ed),
-                                 "Dmax": fm.bond_dimension(env1.mps)}
-    del env1, psi1
+    # chain, start and truncation as the FP64 DMRG2 run above, with the reference's
+    # expansion and with the capped one
+    res1 = {}
+    for cap in (False, True):
+        rng = np.random.default_rng(20)
+        psi1 = fm.randommps(20, 2, 8, rng, handle=h)
+        fm.canonicalize_(psi1, normalize=True)
+        env1 = fm.environments(fm.FiniteMPO(hx, 20), psi1)
+        alg1 = fm.DMRG1S(eig_maxiter=30, eig_tol=1e-12, trunc=fm.MPSTruncation(64, 1e-10),
+                         expan=fm.OptimalExpansion(cap=cap), verbosity=0)
+        t1s = []
+        for _ in range(6):
+            h.synchronize()
+            t0 = _t.perf_counter()
+            fm.sweep_(env1, alg1)
+            h.synchronize()
+            t1s.append(_t.perf_counter() - t0)
+        E1 = float(fm.expectation(env1.mps, fm.FiniteMPO(hx, 20)))
+        res1["capped_expansion" if cap else "reference_expansion"] = {
+            "sweep_s_fp64": t1s, "E_fp64": E1, "dE_rel_vs_ed": abs(E1 - e_ed) / abs(e_ed),
+            "Dmax": fm.bond_dimension(env1.mps)}
+        del env1, psi1
+    res1["E_ed"] = e_ed
+    res1["note"] = ("reference expansion: once D saturates, truncating [B ; V1 NR] (all singular "
+                    "values 1) drops part of the state and the energy stalls; capped: at most "
+                    "D_max - D new directions (not in the reference)")
+    out["xxz_L20_D64_dmrg1s"] = res1
     if _t.perf_counter() - t_start > budget_s:
         return out
     hj = fm.j1j2_heisenberg_mpo(1.0, 0.3)
@@ -584,11 +592,11 @@ def next_rows_section(h, fm):
     layer = fm.QuantumCircuit(fm.QuantumGate((i, i + 1), G) for i in range(1, L))
     res = {}
     for name, svd, meth in (("gesvd", "gesvd", "gesvd"), ("gesvdp", "gesvd", "gesvdp"),
-                            ("dm", "dm", "gesvd")):
+                            ("gesvdj", "gesvd", "gesvdj"), ("dm", "dm", "gesvd")):
         h.set_svd_method(meth)
-        psi_t = fm.FiniteMPS.from_numpy(mps)
+        psi_t = fm.FiniteMPS.from_numpy(mps, handle=h)
         for i in range(1, L + 2):
-            psi_t.s[i] = fm.DeviceTensor.from_numpy(np.asarray(sv[i - 1], dtype=np.float64))
+            psi_t.s[i] = fm.DeviceTensor.from_numpy(np.asarray(sv[i - 1], dtype=np.float64), h)
         centre = layer[L // 2 - 1]                                   # gate on (L/2, L/2+1)
         fm.apply_([centre], psi_t, trunc=fm.MPSTruncation(D, 1e-12), svd=svd)   # warm-up
         h.synchronize()

@@ -357,7 +357,7 @@ int fmpt_tuning_info(fmpt_handle* h, int* entries, int64_t* timed) {
 
 int fmpt_set_svd_method(fmpt_handle* h, int method) {
   if (!h) return FMPT_ERR_ARG;
-  if (method != 0 && method != 1) return set_error(h, FMPT_ERR_ARG, "svd method must be 0 or 1");
+  if (method < 0 || method > 2) return set_error(h, FMPT_ERR_ARG, "svd method must be 0, 1 or 2");
   h->svd_method = method;
   return FMPT_OK;
 }

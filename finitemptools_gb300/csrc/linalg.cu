@@ -87,6 +87,9 @@ static int read_info(fmpt_handle* h, const int* dinfo, int* out) {
   return FMPT_OK;
 }
 
+static int svd_tall_jacobi(fmpt_handle* h, int cplx, int m, int n, double* Awork, double* S,
+                           double* U, double* VT);
+
 // Thin SVD through the polar decomposition A = U_p H (cuSOLVER Xgesvdp, the
 // QDWH iteration followed by an eigendecomposition of H): mostly level-3 work,
 // where gesvd's bidiagonalisation is level-2 bound.  Returns FMPT_OK and
@@ -130,10 +133,11 @@ static int svd_tall_polar(fmpt_handle* h, int cplx, int m, int n, double* Awork,
 
 // Full thin SVD of a tall (m >= n) matrix given in solver layout (real, or
 // interleaved complex) in Awork (overwritten).  U: m x n, S: n, VT: n x n.
-// The handle's svd_method selects gesvd (default) or the polar-decomposition
-// SVD; a failure of either falls back to the one-sided Jacobi SVD.
+// The handle's svd_method selects gesvd (default), the polar-decomposition SVD
+// or the one-sided Jacobi SVD; a failure of the first two falls back to Jacobi.
 int svd_tall(fmpt_handle* h, int cplx, int m, int n, double* Awork, double* S, double* U,
              double* VT) {
+  if (h->svd_method == 2) return svd_tall_jacobi(h, cplx, m, n, Awork, S, U, VT);
   if (h->svd_method == 1) {
     DevBuf Acopy;
     const size_t abytes = (size_t)m * n * sizeof(double) * (cplx ? 2 : 1);
@@ -169,6 +173,17 @@ int svd_tall(fmpt_handle* h, int cplx, int m, int n, double* Awork, double* S, d
   if (info == 0) return FMPT_OK;
   if (info < 0) return set_error(h, FMPT_ERR_CUSOLVER, "gesvd: illegal argument %d", -info);
   // not converged: retry with the one-sided Jacobi SVD (stable_svd.jl:12-18 pattern)
+  return svd_tall_jacobi(h, cplx, m, n, Acopy.d(), S, U, VT);
+}
+
+// One-sided Jacobi SVD (cuSOLVER gesvdj, default tolerance and sweep limit) of a
+// tall matrix in solver layout; A is overwritten.
+static int svd_tall_jacobi(fmpt_handle* h, int cplx, int m, int n, double* Awork, double* S,
+                           double* U, double* VT) {
+  DevBuf dinfo;
+  FMPT_TRY(dinfo.alloc(h, sizeof(int)));
+  double* Aj = Awork;
+  int info = 0;
   gesvdjInfo_t params;
   FMPT_SOLVER(h, cusolverDnCreateGesvdjInfo(&params));
   DevBuf V;
@@ -177,10 +192,10 @@ int svd_tall(fmpt_handle* h, int cplx, int m, int n, double* Awork, double* S, d
   cusolverStatus_t st;
   if (cplx)
     st = cusolverDnZgesvdj_bufferSize(h->solver, CUSOLVER_EIG_MODE_VECTOR, 1, m, n,
-                                      (cuDoubleComplex*)Acopy.p, m, S, (cuDoubleComplex*)U, m,
+                                      (cuDoubleComplex*)Aj, m, S, (cuDoubleComplex*)U, m,
                                       (cuDoubleComplex*)V.p, n, &lw2, params);
   else
-    st = cusolverDnDgesvdj_bufferSize(h->solver, CUSOLVER_EIG_MODE_VECTOR, 1, m, n, Acopy.d(), m,
+    st = cusolverDnDgesvdj_bufferSize(h->solver, CUSOLVER_EIG_MODE_VECTOR, 1, m, n, Aj, m,
                                       S, U, m, V.d(), n, &lw2, params);
   DevBuf w2;
   if (st == CUSOLVER_STATUS_SUCCESS) {
@@ -188,18 +203,18 @@ int svd_tall(fmpt_handle* h, int cplx, int m, int n, double* Awork, double* S, d
     if (s2 != FMPT_OK) { cusolverDnDestroyGesvdjInfo(params); return s2; }
     if (cplx)
       st = cusolverDnZgesvdj(h->solver, CUSOLVER_EIG_MODE_VECTOR, 1, m, n,
-                             (cuDoubleComplex*)Acopy.p, m, S, (cuDoubleComplex*)U, m,
+                             (cuDoubleComplex*)Aj, m, S, (cuDoubleComplex*)U, m,
                              (cuDoubleComplex*)V.p, n, (cuDoubleComplex*)w2.p, lw2,
                              (int*)dinfo.p, params);
     else
-      st = cusolverDnDgesvdj(h->solver, CUSOLVER_EIG_MODE_VECTOR, 1, m, n, Acopy.d(), m, S, U, m,
+      st = cusolverDnDgesvdj(h->solver, CUSOLVER_EIG_MODE_VECTOR, 1, m, n, Aj, m, S, U, m,
                              V.d(), n, w2.d(), lw2, (int*)dinfo.p, params);
   }
   cusolverDnDestroyGesvdjInfo(params);
   if (st != CUSOLVER_STATUS_SUCCESS)
-    return set_error(h, FMPT_ERR_CUSOLVER, "gesvdj fallback failed (status %d)", (int)st);
+    return set_error(h, FMPT_ERR_CUSOLVER, "gesvdj failed (status %d)", (int)st);
   FMPT_TRY(read_info(h, (const int*)dinfo.p, &info));
-  if (info != 0) return set_error(h, FMPT_ERR_CUSOLVER, "gesvd and gesvdj failed (info %d)", info);
+  if (info != 0) return set_error(h, FMPT_ERR_CUSOLVER, "gesvdj did not converge (info %d)", info);
   // VT = V^H (interleaved layout, n x n)
   return copy_mat(h, cplx, n, n, V.d(), n, cplx ? -1 : 0, 1, cplx, VT, n, cplx ? -1 : 0);
 }

@@ -29,11 +29,11 @@ class Handle:
         check(lib().fmpt_synchronize(self.ptr), self.ptr)
 
     def set_svd_method(self, method="gesvd"):
-        """SVD routine of the truncated splits: "gesvd" (default) or "gesvdp"
-        (polar decomposition)."""
-        codes = {"gesvd": 0, "gesvdp": 1}
+        """SVD routine of the truncated splits: "gesvd" (default), "gesvdp"
+        (polar decomposition) or "gesvdj" (one-sided Jacobi)."""
+        codes = {"gesvd": 0, "gesvdp": 1, "gesvdj": 2}
         if method not in codes:
-            raise ValueError("svd method must be 'gesvd' or 'gesvdp'")
+            raise ValueError("svd method must be 'gesvd', 'gesvdp' or 'gesvdj'")
         self.check(lib().fmpt_set_svd_method(self.ptr, codes[method]))
 
     def set_graphs(self, on=True):

@@ -31,7 +31,17 @@ __all__ = ["OptimalExpansion", "default_expansion", "DMRG1S", "TDVP2", "TDVP1S",
 
 
 class OptimalExpansion:
-    """struct OptimalExpansion (optimalexpand.jl:4)."""
+    """struct OptimalExpansion (optimalexpand.jl:4).
+
+    ``cap`` (not in the reference, off by default): add at most trunc.D - D new
+    directions.  The expanded matrix [B ; V1 NR] has orthonormal rows, so all
+    its singular values are 1; once D + k exceeds trunc.D, the reference's
+    truncation of it keeps an arbitrary D-dimensional subspace and drops part of
+    the state, and DMRG1S stalls near 1e-3 (XXZ L=20, D=64).  With the cap a
+    saturated bond is not expanded, and the sweep converges like DMRG2."""
+
+    def __init__(self, cap=False):
+        self.cap = bool(cap)
 
 
 def default_expansion():
@@ -97,7 +107,7 @@ def _complement(M, m, n, QL, QR):
     return M
 
 
-def _residual_directions(m, site, trunc):
+def _residual_directions(m, site, trunc, cap=False):
     """Truncated SVD of NL' * ac2_prime(mps[site] mps[site+1]) * NR' in the full
     space: (u = NL U1 [Dl*d x k], v = V1 NR [k x d*Dr]) or None."""
     mps, mpo, hs = m.mps, m.mpo, m.hstorage
@@ -107,9 +117,10 @@ def _residual_directions(m, site, trunc):
     # dimensions of leftnull(A) and rightnull(B) (full-rank site tensors): nothing to
     # expand into when either is empty; at most min of the two directions otherwise
     cl, cr = Dl * d1 - D, d2 * Dr - D
-    if cl <= 0 or cr <= 0:
+    room = trunc.D - D if cap else trunc.D
+    if cl <= 0 or cr <= 0 or room <= 0:
         return None
-    trunc = MPSTruncation(min(trunc.D, cl, cr), trunc.eps, trunc.verbosity)
+    trunc = MPSTruncation(min(trunc.D, cl, cr, room), trunc.eps, trunc.verbosity)
     x2 = gemm(A, B, (Dl, d1, d2, Dr), Dl * d1, d2 * Dr, D)
     op = HeffOp("ac2", hs[site], hs[site + 2], W1=mpo[site], W2=mpo[site + 1], dtype=A.dtype)
     ac2 = op(x2)
@@ -130,7 +141,7 @@ def right_expansion_(m, site, expan, trunc):
     A, B = mps[site], mps[site + 1]
     Dl, d1, D = A.shape
     _, d2, Dr = B.shape
-    r = _residual_directions(m, site, trunc)
+    r = _residual_directions(m, site, trunc, getattr(expan, "cap", False))
     k = 0 if r is None else r[2].shape[0]
     # b = [B ; V1 NR]  ((D + k) x (d2 Dr))
     bcat = DeviceTensor((D + k, d2 * Dr), B.dtype, B.h)
@@ -153,7 +164,7 @@ def left_expansion_(m, site, expan, trunc):
     A, B = mps[site - 1], mps[site]
     Dl, d1, D = A.shape
     _, d2, Dr = B.shape
-    r = _residual_directions(m, site - 1, trunc)
+    r = _residual_directions(m, site - 1, trunc, getattr(expan, "cap", False))
     k = 0 if r is None else r[0].shape[1]
     # a = [A | NL U1]  ((Dl d1) x (D + k)), columns are contiguous
     acat = DeviceTensor((Dl * d1, D + k), A.dtype, A.h)

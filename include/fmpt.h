@@ -67,8 +67,8 @@ int fmpt_synchronize(fmpt_handle* h);
  * U(1) per-sector SVD, the TEBD bond updates): 0 = cuSOLVER gesvd
  * (bidiagonalisation; the default, as the reference's LAPACK fallback in
  * auxiliary/stable_svd.jl:12-18), 1 = cuSOLVER Xgesvdp (polar decomposition,
- * level-3 bound, faster from a few hundred columns).  Either falls back to the
- * one-sided Jacobi SVD when it reports failure. */
+ * level-3 bound), 2 = cuSOLVER gesvdj (one-sided Jacobi).  0 and 1 fall back
+ * to the Jacobi SVD when they report failure. */
 int fmpt_set_svd_method(fmpt_handle* h, int method);
 
 /* CUDA graphs for the Krylov solvers (default on): fmpt_lanczos_ground on a

@@ -33,8 +33,14 @@ def _rightnull(B):
     return scipy.linalg.null_space(M).conj().T            # r x (d Dr)
 
 
-def _residual(env, site, trunc):
+def _residual(env, site, trunc, cap=False):
     A, B = env.mps[site - 1], env.mps[site]
+    if cap:
+        # not in the reference: at most trunc.D - D new directions
+        room = trunc.D - A.shape[2]
+        if room <= 0:
+            return None
+        trunc = type(trunc)(min(trunc.D, room), trunc.eps)
     x2 = np.tensordot(A, B, axes=([2], [0]))
     ac2 = ac2_prime(x2, env.mpo[site - 1], env.mpo[site], env.hstorage[site - 1],
                     env.hstorage[site + 1])
@@ -47,12 +53,12 @@ def _residual(env, site, trunc):
     return NL @ U1, V1 @ NR
 
 
-def right_expansion(env, site, trunc):
+def right_expansion(env, site, trunc, cap=False):
     """right_expansion! (optimalexpand.jl:42-69)."""
     A, B = env.mps[site - 1], env.mps[site]
     Dl, d1, D = A.shape
     _, d2, Dr = B.shape
-    r = _residual(env, site, trunc)
+    r = _residual(env, site, trunc, cap)
     Bm = B.reshape(D, d2 * Dr, order="F")
     bcat = Bm if r is None else np.vstack([Bm, r[1]])
     u, s, v, _ = stable_tsvd(bcat, trunc)
@@ -63,12 +69,12 @@ def right_expansion(env, site, trunc):
     env.updateright_(site + 1)
 
 
-def left_expansion(env, site, trunc):
+def left_expansion(env, site, trunc, cap=False):
     """left_expansion! (optimalexpand.jl:12-38)."""
     A, B = env.mps[site - 2], env.mps[site - 1]
     Dl, d1, D = A.shape
     _, d2, Dr = B.shape
-    r = _residual(env, site - 1, trunc)
+    r = _residual(env, site - 1, trunc, cap)
     Am = A.reshape(Dl * d1, D, order="F")
     acat = Am if r is None else np.hstack([Am, r[0]])
     u, s, v, _ = stable_tsvd(acat, trunc)
@@ -91,12 +97,12 @@ def _lanczos(env, site, eig_maxiter, eig_tol):
     return E, vec.reshape(A.shape, order="F")
 
 
-def dmrg1s_sweep(env, trunc, eig_maxiter=10, eig_tol=1e-12):
+def dmrg1s_sweep(env, trunc, eig_maxiter=10, eig_tol=1e-12, cap=False):
     """sweep!(m, ::DMRG1S): leftsweep! + rightsweep! (dmrg.jl:158-215)."""
     L = len(env.mps)
     Es, delta = [], 0.0
     for site in range(1, L):
-        right_expansion(env, site, trunc)
+        right_expansion(env, site, trunc, cap)
         E, vec = _lanczos(env, site, eig_maxiter, eig_tol)
         Es.append(E)
         delta = max(delta, _galerkin(env, site, env.mps[site - 1]))
@@ -105,7 +111,7 @@ def dmrg1s_sweep(env, trunc, eig_maxiter=10, eig_tol=1e-12):
         env.mps[site] = np.tensordot(R, env.mps[site], axes=([1], [0]))
         env.updateleft_(site)
     for site in range(L, 1, -1):
-        left_expansion(env, site, trunc)
+        left_expansion(env, site, trunc, cap)
         E, vec = _lanczos(env, site, eig_maxiter, eig_tol)
         Es.append(E)
         delta = max(delta, _galerkin(env, site, env.mps[site - 1]))

@@ -39,6 +39,28 @@ def test_dmrg1s_matches_oracle_and_ed():
     assert fm.bond_dimension(env_g.mps) == O.bond_dimension(env_o.mps)
 
 
+def test_dmrg1s_capped_expansion_at_saturated_bonds():
+    """OptimalExpansion(cap=True) at a bond dimension the chain saturates (D=12 <
+    32): no degenerate truncation of [B ; V1 NR], so the device and the oracle
+    agree entry for entry and the energy settles."""
+    L, D = 10, 12
+    rng = np.random.default_rng(5)
+    st, _ = O.canonicalize(O.randommps(L, 2, 4, rng), normalize=True)
+    h = heisenberg_xxz_mpo()
+    env_o = O.environments(h.site_tensors(L), st, schur=True)
+    env_g = fm.environments(h, _upload(st))
+    tr_o = O.MPSTruncation(D, 1e-12)
+    alg = fm.DMRG1S(eig_maxiter=20, eig_tol=1e-12, trunc=fm.MPSTruncation(D, 1e-12),
+                    expan=fm.OptimalExpansion(cap=True), verbosity=0)
+    for _ in range(6):
+        Eo, _ = OX.dmrg1s_sweep(env_o, tr_o, 20, 1e-12, cap=True)
+        Eg, _ = fm.sweep_(env_g, alg)
+        assert np.abs(np.asarray(Eg) - np.asarray(Eo)).max() < 1e-8 * abs(Eo[-1])
+    assert fm.bond_dimension(env_g.mps) == D
+    assert abs(Eg[-1] - Eg[-L]) < 1e-9 * abs(Eg[-1])
+    assert abs(Eg[-1] - ed.xxz_ground_energy(L)) < 1e-3 * abs(Eg[-1])
+
+
 def test_ground_state_default_is_dmrg1s():
     L = 6
     rng = np.random.default_rng(4)

@@ -100,14 +100,16 @@ def test_uninitialised_svectors_are_canonicalised_and_dtype_checked():
     assert np.abs(_dense(psi) - ref).max() < 1e-12
 
 
+@pytest.mark.parametrize("method", ["gesvdp", "gesvdj"])
 @pytest.mark.parametrize("shape,cplx,rank", [((512, 512), True, None), ((300, 700), False, None),
                                              ((1024, 1024), False, None), ((200, 90), True, 40)])
-def test_polar_svd_matches_gesvd(shape, cplx, rank):
-    """fmpt_set_svd_method(1): the polar-decomposition SVD gives the gesvd
-    singular values (descending) and an exact factorisation.  Measured: 1e-11
-    relative for full-rank matrices; on a rank-deficient matrix its zero
-    singular values come out near 1e-11 sigma_max and the others agree to about
-    1e-8 relative, which is why gesvd stays the default."""
+def test_alternative_svd_matches_gesvd(shape, cplx, rank, method):
+    """fmpt_set_svd_method(1 / 2): the polar-decomposition and Jacobi SVDs give
+    the gesvd singular values (descending) and an exact factorisation.
+    Measured for the polar form: 1e-11 relative on full-rank matrices; on a
+    rank-deficient matrix its zero singular values come out near 1e-11 sigma_max
+    and the others agree to about 1e-8 relative, which is why gesvd stays the
+    default."""
     from finitemptools_gb300.auxiliary import stable_tsvd
     rng = np.random.default_rng(sum(shape))
     m, n = shape
@@ -116,12 +118,12 @@ def test_polar_svd_matches_gesvd(shape, cplx, rank):
         A = A[:, :rank] @ rng.standard_normal((rank, n))
     h = fm.default_handle()
     out = {}
-    for meth in ("gesvd", "gesvdp"):
+    for meth in ("gesvd", method):
         h.set_svd_method(meth)
         u, s, vt, _ = stable_tsvd(DT.from_numpy(A), m, n)
         out[meth] = (u.numpy(), s.numpy(), vt.numpy())
     h.set_svd_method("gesvd")
-    u, s, vt = out["gesvdp"]
+    u, s, vt = out[method]
     s0 = out["gesvd"][1]
     scale = max(1.0, np.abs(s0).max())
     tol = 1e-11 if rank is None else 1e-9
