@@ -88,6 +88,9 @@ SIGNATURES = {
     "fmpt_op_destroy": (c_int, [c_void_p]),
     "fmpt_op_set_projectors": (c_int, [c_void_p, c_int, P(c_void_p)]),
     "fmpt_set_svd_method": (c_int, [c_void_p, c_int]),
+    "fmpt_ac2_prime_host": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p,
+                                    c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_int,
+                                    c_int, c_int, c_int]),
     "fmpt_apply_gate": (c_int, [c_void_p, c_int, c_void_p, c_int, dptr, dptr, c_int, c_int]),
     "fmpt_eigsolve": (c_int, [c_void_p, dptr, c_int, c_int, c_int, c_double, c_int, P(c_double),
                               dptr, P(c_double), P(c_int), P(c_int)]),

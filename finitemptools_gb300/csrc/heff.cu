@@ -288,7 +288,8 @@ static int check_dtype_prec(fmpt_handle* h, int dtype, int precision) {
 
 static int make_op(fmpt_handle* h, int kind, int dtype, int precision, const double* W1,
                    const double* W2, const double* hleft, const double* hright, int Dl, int d1,
-                   int d2, int Dr, int wl, int wm, int wr, fmpt_op** out) {
+                   int d2, int Dr, int wl, int wm, int wr, fmpt_op** out,
+                   bool defer_right = false) {
   FMPT_TRY(check_dtype_prec(h, dtype, precision));
   if (!out || !hleft || !hright) return set_error(h, FMPT_ERR_ARG, "null pointer");
   if (Dl < 1 || Dr < 1 || d1 < 1 || d2 < 1 || wl < 1 || wm < 1 || wr < 1)
@@ -297,6 +298,7 @@ static int make_op(fmpt_handle* h, int kind, int dtype, int precision, const dou
   op->h = h; op->kind = kind; op->dtype = dtype; op->precision = precision;
   op->Dl = Dl; op->Dr = Dr; op->d1 = d1; op->d2 = d2; op->wl = wl; op->wm = wm; op->wr = wr;
   op->hleft = hleft; op->hright = hright;
+  op->defer_right = defer_right && precision != FMPT_PREC_FP64 && dtype == FMPT_F64 && kind == 0;
   const int cp = dtype == FMPT_C128;
   int st = FMPT_OK;
   if (kind == 0) {
@@ -370,6 +372,88 @@ int fmpt_ac2_prime(fmpt_handle* h, int dtype, int precision, const double* x, co
                        &op));
   int st = fmpt_op_apply(op, x, y);
   fmpt_op_destroy(op);
+  return st;
+}
+
+int fmpt_ac2_prime_host(fmpt_handle* h, int dtype, int precision, const double* x,
+                        const double* W1, const double* W2, const double* hleft,
+                        const double* hright, double* y, int Dl, int d1, int d2, int Dr, int wl,
+                        int wm, int wr) {
+  FMPT_TRY(check_dtype_prec(h, dtype, precision));
+  if (!x || !W1 || !W2 || !hleft || !hright || !y)
+    return set_error(h, FMPT_ERR_ARG, "ac2_prime_host: null pointer");
+  if (Dl < 1 || Dr < 1 || d1 < 1 || d2 < 1 || wl < 1 || wm < 1 || wr < 1)
+    return set_error(h, FMPT_ERR_SHAPE, "non-positive dimension");
+  const size_t es = sizeof(double) * (dtype == FMPT_C128 ? 2 : 1);
+  const size_t bx = (size_t)Dl * d1 * d2 * Dr * es, bL = (size_t)Dl * wl * Dl * es,
+               bR = (size_t)Dr * wr * Dr * es;
+  DevBuf dx, dL, dR, dy;
+  FMPT_TRY(dx.alloc(h, bx));
+  FMPT_TRY(dL.alloc(h, bL));
+  FMPT_TRY(dR.alloc(h, bR));
+  FMPT_TRY(dy.alloc(h, bx));
+  cudaStream_t ms = h->stream;
+  const bool pipeline = precision != FMPT_PREC_FP64 && dtype == FMPT_F64;
+  if (!pipeline) {
+    FMPT_CUDA(h, cudaMemcpyAsync(dx.p, x, bx, cudaMemcpyHostToDevice, ms));
+    FMPT_CUDA(h, cudaMemcpyAsync(dL.p, hleft, bL, cudaMemcpyHostToDevice, ms));
+    FMPT_CUDA(h, cudaMemcpyAsync(dR.p, hright, bR, cudaMemcpyHostToDevice, ms));
+    FMPT_TRY(fmpt_ac2_prime(h, dtype, precision, dx.d(), W1, W2, dL.d(), dR.d(), dy.d(), Dl, d1,
+                            d2, Dr, wl, wm, wr));
+    FMPT_CUDA(h, cudaMemcpyAsync(y, dy.p, bx, cudaMemcpyDeviceToHost, ms));
+    FMPT_CUDA(h, cudaStreamSynchronize(ms));
+    return FMPT_OK;
+  }
+  // One copy queue (auxiliary stream) in the order L, x, R; the compute on the main
+  // stream starts on each operand as soon as it has arrived: the L conversion overlaps
+  // the x copy, and the x conversion, GEMM 1 and the MPO step overlap the R copy.
+  FMPT_TRY(aux_fork(h, 1));        // the copies follow the allocations above
+  cudaStream_t as = h->aux_stream[0];
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+  int st = FMPT_OK;
+  for (int i = 0; i < 3 && st == FMPT_OK; i++)
+    if (cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming) != cudaSuccess)
+      st = set_error(h, FMPT_ERR_CUDA, "ac2_prime_host: event creation failed");
+  const void* src[3] = {hleft, x, hright};
+  void* dst[3] = {dL.p, dx.p, dR.p};
+  const size_t nb[3] = {bL, bx, bR};
+  for (int i = 0; i < 3 && st == FMPT_OK; i++) {
+    if (cudaMemcpyAsync(dst[i], src[i], nb[i], cudaMemcpyHostToDevice, as) != cudaSuccess ||
+        cudaEventRecord(ev[i], as) != cudaSuccess)
+      st = set_error(h, FMPT_ERR_CUDA, "ac2_prime_host: copy submission failed");
+  }
+  fmpt_op* op = nullptr;
+  if (st == FMPT_OK && cudaStreamWaitEvent(ms, ev[0], 0) != cudaSuccess)
+    st = set_error(h, FMPT_ERR_CUDA, "ac2_prime_host: stream wait failed");
+  if (st == FMPT_OK)
+    st = make_op(h, 0, dtype, precision, W1, W2, dL.d(), dR.d(), Dl, d1, d2, Dr, wl, wm, wr, &op,
+                 true);
+  if (st == FMPT_OK && cudaStreamWaitEvent(ms, ev[1], 0) != cudaSuccess)
+    st = set_error(h, FMPT_ERR_CUDA, "ac2_prime_host: stream wait failed");
+  if (st == FMPT_OK) st = op->defer_right ? op_tc_apply_head(op, dx.d()) : FMPT_OK;
+  if (st == FMPT_OK && cudaStreamWaitEvent(ms, ev[2], 0) != cudaSuccess)
+    st = set_error(h, FMPT_ERR_CUDA, "ac2_prime_host: stream wait failed");
+  if (st == FMPT_OK) {
+    if (op->defer_right) {
+      st = op_tc_prepare_right(op);
+      if (st == FMPT_OK) st = op_tc_apply_tail(op, dy.d());
+    } else {
+      st = fmpt_op_apply(op, dx.d(), dy.d());
+    }
+  }
+  if (st == FMPT_OK && cudaMemcpyAsync(y, dy.p, bx, cudaMemcpyDeviceToHost, ms) != cudaSuccess)
+    st = set_error(h, FMPT_ERR_CUDA, "ac2_prime_host: copy submission failed");
+  // every queued copy and kernel ends before the buffers are released
+  if (cudaStreamSynchronize(as) != cudaSuccess && st == FMPT_OK)
+    st = set_error(h, FMPT_ERR_CUDA, "ac2_prime_host: copy stream failed");
+  if (cudaStreamSynchronize(ms) != cudaSuccess && st == FMPT_OK)
+    st = set_error(h, FMPT_ERR_CUDA, "ac2_prime_host: %s", cudaGetErrorString(cudaGetLastError()));
+  if (op) {
+    if (st == FMPT_OK) st = op_tc_check(op);
+    fmpt_op_destroy(op);
+  }
+  for (int i = 0; i < 3; i++)
+    if (ev[i]) cudaEventDestroy(ev[i]);
   return st;
 }
 

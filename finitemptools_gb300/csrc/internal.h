@@ -234,6 +234,7 @@ struct fmpt_op {
   int64_t n = 0;          // vector length (complex elements for C128)
   void* tc = nullptr;     // tensor-core state (mixed precision), owned
   void* u1 = nullptr;     // U(1) block-sparse state (grouped program + scratch), owned
+  bool defer_right = false;  // mixed precision: the right environment is converted later
   // projectors of the excited-state sweeps: after every application
   // y -= dot(y, p) p for each p in order (device vectors of n elements, not owned)
   std::vector<const double*> proj;
@@ -245,6 +246,12 @@ namespace fmpt {
 int op_apply_fp64(fmpt_op* op, const double* x, double* y);
 int op_tc_prepare(fmpt_op* op);
 int op_tc_apply(fmpt_op* op, const double* x, double* y);
+// split application of a real tensor-core two-site operator (host-buffer pipeline):
+// head = x conversion, GEMM 1 and MPO step; tail = GEMM 2; prepare_right converts the
+// right environment of an operator created with defer_right
+int op_tc_apply_head(fmpt_op* op, const double* x);
+int op_tc_apply_tail(fmpt_op* op, double* y);
+int op_tc_prepare_right(fmpt_op* op);
 int op_tc_check(fmpt_op* op);   // reads the device timeout flag (synchronises)
 // mixed-precision environment update (real data), FP64 output in the reference layout
 int env_update_tc(fmpt_handle* h, bool right, int precision, const double* hold, const double* A,

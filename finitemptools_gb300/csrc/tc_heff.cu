@@ -378,10 +378,21 @@ int op_tc_prepare(fmpt_op* op) {
   // Lg[a + Kp*(a' + Dl*w)] = L[a' + Dl*w + Dl*wl*a]: per w, (r=a', c=a)
   FMPT_TRY(transpose_any(h, st->mode, op->hleft, (int64_t)Dl * wl, Dl, Dl, Dl, st->Kp, wl,
                          st->Lg[0].p, lo_L, st->Kp, (int64_t)st->Kp * Dl));
-  // Rg[b + Drp*w2 + K2*b'] = R[b' + Dr*w2 + Dr*wr*b]: per w2, (r=b', c=b)
-  FMPT_TRY(transpose_any(h, st->mode, op->hright, (int64_t)Dr * wr, Dr, Dr, Dr, st->Drp, wr,
-                         st->Rg[0].p, lo_R, st->K2, st->Drp));
-  return FMPT_OK;
+  if (op->defer_right) return FMPT_OK;
+  return op_tc_prepare_right(op);
+}
+
+// Rg[b + Drp*w2 + K2*b'] = R[b' + Dr*w2 + Dr*wr*b]: per w2, (r=b', c=b).  Part of
+// op_tc_prepare, run later for an operator created with defer_right (real data), once
+// the right environment has arrived.
+int op_tc_prepare_right(fmpt_op* op) {
+  fmpt_handle* h = op->h;
+  TcState* st = static_cast<TcState*>(op->tc);
+  if (!st || st->cplx) return set_error(h, FMPT_ERR_ARG, "prepare_right: real tensor-core operator only");
+  const int Dr = op->Dr, wr = op->wr;
+  void* lo_R = st->mode == M_TF32X3 ? st->Rg[1].p : nullptr;
+  return transpose_any(h, st->mode, op->hright, (int64_t)Dr * wr, Dr, Dr, Dr, st->Drp, wr,
+                       st->Rg[0].p, lo_R, st->K2, st->Drp);
 }
 
 int op_tc_apply_complex(fmpt_op* op, TcState* st, const double* x, double* y);
@@ -391,6 +402,16 @@ int op_tc_apply(fmpt_op* op, const double* x, double* y) {
   TcState* st = static_cast<TcState*>(op->tc);
   if (!st) return set_error(h, FMPT_ERR_ARG, "operator has no tensor-core state");
   if (st->cplx) return op_tc_apply_complex(op, st, x, y);
+  FMPT_TRY(op_tc_apply_head(op, x));
+  return op_tc_apply_tail(op, y);
+}
+
+// The part of a real two-site application that needs x and the left environment
+// only: x conversion, GEMM 1 and the MPO step (T3 is left in the operator).
+int op_tc_apply_head(fmpt_op* op, const double* x) {
+  fmpt_handle* h = op->h;
+  TcState* st = static_cast<TcState*>(op->tc);
+  if (!st || st->cplx) return set_error(h, FMPT_ERR_ARG, "apply_head: real tensor-core operator only");
   const int Dl = op->Dl, Dr = op->Dr, wl = op->wl, P = st->P;
   const int split = st->mode == M_TF32X3 ? 2 : 1;
   void* xlo = split > 1 ? st->xg[1].p : nullptr;
@@ -440,7 +461,18 @@ int op_tc_apply(fmpt_op* op, const double* x, double* y) {
 #undef MIDTC
     FMPT_LAUNCHED(h);
   }
-  // GEMM 2: y[(a' s'), b'] = sum_(b w2) T3[(b w2), (a' s')] Rg[(b w2), b']
+  return FMPT_OK;
+}
+
+// GEMM 2 of a real application, after op_tc_apply_head:
+// y[(a' s'), b'] = sum_(b w2) T3[(b w2), (a' s')] Rg[(b w2), b']
+int op_tc_apply_tail(fmpt_op* op, double* y) {
+  fmpt_handle* h = op->h;
+  TcState* st = static_cast<TcState*>(op->tc);
+  if (!st || st->cplx) return set_error(h, FMPT_ERR_ARG, "apply_tail: real tensor-core operator only");
+  const int Dl = op->Dl, Dr = op->Dr, P = st->P;
+  const int split = st->mode == M_TF32X3 ? 2 : 1;
+  void* tlo = split > 1 ? st->T3[1].p : nullptr;
   TcOperand A2{st->T3[0].p, tlo, st->K2, 0};
   TcOperand B2{st->Rg[0].p, split > 1 ? st->Rg[1].p : nullptr, st->K2, 0};
   FMPT_TRY(tc_gemm(h, st->mode, P * Dl, Dr, (int)st->K2, 1, A2, B2, y, 1, (int64_t)P * Dl, 0,

@@ -172,6 +172,34 @@ def ac2_prime(x, h1, h2, hleft, hright, precision="fp64"):
     return HeffOp("ac2", hleft, hright, W1=h1, W2=h2, precision=precision, dtype=x.dtype)(x)
 
 
+def ac2_prime_host(x, h1, h2, hleft, hright, precision="fp64", handle=None):
+    """derivatives.jl:20-22 on host arrays (fmpt_ac2_prime_host): numpy x [Dl,d1,d2,Dr],
+    hleft [Dl,wl,Dl], hright [Dr,wr,Dr], MPO tensors [wl,d1',wm,d1] and [wm,d2',wr,d2];
+    returns y as a numpy array.  Real data in a mixed precision pipelines the
+    transfers with the compute."""
+    from .device import default_handle, to_host_buffer
+    h = handle or default_handle()
+    x, hleft, hright = np.asarray(x), np.asarray(hleft), np.asarray(hright)
+    W1, W2 = np.asarray(h1), np.asarray(h2)
+    cplx = any(np.iscomplexobj(a) for a in (x, hleft, hright, W1, W2))
+    dt = np.complex128 if cplx else np.float64
+    Dl, d1, d2, Dr = x.shape
+    wl, wm, wr = W1.shape[0], W1.shape[2], W2.shape[2]
+    if hleft.shape != (Dl, wl, Dl) or hright.shape != (Dr, wr, Dr) or W2.shape[0] != wm:
+        raise ValueError("DimensionMismatch in ac2_prime_host")
+    # every host buffer stays referenced here until the call returns
+    bufs = [to_host_buffer(a, dt) for a in (x, W1, W2, hleft, hright)]
+    y = np.empty_like(bufs[0])
+    h.check(lib().fmpt_ac2_prime_host(h.ptr, C128 if cplx else 0, _prec(precision),
+                                      bufs[0].ctypes.data, bufs[1].ctypes.data,
+                                      bufs[2].ctypes.data, bufs[3].ctypes.data,
+                                      bufs[4].ctypes.data, y.ctypes.data, Dl, d1, d2, Dr, wl, wm,
+                                      wr))
+    n = x.size
+    flat = y[:n] + 1j * y[n:] if cplx else y
+    return flat.reshape(x.shape, order="F")
+
+
 def c_prime(x, hleft, hright, precision="fp64"):
     """derivatives.jl:52-54 -- zero-site H_eff * C."""
     return HeffOp("c", hleft, hright, precision=precision, dtype=x.dtype)(x)

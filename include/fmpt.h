@@ -149,6 +149,18 @@ int fmpt_ac2_prime(fmpt_handle* h, int dtype, int precision, const double* x,
                    const double* W1_host, const double* W2_host, const double* hleft,
                    const double* hright, double* y, int Dl, int d1, int d2, int Dr,
                    int wl, int wm, int wr);
+/* ac2_prime with HOST buffers: x, hleft, hright and y live in host memory, W1/W2 as
+ * for fmpt_ac2_prime.  The result is identical to copying in, calling fmpt_ac2_prime
+ * and copying out.  For real data in a mixed precision the transfers are pipelined
+ * on a second stream (L, then x, then R): the L conversion overlaps the x copy, and
+ * the x conversion, GEMM 1 and the MPO step overlap the R copy.  Use page-locked
+ * buffers (cudaHostAlloc / cudaHostRegister) for the overlap; pageable memory works
+ * but copies synchronously.  Returns after y has been written. */
+int fmpt_ac2_prime_host(fmpt_handle* h, int dtype, int precision, const double* x_host,
+                        const double* W1_host, const double* W2_host, const double* hleft_host,
+                        const double* hright_host, double* y_host, int Dl, int d1, int d2,
+                        int Dr, int wl, int wm, int wr);
+
 /* ac_prime (derivatives.jl:2-4): y[a',s',b'] = sum L[a',w,a] x[a,s,b] W[w,s',w2,s] R[b',w2,b] */
 int fmpt_ac_prime(fmpt_handle* h, int dtype, int precision, const double* x,
                   const double* W_host, const double* hleft, const double* hright, double* y,

@@ -210,3 +210,40 @@ def test_tdvp1_complex_mixed_matches_fp64():
             fm.sweep_(env, alg)
         vals[prec] = [float(np.real(fm.expectation_local(env.mps, i, Z))) for i in (3, 6, 9)]
     assert np.abs(np.array(vals["tf32x3"]) - np.array(vals["fp64"])).max() < 1e-5
+
+
+@pytest.mark.parametrize("prec,cplx,D", [("bf16", False, 100), ("tf32x3", False, 256),
+                                         ("tf32", False, 37), ("fp64", False, 64),
+                                         ("bf16", True, 48)])
+def test_ac2_prime_host_matches_device_path(prec, cplx, D):
+    """fmpt_ac2_prime_host (host buffers, pipelined transfers for real mixed
+    precision) gives exactly the result of copy-in + fmpt_ac2_prime + copy-out."""
+    import torch
+    from finitemptools_gb300.derivatives import ac2_prime_host
+    rng = np.random.default_rng(D)
+    W = heisenberg_xxz_mpo()[1].dense()
+    w = W.shape[0]
+
+    def r(*s):
+        a = rng.standard_normal(s)
+        return a + 1j * rng.standard_normal(s) if cplx else a
+
+    x, L, R = r(D, 2, 2, D), r(D, w, D), r(D, w, D)
+    dt = np.complex128 if cplx else np.float64
+    ref = fm.ac2_prime(DT.from_numpy(x, dtype=dt), W, W, DT.from_numpy(L, dtype=dt),
+                       DT.from_numpy(R, dtype=dt), precision=prec).numpy()
+    y = ac2_prime_host(x, W, W, L, R, precision=prec)
+    assert np.array_equal(y, ref)
+    if not cplx:
+        # page-locked host buffers through the C ABI, as the bench's end-to-end step uses
+        from finitemptools_gb300._native import lib, PREC
+        h = fm.default_handle()
+        px = torch.from_numpy(x.ravel(order="F").copy()).pin_memory()
+        pL = torch.from_numpy(L.ravel(order="F").copy()).pin_memory()
+        pR = torch.from_numpy(R.ravel(order="F").copy()).pin_memory()
+        py = torch.empty(x.size, dtype=torch.float64).pin_memory()
+        Wb = np.ascontiguousarray(W.ravel(order="F"))
+        h.check(lib().fmpt_ac2_prime_host(h.ptr, 0, PREC[prec], px.data_ptr(), Wb.ctypes.data,
+                                          Wb.ctypes.data, pL.data_ptr(), pR.data_ptr(),
+                                          py.data_ptr(), D, 2, 2, D, w, w, w))
+        assert np.array_equal(py.numpy().reshape(x.shape, order="F"), ref)
