@@ -404,56 +404,67 @@ int fmpt_ac2_prime_host(fmpt_handle* h, int dtype, int precision, const double* 
     FMPT_CUDA(h, cudaStreamSynchronize(ms));
     return FMPT_OK;
   }
-  // One copy queue (auxiliary stream) in the order L, x, R; the compute on the main
-  // stream starts on each operand as soon as it has arrived: the L conversion overlaps
-  // the x copy, and the x conversion, GEMM 1 and the MPO step overlap the R copy.
-  FMPT_TRY(aux_fork(h, 1));        // the copies follow the allocations above
-  cudaStream_t as = h->aux_stream[0];
-  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+  // Uploads on one copy stream in the order L, x, R (R in column blocks of b'), downloads
+  // of y on a second one.  The main stream starts on each operand as soon as it has
+  // arrived: the L conversion overlaps the x copy; the x conversion, GEMM 1 and the MPO
+  // step overlap the R copy; block c of R is converted and multiplied (GEMM 2 for the
+  // columns b' of block c) while block c+1 is uploaded, and y's block c is downloaded
+  // meanwhile.  A block of R[b', w2, b] (b' fastest) is a pitched 2-D copy.
+  const int nblk = Dr >= 1024 ? 4 : (Dr >= 256 ? 2 : 1);
+  FMPT_TRY(aux_fork(h, 2));        // the copies follow the allocations above
+  cudaStream_t as = h->aux_stream[0], ds = h->aux_stream[1];
+  std::vector<cudaEvent_t> ev(2 + 2 * nblk, nullptr);   // L, x, R blocks, y blocks
   int st = FMPT_OK;
-  for (int i = 0; i < 3 && st == FMPT_OK; i++)
+  for (size_t i = 0; i < ev.size() && st == FMPT_OK; i++)
     if (cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming) != cudaSuccess)
       st = set_error(h, FMPT_ERR_CUDA, "ac2_prime_host: event creation failed");
-  const void* src[3] = {hleft, x, hright};
-  void* dst[3] = {dL.p, dx.p, dR.p};
-  const size_t nb[3] = {bL, bx, bR};
-  for (int i = 0; i < 3 && st == FMPT_OK; i++) {
-    if (cudaMemcpyAsync(dst[i], src[i], nb[i], cudaMemcpyHostToDevice, as) != cudaSuccess ||
-        cudaEventRecord(ev[i], as) != cudaSuccess)
-      st = set_error(h, FMPT_ERR_CUDA, "ac2_prime_host: copy submission failed");
-  }
-  fmpt_op* op = nullptr;
-  if (st == FMPT_OK && cudaStreamWaitEvent(ms, ev[0], 0) != cudaSuccess)
-    st = set_error(h, FMPT_ERR_CUDA, "ac2_prime_host: stream wait failed");
-  if (st == FMPT_OK)
-    st = make_op(h, 0, dtype, precision, W1, W2, dL.d(), dR.d(), Dl, d1, d2, Dr, wl, wm, wr, &op,
-                 true);
-  if (st == FMPT_OK && cudaStreamWaitEvent(ms, ev[1], 0) != cudaSuccess)
-    st = set_error(h, FMPT_ERR_CUDA, "ac2_prime_host: stream wait failed");
-  if (st == FMPT_OK) st = op->defer_right ? op_tc_apply_head(op, dx.d()) : FMPT_OK;
-  if (st == FMPT_OK && cudaStreamWaitEvent(ms, ev[2], 0) != cudaSuccess)
-    st = set_error(h, FMPT_ERR_CUDA, "ac2_prime_host: stream wait failed");
+  auto rows = [&](int c) { return std::make_pair((int)((int64_t)Dr * c / nblk),
+                                                 (int)((int64_t)Dr * (c + 1) / nblk)); };
+  auto ok = [&](cudaError_t e) {
+    if (e != cudaSuccess && st == FMPT_OK)
+      st = set_error(h, FMPT_ERR_CUDA, "ac2_prime_host: %s", cudaGetErrorString(e));
+    return st == FMPT_OK;
+  };
   if (st == FMPT_OK) {
-    if (op->defer_right) {
-      st = op_tc_prepare_right(op);
-      if (st == FMPT_OK) st = op_tc_apply_tail(op, dy.d());
-    } else {
-      st = fmpt_op_apply(op, dx.d(), dy.d());
+    ok(cudaMemcpyAsync(dL.p, hleft, bL, cudaMemcpyHostToDevice, as)) && ok(cudaEventRecord(ev[0], as));
+    ok(cudaMemcpyAsync(dx.p, x, bx, cudaMemcpyHostToDevice, as)) && ok(cudaEventRecord(ev[1], as));
+    for (int c = 0; c < nblk && st == FMPT_OK; c++) {
+      const auto r = rows(c);
+      ok(cudaMemcpy2DAsync(dR.d() + r.first, (size_t)Dr * sizeof(double), hright + r.first,
+                           (size_t)Dr * sizeof(double), (size_t)(r.second - r.first) * sizeof(double),
+                           (size_t)wr * Dr, cudaMemcpyHostToDevice, as)) &&
+          ok(cudaEventRecord(ev[2 + c], as));
     }
   }
-  if (st == FMPT_OK && cudaMemcpyAsync(y, dy.p, bx, cudaMemcpyDeviceToHost, ms) != cudaSuccess)
-    st = set_error(h, FMPT_ERR_CUDA, "ac2_prime_host: copy submission failed");
+  fmpt_op* op = nullptr;
+  if (st == FMPT_OK && ok(cudaStreamWaitEvent(ms, ev[0], 0)))
+    st = make_op(h, 0, dtype, precision, W1, W2, dL.d(), dR.d(), Dl, d1, d2, Dr, wl, wm, wr, &op,
+                 true);
+  if (st == FMPT_OK && !op->defer_right)
+    st = set_error(h, FMPT_ERR_ARG, "ac2_prime_host: operator without a deferred right side");
+  if (st == FMPT_OK && ok(cudaStreamWaitEvent(ms, ev[1], 0))) st = op_tc_apply_head(op, dx.d());
+  const size_t col = (size_t)Dl * d1 * d2 * sizeof(double);    // bytes of one column b' of y
+  for (int c = 0; c < nblk && st == FMPT_OK; c++) {
+    const auto r = rows(c);
+    if (!ok(cudaStreamWaitEvent(ms, ev[2 + c], 0))) break;
+    st = op_tc_prepare_right_rows(op, r.first, r.second);
+    if (st == FMPT_OK) st = op_tc_apply_tail_rows(op, dy.d(), r.first, r.second);
+    if (st == FMPT_OK && ok(cudaEventRecord(ev[2 + nblk + c], ms)) &&
+        ok(cudaStreamWaitEvent(ds, ev[2 + nblk + c], 0)))
+      ok(cudaMemcpyAsync(reinterpret_cast<char*>(y) + col * r.first,
+                         reinterpret_cast<char*>(dy.p) + col * r.first,
+                         col * (r.second - r.first), cudaMemcpyDeviceToHost, ds));
+  }
   // every queued copy and kernel ends before the buffers are released
-  if (cudaStreamSynchronize(as) != cudaSuccess && st == FMPT_OK)
-    st = set_error(h, FMPT_ERR_CUDA, "ac2_prime_host: copy stream failed");
-  if (cudaStreamSynchronize(ms) != cudaSuccess && st == FMPT_OK)
-    st = set_error(h, FMPT_ERR_CUDA, "ac2_prime_host: %s", cudaGetErrorString(cudaGetLastError()));
+  ok(cudaStreamSynchronize(as));
+  ok(cudaStreamSynchronize(ms));
+  ok(cudaStreamSynchronize(ds));
   if (op) {
     if (st == FMPT_OK) st = op_tc_check(op);
     fmpt_op_destroy(op);
   }
-  for (int i = 0; i < 3; i++)
-    if (ev[i]) cudaEventDestroy(ev[i]);
+  for (cudaEvent_t e : ev)
+    if (e) cudaEventDestroy(e);
   return st;
 }
 

@@ -252,6 +252,9 @@ int op_tc_apply(fmpt_op* op, const double* x, double* y);
 int op_tc_apply_head(fmpt_op* op, const double* x);
 int op_tc_apply_tail(fmpt_op* op, double* y);
 int op_tc_prepare_right(fmpt_op* op);
+// the same for the rows b' in [r0, r1) of the right environment / columns of y
+int op_tc_prepare_right_rows(fmpt_op* op, int r0, int r1);
+int op_tc_apply_tail_rows(fmpt_op* op, double* y, int r0, int r1);
 int op_tc_check(fmpt_op* op);   // reads the device timeout flag (synchronises)
 // mixed-precision environment update (real data), FP64 output in the reference layout
 int env_update_tc(fmpt_handle* h, bool right, int precision, const double* hold, const double* A,

@@ -385,14 +385,20 @@ int op_tc_prepare(fmpt_op* op) {
 // Rg[b + Drp*w2 + K2*b'] = R[b' + Dr*w2 + Dr*wr*b]: per w2, (r=b', c=b).  Part of
 // op_tc_prepare, run later for an operator created with defer_right (real data), once
 // the right environment has arrived.
-int op_tc_prepare_right(fmpt_op* op) {
+int op_tc_prepare_right(fmpt_op* op) { return op_tc_prepare_right_rows(op, 0, op->Dr); }
+
+// Rows b' in [r0, r1) of the converted right environment (they need R[b', :, :] only).
+int op_tc_prepare_right_rows(fmpt_op* op, int r0, int r1) {
   fmpt_handle* h = op->h;
   TcState* st = static_cast<TcState*>(op->tc);
   if (!st || st->cplx) return set_error(h, FMPT_ERR_ARG, "prepare_right: real tensor-core operator only");
   const int Dr = op->Dr, wr = op->wr;
+  if (r0 < 0 || r1 > Dr || r0 >= r1) return set_error(h, FMPT_ERR_ARG, "prepare_right: bad row range");
   void* lo_R = st->mode == M_TF32X3 ? st->Rg[1].p : nullptr;
-  return transpose_any(h, st->mode, op->hright, (int64_t)Dr * wr, Dr, Dr, Dr, st->Drp, wr,
-                       st->Rg[0].p, lo_R, st->K2, st->Drp);
+  const int64_t off = st->K2 * r0;
+  return transpose_any(h, st->mode, op->hright + r0, (int64_t)Dr * wr, Dr, r1 - r0, Dr, st->Drp,
+                       wr, offset(st->Rg[0].p, off, st->es), offset(lo_R, off, st->es), st->K2,
+                       st->Drp);
 }
 
 int op_tc_apply_complex(fmpt_op* op, TcState* st, const double* x, double* y);
@@ -466,15 +472,24 @@ int op_tc_apply_head(fmpt_op* op, const double* x) {
 
 // GEMM 2 of a real application, after op_tc_apply_head:
 // y[(a' s'), b'] = sum_(b w2) T3[(b w2), (a' s')] Rg[(b w2), b']
-int op_tc_apply_tail(fmpt_op* op, double* y) {
+int op_tc_apply_tail(fmpt_op* op, double* y) { return op_tc_apply_tail_rows(op, y, 0, op->Dr); }
+
+// GEMM 2 for the output columns b' in [r0, r1): y[:, b'] needs rows b' of Rg only.  The
+// B operand starts K2*r0 elements in (16-byte aligned: K2 is a multiple of 8 elements of
+// at least 2 bytes) and the output P*Dl*r0 doubles in.
+int op_tc_apply_tail_rows(fmpt_op* op, double* y, int r0, int r1) {
   fmpt_handle* h = op->h;
   TcState* st = static_cast<TcState*>(op->tc);
   if (!st || st->cplx) return set_error(h, FMPT_ERR_ARG, "apply_tail: real tensor-core operator only");
-  const int Dl = op->Dl, Dr = op->Dr, P = st->P;
+  const int Dl = op->Dl, P = st->P;
+  if (r0 < 0 || r1 > op->Dr || r0 >= r1) return set_error(h, FMPT_ERR_ARG, "apply_tail: bad row range");
+  const int Dr = r1 - r0;
   const int split = st->mode == M_TF32X3 ? 2 : 1;
   void* tlo = split > 1 ? st->T3[1].p : nullptr;
+  y += (int64_t)P * Dl * r0;
   TcOperand A2{st->T3[0].p, tlo, st->K2, 0};
-  TcOperand B2{st->Rg[0].p, split > 1 ? st->Rg[1].p : nullptr, st->K2, 0};
+  TcOperand B2{offset(st->Rg[0].p, st->K2 * r0, st->es),
+               split > 1 ? offset(st->Rg[1].p, st->K2 * r0, st->es) : nullptr, st->K2, 0};
   FMPT_TRY(tc_gemm(h, st->mode, P * Dl, Dr, (int)st->K2, 1, A2, B2, y, 1, (int64_t)P * Dl, 0,
                    st->err));
   return FMPT_OK;
