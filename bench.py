@@ -675,6 +675,40 @@ def tdvp_grad_section(h, fm, nsteps=5):
                     % (100 * t_grad / nsteps)}
 
 
+def ed_heff_case(args):
+    """The device ED operator alone: ac_prime at the centre of an ExactFiniteMPS of the
+    XXZ chain (L = args.ed_heff sites; at L=20 the centre is 512 x 2 x 1024 with
+    environments 512 x 5 x 512 and 1024 x 5 x 1024), FP64, seeded random x.  Warm-up
+    applications, then timed ones; its FP64 GEMMs are the process's only gemm_kernel
+    launches after the environment build, which is what an ncu capture with
+    -k regex:gemm_kernel -s <n> needs."""
+    import time as _t
+    import finitemptools_gb300 as fm
+    h = fm.default_handle()
+    L = args.ed_heff
+    hx = fm.heisenberg_xxz_mpo()
+    psi = fm.ExactFiniteMPS.random([2] * L, rng=np.random.default_rng(L), handle=h)
+    left, right, Wc = fm.init_h_center(hx, psi)
+    op = fm.HeffOp("ac", left, right, W1=Wc)
+    x = psi[psi.center]
+    y = fm.DeviceTensor(x.shape, np.float64, h)
+    for _ in range(args.warmup):
+        op(x, y)
+    h.synchronize()
+    t0 = _t.perf_counter()
+    for _ in range(args.steps):
+        op(x, y)
+    h.synchronize()
+    ms = 1e3 * (_t.perf_counter() - t0) / args.steps
+    Dl, d, Dr = x.shape
+    w = Wc.shape[0]
+    # pairwise order of ac_prime (derivatives.jl:2-4): L.x, then W, then .R
+    flops = 2.0 * Dl * w * Dl * d * Dr + 2.0 * Dl * w * d * w * d * Dr + 2.0 * Dl * d * w * Dr * Dr
+    print(json.dumps({"case": "ed_heff", "L": L, "centre": list(x.shape), "w": w,
+                      "ms_per_apply": ms, "gflop_per_apply": flops / 1e9,
+                      "tflops": flops / (ms / 1e3) / 1e12}), flush=True)
+
+
 def u1_heff_case(args):
     """The block-sparse two-site H_eff*x alone: legs of the centre bond of an L=64,
     total-Sz=0 chain with bond dimension D (sector dimensions from the product-state
@@ -743,6 +777,8 @@ def main():
     ap.add_argument("--no-u1", action="store_true")
     ap.add_argument("--no-grad", action="store_true")
     ap.add_argument("--no-next", action="store_true")
+    ap.add_argument("--ed-heff", type=int, default=0, metavar="L",
+                    help="time the exact-diagonalisation operator of an L-site XXZ chain alone")
     ap.add_argument("--u1-heff", type=int, default=0, metavar="D",
                     help="only time the block-sparse H_eff*x of an L=64, Sz=0 centre bond "
                          "with bond dimension D (profiling case) and exit")
@@ -752,6 +788,8 @@ def main():
         return run_reference(args)
     if args.u1_heff:
         return u1_heff_case(args)
+    if args.ed_heff:
+        return ed_heff_case(args)
 
     import torch
     import finitemptools_gb300 as fm
