@@ -17,6 +17,7 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <cstring>
 
 #include "internal.h"
 
@@ -59,6 +60,34 @@ __global__ void conv_state(const double* __restrict__ x, int Dl, int Kp, int64_t
     const int a = (int)(t % Kp);
     const int64_t m = t / Kp;
     put<MODE>(hi, lo, a + dld * m, a < Dl ? x[a + (int64_t)Dl * m] : 0.0);
+  }
+}
+
+// conv_state for the identity layout (Dl == Kp == dld): four consecutive elements per
+// thread, 32-byte loads and 8-byte (BF16) / 16-byte (TF32) stores; x 16-byte aligned and
+// n4 = Kp*M/4 (Kp is a multiple of 8).  Same rounding per element as put().
+template <int MODE>
+__global__ void conv_state_vec(const double* __restrict__ x, int64_t n4, void* hi, void* lo) {
+  const double2* x2 = reinterpret_cast<const double2*>(x);
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n4;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const double2 p = x2[2 * t], q = x2[2 * t + 1];
+    if (MODE == M_BF16) {
+      const __nv_bfloat162 u = __floats2bfloat162_rn((float)p.x, (float)p.y);
+      const __nv_bfloat162 w = __floats2bfloat162_rn((float)q.x, (float)q.y);
+      uint2 o;
+      o.x = *reinterpret_cast<const uint32_t*>(&u);
+      o.y = *reinterpret_cast<const uint32_t*>(&w);
+      reinterpret_cast<uint2*>(hi)[t] = o;
+    } else {
+      const float4 hv = make_float4(tf32_rna((float)p.x), tf32_rna((float)p.y),
+                                    tf32_rna((float)q.x), tf32_rna((float)q.y));
+      reinterpret_cast<float4*>(hi)[t] = hv;
+      if (MODE == M_TF32X3)
+        reinterpret_cast<float4*>(lo)[t] =
+            make_float4(tf32_rna((float)(p.x - (double)hv.x)), tf32_rna((float)(p.y - (double)hv.y)),
+                        tf32_rna((float)(q.x - (double)hv.z)), tf32_rna((float)(q.y - (double)hv.w)));
+    }
   }
 }
 
@@ -135,29 +164,37 @@ __device__ __forceinline__ float4 load4(const uint2* p) {
                      __uint_as_float(u.y << 16), __uint_as_float(u.y & 0xffff0000u));
 }
 
-template <int MODE, typename V4>
+// The block coefficients travel as a by-value kernel parameter (constant bank): every
+// index below is a compile-time constant after unrolling, so each FFMA reads its
+// coefficient as a constant-bank operand instead of issuing a shared-memory load (with
+// ~13 nonzero blocks of 16 coefficients the loads, not DRAM, bounded the kernel).
+struct MidCoef {
+  float c[64][16];                                // [wi*8 + wo][q*4 + s]
+};
+
+template <int MODE, typename V4, int NW>
 __global__ void __launch_bounds__(256) mid_tc_p4(const V4* __restrict__ T1, int Dl, int Dr,
                                                  int Drp, int64_t K2, int nw_in, int nw_out,
-                                                 uint64_t mask, const float* __restrict__ cdev,
+                                                 uint64_t mask, const __grid_constant__ MidCoef cp,
                                                  void* hi, void* lo) {
-  __shared__ float c[64][16];                     // [wi*8 + wo][q*4 + s]
-  for (int i = threadIdx.x; i < 64 * 16; i += blockDim.x) c[i / 16][i % 16] = cdev[i];
-  __syncthreads();
+  const auto& c = cp.c;
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (int64_t)Dl * Dr) return;
   const int b = (int)(t % Dr), ap = (int)(t / Dr);
   const int64_t in_w = (int64_t)Dr * Dl;          // float4 stride between w planes
   const V4* ib = T1 + b + (int64_t)Dr * ap;
-  float4 v[8];
+  // NW (4, 6 or 8) bounds both MPO bonds at compile time: only NW input planes are held
+  // in registers (fewer registers per thread, more threads and loads in flight per SM)
+  float4 v[NW];
 #pragma unroll
-  for (int wi = 0; wi < 8; wi++)
+  for (int wi = 0; wi < NW; wi++)
     v[wi] = wi < nw_in ? load4(ib + in_w * wi) : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-  for (int wo = 0; wo < 8; wo++) {
+  for (int wo = 0; wo < NW; wo++) {
     if (wo >= nw_out) break;
     float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
 #pragma unroll
-    for (int wi = 0; wi < 8; wi++) {
+    for (int wi = 0; wi < NW; wi++) {
       if (!((mask >> (wi * 8 + wo)) & 1ull)) continue;
       const float* cc = c[wi * 8 + wo];
       a0 = fmaf(cc[0], v[wi].x, fmaf(cc[1], v[wi].y, fmaf(cc[2], v[wi].z, fmaf(cc[3], v[wi].w, a0))));
@@ -226,7 +263,7 @@ struct TcState {
   // fast MPO step (P = 4, w <= 8): block bitmask and dense float coefficients
   bool fast_mid = false;
   uint64_t mask = 0;
-  DevBuf cfast;
+  MidCoef cpar;             // block coefficients, passed to mid_tc_p4 by value
 };
 
 inline int round_up8(int v) { return (v + 7) / 8 * 8; }
@@ -348,10 +385,7 @@ int op_tc_prepare(fmpt_op* op) {
           mask |= 1ull << (wi * 8 + wo);
           for (int q = 0; q < 16; q++) cf[(wi * 8 + wo) * 16 + q] += (float)ms.coef[(size_t)e * 16 + q];
         }
-      FMPT_TRY(st->cfast.alloc(h, cf.size() * sizeof(float)));
-      FMPT_CUDA(h, cudaMemcpyAsync(st->cfast.p, cf.data(), cf.size() * sizeof(float),
-                                   cudaMemcpyHostToDevice, h->stream));
-      FMPT_CUDA(h, cudaStreamSynchronize(h->stream));
+      std::memcpy(st->cpar.c, cf.data(), sizeof(st->cpar.c));
       st->mask = mask;
       st->fast_mid = true;
     }
@@ -425,7 +459,16 @@ int op_tc_apply_head(fmpt_op* op, const double* x) {
   const int64_t nx = (int64_t)st->Kp * P * Dr;
   {
   ProfScope prof(h, FMPT_K_CONVERT);
-  if (st->mode == M_TF32)
+  const bool ident = st->Kp == Dl && (reinterpret_cast<uintptr_t>(x) & 15) == 0;
+  if (ident) {
+    const int64_t n4 = nx / 4;
+    if (st->mode == M_TF32)
+      conv_state_vec<M_TF32><<<grid1(h, n4), 256, 0, h->stream>>>(x, n4, st->xg[0].p, xlo);
+    else if (st->mode == M_TF32X3)
+      conv_state_vec<M_TF32X3><<<grid1(h, n4), 256, 0, h->stream>>>(x, n4, st->xg[0].p, xlo);
+    else
+      conv_state_vec<M_BF16><<<grid1(h, n4), 256, 0, h->stream>>>(x, n4, st->xg[0].p, xlo);
+  } else if (st->mode == M_TF32)
     conv_state<M_TF32><<<grid1(h, nx), 256, 0, h->stream>>>(x, Dl, st->Kp, (int64_t)P * Dr, st->xg[0].p, xlo, st->Kp);
   else if (st->mode == M_TF32X3)
     conv_state<M_TF32X3><<<grid1(h, nx), 256, 0, h->stream>>>(x, Dl, st->Kp, (int64_t)P * Dr, st->xg[0].p, xlo, st->Kp);
@@ -447,13 +490,22 @@ int op_tc_apply_head(fmpt_op* op, const double* x) {
     ProfScope prof(h, FMPT_K_MPO_STEP);
     if (st->fast_mid) {
       const float4* t1 = (const float4*)st->T1.p;
-      const float* cf = (const float*)st->cfast.p;
-      if (st->mode == M_TF32)
-        mid_tc_p4<M_TF32><<<blocks, 256, 0, h->stream>>>(t1, Dl, Dr, st->Drp, st->K2, s.nw_in, s.nw_out, st->mask, cf, st->T3[0].p, tlo);
-      else if (st->mode == M_TF32X3)
-        mid_tc_p4<M_TF32X3><<<blocks, 256, 0, h->stream>>>(t1, Dl, Dr, st->Drp, st->K2, s.nw_in, s.nw_out, st->mask, cf, st->T3[0].p, tlo);
-      else
-        mid_tc_p4<M_BF16><<<blocks, 256, 0, h->stream>>>((const uint2*)st->T1.p, Dl, Dr, st->Drp, st->K2, s.nw_in, s.nw_out, st->mask, cf, st->T3[0].p, tlo);
+      const int nw = std::max(s.nw_in, s.nw_out);
+#define MIDP4(NW_)                                                                                \
+  do {                                                                                            \
+    if (st->mode == M_TF32)                                                                       \
+      mid_tc_p4<M_TF32, float4, NW_><<<blocks, 256, 0, h->stream>>>(                              \
+          t1, Dl, Dr, st->Drp, st->K2, s.nw_in, s.nw_out, st->mask, st->cpar, st->T3[0].p, tlo); \
+    else if (st->mode == M_TF32X3)                                                                \
+      mid_tc_p4<M_TF32X3, float4, NW_><<<blocks, 256, 0, h->stream>>>(                            \
+          t1, Dl, Dr, st->Drp, st->K2, s.nw_in, s.nw_out, st->mask, st->cpar, st->T3[0].p, tlo); \
+    else                                                                                          \
+      mid_tc_p4<M_BF16, uint2, NW_><<<blocks, 256, 0, h->stream>>>(                               \
+          (const uint2*)st->T1.p, Dl, Dr, st->Drp, st->K2, s.nw_in, s.nw_out, st->mask, st->cpar, \
+          st->T3[0].p, tlo);                                                                      \
+  } while (0)
+      if (nw <= 4) MIDP4(4); else if (nw <= 6) MIDP4(6); else MIDP4(8);
+#undef MIDP4
     } else
 #define MIDTC(MODE_, MP_)                                                                    \
   mid_tc<MODE_, MP_><<<blocks, 256, 0, h->stream>>>((const float*)st->T1.p,                \
@@ -541,13 +593,12 @@ int op_tc_apply_complex(fmpt_op* op, TcState* st, const double* x, double* y) {
       void* hi = offset(st->T3[0].p, part * st->K2, es);
       void* lo = offset(tlo, part * st->K2, es);
       if (st->fast_mid) {
-        const float* cf = (const float*)st->cfast.p;
-        if (st->mode == M_TF32)
-          mid_tc_p4<M_TF32><<<blocks, 256, 0, h->stream>>>((const float4*)t1, Dl, Dr, st->Drp, K2c, s.nw_in, s.nw_out, st->mask, cf, hi, lo);
+          if (st->mode == M_TF32)
+          mid_tc_p4<M_TF32, float4, 8><<<blocks, 256, 0, h->stream>>>((const float4*)t1, Dl, Dr, st->Drp, K2c, s.nw_in, s.nw_out, st->mask, st->cpar, hi, lo);
         else if (st->mode == M_TF32X3)
-          mid_tc_p4<M_TF32X3><<<blocks, 256, 0, h->stream>>>((const float4*)t1, Dl, Dr, st->Drp, K2c, s.nw_in, s.nw_out, st->mask, cf, hi, lo);
+          mid_tc_p4<M_TF32X3, float4, 8><<<blocks, 256, 0, h->stream>>>((const float4*)t1, Dl, Dr, st->Drp, K2c, s.nw_in, s.nw_out, st->mask, st->cpar, hi, lo);
         else
-          mid_tc_p4<M_BF16><<<blocks, 256, 0, h->stream>>>((const float4*)t1, Dl, Dr, st->Drp, K2c, s.nw_in, s.nw_out, st->mask, cf, hi, lo);
+          mid_tc_p4<M_BF16, float4, 8><<<blocks, 256, 0, h->stream>>>((const float4*)t1, Dl, Dr, st->Drp, K2c, s.nw_in, s.nw_out, st->mask, st->cpar, hi, lo);
       } else {
 #define MIDTCC(MODE_, MP_)                                                                   \
   mid_tc<MODE_, MP_><<<blocks, 256, 0, h->stream>>>(t1, P, Dl, Dr, st->Drp, K2c, s.nw_out,    \
