@@ -217,12 +217,10 @@ template <int MODE, int P>
 __global__ void __launch_bounds__(256) mid_tc_mask(const float* __restrict__ T, int64_t i1,
                                                    int64_t i2, int64_t iw, int64_t is, int n1,
                                                    int n2, int nw_in, int nw_out, uint64_t mask,
-                                                   const float* __restrict__ cdev, void* hi,
+                                                   const __grid_constant__ MidCoef cp, void* hi,
                                                    void* lo, int64_t o1s, int64_t o2s,
                                                    int64_t ows, int64_t oqs) {
-  __shared__ float c[64][P * P];                  // [wi*8 + wo][q*P + s]
-  for (int i = threadIdx.x; i < 64 * P * P; i += blockDim.x) c[i / (P * P)][i % (P * P)] = cdev[i];
-  __syncthreads();
+  const auto& c = cp.c;                           // [wi*8 + wo][q*P + s], constant bank
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (int64_t)n1 * n2) return;
   const int o1 = (int)(t % n1), o2 = (int)(t / n1);
@@ -629,7 +627,7 @@ int op_tc_apply_complex(fmpt_op* op, TcState* st, const double* x, double* y) {
 //                hnew[a',(w,a)]   = sum_(s',b') At[(s',b'),a'] U[...]        (GEMM 2, FP64 out)
 namespace {
 
-int mask_and_coef(fmpt_handle* h, const MidSchedule& ms, int P, uint64_t* mask, DevBuf& cbuf) {
+int mask_and_coef(fmpt_handle* h, const MidSchedule& ms, int P, uint64_t* mask, MidCoef& cp) {
   if (ms.nw_in > 8 || ms.nw_out > 8 || (P != 2 && P != 4))
     return set_error(h, FMPT_ERR_UNSUPPORTED,
                      "mixed-precision environment update needs MPO bonds <= 8 and d = 2 or 4");
@@ -642,17 +640,16 @@ int mask_and_coef(fmpt_handle* h, const MidSchedule& ms, int P, uint64_t* mask, 
       for (int q = 0; q < P * P; q++)
         cf[(size_t)(wi * 8 + wo) * P * P + q] += (float)ms.coef[(size_t)e * P * P + q];
     }
-  FMPT_TRY(cbuf.alloc(h, cf.size() * sizeof(float)));
-  FMPT_CUDA(h, cudaMemcpyAsync(cbuf.p, cf.data(), cf.size() * sizeof(float),
-                               cudaMemcpyHostToDevice, h->stream));
-  FMPT_CUDA(h, cudaStreamSynchronize(h->stream));   // cf must outlive the copy
+  std::memset(&cp, 0, sizeof(cp));
+  for (int blk = 0; blk < 64; blk++)
+    for (int q = 0; q < P * P; q++) cp.c[blk][q] = cf[(size_t)blk * P * P + q];
   *mask = m;
   return FMPT_OK;
 }
 
 template <int MODE>
 int launch_mask(fmpt_handle* h, int P, const float* T, int64_t i1, int64_t i2, int64_t iw,
-                int64_t is, int n1, int n2, int nw_in, int nw_out, uint64_t mask, const float* c,
+                int64_t is, int n1, int n2, int nw_in, int nw_out, uint64_t mask, const MidCoef& c,
                 void* hi, void* lo, int64_t o1, int64_t o2, int64_t ow, int64_t oq) {
   const int64_t nt = (int64_t)n1 * n2;
   const unsigned blocks = (unsigned)((nt + 255) / 256);
@@ -705,8 +702,8 @@ int env_left_tc(fmpt_handle* h, int precision, const double* hold, const double*
   MidSchedule ms;
   FMPT_TRY(schedule_env(h, 0, W, d, wl, wr, false, ms));
   uint64_t mask = 0;
-  DevBuf cbuf;
-  int st = mask_and_coef(h, ms, d, &mask, cbuf);
+  MidCoef cpar;
+  int st = mask_and_coef(h, ms, d, &mask, cpar);
   mid_free(h, ms);
   FMPT_TRY(st);
   const int Kp = round_up8(Dl), K2 = round_up8(Dl * d);
@@ -731,7 +728,7 @@ int env_left_tc(fmpt_handle* h, int precision, const double* hold, const double*
   // out: U[(a' + Dl s') + K2 (w2 + wr b)]
   if (st == FMPT_OK) {
     const float* t1 = (const float*)T1.p;
-    const float* c = (const float*)cbuf.p;
+    const MidCoef& c = cpar;
     const int64_t i1 = d, i2 = (int64_t)d * Dr, iw = (int64_t)d * Dr * Dl, is = 1;
     const int64_t o1 = (int64_t)K2 * wr, o2 = 1, ow = K2, oq = Dl;
     if (mode == M_TF32)
@@ -763,8 +760,8 @@ int env_right_tc(fmpt_handle* h, int precision, const double* hold, const double
   MidSchedule ms;
   FMPT_TRY(schedule_env(h, 0, W, d, wl, wr, true, ms));
   uint64_t mask = 0;
-  DevBuf cbuf;
-  int st = mask_and_coef(h, ms, d, &mask, cbuf);
+  MidCoef cpar;
+  int st = mask_and_coef(h, ms, d, &mask, cpar);
   mid_free(h, ms);
   FMPT_TRY(st);
   const int Kb = round_up8(Dr), Kq = round_up8(d * Dr);
@@ -792,7 +789,7 @@ int env_right_tc(fmpt_handle* h, int precision, const double* hold, const double
   // out: U[(s' + d b') + Kq (w + wl a)]
   if (st == FMPT_OK) {
     const float* t1 = (const float*)T1.p;
-    const float* c = (const float*)cbuf.p;
+    const MidCoef& c = cpar;
     const int64_t i1 = 1, i2 = (int64_t)Dl * d, iw = (int64_t)Dl * d * Dr, is = Dl;
     const int64_t o1 = (int64_t)Kq * wl, o2 = d, ow = Kq, oq = 1;
     if (mode == M_TF32)
