@@ -51,6 +51,20 @@ def test_ac2_prime_mixed(prec, Dl, Dr):
     assert rel(y, ref) < tol(prec, Dl + 5 * Dr), rel(y, ref)
 
 
+@pytest.mark.parametrize("D", [2048, 1536])
+def test_ac2_prime_bf16_large_grids(D):
+    """The bench's size and a non-power-of-two one with several waves of GEMM tiles,
+    against the device FP64 form (the oracle pins FP64 at the smaller sizes above)."""
+    rng = np.random.default_rng(D)
+    W = heisenberg_xxz_mpo(1.0, 1.0, 0.0)[1].dense()
+    x = rng.standard_normal((D, 2, 2, D))
+    L, R = herm(rng, D, 5), herm(rng, D, 5)
+    args = (DT.from_numpy(x), W, W, DT.from_numpy(L), DT.from_numpy(R))
+    ref = fm.ac2_prime(*args, precision="fp64").numpy()
+    y = fm.ac2_prime(*args, precision="bf16").numpy()
+    assert rel(y, ref) < TOL["bf16"], rel(y, ref)
+
+
 @pytest.mark.parametrize("prec", ["tf32x3", "tf32", "bf16"])
 def test_ac2_prime_mixed_j1j2_and_boundary(prec):
     rng = np.random.default_rng(7)
