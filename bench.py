@@ -509,6 +509,31 @@ def u1_section(h, fm, budget_s=150.0):
     return out
 
 
+def cublas_same_shapes(D, stream, reps=10):
+    """cuBLAS (torch.matmul, bf16 operands, FP32 accumulation) on the two GEMM shapes of
+    the BF16 two-site H_eff*x at bond dimension D: GEMM 1 M = 4D, N = 5D, K = D and
+    GEMM 2 M = 4D, N = D, K = 5D (w=5, d=2), each timed with CUDA events after a
+    warm-up; a yardstick for the hand-written tcgen05 GEMM on the same problems."""
+    import torch
+    out = {}
+    for name, (M, N, K) in (("gemm1", (4 * D, W_MPO * D, D)), ("gemm2", (4 * D, D, W_MPO * D))):
+        a = torch.randn(M, K, device="cuda", dtype=torch.bfloat16)
+        b = torch.randn(K, N, device="cuda", dtype=torch.bfloat16)
+        for _ in range(3):
+            torch.matmul(a, b)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            torch.matmul(a, b)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        out[name] = {"M": M, "N": N, "K": K, "ms": ms, "tflops": 2.0 * M * N * K / (ms / 1e3) / 1e12}
+        del a, b
+    return out
+
+
 def next_rows_section(h, fm):
     """The paths beside the hot path, each timed once on synthetic inputs:
       ed_xxz_L20: exact_diagonalization of the XXZ chain L=20 (Delta=1) through the
@@ -880,6 +905,8 @@ def main():
                 "share_of_step": tc_ms / tot_ms if tot_ms else None,
                 "other_kernels_ms_per_step": {"mpo_step": mid_ms / args.steps,
                                               "convert": cv_ms / args.steps}}
+        if prec == "bf16" and rank == 0:
+            roof["cublas_same_shapes"] = cublas_same_shapes(D, stream)
 
     # ---- end to end through the C ABI with host buffers (pinned)
     e2e = None
