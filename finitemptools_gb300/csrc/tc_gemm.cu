@@ -402,10 +402,10 @@ int tc_gemm(fmpt_handle* h, int mode, int M, int N, int K, int batch, const TcOp
   using namespace tc;
   if (M <= 0 || N <= 0 || K <= 0 || batch <= 0) return FMPT_OK;
   CUtensorMap ma, mb, ma2, mb2;
-  // 256-wide N tiles for TF32/BF16.  A 128-wide BF16 tile fills the last wave of the
-  // D=2048 GEMM-2 grid better (1024 tiles instead of 512 on 152 SMs) but measured slower
-  // there (0.2745 vs 0.2455 ms per GEMM on average): its halved B-operand reuse costs more
-  // than the idle part of the last wave.
+  // 256-wide N tiles with 4 stages for TF32/BF16.  Measured on the D=2048 step (average
+  // per GEMM): 256 x 4 stages 0.2455 ms; 256 x 3 stages 0.2743 ms; 192 x 5 stages 0.2576 ms;
+  // 128 x 6 stages 0.2745 ms.  Pipeline depth matters, but not at the cost of the
+  // 256-wide MMA's operand reuse.
   const int BN = mode == TF32X3 ? 128 : 256;
   FMPT_TRY(make_map(h, &ma, A.hi, mode, K, M, A.ld, batch, A.bstride, BM));
   FMPT_TRY(make_map(h, &mb, B.hi, mode, K, N, B.ld, batch, B.bstride, BN));
