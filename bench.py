@@ -186,6 +186,29 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def cpu_dmrg_sweeps(mpo, e_ed, e_gpu, budget_s=40.0):
+    """The oracle's FP64 DMRG2 (numpy, the reference's algorithm step for step) on the
+    XXZ chain L=20: seeded D=8 start (the GPU run's seed), right-canonicalised, 4 sweeps
+    at D=64, cutoff 1e-10, Lanczos 30 vectors / tol 1e-12, on all host cores; stops early
+    past budget_s."""
+    import oracle as O
+    from finitemptools_gb300.utilities import FiniteMPO
+    rng = np.random.default_rng(20)
+    st, _ = O.canonicalize(O.randommps(20, 2, 8, rng), normalize=True)
+    env = O.environments(FiniteMPO(mpo, 20), st)
+    times, t_all = [], time.perf_counter()
+    for _ in range(4):
+        t0 = time.perf_counter()
+        Es, _ = O.dmrg2_sweep(env, O.MPSTruncation(64, 1e-10), 30, 1e-12)
+        times.append(time.perf_counter() - t0)
+        if time.perf_counter() - t_all > budget_s:
+            break
+    E = float(Es[-1])
+    return {"sweep_s": times, "E_last_bond": E, "dE_rel_vs_ed": abs(E - e_ed) / abs(e_ed),
+            "dE_rel_vs_gpu_fp64": abs(E - e_gpu) / abs(e_gpu), "threads": os.cpu_count(),
+            "note": "numpy/OpenBLAS with all host threads; E is the last Ritz value"}
+
+
 def dmrg_section(h, fm, budget_s=150.0):
     """DMRG sweep seconds, plain FP64 vs the mixed form (3xTF32 contractions and
     environment updates, FP64 Lanczos reorthogonalisation, FP64 density-matrix
@@ -232,6 +255,9 @@ def dmrg_section(h, fm, budget_s=150.0):
     out["xxz_L20_D64"] = {"sweep_s_fp64": t64, "sweep_s_mixed": tmx, "E_fp64": E64,
                           "E_mixed_fp64_eval": Emx, "dE_rel_mixed_vs_fp64": abs(Emx - E64) / abs(E64),
                           "E_ed": e_ed, "dE_rel_fp64_vs_ed": abs(E64 - e_ed) / abs(e_ed)}
+    # the same 4 FP64 sweeps (same seed, start and truncation) by the oracle's DMRG2 on the
+    # host cores: the CPU run this workload is checked against
+    out["xxz_L20_D64"]["cpu_reference"] = cpu_dmrg_sweeps(hx, e_ed, E64)
     # DMRG1S with OptimalExpansion (the reference's default ground-state algorithm), same
     # chain, start and truncation as the FP64 DMRG2 run above, with the reference's
     # expansion and with the capped one
