@@ -53,6 +53,21 @@ ProfScope::~ProfScope() {
   h->prof_ev[cls].push_back({b, e});
 }
 
+int grow_buffer(fmpt_handle* h, void** buf, size_t* cap, size_t bytes) {
+  if (*cap >= bytes && *buf) return FMPT_OK;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(h->stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
+    cudaGetLastError();
+    return set_error(h, FMPT_ERR_UNSUPPORTED, "buffer growth during stream capture");
+  }
+  if (*buf) cudaFreeAsync(*buf, h->stream);
+  *buf = nullptr;
+  *cap = 0;
+  FMPT_CUDA(h, cudaMallocAsync(buf, bytes, h->stream));
+  *cap = bytes;
+  return FMPT_OK;
+}
+
 int ensure_pinned(fmpt_handle* h, size_t n) {
   if (h->pinned_len >= n) return FMPT_OK;
   if (h->pinned) {
@@ -330,6 +345,8 @@ int fmpt_destroy(fmpt_handle* h) {
   for (auto st : h->aux_stream) cudaStreamDestroy(st);
   for (auto ev : h->aux_event) cudaEventDestroy(ev);
   if (h->lanczos_exec) cudaGraphExecDestroy(h->lanczos_exec);
+  for (auto& kv : h->arnoldi_exec) cudaGraphExecDestroy(kv.second);
+  if (h->gemm_ws) cudaFree(h->gemm_ws);
   if (h->gstatus) cudaFree(h->gstatus);
   if (h->pinned) cudaFreeHost(h->pinned);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);

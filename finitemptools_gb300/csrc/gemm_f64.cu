@@ -205,19 +205,23 @@ int launch(fmpt_handle* h, const GemmArgs& g) {
   if (grid.y > 65535 || grid.z > 65535)
     return set_error(h, FMPT_ERR_SHAPE, "gemm: grid too large (%d x %d x %d)", grid.x, grid.y,
                      grid.z);
-  DevBuf ws;
-  if (splits > 1)
-    FMPT_TRY(ws.alloc(h, (size_t)splits * g.m * g.n * sizeof(double) * (CPLX ? 2 : 1)));
+  // the split partials live in the handle's workspace (reused in stream order)
+  double* ws = nullptr;
+  if (splits > 1) {
+    FMPT_TRY(grow_buffer(h, &h->gemm_ws, &h->gemm_ws_bytes,
+                         (size_t)splits * g.m * g.n * sizeof(double) * (CPLX ? 2 : 1)));
+    ws = static_cast<double*>(h->gemm_ws);
+  }
   ProfScope prof(h, FMPT_K_F64_GEMM);
   if (bmn == 64)
-    gemm_kernel<CPLX, 64><<<grid, NT, 0, h->stream>>>(g, splits, kchunk, ws.d());
+    gemm_kernel<CPLX, 64><<<grid, NT, 0, h->stream>>>(g, splits, kchunk, ws);
   else
-    gemm_kernel<CPLX, 32><<<grid, NT, 0, h->stream>>>(g, splits, kchunk, ws.d());
+    gemm_kernel<CPLX, 32><<<grid, NT, 0, h->stream>>>(g, splits, kchunk, ws);
   FMPT_LAUNCHED(h);
   if (splits > 1) {
     const int64_t mn = (int64_t)g.m * g.n;
     const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((mn + 255) / 256, 4LL * sms));
-    split_reduce<CPLX><<<blocks, 256, 0, h->stream>>>(g, splits, ws.d());
+    split_reduce<CPLX><<<blocks, 256, 0, h->stream>>>(g, splits, ws);
     FMPT_LAUNCHED(h);
   }
   return FMPT_OK;

@@ -238,15 +238,17 @@ int op_apply_fp64(fmpt_op* op, const double* x, double* y) {
   fmpt_handle* h = op->h;
   const int cp = op->dtype == FMPT_C128;
   const int Dl = op->Dl, Dr = op->Dr;
+  const size_t es = sizeof(double) * (cp ? 2 : 1);
   if (op->kind == 2) {  // c_prime: y = sum_w L_w C R_w^T
     const int w = op->wl;
     int64_t nT = (int64_t)Dl * w * Dr;
-    DevBuf T;
-    FMPT_TRY(T.alloc(h, nT * sizeof(double) * (cp ? 2 : 1)));
+    FMPT_TRY(grow_buffer(h, reinterpret_cast<void**>(&op->scratch), &op->scratch_bytes,
+                         (size_t)nT * es));
+    double* Td = op->scratch;
     FMPT_TRY(gemm_f64(h, gemm_args(cp, FMPT_N, FMPT_N, Dl * w, Dr, Dl, op->hleft, (int64_t)Dl * w,
-                                   (int64_t)Dl * w * Dl, x, Dl, (int64_t)Dl * Dr, T.d(),
+                                   (int64_t)Dl * w * Dl, x, Dl, (int64_t)Dl * Dr, Td,
                                    (int64_t)Dl * w, nT)));
-    FMPT_TRY(gemm_f64(h, gemm_args(cp, FMPT_N, FMPT_T, Dl, Dr, w * Dr, T.d(), Dl, nT,
+    FMPT_TRY(gemm_f64(h, gemm_args(cp, FMPT_N, FMPT_T, Dl, Dr, w * Dr, Td, Dl, nT,
                                    op->hright, Dr, (int64_t)Dr * w * Dr, y, Dl,
                                    (int64_t)Dl * Dr)));
     return FMPT_OK;
@@ -255,19 +257,21 @@ int op_apply_fp64(fmpt_op* op, const double* x, double* y) {
   const int wl = op->wl, wr = op->wr;
   const int64_t nx = (int64_t)Dl * P * Dr;
   const int64_t n1 = (int64_t)Dl * wl * P * Dr, n3 = (int64_t)Dl * P * wr * Dr;
-  DevBuf T1, T3;
-  FMPT_TRY(T1.alloc(h, n1 * sizeof(double) * (cp ? 2 : 1)));
-  FMPT_TRY(T3.alloc(h, n3 * sizeof(double) * (cp ? 2 : 1)));
+  // T1 and T3 in the operator's scratch (one buffer, T3 after T1)
+  FMPT_TRY(grow_buffer(h, reinterpret_cast<void**>(&op->scratch), &op->scratch_bytes,
+                       (size_t)(n1 + n3) * es));
+  double* T1 = op->scratch;
+  double* T3 = op->scratch + n1 * (cp ? 2 : 1);
   // 1. T1[(a' w), (s b)] = L[(a' w), a] x[a, (s b)]
   FMPT_TRY(gemm_f64(h, gemm_args(cp, FMPT_N, FMPT_N, Dl * wl, P * Dr, Dl, op->hleft,
-                                 (int64_t)Dl * wl, (int64_t)Dl * wl * Dl, x, Dl, nx, T1.d(),
+                                 (int64_t)Dl * wl, (int64_t)Dl * wl * Dl, x, Dl, nx, T1,
                                  (int64_t)Dl * wl, n1)));
   // 2. T3[a', s', w2, b] = sum_blocks O[s', s] T1[a', w, s, b]
   MidStrides si{1, (int64_t)Dl * wl * P, Dl, (int64_t)Dl * wl};
   MidStrides so{1, (int64_t)Dl * P * wr, (int64_t)Dl * P, Dl};
-  FMPT_TRY(mid_apply(h, op->sched, T1.d(), n1, si, T3.d(), n3, so, Dl, Dr));
+  FMPT_TRY(mid_apply(h, op->sched, T1, n1, si, T3, n3, so, Dl, Dr));
   // 3. y[(a' s'), b'] = T3[(a' s'), (w2 b)] R[b', (w2 b)]^T
-  FMPT_TRY(gemm_f64(h, gemm_args(cp, FMPT_N, FMPT_T, Dl * P, Dr, wr * Dr, T3.d(),
+  FMPT_TRY(gemm_f64(h, gemm_args(cp, FMPT_N, FMPT_T, Dl * P, Dr, wr * Dr, T3,
                                  (int64_t)Dl * P, n3, op->hright, Dr, (int64_t)Dr * wr * Dr, y,
                                  (int64_t)Dl * P, nx)));
   return FMPT_OK;
@@ -360,6 +364,7 @@ int fmpt_op_destroy(fmpt_op* op) {
   op_tc_free(op);
   op_u1_free(op);
   if (op->proj_part) cudaFreeAsync(op->proj_part, op->h->stream);
+  if (op->scratch) cudaFreeAsync(op->scratch, op->h->stream);
   delete op;
   return FMPT_OK;
 }

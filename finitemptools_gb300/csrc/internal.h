@@ -38,6 +38,12 @@ struct fmpt_handle {
   // CUDA graphs for the Krylov solvers of block-sparse operators (fmpt_set_graphs)
   bool graphs = true;
   int svd_method = 0;          // 0 gesvd (bidiagonalisation), 1 gesvdp (polar decomposition)
+  // split-K workspace of the FP64 GEMM, grown outside stream capture only (stream-ordered
+  // reuse on h->stream)
+  void* gemm_ws = nullptr;
+  size_t gemm_ws_bytes = 0;
+  // executable graphs of the captured Arnoldi basis, one per operator structure
+  std::map<std::string, cudaGraphExec_t> arnoldi_exec;
   cudaGraphExec_t lanczos_exec = nullptr;   // reused through cudaGraphExecUpdate
   uint64_t graph_launches = 0;
   // grouped-kernel tile autotuner (fmpt_set_tuning): 0 measure, 1 force the
@@ -91,6 +97,9 @@ struct DevBuf {
 };
 
 int ensure_pinned(fmpt_handle* h, size_t n_doubles);
+// a device buffer of at least `bytes` held in *buf / *cap (stream-ordered on h->stream);
+// growing it while h->stream is being captured returns FMPT_ERR_UNSUPPORTED
+int grow_buffer(fmpt_handle* h, void** buf, size_t* cap, size_t bytes);
 // At least n auxiliary streams/solvers; aux_fork makes them wait for the work
 // queued so far on h->stream, aux_join makes h->stream wait for them.
 int ensure_aux(fmpt_handle* h, int n);
@@ -235,6 +244,9 @@ struct fmpt_op {
   void* tc = nullptr;     // tensor-core state (mixed precision), owned
   void* u1 = nullptr;     // U(1) block-sparse state (grouped program + scratch), owned
   bool defer_right = false;  // mixed precision: the right environment is converted later
+  // FP64 intermediates of one application (T1/T3 or T), grown outside stream capture only
+  double* scratch = nullptr;
+  size_t scratch_bytes = 0;
   // projectors of the excited-state sweeps: after every application
   // y -= dot(y, p) p for each p in order (device vectors of n elements, not owned)
   std::vector<const double*> proj;

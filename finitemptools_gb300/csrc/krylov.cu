@@ -103,50 +103,79 @@ __global__ void lanczos_scale(int64_t n, double* __restrict__ y, const double* _
 
 // ---- multi-vector kernels over the Krylov basis V (j vectors of length n,
 // complex split planes when cplx: V_i re at V + i*2n, im at V + i*2n + n)
-// partial dots h_i = <V_i, z> ; part layout [G][j][2]
+// partial dots h_i = <V_i, z> ; part layout [G][j][2].  Chunks of MD_CH vectors per pass
+// over z: every thread keeps MD_CH running sums (re, im), reduced by warp shuffles and one
+// shared-memory pass per chunk -- instead of one full block reduction per vector.  Fixed
+// summation order throughout (deterministic).
+constexpr int MD_CH = 8;
 __global__ void multidot_partial(int cplx, int64_t n, int j, const double* __restrict__ V,
                                  int64_t vstride, const double* __restrict__ z,
                                  double* __restrict__ part, const int* gate = nullptr) {
   if (gate && *gate) return;
-  for (int i = 0; i < j; i++) {
-    const double* v = V + (int64_t)i * vstride;
-    double sr = 0.0, si = 0.0;
+  __shared__ double red[KT / 32][2 * MD_CH];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int i0 = 0; i0 < j; i0 += MD_CH) {
+    double sr[MD_CH], si[MD_CH];
+#pragma unroll
+    for (int c = 0; c < MD_CH; c++) {
+      sr[c] = 0.0;
+      si[c] = 0.0;
+    }
     for (int64_t e = (int64_t)blockIdx.x * KT + threadIdx.x; e < n; e += (int64_t)gridDim.x * KT) {
-      double vr = v[e], zr = z[e];
-      sr = fma(vr, zr, sr);
-      if (cplx) {
-        double vi = v[n + e], zi = z[n + e];
-        sr = fma(vi, zi, sr);
-        si = fma(vr, zi, si);
-        si = fma(-vi, zr, si);
+      const double zr = z[e], zi = cplx ? z[n + e] : 0.0;
+#pragma unroll
+      for (int c = 0; c < MD_CH; c++) {
+        if (i0 + c < j) {
+          const double* v = V + (int64_t)(i0 + c) * vstride;
+          const double vr = v[e];
+          sr[c] = fma(vr, zr, sr[c]);
+          if (cplx) {
+            const double vi = v[n + e];
+            sr[c] = fma(vi, zi, sr[c]);
+            si[c] = fma(vr, zi, si[c]);
+            si[c] = fma(-vi, zr, si[c]);
+          }
+        }
       }
     }
-    sr = block_sum(sr);
-    if (cplx) si = block_sum(si);
-    if (threadIdx.x == 0) {
-      part[((int64_t)blockIdx.x * j + i) * 2] = sr;
-      part[((int64_t)blockIdx.x * j + i) * 2 + 1] = si;
+#pragma unroll
+    for (int c = 0; c < MD_CH; c++) {
+      sr[c] = warp_sum(sr[c]);
+      si[c] = warp_sum(si[c]);
     }
+    if (lane == 0) {
+#pragma unroll
+      for (int c = 0; c < MD_CH; c++) {
+        red[wid][2 * c] = sr[c];
+        red[wid][2 * c + 1] = si[c];
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x < 2 * MD_CH) {
+      const int c = threadIdx.x >> 1;
+      double t = 0.0;
+      for (int w = 0; w < KT / 32; w++) t += red[w][threadIdx.x];
+      if (i0 + c < j) part[((int64_t)blockIdx.x * j + i0 + c) * 2 + (threadIdx.x & 1)] = t;
+    }
+    __syncthreads();
   }
 }
 
-// coef[i] (re, im) = sum over G partials; written by one block
+// coef[i] (re, im) = sum over the G partials, one warp per value (lanes stride over the
+// partials in a fixed order, then a shuffle sum); launched with one block of KT threads
 __global__ void multidot_finalize(int j, int G, const double* __restrict__ part,
                                   double* __restrict__ coef, double* __restrict__ accum,
                                   const int* gate = nullptr) {
   if (gate && *gate) return;
-  for (int i = 0; i < j; i++) {
-    double sr = 0.0, si = 0.0;
-    for (int g = threadIdx.x; g < G; g += KT) {
-      sr += part[((int64_t)g * j + i) * 2];
-      si += part[((int64_t)g * j + i) * 2 + 1];
-    }
-    sr = block_sum(sr);
-    si = block_sum(si);
-    if (threadIdx.x == 0) {
-      coef[2 * i] = sr;
-      coef[2 * i + 1] = si;
-      if (accum) { accum[2 * i] += sr; accum[2 * i + 1] += si; }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  for (int t = wid; t < 2 * j; t += nwarp) {
+    const int i = t >> 1, comp = t & 1;
+    double s = 0.0;
+    for (int g = lane; g < G; g += 32) s += part[((int64_t)g * j + i) * 2 + comp];
+    s = warp_sum(s);
+    if (lane == 0) {
+      coef[t] = s;
+      if (accum) accum[t] += s;
     }
   }
 }
@@ -815,6 +844,83 @@ int op_project(fmpt_op* op, double* y, const int* gate) {
   return FMPT_OK;
 }
 
+// The Arnoldi basis V_1..V_M of fmpt_exponentiate / fmpt_expm_nodes (two-pass classical
+// Gram-Schmidt; the columns of H into Hdev), device launches only.  With graphs enabled the
+// launches are captured into one CUDA graph per operator structure and replayed: the
+// executable graph is updated in place (cudaGraphExecUpdate) for the next operator of the
+// same structure, so the host issues one launch per basis instead of about a dozen per
+// vector.  Any capture, instantiation, update or launch failure -- the first call on a
+// fresh operator among them, whose scratch is sized outside capture -- runs the same
+// launches directly.
+int arnoldi_basis(fmpt_op* op, int cp, int64_t n, int64_t nr, int G, int M, int ldh, double* V,
+                  double* z, double* part, double* partM, double* coef, DevBuf& Hdev) {
+  fmpt_handle* h = op->h;
+  cudaStream_t st = h->stream;
+  auto record = [&]() -> int {
+    FMPT_CUDA(h, cudaMemsetAsync(Hdev.p, 0, Hdev.bytes, st));
+    for (int j = 0; j < M; j++) {
+      double* Hcol = Hdev.d() + (size_t)2 * ldh * j;
+      double* vj = V + (int64_t)j * nr;
+      FMPT_TRY(fmpt_op_apply(op, vj, z));
+      for (int pass = 0; pass < 2; pass++) {
+        multidot_partial<<<G, KT, 0, st>>>(cp, n, j + 1, V, nr, z, partM);
+        FMPT_LAUNCHED(h);
+        multidot_finalize<<<1, KT, 0, st>>>(j + 1, G, partM, coef, Hcol);
+        FMPT_LAUNCHED(h);
+        multi_axpy_sub<<<G, KT, 0, st>>>(cp, n, j + 1, V, nr, coef, z, part);
+        FMPT_LAUNCHED(h);
+      }
+      arnoldi_normalize<<<G, KT, 0, st>>>(nr, z, part, G, Hcol, j, vj + nr);
+      FMPT_LAUNCHED(h);
+    }
+    return FMPT_OK;
+  };
+  cudaStreamCaptureStatus cap0 = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cap0) != cudaSuccess) {
+    cudaGetLastError();
+    return record();
+  }
+  if (!h->graphs || cap0 != cudaStreamCaptureStatusNone) return record();
+  if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaGetLastError();
+    return record();
+  }
+  const int rs = record();
+  cudaGraph_t graph = nullptr;
+  const cudaError_t ce = cudaStreamEndCapture(st, &graph);
+  if (rs != FMPT_OK || ce != cudaSuccess || !graph) {
+    if (graph) cudaGraphDestroy(graph);
+    cudaGetLastError();
+    return record();
+  }
+  char key[96];
+  std::snprintf(key, sizeof(key), "k%d p%d c%d u%d q%zu M%d", op->kind, op->precision, cp,
+                op->u1 ? 1 : 0, op->proj.size(), M);
+  cudaGraphExec_t& ex = h->arnoldi_exec[key];
+  bool ready = false;
+  if (ex) {
+    cudaGraphExecUpdateResultInfo ri;
+    if (cudaGraphExecUpdate(ex, graph, &ri) == cudaSuccess) {
+      ready = true;
+    } else {
+      cudaGetLastError();
+      cudaGraphExecDestroy(ex);
+      ex = nullptr;
+    }
+  }
+  if (!ready && cudaGraphInstantiate(&ex, graph, 0) != cudaSuccess) {
+    cudaGetLastError();
+    ex = nullptr;
+  }
+  cudaGraphDestroy(graph);
+  if (!ex || cudaGraphLaunch(ex, st) != cudaSuccess) {
+    cudaGetLastError();
+    return record();
+  }
+  h->graph_launches++;
+  return FMPT_OK;
+}
+
 }  // namespace fmpt
 
 using namespace fmpt;
@@ -1024,21 +1130,8 @@ int fmpt_exponentiate(fmpt_op* op, double t_re, double t_im, const double* x, do
   while (tau_done < tabs * (1.0 - 1e-15)) {
     if (++steps > 1000) return set_error(h, FMPT_ERR_NOCONV, "exponentiate: too many steps");
     // ---- Arnoldi (two-pass classical Gram-Schmidt) entirely on the device
-    FMPT_CUDA(h, cudaMemsetAsync(Hdev.p, 0, Hdev.bytes, h->stream));
-    for (int j = 0; j < M; j++) {
-      double* Hcol = Hdev.d() + (size_t)2 * ldh * j;
-      FMPT_TRY(fmpt_op_apply(op, V_(j), zb.d()));
-      for (int pass = 0; pass < 2; pass++) {
-        multidot_partial<<<G, KT, 0, h->stream>>>(cp, n, j + 1, V, nr, zb.d(), partM.d());
-        FMPT_LAUNCHED(h);
-        multidot_finalize<<<1, KT, 0, h->stream>>>(j + 1, G, partM.d(), coef.d(), Hcol);
-        FMPT_LAUNCHED(h);
-        multi_axpy_sub<<<G, KT, 0, h->stream>>>(cp, n, j + 1, V, nr, coef.d(), zb.d(), part.d());
-        FMPT_LAUNCHED(h);
-      }
-      arnoldi_normalize<<<G, KT, 0, h->stream>>>(nr, zb.d(), part.d(), G, Hcol, j, V_(j + 1));
-      FMPT_LAUNCHED(h);
-    }
+    FMPT_TRY(arnoldi_basis(op, cp, n, nr, G, M, ldh, V, zb.d(), part.d(), partM.d(), coef.d(),
+                           Hdev));
     FMPT_CUDA(h, cudaMemcpyAsync(h->pinned, Hdev.p, Hdev.bytes, cudaMemcpyDeviceToHost,
                                  h->stream));
     FMPT_CUDA(h, cudaStreamSynchronize(h->stream));
@@ -1135,21 +1228,8 @@ int fmpt_expm_nodes(fmpt_op* op, double t_re, double t_im, const double* x, int 
   FMPT_LAUNCHED(h);
   normalize_from_parts<<<G, KT, 0, h->stream>>>(nr, x, V_(0), part.d(), G, acc.d());
   FMPT_LAUNCHED(h);
-  FMPT_CUDA(h, cudaMemsetAsync(Hdev.p, 0, Hdev.bytes, h->stream));
-  for (int j = 0; j < M; j++) {
-    double* Hcol = Hdev.d() + (size_t)2 * ldh * j;
-    FMPT_TRY(fmpt_op_apply(op, V_(j), zb.d()));
-    for (int pass = 0; pass < 2; pass++) {
-      multidot_partial<<<G, KT, 0, h->stream>>>(cp, n, j + 1, V, nr, zb.d(), partM.d());
-      FMPT_LAUNCHED(h);
-      multidot_finalize<<<1, KT, 0, h->stream>>>(j + 1, G, partM.d(), coef.d(), Hcol);
-      FMPT_LAUNCHED(h);
-      multi_axpy_sub<<<G, KT, 0, h->stream>>>(cp, n, j + 1, V, nr, coef.d(), zb.d(), part.d());
-      FMPT_LAUNCHED(h);
-    }
-    arnoldi_normalize<<<G, KT, 0, h->stream>>>(nr, zb.d(), part.d(), G, Hcol, j, V_(j + 1));
-    FMPT_LAUNCHED(h);
-  }
+  FMPT_TRY(arnoldi_basis(op, cp, n, nr, G, M, ldh, V, zb.d(), part.d(), partM.d(), coef.d(),
+                         Hdev));
   std::vector<double> Hh((size_t)ldh * M * 2);
   FMPT_CUDA(h, cudaMemcpyAsync(h->pinned, Hdev.p, Hdev.bytes, cudaMemcpyDeviceToHost, h->stream));
   FMPT_CUDA(h, cudaStreamSynchronize(h->stream));
