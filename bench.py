@@ -40,6 +40,12 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "DMRG sweep s & H_eff·x TFLOP/s, mixed vs FP64 on one GB300 at ΔE≤1e-8"
+# DRAM bytes (read + write) per tc_gemm launch from one ncu capture of this workload
+# (dram__bytes_read.sum + dram__bytes_write.sum, the average over GEMM 1 and GEMM 2 of one
+# step; profiles/ac2_bf16_D2048_dram.md gives the command and the per-kernel split)
+NCU_TRAFFIC = {("bf16", 2048): {"bytes_per_launch": (76.94e6 + 132.16e6 + 333.65e6 + 105.42e6) / 2,
+                                "gemm1_bytes": 76.94e6 + 132.16e6, "gemm2_bytes": 333.65e6 + 105.42e6,
+                                "algorithmic_operand_bytes": {"gemm1": 76.0e6, "gemm2": 210.0e6}}}
 UNIT = "TFLOP/s"
 W_MPO, D_PHYS = 5, 2
 
@@ -927,7 +933,8 @@ def main():
         roof = {"bound": "tensor", "kernel": "tc_gemm (tcgen05 %s)" % prec,
                 "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": achieved / peak if peak else None, "peak_source": peak_note,
-                "traffic": None, "launches": tc_n, "avg_launch_ms": tc_ms / tc_n,
+                "traffic": NCU_TRAFFIC.get((prec, D)), "launches": tc_n,
+                "avg_launch_ms": tc_ms / tc_n,
                 "share_of_step": tc_ms / tot_ms if tot_ms else None,
                 "other_kernels_ms_per_step": {"mpo_step": mid_ms / args.steps,
                                               "convert": cv_ms / args.steps}}
