@@ -41,8 +41,8 @@ sys.path.insert(0, ROOT)
 
 METRIC = "DMRG sweep s & H_eff·x TFLOP/s, mixed vs FP64 on one GB300 at ΔE≤1e-8"
 # DRAM bytes (read + write) per tc_gemm launch from one ncu capture of this workload
-# (dram__bytes_read.sum + dram__bytes_write.sum, the average over GEMM 1 and GEMM 2 of one
-# step; profiles/ac2_bf16_D2048_dram.md gives the command and the per-kernel split)
+# (dram__bytes_read.sum + dram__bytes_write.sum of the third step of
+# `bench.py --steps 2 --warmup 3`, averaged over its GEMM 1 and GEMM 2)
 NCU_TRAFFIC = {("bf16", 2048): {"bytes_per_launch": (76.94e6 + 132.16e6 + 333.65e6 + 105.42e6) / 2,
                                 "gemm1_bytes": 76.94e6 + 132.16e6, "gemm2_bytes": 333.65e6 + 105.42e6,
                                 "algorithmic_operand_bytes": {"gemm1": 76.0e6, "gemm2": 210.0e6}}}
