@@ -393,7 +393,12 @@ int fmpt_synchronize(fmpt_handle* h) {
 
 int fmpt_set_stream(fmpt_handle* h, void* s) {
   if (!h) return FMPT_ERR_ARG;
-  h->stream = s ? (cudaStream_t)s : h->own_stream;
+  // the handle's workspaces (GEMM split-K buffer, operator scratch, pinned staging) are
+  // reused in stream order: work queued on the old stream must finish before the new
+  // stream may touch them
+  const cudaStream_t ns = s ? (cudaStream_t)s : h->own_stream;
+  if (ns != h->stream) FMPT_CUDA(h, cudaStreamSynchronize(h->stream));
+  h->stream = ns;
   cusolverDnSetStream(h->solver, h->stream);
   return FMPT_OK;
 }
