@@ -88,6 +88,7 @@ SIGNATURES = {
     "fmpt_op_destroy": (c_int, [c_void_p]),
     "fmpt_op_set_projectors": (c_int, [c_void_p, c_int, P(c_void_p)]),
     "fmpt_set_svd_method": (c_int, [c_void_p, c_int]),
+    "fmpt_set_tc_tile": (c_int, [c_void_p, c_int]),
     "fmpt_ac2_prime_host": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p,
                                     c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_int,
                                     c_int, c_int, c_int]),

@@ -379,6 +379,13 @@ int fmpt_set_svd_method(fmpt_handle* h, int method) {
   return FMPT_OK;
 }
 
+int fmpt_set_tc_tile(fmpt_handle* h, int mode) {
+  if (!h) return FMPT_ERR_ARG;
+  if (mode < 0 || mode > 1) return set_error(h, FMPT_ERR_ARG, "tc tile mode must be 0 or 1");
+  h->tc_tile = mode;
+  return FMPT_OK;
+}
+
 int fmpt_set_graphs(fmpt_handle* h, int on) {
   if (!h) return FMPT_ERR_ARG;
   h->graphs = on != 0;

@@ -175,6 +175,33 @@ __device__ __forceinline__ void tile_coords(int tile, int tiles_m, int tiles_n, 
   }
 }
 
+// One thread's accumulator row (TMEM lane) of a 128 x BN tile -> C[row, n0 .. n0+BN)
+template <int BN, int OUT>
+__device__ __forceinline__ void store_acc(uint32_t tbase, int row, int n0, int z,
+                                          const EpiArgs& ep) {
+#pragma unroll 1
+  for (int c0 = 0; c0 < BN; c0 += 16) {
+    uint32_t r[16];
+    tmem_ld16(tbase + c0, r);
+    if (row < ep.M) {
+#pragma unroll
+      for (int j = 0; j < 16; j++) {
+        const int n = n0 + c0 + j;
+        if (n < ep.N) {
+          const int64_t idx = (int64_t)row + ep.ldc * n + ep.strideC * z;
+          const float v = __uint_as_float(r[j]);
+          if (OUT == 1)
+            static_cast<double*>(ep.C)[idx] = (double)v;
+          else if (OUT == 2)
+            static_cast<__nv_bfloat16*>(ep.C)[idx] = __float2bfloat16_rn(v);
+          else
+            static_cast<float*>(ep.C)[idx] = v;
+        }
+      }
+    }
+  }
+}
+
 template <int MODE, int BN, int STAGES, int OUT>
 struct Cfg {
   static constexpr int KBYTES = 128;                            // bytes of K per stage row
@@ -325,29 +352,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       int mt, nt, z;
       tile_coords(tile, tiles_m, tiles_n, ep.nfast, mt, nt, z);
       const int row = mt * BM + 32 * q + lane;
-      const int n0 = nt * BN;
-      const uint32_t tbase = tmem + buf * C_::TMEM_COLS + ((uint32_t)(32 * q) << 16);
-#pragma unroll 1
-      for (int c0 = 0; c0 < BN; c0 += 16) {
-        uint32_t r[16];
-        tmem_ld16(tbase + c0, r);
-        if (row < ep.M) {
-#pragma unroll
-          for (int j = 0; j < 16; j++) {
-            const int n = n0 + c0 + j;
-            if (n < ep.N) {
-              const int64_t idx = (int64_t)row + ep.ldc * n + ep.strideC * z;
-              const float v = __uint_as_float(r[j]);
-              if (OUT == 1)
-                static_cast<double*>(ep.C)[idx] = (double)v;
-              else if (OUT == 2)
-                static_cast<__nv_bfloat16*>(ep.C)[idx] = __float2bfloat16_rn(v);
-              else
-                static_cast<float*>(ep.C)[idx] = v;
-            }
-          }
-        }
-      }
+      store_acc<BN, OUT>(tmem + buf * C_::TMEM_COLS + ((uint32_t)(32 * q) << 16), row, nt * BN,
+                         z, ep);
       // the accumulator buffer may be refilled once all four warps have read it
       tc_fence_before();
       __syncwarp();
@@ -370,6 +376,254 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     }
     __syncwarp();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(2 * C_::TMEM_COLS)
+                 : "memory");
+  }
+}
+
+// ------------------------------------------------- CTA-pair kernel (cta_group::2)
+// A cluster of two CTAs owns a 256 x 256 output tile.  CTA r (cluster rank r) holds A rows
+// m0 + 128 r and B rows n0 + 128 r of each K-slice in its own shared memory; the even CTA
+// issues tcgen05.mma.cta_group::2 (M = 256, N = 256), which reads both CTAs' operands and
+// writes CTA r's 128 output rows into CTA r's TMEM.  Per SM and K-slice of 64 BF16 the
+// TMA brings 32 KB (48 KB for a one-CTA 128 x 256 tile) and per K=16 step the MMA reads
+// 8 KB of shared memory (12 KB): the one-CTA tile asks the shared memory for about 1.5x
+// the bandwidth the tensor core's rate leaves it, the pair stays within it, and the
+// 32 KB stage leaves room for 6 stages.
+//
+// Barriers: full[s] lives in the even CTA; its producer arms it with both CTAs' bytes and
+// both CTAs' loads (.cta_group::2) complete on it.  empty[s] and acc_full[b] live in both
+// CTAs and take the even CTA's multicast commits.  acc_empty[b] lives in the even CTA and
+// counts the pair's 8 epilogue warps.
+template <int MODE, int STAGES>
+struct PairCfg {
+  static constexpr int BN = 256;
+  static constexpr int KELEMS = MODE == BF16 ? 64 : 32;
+  static constexpr int A_BYTES = BM * 128;          // this CTA's 128 A rows x 128 B of K
+  static constexpr int B_BYTES = 128 * 128;         // this CTA's 128 B rows
+  static constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
+  static constexpr int SMEM = STAGES * STAGE_BYTES + 1024 + 256;
+  static constexpr int TMEM_COLS = 256;             // per accumulator buffer
+  static_assert(SMEM <= 227 * 1024, "shared memory");
+  static_assert((2 * STAGES + 5) * 8 + 8 <= 256, "barrier area");
+};
+
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+
+// shared::cluster address of this CTA's shared-memory offset `a` in CTA `rank`
+__device__ __forceinline__ uint32_t cluster_addr(uint32_t a, uint32_t rank) {
+  uint32_t d;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(rank));
+  return d;
+}
+
+__device__ __forceinline__ void cluster_sync() {
+  asm volatile("barrier.cluster.arrive.release;\n\tbarrier.cluster.wait.acquire;" ::: "memory");
+}
+
+// tile load into this CTA's shared memory, completing on an mbarrier of either CTA
+__device__ __forceinline__ void tma_load_3d_pair(uint32_t dst, const CUtensorMap* map,
+                                                 uint32_t bar_cluster, int c0, int c1, int c2) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes.cta_group::2"
+      " [%0], [%1, {%3, %4, %5}], [%2];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(bar_cluster), "r"(c0), "r"(c1), "r"(c2)
+      : "memory");
+}
+
+template <int MODE>
+__device__ __forceinline__ void mma_pair(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                         uint32_t accum) {
+  if (MODE == BF16) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(accum));
+  } else {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::2.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(accum));
+  }
+}
+
+// arrive on the mbarrier at this offset in every CTA of `mask` once the issuing
+// thread's MMAs have completed
+__device__ __forceinline__ void mma_commit_pair(uint32_t bar, uint16_t mask) {
+  asm volatile(
+      "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64"
+      " [%0], %1;" ::"r"(bar),
+      "h"(mask)
+      : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_cluster(uint32_t bar_cluster) {
+  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(bar_cluster)
+               : "memory");
+}
+
+template <int MODE, int STAGES, int OUT>
+__global__ void __launch_bounds__(NTHREADS, 1)
+    gemm_pair_kernel(const __grid_constant__ CUtensorMap mapA,
+                     const __grid_constant__ CUtensorMap mapB, int K, int tiles_m2, int tiles_n,
+                     int batch, EpiArgs ep) {
+  // Persistent over 256 x 256 tiles: cluster c (CTAs 2c, 2c+1) takes tiles c, c + clusters, ...
+  // Warp roles as in gemm_kernel; only the even CTA's warp 1 issues MMAs.
+  using C_ = PairCfg<MODE, STAGES>;
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                             ~uintptr_t(1023));
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * C_::STAGE_BYTES);
+  uint64_t* acc_full = bars + 2 * STAGES;
+  uint64_t* acc_empty = bars + 2 * STAGES + 2;
+  uint64_t* drain = bars + 2 * STAGES + 4;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 5);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const uint32_t rank = cluster_rank();
+  const bool lead = rank == 0;
+  const int cl = blockIdx.x >> 1, ncl = gridDim.x >> 1;
+  const int nk = (K + C_::KELEMS - 1) / C_::KELEMS;
+  const int num_units = tiles_m2 * tiles_n * batch;
+  auto stageA = [&](int s) { return smem + s * C_::STAGE_BYTES; };
+  auto stageB = [&](int s) { return smem + s * C_::STAGE_BYTES + C_::A_BYTES; };
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; s++) {
+      mbar_init(smem_u32(&bars[s]), 1);
+      mbar_init(smem_u32(&bars[STAGES + s]), 1);
+    }
+    for (int b = 0; b < 2; b++) {
+      mbar_init(smem_u32(&acc_full[b]), 1);
+      mbar_init(smem_u32(&acc_empty[b]), 8);          // 4 epilogue warps in each CTA
+    }
+    mbar_init(smem_u32(drain), 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&mapA)) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&mapB)) : "memory");
+  }
+  if (warp == 1) {
+    // one warp of each CTA allocates the pair's accumulator columns together
+    asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "r"(2 * C_::TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  cluster_sync();                 // both CTAs' barriers exist before either signals the other
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      int it = 0, last = -1;
+      for (int u = cl; u < num_units && !*abort_flag; u += ncl) {
+        int mt2, nt, z;
+        tile_coords(u, tiles_m2, tiles_n, ep.nfast, mt2, nt, z);
+        // a half tile wholly past the last row or column is loaded from the last one: the
+        // MMA then fills only accumulator rows / columns the epilogue does not store
+        const int m0 = min(mt2 * 2 * BM + (int)rank * BM, ep.M - 1);
+        const int n0 = min(nt * C_::BN + (int)rank * 128, ep.N - 1);
+        for (int kb = 0; kb < nk; kb++, it++) {
+          const int s = it % STAGES;
+          const uint32_t ph = (it / STAGES) & 1;
+          if (!mbar_wait(smem_u32(&bars[STAGES + s]), ph ^ 1, abort_flag, ep.err)) break;
+          const uint32_t full = smem_u32(&bars[s]);
+          if (lead) mbar_expect_tx(full, 2 * C_::STAGE_BYTES);
+          const uint32_t full_lead = cluster_addr(full, 0);
+          const int kc = kb * C_::KELEMS;
+          tma_load_3d_pair(smem_u32(stageA(s)), &mapA, full_lead, kc, m0, z);
+          tma_load_3d_pair(smem_u32(stageB(s)), &mapB, full_lead, kc, n0, z);
+          last = it;
+        }
+      }
+      if (*abort_flag && last >= 0) {
+        // every load this thread issued must land before the CTA exits: the even CTA
+        // watches the full barriers; the odd CTA's loads complete on the even CTA's
+        // barriers, so it allows them a fixed, ample time
+        const unsigned long long t0 = globaltimer();
+        if (lead) {
+          for (int j = max(0, last - STAGES + 1); j <= last; j++) {
+            const uint32_t bar = smem_u32(&bars[j % STAGES]);
+            while (!mbar_try(bar, (j / STAGES) & 1) && globaltimer() - t0 < WAIT_NS) {
+            }
+          }
+        } else {
+          while (globaltimer() - t0 < 1000000ull) {
+          }
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0 && lead) {
+      constexpr uint32_t idesc = make_idesc(MODE, 2 * BM, C_::BN);
+      int it = 0, local = 0;
+      for (int u = cl; u < num_units && !*abort_flag; u += ncl, local++) {
+        const int buf = local & 1;
+        const uint32_t use = (uint32_t)(local >> 1);
+        if (!mbar_wait(smem_u32(&acc_empty[buf]), (use & 1) ^ 1, abort_flag, ep.err)) break;
+        tc_fence_after();
+        const uint32_t tacc = tmem + buf * C_::TMEM_COLS;
+        for (int kb = 0; kb < nk; kb++, it++) {
+          const int s = it % STAGES;
+          const uint32_t ph = (it / STAGES) & 1;
+          if (!mbar_wait(smem_u32(&bars[s]), ph, abort_flag, ep.err)) break;
+          tc_fence_after();
+          const uint32_t a0 = smem_u32(stageA(s)), b0 = smem_u32(stageB(s));
+#pragma unroll
+          for (int ks = 0; ks < 4; ks++) {
+            const uint32_t acc = (kb > 0 || ks > 0) ? 1u : 0u;
+            mma_pair<MODE>(tacc, smem_desc(a0 + ks * 32), smem_desc(b0 + ks * 32), idesc, acc);
+          }
+          mma_commit_pair(smem_u32(&bars[STAGES + s]), 3);     // frees the stage in both CTAs
+        }
+        mma_commit_pair(smem_u32(&acc_full[buf]), 3);          // both halves of the tile ready
+      }
+    }
+  } else {
+    const int q = warp & 3;
+    int local = 0;
+    for (int u = cl; u < num_units; u += ncl, local++) {
+      const int buf = local & 1;
+      const uint32_t use = (uint32_t)(local >> 1);
+      const bool ok = mbar_wait(smem_u32(&acc_full[buf]), use & 1, abort_flag, ep.err);
+      if (!ok || *abort_flag) break;
+      tc_fence_after();
+      int mt2, nt, z;
+      tile_coords(u, tiles_m2, tiles_n, ep.nfast, mt2, nt, z);
+      const int row = mt2 * 2 * BM + (int)rank * BM + 32 * q + lane;
+      store_acc<C_::BN, OUT>(tmem + buf * C_::TMEM_COLS + ((uint32_t)(32 * q) << 16), row,
+                             nt * C_::BN, z, ep);
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive_cluster(cluster_addr(smem_u32(&acc_empty[buf]), 0));
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1 && lead) {
+    tc_fence_after();
+    if (lane == 0) {
+      // every MMA of the pair has retired before either CTA releases TMEM or exits
+      mma_commit_pair(smem_u32(drain), 1);
+      const unsigned long long t0 = globaltimer();
+      while (!mbar_try(smem_u32(drain), 0) && globaltimer() - t0 < WAIT_NS) {
+      }
+    }
+    __syncwarp();
+  }
+  cluster_sync();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem),
                  "r"(2 * C_::TMEM_COLS)
                  : "memory");
   }
@@ -417,6 +671,53 @@ int make_map(fmpt_handle* h, CUtensorMap* map, const void* base, int mode, int64
 
 }  // namespace tc
 
+// ----------------------------------------------------- CTA-pair launch
+// FMPT_ERR_UNSUPPORTED (nothing launched) when no cluster of two fits on the device.
+static int tc_gemm_pair(fmpt_handle* h, int M, int N, int K, int batch, const TcOperand& A,
+                        const TcOperand& B, const tc::EpiArgs& ep, int out_f64) {
+  using namespace tc;
+  constexpr int ST = 6;
+  using C_ = PairCfg<BF16, ST>;
+  CUtensorMap ma, mb;
+  FMPT_TRY(make_map(h, &ma, A.hi, BF16, K, M, A.ld, batch, A.bstride, BM));
+  FMPT_TRY(make_map(h, &mb, B.hi, BF16, K, N, B.ld, batch, B.bstride, 128));
+  const int tiles_m2 = (M + 2 * BM - 1) / (2 * BM), tiles_n = (N + C_::BN - 1) / C_::BN;
+  const int64_t units = (int64_t)tiles_m2 * tiles_n * batch;
+  if (units > INT32_MAX) return set_error(h, FMPT_ERR_SHAPE, "tc_gemm: too many tiles");
+  void (*kfn)(CUtensorMap, CUtensorMap, int, int, int, int, EpiArgs) =
+      out_f64 == 1 ? gemm_pair_kernel<BF16, ST, 1>
+                   : out_f64 == 2 ? gemm_pair_kernel<BF16, ST, 2> : gemm_pair_kernel<BF16, ST, 0>;
+  const int vi = out_f64 == 1 ? 1 : out_f64 == 2 ? 2 : 0;
+  static int clusters[3] = {-1, -1, -1};           // resident 2-CTA clusters, per variant
+  cudaLaunchConfig_t cfg{};
+  cfg.blockDim = dim3(NTHREADS);
+  cfg.dynamicSmemBytes = C_::SMEM;
+  cfg.stream = h->stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = 2;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (clusters[vi] < 0) {
+    FMPT_CUDA(h, cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, C_::SMEM));
+    cfg.gridDim = dim3(2 * std::max(1, h->sm_count / 2));
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, kfn, &cfg) != cudaSuccess) {
+      (void)cudaGetLastError();
+      n = 0;
+    }
+    clusters[vi] = n;
+  }
+  if (clusters[vi] <= 0) return FMPT_ERR_UNSUPPORTED;
+  cfg.gridDim = dim3((unsigned)(2 * std::min<int64_t>(units, clusters[vi])));
+  ProfScope prof(h, FMPT_K_TC_GEMM);
+  FMPT_CUDA(h, cudaLaunchKernelEx(&cfg, kfn, ma, mb, K, tiles_m2, tiles_n, batch, ep));
+  FMPT_LAUNCHED(h);
+  return FMPT_OK;
+}
+
 // ----------------------------------------------------- public engine call
 int tc_gemm(fmpt_handle* h, int mode, int M, int N, int K, int batch, const TcOperand& A,
             const TcOperand& B, void* C, int out_f64, int64_t ldc, int64_t strideC, int* err_dev) {
@@ -439,6 +740,12 @@ int tc_gemm(fmpt_handle* h, int mode, int M, int N, int K, int batch, const TcOp
     mb2 = mb;
   }
   EpiArgs ep{C, ldc, strideC, M, N, err_dev, M > N ? 1 : 0};   // A and B share K
+  // BF16 GEMMs of more than one 128-row tile run on the CTA-pair kernel (256 x 256 tiles,
+  // 6 stages) unless the handle asks for the one-CTA tile
+  if (mode == BF16 && M > BM && h->tc_tile == 0) {
+    int st = tc_gemm_pair(h, M, N, K, batch, A, B, ep, out_f64);
+    if (st != FMPT_ERR_UNSUPPORTED) return st;
+  }
   const int tiles_m = (M + BM - 1) / BM, tiles_n = (N + BN - 1) / BN;
   const int64_t tiles = (int64_t)tiles_m * tiles_n * batch;
   if (tiles > INT32_MAX) return set_error(h, FMPT_ERR_SHAPE, "tc_gemm: too many tiles");

@@ -36,6 +36,14 @@ class Handle:
             raise ValueError("svd method must be 'gesvd', 'gesvdp' or 'gesvdj'")
         self.check(lib().fmpt_set_svd_method(self.ptr, codes[method]))
 
+    def set_tc_tile(self, tile="pair"):
+        """Tile of the BF16 tensor-core GEMMs: "pair" (default; 256x256 on two-CTA
+        clusters where the GEMM has more than 128 rows) or "single" (128x256)."""
+        codes = {"pair": 0, "single": 1}
+        if tile not in codes:
+            raise ValueError("tc tile must be 'pair' or 'single'")
+        self.check(lib().fmpt_set_tc_tile(self.ptr, codes[tile]))
+
     def set_graphs(self, on=True):
         """CUDA-graph Krylov solves for block-sparse operators (default on)."""
         self.check(lib().fmpt_set_graphs(self.ptr, 1 if on else 0))

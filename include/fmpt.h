@@ -89,6 +89,12 @@ uint64_t fmpt_graph_launch_count(fmpt_handle* h);
  * the same order: the choice never changes results.  No counterpart in the
  * reference. */
 int fmpt_set_tuning(fmpt_handle* h, int mode);
+/* Output tile of the BF16 tensor-core GEMMs.  mode 0 (default): GEMMs of more
+ * than 128 rows run 256x256 tiles on two-CTA clusters (tcgen05.mma.cta_group::2),
+ * the rest 128x256 tiles on one CTA; mode 1: always the one-CTA tile.  Both
+ * accumulate in FP32 over the same K slices; the last bits may differ.  No
+ * counterpart in the reference. */
+int fmpt_set_tc_tile(fmpt_handle* h, int mode);
 /* Number of cached tuning decisions and of timed tunings so far. */
 int fmpt_tuning_info(fmpt_handle* h, int* entries, int64_t* timed);
 /* Output tile edge (32 or 64) a block-sparse operator runs with (0: dense op). */

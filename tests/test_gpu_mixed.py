@@ -65,6 +65,32 @@ def test_ac2_prime_bf16_large_grids(D):
     assert rel(y, ref) < TOL["bf16"], rel(y, ref)
 
 
+@pytest.mark.parametrize("Dl,Dr", [(48, 48), (80, 80), (100, 37), (512, 512)])
+def test_bf16_pair_tile_matches_single_tile(Dl, Dr):
+    """The two-CTA 256x256 tile (tcgen05.mma.cta_group::2) against the one-CTA 128x256
+    tile on the same inputs.  Both sum the same BF16 products in FP32; a different
+    summation order may flip the BF16 rounding of a few intermediate elements, so the
+    bound between them is 1e-4, far below the BF16 bound.  GEMM 1 is (4 Dr) x (5 Dl), GEMM 2 (4 Dl) x Dr: the sizes leave
+    the odd CTA's half of the last tile partly (M = 192, 148, 400; N = 240, 400, 500) and
+    wholly (M = 320; N = 48, 80, 37) past the last row or column."""
+    from finitemptools_gb300.device import default_handle
+    rng = np.random.default_rng(Dl + 7 * Dr)
+    W = heisenberg_xxz_mpo(1.0, 1.0, 0.0)[1].dense()
+    x = rng.standard_normal((Dl, 2, 2, Dr))
+    L, R = herm(rng, Dl, 5), herm(rng, Dr, 5)
+    args = (DT.from_numpy(x), W, W, DT.from_numpy(L), DT.from_numpy(R))
+    h = default_handle()
+    y_pair = fm.ac2_prime(*args, precision="bf16").numpy()
+    h.set_tc_tile("single")
+    try:
+        y_single = fm.ac2_prime(*args, precision="bf16").numpy()
+    finally:
+        h.set_tc_tile("pair")
+    ref = O.ac2_prime(x, W, W, L, R)
+    assert rel(y_pair, ref) < TOL["bf16"], rel(y_pair, ref)
+    assert rel(y_pair, y_single) < 1e-4, rel(y_pair, y_single)
+
+
 @pytest.mark.parametrize("prec", ["tf32x3", "tf32", "bf16"])
 def test_ac2_prime_mixed_j1j2_and_boundary(prec):
     rng = np.random.default_rng(7)
