@@ -3,11 +3,13 @@
 //
 //   C[m, n] = sum_k A[m, k] B[n, k]      (A, B "K-major": k contiguous)
 //
-// One CTA owns a 128 x BN output tile.  Warp 0 streams A/B K-slices into a
-// STAGES-deep shared-memory ring with cp.async.bulk.tensor (128-byte
-// swizzle, no multicast), warp 1 allocates the TMEM accumulator and issues
-// tcgen05.mma from one thread (kind::tf32 or kind::f16 with BF16 operands,
-// FP32 accumulation), warps 2-5 drain TMEM with tcgen05.ld and store.
+// gemm_kernel: one CTA owns a 128 x BN output tile.  Warp 0 streams A/B
+// K-slices into a STAGES-deep shared-memory ring with cp.async.bulk.tensor
+// (128-byte swizzle, no multicast), warp 1 allocates the TMEM accumulator and
+// issues tcgen05.mma from one thread (kind::tf32 or kind::f16 with BF16
+// operands, FP32 accumulation), warps 2-5 drain TMEM with tcgen05.ld and store.
+// gemm_pair_kernel: the same roles on a cluster of two CTAs sharing a 256 x 256
+// tile through tcgen05.mma.cta_group::2 (BF16 GEMMs of more than 128 rows).
 // 3xTF32 issues three MMAs per K-step (hi*hi + hi*lo + lo*hi) into the same
 // accumulator from operands pre-split into TF32 hi/lo planes.
 //
@@ -137,17 +139,6 @@ __device__ __forceinline__ void mma_commit(uint32_t bar) {
                : "memory");
 }
 
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
-      "%11, %12, %13, %14, %15}, [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-        "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-}
-
 struct EpiArgs {
   void* C;            // float or double
   int64_t ldc;        // column stride (elements)
@@ -175,30 +166,84 @@ __device__ __forceinline__ void tile_coords(int tile, int tiles_m, int tiles_n, 
   }
 }
 
-// One thread's accumulator row (TMEM lane) of a 128 x BN tile -> C[row, n0 .. n0+BN)
+__device__ __forceinline__ void tmem_ld32_async(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
+      "%11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, "
+      "%28, %29, %30, %31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+}
+
+// waits for this thread's TMEM loads; the registers of the load in flight are in-out
+// operands, so no use of them is scheduled before the wait
+__device__ __forceinline__ void tmem_wait_ld(uint32_t (&r)[32]) {
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]),
+                 "+r"(r[6]), "+r"(r[7]), "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]),
+                 "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15]), "+r"(r[16]), "+r"(r[17]),
+                 "+r"(r[18]), "+r"(r[19]), "+r"(r[20]), "+r"(r[21]), "+r"(r[22]), "+r"(r[23]),
+                 "+r"(r[24]), "+r"(r[25]), "+r"(r[26]), "+r"(r[27]), "+r"(r[28]), "+r"(r[29]),
+                 "+r"(r[30]), "+r"(r[31])
+               :
+               : "memory");
+}
+
+template <int OUT>
+__device__ __forceinline__ void store_cols(void* base, int64_t ldc, int n_base, int n_lim,
+                                           const uint32_t (&r)[32]) {
+  // base points at C[row, n_base]; columns n_base + j for j < 32, those >= n_lim skipped
+  if (n_base + 32 <= n_lim) {
+#pragma unroll
+    for (int j = 0; j < 32; j++) {
+      const float v = __uint_as_float(r[j]);
+      if (OUT == 1)
+        static_cast<double*>(base)[ldc * j] = (double)v;
+      else if (OUT == 2)
+        static_cast<__nv_bfloat16*>(base)[ldc * j] = __float2bfloat16_rn(v);
+      else
+        static_cast<float*>(base)[ldc * j] = v;
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < 32; j++) {
+      if (n_base + j < n_lim) {
+        const float v = __uint_as_float(r[j]);
+        if (OUT == 1)
+          static_cast<double*>(base)[ldc * j] = (double)v;
+        else if (OUT == 2)
+          static_cast<__nv_bfloat16*>(base)[ldc * j] = __float2bfloat16_rn(v);
+        else
+          static_cast<float*>(base)[ldc * j] = v;
+      }
+    }
+  }
+}
+
+// One thread's accumulator row (TMEM lane) of a 128 x BN tile -> C[row, n0 .. n0+BN).
+// 32-column TMEM loads, the next one in flight while the previous one is stored.
 template <int BN, int OUT>
 __device__ __forceinline__ void store_acc(uint32_t tbase, int row, int n0, int z,
                                           const EpiArgs& ep) {
+  constexpr int es = OUT == 1 ? 8 : OUT == 2 ? 2 : 4;
+  char* base = static_cast<char*>(ep.C) + es * ((int64_t)row + ep.strideC * z + ep.ldc * n0);
+  const bool live = row < ep.M;
+  static_assert(BN % 64 == 0, "epilogue chunk pairs");
+  uint32_t ra[32], rb[32];
+  tmem_ld32_async(tbase, ra);
+  tmem_wait_ld(ra);
 #pragma unroll 1
-  for (int c0 = 0; c0 < BN; c0 += 16) {
-    uint32_t r[16];
-    tmem_ld16(tbase + c0, r);
-    if (row < ep.M) {
-#pragma unroll
-      for (int j = 0; j < 16; j++) {
-        const int n = n0 + c0 + j;
-        if (n < ep.N) {
-          const int64_t idx = (int64_t)row + ep.ldc * n + ep.strideC * z;
-          const float v = __uint_as_float(r[j]);
-          if (OUT == 1)
-            static_cast<double*>(ep.C)[idx] = (double)v;
-          else if (OUT == 2)
-            static_cast<__nv_bfloat16*>(ep.C)[idx] = __float2bfloat16_rn(v);
-          else
-            static_cast<float*>(ep.C)[idx] = v;
-        }
-      }
-    }
+  for (int c0 = 0; c0 < BN; c0 += 64) {
+    tmem_ld32_async(tbase + c0 + 32, rb);
+    if (live) store_cols<OUT>(base + es * ep.ldc * c0, ep.ldc, n0 + c0, ep.N, ra);
+    tmem_wait_ld(rb);
+    if (c0 + 64 < BN) tmem_ld32_async(tbase + c0 + 64, ra);
+    if (live) store_cols<OUT>(base + es * ep.ldc * (c0 + 32), ep.ldc, n0 + c0 + 32, ep.N, rb);
+    tmem_wait_ld(ra);
   }
 }
 
@@ -673,10 +718,10 @@ int make_map(fmpt_handle* h, CUtensorMap* map, const void* base, int mode, int64
 
 // ----------------------------------------------------- CTA-pair launch
 // FMPT_ERR_UNSUPPORTED (nothing launched) when no cluster of two fits on the device.
-static int tc_gemm_pair(fmpt_handle* h, int M, int N, int K, int batch, const TcOperand& A,
+template <int ST>
+static int tc_gemm_pair_st(fmpt_handle* h, int M, int N, int K, int batch, const TcOperand& A,
                         const TcOperand& B, const tc::EpiArgs& ep, int out_f64) {
   using namespace tc;
-  constexpr int ST = 6;
   using C_ = PairCfg<BF16, ST>;
   CUtensorMap ma, mb;
   FMPT_TRY(make_map(h, &ma, A.hi, BF16, K, M, A.ld, batch, A.bstride, BM));
@@ -718,14 +763,20 @@ static int tc_gemm_pair(fmpt_handle* h, int M, int N, int K, int batch, const Tc
   return FMPT_OK;
 }
 
+// 6 stages: on the D=2048 step 5 stages measured 2% slower and 7 no faster
+static int tc_gemm_pair(fmpt_handle* h, int M, int N, int K, int batch, const TcOperand& A,
+                        const TcOperand& B, const tc::EpiArgs& ep, int out_f64) {
+  return tc_gemm_pair_st<6>(h, M, N, K, batch, A, B, ep, out_f64);
+}
+
 // ----------------------------------------------------- public engine call
 int tc_gemm(fmpt_handle* h, int mode, int M, int N, int K, int batch, const TcOperand& A,
             const TcOperand& B, void* C, int out_f64, int64_t ldc, int64_t strideC, int* err_dev) {
   using namespace tc;
   if (M <= 0 || N <= 0 || K <= 0 || batch <= 0) return FMPT_OK;
   CUtensorMap ma, mb, ma2, mb2;
-  // 256-wide N tiles with 4 stages for TF32/BF16.  Measured on the D=2048 step (average
-  // per GEMM): 256 x 4 stages 0.2455 ms; 256 x 3 stages 0.2743 ms; 192 x 5 stages 0.2576 ms;
+  // One-CTA kernel: 256-wide N tiles with 4 stages for TF32/BF16.  Measured on the D=2048
+  // step (average per GEMM, 16-column epilogue): 256 x 4 stages 0.2455 ms; 256 x 3 stages 0.2743 ms; 192 x 5 stages 0.2576 ms;
   // 128 x 6 stages 0.2745 ms.  Pipeline depth matters, but not at the cost of the
   // 256-wide MMA's operand reuse.
   const int BN = mode == TF32X3 ? 128 : 256;
@@ -741,7 +792,10 @@ int tc_gemm(fmpt_handle* h, int mode, int M, int N, int K, int batch, const TcOp
   }
   EpiArgs ep{C, ldc, strideC, M, N, err_dev, M > N ? 1 : 0};   // A and B share K
   // BF16 GEMMs of more than one 128-row tile run on the CTA-pair kernel (256 x 256 tiles,
-  // 6 stages) unless the handle asks for the one-CTA tile
+  // 6 stages) unless the handle asks for the one-CTA tile.  Average per GEMM of the D=2048
+  // step: one CTA 0.2363 ms; pair 0.2200 ms; pair with the overlapped 32-column TMEM
+  // epilogue 0.1964 ms (the 16-column load-wait-store epilogue had not kept up with the
+  // K = 2048 main loop of GEMM 1).
   if (mode == BF16 && M > BM && h->tc_tile == 0) {
     int st = tc_gemm_pair(h, M, N, K, batch, A, B, ep, out_f64);
     if (st != FMPT_ERR_UNSUPPORTED) return st;
