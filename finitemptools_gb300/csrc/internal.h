@@ -43,6 +43,9 @@ struct fmpt_handle {
   // reuse on h->stream)
   void* gemm_ws = nullptr;
   size_t gemm_ws_bytes = 0;
+  // partial tiles and arrival counters of the BF16 pair GEMM's K-split last round
+  void* tc_ws = nullptr;
+  size_t tc_ws_bytes = 0;
   // executable graphs of the captured Arnoldi basis, one per operator structure
   std::map<std::string, cudaGraphExec_t> arnoldi_exec;
   cudaGraphExec_t lanczos_exec = nullptr;   // reused through cudaGraphExecUpdate

@@ -511,12 +511,67 @@ __device__ __forceinline__ void mbar_arrive_cluster(uint32_t bar_cluster) {
                : "memory");
 }
 
+// Work items of the pair kernel.  Items [0, full) are whole tiles (units).  When the last
+// round of tiles would leave clusters idle, the `tail` units after them are each cut into
+// S pieces along K (items [full, full + tail S)): piece p sums K-slices
+// [p nk / S, (p+1) nk / S) and writes its FP32 partial tile to ws; the last piece of a
+// tile to finish (per CTA half and epilogue warp, counted in cnt) adds the S partials in
+// piece order and stores the tile, so the result does not depend on which piece ends last.
+struct PairSched {
+  int full, tail, S;
+  float* ws;          // [tail * S][256 columns][256 rows]
+  int* cnt;           // [tail][2 CTAs][4 warps], zero at launch, reset by the last piece
+};
+
+__device__ __forceinline__ void pair_item(const PairSched& sp, int item, int nk, int& u,
+                                          int& kb0, int& kb1, int& t) {
+  if (item < sp.full) {
+    u = item;
+    kb0 = 0;
+    kb1 = nk;
+    t = -1;
+  } else {
+    t = item - sp.full;
+    const int p = t % sp.S;
+    u = sp.full + t / sp.S;
+    kb0 = (int)((int64_t)p * nk / sp.S);
+    kb1 = (int)((int64_t)(p + 1) * nk / sp.S);
+  }
+}
+
+// One row of a K-split tile: the S partial rows at w0 (pieces 65536 floats apart, columns
+// 256 apart) summed in piece order into C.  All 32 S loads of a 32-column chunk are issued
+// before the first add.
+template <int S, int OUT>
+__device__ __forceinline__ void sum_pieces(const float* w0, char* base, int64_t ldc, int n0,
+                                           int N) {
+  constexpr int es = OUT == 1 ? 8 : OUT == 2 ? 2 : 4;
+#pragma unroll 1
+  for (int c0 = 0; c0 < 256; c0 += 32) {
+    float v[S][32];
+#pragma unroll
+    for (int pc = 0; pc < S; pc++)
+#pragma unroll
+      for (int j = 0; j < 32; j++)
+        v[pc][j] = __ldcg(w0 + (int64_t)pc * 65536 + (int64_t)(c0 + j) * 256);
+    uint32_t r[32];
+#pragma unroll
+    for (int j = 0; j < 32; j++) {
+      float a = v[0][j];
+#pragma unroll
+      for (int pc = 1; pc < S; pc++) a += v[pc][j];
+      r[j] = __float_as_uint(a);
+    }
+    store_cols<OUT>(base + es * ldc * c0, ldc, n0 + c0, N, r);
+  }
+}
+
 template <int MODE, int STAGES, int OUT>
 __global__ void __launch_bounds__(NTHREADS, 1)
     gemm_pair_kernel(const __grid_constant__ CUtensorMap mapA,
                      const __grid_constant__ CUtensorMap mapB, int K, int tiles_m2, int tiles_n,
-                     int batch, EpiArgs ep) {
-  // Persistent over 256 x 256 tiles: cluster c (CTAs 2c, 2c+1) takes tiles c, c + clusters, ...
+                     int batch, EpiArgs ep, PairSched sp) {
+  // Persistent over work items: cluster c (CTAs 2c, 2c+1) takes items c, c + clusters, ...
   // Warp roles as in gemm_kernel; only the even CTA's warp 1 issues MMAs.
   using C_ = PairCfg<MODE, STAGES>;
   extern __shared__ __align__(1024) uint8_t smem_raw[];
@@ -534,7 +589,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   const bool lead = rank == 0;
   const int cl = blockIdx.x >> 1, ncl = gridDim.x >> 1;
   const int nk = (K + C_::KELEMS - 1) / C_::KELEMS;
-  const int num_units = tiles_m2 * tiles_n * batch;
+  const int num_items = sp.full + sp.tail * sp.S;
+  (void)batch;
   auto stageA = [&](int s) { return smem + s * C_::STAGE_BYTES; };
   auto stageB = [&](int s) { return smem + s * C_::STAGE_BYTES + C_::A_BYTES; };
 
@@ -570,14 +626,15 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   if (warp == 0) {
     if (lane == 0) {
       int it = 0, last = -1;
-      for (int u = cl; u < num_units && !*abort_flag; u += ncl) {
-        int mt2, nt, z;
+      for (int item = cl; item < num_items && !*abort_flag; item += ncl) {
+        int u, kb0, kb1, t, mt2, nt, z;
+        pair_item(sp, item, nk, u, kb0, kb1, t);
         tile_coords(u, tiles_m2, tiles_n, ep.nfast, mt2, nt, z);
         // a half tile wholly past the last row or column is loaded from the last one: the
         // MMA then fills only accumulator rows / columns the epilogue does not store
         const int m0 = min(mt2 * 2 * BM + (int)rank * BM, ep.M - 1);
         const int n0 = min(nt * C_::BN + (int)rank * 128, ep.N - 1);
-        for (int kb = 0; kb < nk; kb++, it++) {
+        for (int kb = kb0; kb < kb1; kb++, it++) {
           const int s = it % STAGES;
           const uint32_t ph = (it / STAGES) & 1;
           if (!mbar_wait(smem_u32(&bars[STAGES + s]), ph ^ 1, abort_flag, ep.err)) break;
@@ -611,13 +668,15 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     if (lane == 0 && lead) {
       constexpr uint32_t idesc = make_idesc(MODE, 2 * BM, C_::BN);
       int it = 0, local = 0;
-      for (int u = cl; u < num_units && !*abort_flag; u += ncl, local++) {
+      for (int item = cl; item < num_items && !*abort_flag; item += ncl, local++) {
+        int u, kb0, kb1, t;
+        pair_item(sp, item, nk, u, kb0, kb1, t);
         const int buf = local & 1;
         const uint32_t use = (uint32_t)(local >> 1);
         if (!mbar_wait(smem_u32(&acc_empty[buf]), (use & 1) ^ 1, abort_flag, ep.err)) break;
         tc_fence_after();
         const uint32_t tacc = tmem + buf * C_::TMEM_COLS;
-        for (int kb = 0; kb < nk; kb++, it++) {
+        for (int kb = kb0; kb < kb1; kb++, it++) {
           const int s = it % STAGES;
           const uint32_t ph = (it / STAGES) & 1;
           if (!mbar_wait(smem_u32(&bars[s]), ph, abort_flag, ep.err)) break;
@@ -625,7 +684,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           const uint32_t a0 = smem_u32(stageA(s)), b0 = smem_u32(stageB(s));
 #pragma unroll
           for (int ks = 0; ks < 4; ks++) {
-            const uint32_t acc = (kb > 0 || ks > 0) ? 1u : 0u;
+            const uint32_t acc = (kb > kb0 || ks > 0) ? 1u : 0u;
             mma_pair<MODE>(tacc, smem_desc(a0 + ks * 32), smem_desc(b0 + ks * 32), idesc, acc);
           }
           mma_commit_pair(smem_u32(&bars[STAGES + s]), 3);     // frees the stage in both CTAs
@@ -636,20 +695,55 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   } else {
     const int q = warp & 3;
     int local = 0;
-    for (int u = cl; u < num_units; u += ncl, local++) {
+    for (int item = cl; item < num_items; item += ncl, local++) {
+      int u, kb0, kb1, t, mt2, nt, z;
+      pair_item(sp, item, nk, u, kb0, kb1, t);
       const int buf = local & 1;
       const uint32_t use = (uint32_t)(local >> 1);
       const bool ok = mbar_wait(smem_u32(&acc_full[buf]), use & 1, abort_flag, ep.err);
       if (!ok || *abort_flag) break;
       tc_fence_after();
-      int mt2, nt, z;
       tile_coords(u, tiles_m2, tiles_n, ep.nfast, mt2, nt, z);
-      const int row = mt2 * 2 * BM + (int)rank * BM + 32 * q + lane;
-      store_acc<C_::BN, OUT>(tmem + buf * C_::TMEM_COLS + ((uint32_t)(32 * q) << 16), row,
-                             nt * C_::BN, z, ep);
+      const int rloc = (int)rank * BM + 32 * q + lane;          // row within the 256-row tile
+      const int row = mt2 * 2 * BM + rloc;
+      const uint32_t tbase = tmem + buf * C_::TMEM_COLS + ((uint32_t)(32 * q) << 16);
+      if (t < 0) {
+        store_acc<C_::BN, OUT>(tbase, row, nt * C_::BN, z, ep);
+      } else {
+        EpiArgs pe{sp.ws + (int64_t)t * 65536, 256, 0, 256, 256, ep.err, 0};
+        store_acc<C_::BN, 0>(tbase, rloc, 0, 0, pe);
+      }
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive_cluster(cluster_addr(smem_u32(&acc_empty[buf]), 0));
+      if (t >= 0) {
+        // publish this piece, then the last of the S pieces sums them in piece order
+        __threadfence();
+        __syncwarp();
+        const int ut = u - sp.full;
+        int* c = sp.cnt + (ut * 2 + (int)rank) * 4 + q;
+        int prev = 0;
+        if (lane == 0) prev = atomicAdd(c, 1);
+        prev = __shfl_sync(0xffffffffu, prev, 0);
+        if (prev == sp.S - 1) {
+          __threadfence();
+          const float* w0 = sp.ws + (int64_t)ut * sp.S * 65536 + rloc;
+          if (row < ep.M) {
+            const int n0 = nt * C_::BN;
+            char* base = static_cast<char*>(ep.C) +
+                         (OUT == 1 ? 8 : OUT == 2 ? 2 : 4) *
+                             ((int64_t)row + ep.strideC * z + ep.ldc * n0);
+            if (sp.S == 2)
+              sum_pieces<2, OUT>(w0, base, ep.ldc, n0, ep.N);
+            else if (sp.S == 3)
+              sum_pieces<3, OUT>(w0, base, ep.ldc, n0, ep.N);
+            else
+              sum_pieces<4, OUT>(w0, base, ep.ldc, n0, ep.N);
+          }
+          __syncwarp();
+          if (lane == 0) *c = 0;
+        }
+      }
     }
   }
   tc_fence_before();
@@ -729,7 +823,7 @@ static int tc_gemm_pair_st(fmpt_handle* h, int M, int N, int K, int batch, const
   const int tiles_m2 = (M + 2 * BM - 1) / (2 * BM), tiles_n = (N + C_::BN - 1) / C_::BN;
   const int64_t units = (int64_t)tiles_m2 * tiles_n * batch;
   if (units > INT32_MAX) return set_error(h, FMPT_ERR_SHAPE, "tc_gemm: too many tiles");
-  void (*kfn)(CUtensorMap, CUtensorMap, int, int, int, int, EpiArgs) =
+  void (*kfn)(CUtensorMap, CUtensorMap, int, int, int, int, EpiArgs, PairSched) =
       out_f64 == 1 ? gemm_pair_kernel<BF16, ST, 1>
                    : out_f64 == 2 ? gemm_pair_kernel<BF16, ST, 2> : gemm_pair_kernel<BF16, ST, 0>;
   const int vi = out_f64 == 1 ? 1 : out_f64 == 2 ? 2 : 0;
@@ -756,9 +850,39 @@ static int tc_gemm_pair_st(fmpt_handle* h, int M, int N, int K, int batch, const
     clusters[vi] = n;
   }
   if (clusters[vi] <= 0) return FMPT_ERR_UNSUPPORTED;
-  cfg.gridDim = dim3((unsigned)(2 * std::min<int64_t>(units, clusters[vi])));
+  // Whole tiles fill rounds of `cl` clusters; when the last round holds R < cl / 2 tiles,
+  // those are cut along K into S = min(4, cl / R) pieces (at least 4 K-slices each), so
+  // the round ends after about 1/S of a tile instead of a whole one.
+  const int cl = clusters[vi];
+  const int nk = (K + C_::KELEMS - 1) / C_::KELEMS;
+  PairSched sp{(int)units, 0, 1, nullptr, nullptr};
+  const int rem = (int)(units % cl);
+  const int S = rem > 0 ? std::min(std::min(4, cl / rem), nk / 4) : 1;
+  if (S >= 2) {
+    const size_t part = (size_t)rem * S * 65536 * sizeof(float);
+    const size_t need = part + (size_t)rem * 8 * sizeof(int);
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(h->stream, &cs) != cudaSuccess) {
+      (void)cudaGetLastError();
+      cs = cudaStreamCaptureStatusActive;
+    }
+    // the workspace is grown outside stream capture only; inside, an undersized one
+    // leaves the last round whole
+    if (h->tc_ws_bytes < need && cs == cudaStreamCaptureStatusNone)
+      FMPT_TRY(grow_buffer(h, &h->tc_ws, &h->tc_ws_bytes, need));
+    if (h->tc_ws_bytes >= need) {
+      sp.full = (int)(units - rem);
+      sp.tail = rem;
+      sp.S = S;
+      sp.ws = static_cast<float*>(h->tc_ws);
+      sp.cnt = reinterpret_cast<int*>(static_cast<char*>(h->tc_ws) + part);
+      FMPT_CUDA(h, cudaMemsetAsync(sp.cnt, 0, (size_t)rem * 8 * sizeof(int), h->stream));
+    }
+  }
+  const int64_t items = (int64_t)sp.full + (int64_t)sp.tail * sp.S;
+  cfg.gridDim = dim3((unsigned)(2 * std::min<int64_t>(items, cl)));
   ProfScope prof(h, FMPT_K_TC_GEMM);
-  FMPT_CUDA(h, cudaLaunchKernelEx(&cfg, kfn, ma, mb, K, tiles_m2, tiles_n, batch, ep));
+  FMPT_CUDA(h, cudaLaunchKernelEx(&cfg, kfn, ma, mb, K, tiles_m2, tiles_n, batch, ep, sp));
   FMPT_LAUNCHED(h);
   return FMPT_OK;
 }

@@ -91,6 +91,24 @@ def test_bf16_pair_tile_matches_single_tile(Dl, Dr):
     assert rel(y_pair, y_single) < 1e-4, rel(y_pair, y_single)
 
 
+@pytest.mark.parametrize("D", [512, 1536])
+def test_bf16_pair_tail_split_is_deterministic(D):
+    """The pair GEMM cuts the tiles of a last, part-filled round along K (GEMM 1 of D=1536
+    into 2 pieces; at D=512 GEMM 1 into 2 and GEMM 2 into 4) and adds the partial tiles in
+    piece order: repeated applications give identical bits, within the BF16 bound of the
+    oracle-pinned FP64 form."""
+    rng = np.random.default_rng(D + 3)
+    W = heisenberg_xxz_mpo(1.0, 1.0, 0.0)[1].dense()
+    x = rng.standard_normal((D, 2, 2, D))
+    L, R = herm(rng, D, 5), herm(rng, D, 5)
+    args = (DT.from_numpy(x), W, W, DT.from_numpy(L), DT.from_numpy(R))
+    op = fm.HeffOp("ac2", args[3], args[4], W1=W, W2=W, precision="bf16")
+    ys = [op(args[0]).numpy() for _ in range(3)]
+    assert all(np.array_equal(ys[0], y) for y in ys[1:])
+    ref = fm.ac2_prime(*args, precision="fp64").numpy()
+    assert rel(ys[0], ref) < TOL["bf16"], rel(ys[0], ref)
+
+
 @pytest.mark.parametrize("prec", ["tf32x3", "tf32", "bf16"])
 def test_ac2_prime_mixed_j1j2_and_boundary(prec):
     rng = np.random.default_rng(7)
@@ -258,7 +276,12 @@ def test_tdvp1_complex_mixed_matches_fp64():
                                          ("tf32x3", False, 1024)])
 def test_ac2_prime_host_matches_device_path(prec, cplx, D):
     """fmpt_ac2_prime_host (host buffers, pipelined transfers for real mixed
-    precision) gives exactly the result of copy-in + fmpt_ac2_prime + copy-out."""
+    precision) gives the result of copy-in + fmpt_ac2_prime + copy-out: exactly, except
+    where it runs GEMM 2 of a BF16 operator in column blocks (Dr >= 256).  There the BF16
+    pair GEMM cuts the tiles of each launch's part-filled last round along K, a choice
+    that depends on the launch's width, so the FP32 sums of those tiles may be ordered
+    differently: bound 1e-8 per unit of the summed length K = 2 w D, the FP32 accumulation
+    scale the tolerances above use."""
     import torch
     from finitemptools_gb300.derivatives import ac2_prime_host
     rng = np.random.default_rng(D)
@@ -274,7 +297,13 @@ def test_ac2_prime_host_matches_device_path(prec, cplx, D):
     ref = fm.ac2_prime(DT.from_numpy(x, dtype=dt), W, W, DT.from_numpy(L, dtype=dt),
                        DT.from_numpy(R, dtype=dt), precision=prec).numpy()
     y = ac2_prime_host(x, W, W, L, R, precision=prec)
-    assert np.array_equal(y, ref)
+
+    def same(a, b):
+        if prec == "bf16" and D >= 256:
+            return rel(a, b) < 1e-8 * 2 * w * D
+        return np.array_equal(a, b)
+
+    assert same(y, ref)
     if not cplx:
         # page-locked host buffers through the C ABI, as the bench's end-to-end step uses
         from finitemptools_gb300._native import lib, PREC
@@ -287,4 +316,4 @@ def test_ac2_prime_host_matches_device_path(prec, cplx, D):
         h.check(lib().fmpt_ac2_prime_host(h.ptr, 0, PREC[prec], px.data_ptr(), Wb.ctypes.data,
                                           Wb.ctypes.data, pL.data_ptr(), pR.data_ptr(),
                                           py.data_ptr(), D, 2, 2, D, w, w, w))
-        assert np.array_equal(py.numpy().reshape(x.shape, order="F"), ref)
+        assert same(py.numpy().reshape(x.shape, order="F"), ref)
