@@ -43,8 +43,8 @@ METRIC = "DMRG sweep s & H_eff·x TFLOP/s, mixed vs FP64 on one GB300 at ΔE≤1
 # DRAM bytes (read + write) per tc_gemm launch from one ncu capture of this workload
 # (dram__bytes_read.sum + dram__bytes_write.sum of the third step of
 # `bench.py --steps 2 --warmup 3`, averaged over its GEMM 1 and GEMM 2)
-NCU_TRAFFIC = {("bf16", 2048): {"bytes_per_launch": (76.94e6 + 132.16e6 + 333.65e6 + 105.42e6) / 2,
-                                "gemm1_bytes": 76.94e6 + 132.16e6, "gemm2_bytes": 333.65e6 + 105.42e6,
+NCU_TRAFFIC = {("bf16", 2048): {"bytes_per_launch": (88.77e6 + 134.09e6 + 334.29e6 + 106.94e6) / 2,
+                                "gemm1_bytes": 88.77e6 + 134.09e6, "gemm2_bytes": 334.29e6 + 106.94e6,
                                 "algorithmic_operand_bytes": {"gemm1": 76.0e6, "gemm2": 210.0e6}}}
 UNIT = "TFLOP/s"
 W_MPO, D_PHYS = 5, 2
