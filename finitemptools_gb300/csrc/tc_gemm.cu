@@ -812,20 +812,21 @@ int make_map(fmpt_handle* h, CUtensorMap* map, const void* base, int mode, int64
 
 // ----------------------------------------------------- CTA-pair launch
 // FMPT_ERR_UNSUPPORTED (nothing launched) when no cluster of two fits on the device.
-template <int ST>
+template <int MODE, int ST>
 static int tc_gemm_pair_st(fmpt_handle* h, int M, int N, int K, int batch, const TcOperand& A,
-                        const TcOperand& B, const tc::EpiArgs& ep, int out_f64) {
+                           const TcOperand& B, const tc::EpiArgs& ep, int out_f64) {
   using namespace tc;
-  using C_ = PairCfg<BF16, ST>;
+  using C_ = PairCfg<MODE, ST>;
   CUtensorMap ma, mb;
-  FMPT_TRY(make_map(h, &ma, A.hi, BF16, K, M, A.ld, batch, A.bstride, BM));
-  FMPT_TRY(make_map(h, &mb, B.hi, BF16, K, N, B.ld, batch, B.bstride, 128));
+  FMPT_TRY(make_map(h, &ma, A.hi, MODE, K, M, A.ld, batch, A.bstride, BM));
+  FMPT_TRY(make_map(h, &mb, B.hi, MODE, K, N, B.ld, batch, B.bstride, 128));
   const int tiles_m2 = (M + 2 * BM - 1) / (2 * BM), tiles_n = (N + C_::BN - 1) / C_::BN;
   const int64_t units = (int64_t)tiles_m2 * tiles_n * batch;
   if (units > INT32_MAX) return set_error(h, FMPT_ERR_SHAPE, "tc_gemm: too many tiles");
   void (*kfn)(CUtensorMap, CUtensorMap, int, int, int, int, EpiArgs, PairSched) =
-      out_f64 == 1 ? gemm_pair_kernel<BF16, ST, 1>
-                   : out_f64 == 2 ? gemm_pair_kernel<BF16, ST, 2> : gemm_pair_kernel<BF16, ST, 0>;
+      out_f64 == 1   ? gemm_pair_kernel<MODE, ST, 1>
+      : out_f64 == 2 ? gemm_pair_kernel<MODE, ST, MODE == BF16 ? 2 : 0>
+                     : gemm_pair_kernel<MODE, ST, 0>;
   const int vi = out_f64 == 1 ? 1 : out_f64 == 2 ? 2 : 0;
   static int clusters[3] = {-1, -1, -1};           // resident 2-CTA clusters, per variant
   cudaLaunchConfig_t cfg{};
@@ -888,9 +889,11 @@ static int tc_gemm_pair_st(fmpt_handle* h, int M, int N, int K, int batch, const
 }
 
 // 6 stages: on the D=2048 step 5 stages measured 2% slower and 7 no faster
-static int tc_gemm_pair(fmpt_handle* h, int M, int N, int K, int batch, const TcOperand& A,
-                        const TcOperand& B, const tc::EpiArgs& ep, int out_f64) {
-  return tc_gemm_pair_st<6>(h, M, N, K, batch, A, B, ep, out_f64);
+static int tc_gemm_pair(fmpt_handle* h, int mode, int M, int N, int K, int batch,
+                        const TcOperand& A, const TcOperand& B, const tc::EpiArgs& ep,
+                        int out_f64) {
+  if (mode == tc::TF32) return tc_gemm_pair_st<tc::TF32, 6>(h, M, N, K, batch, A, B, ep, out_f64);
+  return tc_gemm_pair_st<tc::BF16, 6>(h, M, N, K, batch, A, B, ep, out_f64);
 }
 
 // ----------------------------------------------------- public engine call
@@ -898,6 +901,16 @@ int tc_gemm(fmpt_handle* h, int mode, int M, int N, int K, int batch, const TcOp
             const TcOperand& B, void* C, int out_f64, int64_t ldc, int64_t strideC, int* err_dev) {
   using namespace tc;
   if (M <= 0 || N <= 0 || K <= 0 || batch <= 0) return FMPT_OK;
+  EpiArgs ep{C, ldc, strideC, M, N, err_dev, M > N ? 1 : 0};   // A and B share K
+  // TF32 and BF16 GEMMs of more than one 128-row tile run on the CTA-pair kernel
+  // (256 x 256 tiles, 6 stages) unless the handle asks for the one-CTA tile.  Average per
+  // BF16 GEMM of the D=2048 step: one CTA 0.2363 ms; pair 0.2200 ms; pair with the
+  // overlapped 32-column TMEM epilogue 0.1964 ms (the 16-column load-wait-store epilogue
+  // had not kept up with the K = 2048 main loop of GEMM 1); K-split last round 0.1904 ms.
+  if ((mode == BF16 || mode == TF32) && M > BM && h->tc_tile == 0) {
+    int st = tc_gemm_pair(h, mode, M, N, K, batch, A, B, ep, out_f64);
+    if (st != FMPT_ERR_UNSUPPORTED) return st;
+  }
   CUtensorMap ma, mb, ma2, mb2;
   // One-CTA kernel: 256-wide N tiles with 4 stages for TF32/BF16.  Measured on the D=2048
   // step (average per GEMM, 16-column epilogue): 256 x 4 stages 0.2455 ms; 256 x 3 stages 0.2743 ms; 192 x 5 stages 0.2576 ms;
@@ -913,16 +926,6 @@ int tc_gemm(fmpt_handle* h, int mode, int M, int N, int K, int batch, const TcOp
   } else {
     ma2 = ma;
     mb2 = mb;
-  }
-  EpiArgs ep{C, ldc, strideC, M, N, err_dev, M > N ? 1 : 0};   // A and B share K
-  // BF16 GEMMs of more than one 128-row tile run on the CTA-pair kernel (256 x 256 tiles,
-  // 6 stages) unless the handle asks for the one-CTA tile.  Average per GEMM of the D=2048
-  // step: one CTA 0.2363 ms; pair 0.2200 ms; pair with the overlapped 32-column TMEM
-  // epilogue 0.1964 ms (the 16-column load-wait-store epilogue had not kept up with the
-  // K = 2048 main loop of GEMM 1).
-  if (mode == BF16 && M > BM && h->tc_tile == 0) {
-    int st = tc_gemm_pair(h, M, N, K, batch, A, B, ep, out_f64);
-    if (st != FMPT_ERR_UNSUPPORTED) return st;
   }
   const int tiles_m = (M + BM - 1) / BM, tiles_n = (N + BN - 1) / BN;
   const int64_t tiles = (int64_t)tiles_m * tiles_n * batch;

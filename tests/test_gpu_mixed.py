@@ -65,12 +65,13 @@ def test_ac2_prime_bf16_large_grids(D):
     assert rel(y, ref) < TOL["bf16"], rel(y, ref)
 
 
+@pytest.mark.parametrize("prec", ["bf16", "tf32"])
 @pytest.mark.parametrize("Dl,Dr", [(48, 48), (80, 80), (100, 37), (512, 512)])
-def test_bf16_pair_tile_matches_single_tile(Dl, Dr):
+def test_pair_tile_matches_single_tile(prec, Dl, Dr):
     """The two-CTA 256x256 tile (tcgen05.mma.cta_group::2) against the one-CTA 128x256
-    tile on the same inputs.  Both sum the same BF16 products in FP32; a different
+    tile on the same inputs.  Both sum the same BF16 (TF32) products in FP32; a different
     summation order may flip the BF16 rounding of a few intermediate elements, so the
-    bound between them is 1e-4, far below the BF16 bound.  GEMM 1 is (4 Dr) x (5 Dl), GEMM 2 (4 Dl) x Dr: the sizes leave
+    bound between them is 1e-4, far below the BF16 and TF32 bounds.  GEMM 1 is (4 Dr) x (5 Dl), GEMM 2 (4 Dl) x Dr: the sizes leave
     the odd CTA's half of the last tile partly (M = 192, 148, 400; N = 240, 400, 500) and
     wholly (M = 320; N = 48, 80, 37) past the last row or column."""
     from finitemptools_gb300.device import default_handle
@@ -80,19 +81,19 @@ def test_bf16_pair_tile_matches_single_tile(Dl, Dr):
     L, R = herm(rng, Dl, 5), herm(rng, Dr, 5)
     args = (DT.from_numpy(x), W, W, DT.from_numpy(L), DT.from_numpy(R))
     h = default_handle()
-    y_pair = fm.ac2_prime(*args, precision="bf16").numpy()
+    y_pair = fm.ac2_prime(*args, precision=prec).numpy()
     h.set_tc_tile("single")
     try:
-        y_single = fm.ac2_prime(*args, precision="bf16").numpy()
+        y_single = fm.ac2_prime(*args, precision=prec).numpy()
     finally:
         h.set_tc_tile("pair")
     ref = O.ac2_prime(x, W, W, L, R)
-    assert rel(y_pair, ref) < TOL["bf16"], rel(y_pair, ref)
+    assert rel(y_pair, ref) < TOL[prec], rel(y_pair, ref)
     assert rel(y_pair, y_single) < 1e-4, rel(y_pair, y_single)
 
 
-@pytest.mark.parametrize("D", [512, 1536])
-def test_bf16_pair_tail_split_is_deterministic(D):
+@pytest.mark.parametrize("prec,D", [("bf16", 512), ("bf16", 1536), ("tf32", 512)])
+def test_pair_tail_split_is_deterministic(prec, D):
     """The pair GEMM cuts the tiles of a last, part-filled round along K (GEMM 1 of D=1536
     into 2 pieces; at D=512 GEMM 1 into 2 and GEMM 2 into 4) and adds the partial tiles in
     piece order: repeated applications give identical bits, within the BF16 bound of the
@@ -102,11 +103,11 @@ def test_bf16_pair_tail_split_is_deterministic(D):
     x = rng.standard_normal((D, 2, 2, D))
     L, R = herm(rng, D, 5), herm(rng, D, 5)
     args = (DT.from_numpy(x), W, W, DT.from_numpy(L), DT.from_numpy(R))
-    op = fm.HeffOp("ac2", args[3], args[4], W1=W, W2=W, precision="bf16")
+    op = fm.HeffOp("ac2", args[3], args[4], W1=W, W2=W, precision=prec)
     ys = [op(args[0]).numpy() for _ in range(3)]
     assert all(np.array_equal(ys[0], y) for y in ys[1:])
     ref = fm.ac2_prime(*args, precision="fp64").numpy()
-    assert rel(ys[0], ref) < TOL["bf16"], rel(ys[0], ref)
+    assert rel(ys[0], ref) < TOL[prec], rel(ys[0], ref)
 
 
 @pytest.mark.parametrize("prec", ["tf32x3", "tf32", "bf16"])
@@ -277,7 +278,7 @@ def test_tdvp1_complex_mixed_matches_fp64():
 def test_ac2_prime_host_matches_device_path(prec, cplx, D):
     """fmpt_ac2_prime_host (host buffers, pipelined transfers for real mixed
     precision) gives the result of copy-in + fmpt_ac2_prime + copy-out: exactly, except
-    where it runs GEMM 2 of a BF16 operator in column blocks (Dr >= 256).  There the BF16
+    where it runs GEMM 2 of a BF16 or TF32 operator in column blocks (Dr >= 256).  There the
     pair GEMM cuts the tiles of each launch's part-filled last round along K, a choice
     that depends on the launch's width, so the FP32 sums of those tiles may be ordered
     differently: bound 1e-8 per unit of the summed length K = 2 w D, the FP32 accumulation
@@ -299,7 +300,7 @@ def test_ac2_prime_host_matches_device_path(prec, cplx, D):
     y = ac2_prime_host(x, W, W, L, R, precision=prec)
 
     def same(a, b):
-        if prec == "bf16" and D >= 256:
+        if prec in ("bf16", "tf32") and D >= 256:
             return rel(a, b) < 1e-8 * 2 * w * D
         return np.array_equal(a, b)
 
