@@ -38,7 +38,7 @@ struct fmpt_handle {
   // CUDA graphs for the Krylov solvers of block-sparse operators (fmpt_set_graphs)
   bool graphs = true;
   int svd_method = 0;          // 0 gesvd (bidiagonalisation), 1 gesvdp (polar decomposition)
-  int tc_tile = 0;             // BF16 tcgen05 GEMM tile: 0 CTA pair where it applies, 1 one CTA
+  int tc_tile = 0;             // tcgen05 GEMM tile: 0 CTA pair where it applies, 1 one CTA
   // split-K workspace of the FP64 GEMM, grown outside stream capture only (stream-ordered
   // reuse on h->stream)
   void* gemm_ws = nullptr;

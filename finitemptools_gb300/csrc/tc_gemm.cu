@@ -446,7 +446,8 @@ struct PairCfg {
   static constexpr int KELEMS = MODE == BF16 ? 64 : 32;
   static constexpr int A_BYTES = BM * 128;          // this CTA's 128 A rows x 128 B of K
   static constexpr int B_BYTES = 128 * 128;         // this CTA's 128 B rows
-  static constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
+  static constexpr int SPLIT = MODE == TF32X3 ? 2 : 1;   // hi (and lo) operand planes
+  static constexpr int STAGE_BYTES = (A_BYTES + B_BYTES) * SPLIT;
   static constexpr int SMEM = STAGES * STAGE_BYTES + 1024 + 256;
   static constexpr int TMEM_COLS = 256;             // per accumulator buffer
   static_assert(SMEM <= 227 * 1024, "shared memory");
@@ -569,7 +570,9 @@ __device__ __forceinline__ void sum_pieces(const float* w0, char* base, int64_t 
 template <int MODE, int STAGES, int OUT>
 __global__ void __launch_bounds__(NTHREADS, 1)
     gemm_pair_kernel(const __grid_constant__ CUtensorMap mapA,
-                     const __grid_constant__ CUtensorMap mapB, int K, int tiles_m2, int tiles_n,
+                     const __grid_constant__ CUtensorMap mapB,
+                     const __grid_constant__ CUtensorMap mapA2,
+                     const __grid_constant__ CUtensorMap mapB2, int K, int tiles_m2, int tiles_n,
                      int batch, EpiArgs ep, PairSched sp) {
   // Persistent over work items: cluster c (CTAs 2c, 2c+1) takes items c, c + clusters, ...
   // Warp roles as in gemm_kernel; only the even CTA's warp 1 issues MMAs.
@@ -591,8 +594,11 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   const int nk = (K + C_::KELEMS - 1) / C_::KELEMS;
   const int num_items = sp.full + sp.tail * sp.S;
   (void)batch;
-  auto stageA = [&](int s) { return smem + s * C_::STAGE_BYTES; };
-  auto stageB = [&](int s) { return smem + s * C_::STAGE_BYTES + C_::A_BYTES; };
+  // stage s: [A hi][B hi] and, for 3xTF32, [A lo][B lo]
+  auto stageA = [&](int s, int part) {
+    return smem + s * C_::STAGE_BYTES + part * (C_::A_BYTES + C_::B_BYTES);
+  };
+  auto stageB = [&](int s, int part) { return stageA(s, part) + C_::A_BYTES; };
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; s++) {
@@ -608,6 +614,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&mapA)) : "memory");
     asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&mapB)) : "memory");
+    if (MODE == TF32X3) {
+      asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&mapA2)) : "memory");
+      asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&mapB2)) : "memory");
+    }
   }
   if (warp == 1) {
     // one warp of each CTA allocates the pair's accumulator columns together
@@ -642,8 +652,12 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           if (lead) mbar_expect_tx(full, 2 * C_::STAGE_BYTES);
           const uint32_t full_lead = cluster_addr(full, 0);
           const int kc = kb * C_::KELEMS;
-          tma_load_3d_pair(smem_u32(stageA(s)), &mapA, full_lead, kc, m0, z);
-          tma_load_3d_pair(smem_u32(stageB(s)), &mapB, full_lead, kc, n0, z);
+          tma_load_3d_pair(smem_u32(stageA(s, 0)), &mapA, full_lead, kc, m0, z);
+          tma_load_3d_pair(smem_u32(stageB(s, 0)), &mapB, full_lead, kc, n0, z);
+          if (MODE == TF32X3) {
+            tma_load_3d_pair(smem_u32(stageA(s, 1)), &mapA2, full_lead, kc, m0, z);
+            tma_load_3d_pair(smem_u32(stageB(s, 1)), &mapB2, full_lead, kc, n0, z);
+          }
           last = it;
         }
       }
@@ -681,11 +695,17 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           const uint32_t ph = (it / STAGES) & 1;
           if (!mbar_wait(smem_u32(&bars[s]), ph, abort_flag, ep.err)) break;
           tc_fence_after();
-          const uint32_t a0 = smem_u32(stageA(s)), b0 = smem_u32(stageB(s));
+          const uint32_t a0 = smem_u32(stageA(s, 0)), b0 = smem_u32(stageB(s, 0));
 #pragma unroll
           for (int ks = 0; ks < 4; ks++) {
             const uint32_t acc = (kb > kb0 || ks > 0) ? 1u : 0u;
-            mma_pair<MODE>(tacc, smem_desc(a0 + ks * 32), smem_desc(b0 + ks * 32), idesc, acc);
+            const uint64_t ad = smem_desc(a0 + ks * 32), bd = smem_desc(b0 + ks * 32);
+            mma_pair<MODE>(tacc, ad, bd, idesc, acc);
+            if (MODE == TF32X3) {                  // hi*hi + hi*lo + lo*hi
+              const uint32_t a1 = smem_u32(stageA(s, 1)), b1 = smem_u32(stageB(s, 1));
+              mma_pair<MODE>(tacc, ad, smem_desc(b1 + ks * 32), idesc, 1u);
+              mma_pair<MODE>(tacc, smem_desc(a1 + ks * 32), bd, idesc, 1u);
+            }
           }
           mma_commit_pair(smem_u32(&bars[STAGES + s]), 3);     // frees the stage in both CTAs
         }
@@ -817,13 +837,22 @@ static int tc_gemm_pair_st(fmpt_handle* h, int M, int N, int K, int batch, const
                            const TcOperand& B, const tc::EpiArgs& ep, int out_f64) {
   using namespace tc;
   using C_ = PairCfg<MODE, ST>;
-  CUtensorMap ma, mb;
+  CUtensorMap ma, mb, ma2, mb2;
   FMPT_TRY(make_map(h, &ma, A.hi, MODE, K, M, A.ld, batch, A.bstride, BM));
   FMPT_TRY(make_map(h, &mb, B.hi, MODE, K, N, B.ld, batch, B.bstride, 128));
+  if (MODE == TF32X3) {
+    if (!A.lo || !B.lo) return set_error(h, FMPT_ERR_ARG, "3xTF32 needs lo planes");
+    FMPT_TRY(make_map(h, &ma2, A.lo, MODE, K, M, A.ld, batch, A.bstride, BM));
+    FMPT_TRY(make_map(h, &mb2, B.lo, MODE, K, N, B.ld, batch, B.bstride, 128));
+  } else {
+    ma2 = ma;
+    mb2 = mb;
+  }
   const int tiles_m2 = (M + 2 * BM - 1) / (2 * BM), tiles_n = (N + C_::BN - 1) / C_::BN;
   const int64_t units = (int64_t)tiles_m2 * tiles_n * batch;
   if (units > INT32_MAX) return set_error(h, FMPT_ERR_SHAPE, "tc_gemm: too many tiles");
-  void (*kfn)(CUtensorMap, CUtensorMap, int, int, int, int, EpiArgs, PairSched) =
+  void (*kfn)(CUtensorMap, CUtensorMap, CUtensorMap, CUtensorMap, int, int, int, int, EpiArgs,
+              PairSched) =
       out_f64 == 1   ? gemm_pair_kernel<MODE, ST, 1>
       : out_f64 == 2 ? gemm_pair_kernel<MODE, ST, MODE == BF16 ? 2 : 0>
                      : gemm_pair_kernel<MODE, ST, 0>;
@@ -883,7 +912,7 @@ static int tc_gemm_pair_st(fmpt_handle* h, int M, int N, int K, int batch, const
   const int64_t items = (int64_t)sp.full + (int64_t)sp.tail * sp.S;
   cfg.gridDim = dim3((unsigned)(2 * std::min<int64_t>(items, cl)));
   ProfScope prof(h, FMPT_K_TC_GEMM);
-  FMPT_CUDA(h, cudaLaunchKernelEx(&cfg, kfn, ma, mb, K, tiles_m2, tiles_n, batch, ep, sp));
+  FMPT_CUDA(h, cudaLaunchKernelEx(&cfg, kfn, ma, mb, ma2, mb2, K, tiles_m2, tiles_n, batch, ep, sp));
   FMPT_LAUNCHED(h);
   return FMPT_OK;
 }
@@ -893,6 +922,8 @@ static int tc_gemm_pair(fmpt_handle* h, int mode, int M, int N, int K, int batch
                         const TcOperand& A, const TcOperand& B, const tc::EpiArgs& ep,
                         int out_f64) {
   if (mode == tc::TF32) return tc_gemm_pair_st<tc::TF32, 6>(h, M, N, K, batch, A, B, ep, out_f64);
+  if (mode == tc::TF32X3)
+    return tc_gemm_pair_st<tc::TF32X3, 3>(h, M, N, K, batch, A, B, ep, out_f64);
   return tc_gemm_pair_st<tc::BF16, 6>(h, M, N, K, batch, A, B, ep, out_f64);
 }
 
@@ -902,12 +933,13 @@ int tc_gemm(fmpt_handle* h, int mode, int M, int N, int K, int batch, const TcOp
   using namespace tc;
   if (M <= 0 || N <= 0 || K <= 0 || batch <= 0) return FMPT_OK;
   EpiArgs ep{C, ldc, strideC, M, N, err_dev, M > N ? 1 : 0};   // A and B share K
-  // TF32 and BF16 GEMMs of more than one 128-row tile run on the CTA-pair kernel
-  // (256 x 256 tiles, 6 stages) unless the handle asks for the one-CTA tile.  Average per
+  // GEMMs of more than one 128-row tile run on the CTA-pair kernel (256 x 256 tiles; 6
+  // stages of 32 KB, or 3 of 64 KB for the hi/lo planes of 3xTF32) unless the handle asks
+  // for the one-CTA tile.  Average per
   // BF16 GEMM of the D=2048 step: one CTA 0.2363 ms; pair 0.2200 ms; pair with the
   // overlapped 32-column TMEM epilogue 0.1964 ms (the 16-column load-wait-store epilogue
   // had not kept up with the K = 2048 main loop of GEMM 1); K-split last round 0.1904 ms.
-  if ((mode == BF16 || mode == TF32) && M > BM && h->tc_tile == 0) {
+  if (M > BM && h->tc_tile == 0) {
     int st = tc_gemm_pair(h, mode, M, N, K, batch, A, B, ep, out_f64);
     if (st != FMPT_ERR_UNSUPPORTED) return st;
   }

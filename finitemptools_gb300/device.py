@@ -37,8 +37,8 @@ class Handle:
         self.check(lib().fmpt_set_svd_method(self.ptr, codes[method]))
 
     def set_tc_tile(self, tile="pair"):
-        """Tile of the BF16 tensor-core GEMMs: "pair" (default; 256x256 on two-CTA
-        clusters where the GEMM has more than 128 rows) or "single" (128x256)."""
+        """Tile of the tensor-core GEMMs: "pair" (default; 256x256 on two-CTA clusters
+        where the GEMM has more than 128 rows) or "single" (one CTA per tile)."""
         codes = {"pair": 0, "single": 1}
         if tile not in codes:
             raise ValueError("tc tile must be 'pair' or 'single'")

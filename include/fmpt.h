@@ -89,11 +89,11 @@ uint64_t fmpt_graph_launch_count(fmpt_handle* h);
  * the same order: the choice never changes results.  No counterpart in the
  * reference. */
 int fmpt_set_tuning(fmpt_handle* h, int mode);
-/* Output tile of the BF16 tensor-core GEMMs.  mode 0 (default): GEMMs of more
- * than 128 rows run 256x256 tiles on two-CTA clusters (tcgen05.mma.cta_group::2),
- * the rest 128x256 tiles on one CTA; mode 1: always the one-CTA tile.  Both
- * accumulate in FP32 over the same K slices; the last bits may differ.  No
- * counterpart in the reference. */
+/* Output tile of the tensor-core GEMMs (BF16, TF32, 3xTF32).  mode 0 (default):
+ * GEMMs of more than 128 rows run 256x256 tiles on two-CTA clusters
+ * (tcgen05.mma.cta_group::2), the rest one-CTA tiles (128x256; 128x128 for
+ * 3xTF32); mode 1: always the one-CTA tile.  Both accumulate in FP32 over the
+ * same K slices; the last bits may differ.  No counterpart in the reference. */
 int fmpt_set_tc_tile(fmpt_handle* h, int mode);
 /* Number of cached tuning decisions and of timed tunings so far. */
 int fmpt_tuning_info(fmpt_handle* h, int* entries, int64_t* timed);

@@ -65,7 +65,7 @@ def test_ac2_prime_bf16_large_grids(D):
     assert rel(y, ref) < TOL["bf16"], rel(y, ref)
 
 
-@pytest.mark.parametrize("prec", ["bf16", "tf32"])
+@pytest.mark.parametrize("prec", ["bf16", "tf32", "tf32x3"])
 @pytest.mark.parametrize("Dl,Dr", [(48, 48), (80, 80), (100, 37), (512, 512)])
 def test_pair_tile_matches_single_tile(prec, Dl, Dr):
     """The two-CTA 256x256 tile (tcgen05.mma.cta_group::2) against the one-CTA 128x256
@@ -88,11 +88,12 @@ def test_pair_tile_matches_single_tile(prec, Dl, Dr):
     finally:
         h.set_tc_tile("pair")
     ref = O.ac2_prime(x, W, W, L, R)
-    assert rel(y_pair, ref) < TOL[prec], rel(y_pair, ref)
+    assert rel(y_pair, ref) < tol(prec, Dl + 5 * Dr), rel(y_pair, ref)
     assert rel(y_pair, y_single) < 1e-4, rel(y_pair, y_single)
 
 
-@pytest.mark.parametrize("prec,D", [("bf16", 512), ("bf16", 1536), ("tf32", 512)])
+@pytest.mark.parametrize("prec,D", [("bf16", 512), ("bf16", 1536), ("tf32", 512),
+                                    ("tf32x3", 512)])
 def test_pair_tail_split_is_deterministic(prec, D):
     """The pair GEMM cuts the tiles of a last, part-filled round along K (GEMM 1 of D=1536
     into 2 pieces; at D=512 GEMM 1 into 2 and GEMM 2 into 4) and adds the partial tiles in
@@ -107,7 +108,7 @@ def test_pair_tail_split_is_deterministic(prec, D):
     ys = [op(args[0]).numpy() for _ in range(3)]
     assert all(np.array_equal(ys[0], y) for y in ys[1:])
     ref = fm.ac2_prime(*args, precision="fp64").numpy()
-    assert rel(ys[0], ref) < TOL[prec], rel(ys[0], ref)
+    assert rel(ys[0], ref) < tol(prec, 6 * D), rel(ys[0], ref)
 
 
 @pytest.mark.parametrize("prec", ["tf32x3", "tf32", "bf16"])
@@ -278,7 +279,7 @@ def test_tdvp1_complex_mixed_matches_fp64():
 def test_ac2_prime_host_matches_device_path(prec, cplx, D):
     """fmpt_ac2_prime_host (host buffers, pipelined transfers for real mixed
     precision) gives the result of copy-in + fmpt_ac2_prime + copy-out: exactly, except
-    where it runs GEMM 2 of a BF16 or TF32 operator in column blocks (Dr >= 256).  There the
+    where it runs GEMM 2 of a mixed-precision operator in column blocks (Dr >= 256).  There the
     pair GEMM cuts the tiles of each launch's part-filled last round along K, a choice
     that depends on the launch's width, so the FP32 sums of those tiles may be ordered
     differently: bound 1e-8 per unit of the summed length K = 2 w D, the FP32 accumulation
@@ -300,7 +301,7 @@ def test_ac2_prime_host_matches_device_path(prec, cplx, D):
     y = ac2_prime_host(x, W, W, L, R, precision=prec)
 
     def same(a, b):
-        if prec in ("bf16", "tf32") and D >= 256:
+        if prec != "fp64" and D >= 256:
             return rel(a, b) < 1e-8 * 2 * w * D
         return np.array_equal(a, b)
 
