@@ -415,7 +415,8 @@ int fmpt_ac2_prime_host(fmpt_handle* h, int dtype, int precision, const double* 
   // step overlap the R copy; block c of R is converted and multiplied (GEMM 2 for the
   // columns b' of block c) while block c+1 is uploaded, and y's block c is downloaded
   // meanwhile.  A block of R[b', w2, b] (b' fastest) is a pitched 2-D copy.
-  const int nblk = Dr >= 1024 ? 4 : (Dr >= 256 ? 2 : 1);
+  // more blocks shorten the tail after the last upload (one block's GEMM 2 and y download)
+  const int nblk = Dr >= 2048 ? 8 : Dr >= 1024 ? 4 : (Dr >= 256 ? 2 : 1);
   FMPT_TRY(aux_fork(h, 2));        // the copies follow the allocations above
   cudaStream_t as = h->aux_stream[0], ds = h->aux_stream[1];
   std::vector<cudaEvent_t> ev(2 + 2 * nblk, nullptr);   // L, x, R blocks, y blocks

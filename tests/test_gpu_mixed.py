@@ -275,7 +275,7 @@ def test_tdvp1_complex_mixed_matches_fp64():
 @pytest.mark.parametrize("prec,cplx,D", [("bf16", False, 100), ("tf32x3", False, 256),
                                          ("tf32", False, 37), ("fp64", False, 64),
                                          ("bf16", True, 48), ("bf16", False, 1030),
-                                         ("tf32x3", False, 1024)])
+                                         ("tf32x3", False, 1024), ("bf16", False, 2048)])
 def test_ac2_prime_host_matches_device_path(prec, cplx, D):
     """fmpt_ac2_prime_host (host buffers, pipelined transfers for real mixed
     precision) gives the result of copy-in + fmpt_ac2_prime + copy-out: exactly, except
