@@ -188,6 +188,29 @@ def test_svd_trunc_qr_lq(cplx, m, n):
     assert np.allclose(Q2n @ Q2n.conj().T, np.eye(Q2n.shape[0]), atol=1e-13)
 
 
+@pytest.mark.parametrize("m,n,cplx,zero_col", [(128, 64, True, None), (64, 128, True, None),
+                                              (100, 100, False, None), (1, 5, True, None),
+                                              (7, 1, False, None), (50, 20, True, 3),
+                                              (300, 200, True, None), (256, 40, False, 39)])
+def test_qr_conventions_match_lapack(m, n, cplx, zero_col):
+    """leftorth (fmpt_qr, cuSOLVER geqrf/ungqr) against numpy's geqrf/ungqr factors, entry
+    by entry: the same Householder conventions (real diagonal of R, beta = -sign(Re a)
+    |(a, x)|) give the same Q and R up to rounding, so the gauge of the moves matches the
+    reference's LAPACK QR; a zero column takes the tau = 0 reflector."""
+    rng = np.random.default_rng(m * 7 + n)
+    M = rnd(rng, (m, n), cplx)
+    if zero_col is not None:
+        M[:, zero_col] = 0.0
+    Q, R = fm.leftorth(DT.from_numpy(M), m, n)
+    Qn, Rn = Q.numpy(), R.numpy()
+    Qr, Rr = np.linalg.qr(M)
+    assert np.abs(Qn - Qr).max() < 1e-12 * max(1, m), np.abs(Qn - Qr).max()
+    assert np.abs(Rn - Rr).max() < 1e-12 * np.abs(Rr).max() * max(1, m)
+    assert np.allclose(np.imag(np.diag(Rn)), 0)
+    Lm, Q2 = fm.rightorth(DT.from_numpy(M), m, n)
+    assert rel(Lm.numpy() @ Q2.numpy(), M) < 1e-13
+
+
 @pytest.mark.parametrize("cplx", [False, True])
 def test_exponentiate_matches_exact(cplx):
     import scipy.linalg
