@@ -22,7 +22,7 @@ from .device import DeviceTensor, to_host_buffer
 from .mps import canonicalize_
 
 __all__ = ["QuantumGate", "QuantumCircuit", "apply_", "bond_evolution", "bond_evolution3",
-           "bond_evolution4", "swap_gate", "move_", "trotter_propagator"]
+           "bond_evolution4", "swap_gate", "move_", "trotter_propagator", "fuse_gates"]
 
 
 class QuantumGate:
@@ -76,6 +76,82 @@ class QuantumCircuit(list):
     def __mul__(self, other):
         """x * y applies y first (circuit.jl:45)."""
         return QuantumCircuit(list(other) + list(self))
+
+
+# ---------------------------------------------------------------- gate fusion
+# circuit/gate_fusion.jl: host algebra on the gates' small matrices (at most d^8 entries),
+# done once per circuit before it is applied.
+def _commute(a, b):
+    """_is_commutative (gate_fusion.jl:3-25): gates on disjoint sites."""
+    return not (set(a.positions) & set(b.positions))
+
+
+def _embed(g, K, dims):
+    """g's operator on the sorted sites K (a superset of g's), identity on the others."""
+    N = len(K)
+    if N > 8:
+        raise ValueError("gate fusion supports at most 8 sites")
+    out, inn = "abcdefgh"[:N], "ijklmnop"[:N]
+    t = {k: i for i, k in enumerate(K)}
+    subs = ["".join(out[t[p]] for p in g.positions) + "".join(inn[t[p]] for p in g.positions)]
+    ops = [g.op]
+    for i, k in enumerate(K):
+        if k in g.positions:
+            continue
+        subs.append(out[i] + inn[i])
+        ops.append(np.eye(dims[i], dtype=g.op.dtype))
+    return np.einsum(",".join(subs) + "->" + out + inn, *ops)
+
+
+def _try_mul(a, b):
+    """try_mul_two_ops (gate_fusion.jl:357-362, with the per-arity contractions of
+    :49-355): a applied after b as one gate, when the
+    sites of one contain the other's; None otherwise.  The product sits on the larger
+    site set."""
+    big, small = (a, b) if len(a.positions) >= len(b.positions) else (b, a)
+    if not set(small.positions) <= set(big.positions):
+        return None
+    K = big.positions
+    dims = big.op.shape[:len(K)]
+    for p, d in zip(small.positions, small.op.shape[:len(small.positions)]):
+        if dims[K.index(p)] != d:
+            raise ValueError("gates disagree on the dimension of site %d" % p)
+    P = int(np.prod(dims))
+    ma = _embed(a, K, dims).reshape(P, P, order="F")
+    mb = _embed(b, K, dims).reshape(P, P, order="F")
+    return QuantumGate(K, (ma @ mb).reshape(tuple(dims) * 2, order="F"))
+
+
+def _absorb(gates, gate):
+    """try_absorb_one_gate_by_mul! (gate_fusion.jl:364-374): multiply gate into the latest
+    earlier gate it can join, passing only gates it commutes with."""
+    for i in range(len(gates) - 1, -1, -1):
+        r = _try_mul(gate, gates[i])
+        if r is not None:
+            gates[i] = r
+            return True
+        if not _commute(gates[i], gate):
+            return False
+    return False
+
+
+def _fuse_pass(circuit):
+    """try_absorb_by_mul_impl and _fuse_gate_impl (gate_fusion.jl:376-395): from the last gate to the second,
+    each gate that an earlier one absorbs leaves the circuit."""
+    b = list(circuit)
+    for i in range(len(b) - 1, 0, -1):
+        br = b[:i]
+        if _absorb(br, b[i]):
+            b = br + b[i + 1:]
+    return QuantumCircuit(b)
+
+
+def fuse_gates(circuit):
+    """fuse_gates (gate_fusion.jl:397-400): one pass over the adjoint circuit (later gates
+    absorbing earlier ones), then one over the circuit.  The result applies the same
+    operator with fewer gates."""
+    c = circuit if isinstance(circuit, QuantumCircuit) else QuantumCircuit(circuit)
+    return _fuse_pass(_fuse_pass(c.adjoint()).adjoint())
 
 
 # ---------------------------------------------------------------- bond updates

@@ -1,0 +1,82 @@
+"""fuse_gates (circuit/gate_fusion.jl:357-400) on the host: the fused circuit applies
+the same operator (checked on dense state vectors through the oracle's dense_apply), with
+the gates the reference's absorption order leaves."""
+
+import numpy as np
+import pytest
+
+import finitemptools_gb300 as fm
+from finitemptools_gb300.tebd import QuantumCircuit, QuantumGate
+from oracle.tebd import dense_apply
+
+
+def unitary(rng, n):
+    q, r = np.linalg.qr(rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)))
+    return q * (np.diag(r) / np.abs(np.diag(r)))
+
+
+def apply_dense(circuit, psi, L, d):
+    dims = [d] * L
+    for g in circuit:
+        psi = dense_apply(psi, L, dims, list(g.positions), g.matrix())
+    return psi
+
+
+def test_fuse_small_cases_follow_the_absorption_order():
+    """[A(1), B(1,2), C(2,3)] -> [B A on (1,2), C on (2,3)]: A joins B in the pass over the
+    adjoint circuit; B A and C overlap without containing each other, so both stay.
+    [B(1,2), A(1)] -> one gate A B on (1,2)."""
+    rng = np.random.default_rng(1)
+    A, B, C = unitary(rng, 2), unitary(rng, 4), unitary(rng, 4)
+    f = fm.fuse_gates(QuantumCircuit([QuantumGate(1, A), QuantumGate((1, 2), B),
+                                      QuantumGate((2, 3), C)]))
+    assert [g.positions for g in f] == [(1, 2), (2, 3)]
+    assert np.allclose(f[0].matrix(), B @ np.kron(np.eye(2), A))
+    assert np.allclose(f[1].matrix(), C)
+    f2 = fm.fuse_gates(QuantumCircuit([QuantumGate((1, 2), B), QuantumGate(1, A)]))
+    assert [g.positions for g in f2] == [(1, 2)]
+    assert np.allclose(f2[0].matrix(), np.kron(np.eye(2), A) @ B)
+    # no gate contains the sites of A(3): it stays
+    f3 = fm.fuse_gates(QuantumCircuit([QuantumGate((1, 2), B), QuantumGate(3, A)]))
+    assert [g.positions for g in f3] == [(1, 2), (3,)]
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_fuse_random_circuit_keeps_the_operator(seed):
+    rng = np.random.default_rng(seed)
+    L, d = 6, 2
+    gates = []
+    for _ in range(30):
+        n = int(rng.integers(1, 4))
+        start = int(rng.integers(1, L - n + 2))
+        pos = list(range(start, start + n))
+        if n > 1 and rng.random() < 0.5:
+            pos = pos[::-1]                      # unsorted positions, permuted on construction
+        gates.append(QuantumGate(tuple(pos), unitary(rng, d ** n)))
+    circ = QuantumCircuit(gates)
+    fused = fm.fuse_gates(circ)
+    assert 0 < len(fused) < len(circ)
+    for _ in range(3):
+        psi = rng.standard_normal(d ** L) + 1j * rng.standard_normal(d ** L)
+        a = apply_dense(circ, psi, L, d)
+        b = apply_dense(fused, psi, L, d)
+        assert np.linalg.norm(a - b) < 1e-12 * np.linalg.norm(a)
+
+
+def test_fuse_trotter_circuit_merges_the_half_steps():
+    """A second-order Trotter circuit of several steps: consecutive half-step gates on the
+    same bond join, the operator is unchanged."""
+    rng = np.random.default_rng(5)
+    L, d = 6, 2
+    X = np.array([[0.0, 1.0], [1.0, 0.0]])
+    Z = np.diag([1.0, -1.0])
+    bonds = {(i, i + 1): -np.kron(Z, Z) for i in range(1, L)}
+    sites = {i: -0.7 * X for i in range(1, L + 1)}
+    circ = fm.trotter_propagator(L, [d] * L, bonds, sites, tspan=(0.0, -0.3j), order=2,
+                                 stepsize=0.05)
+    fused = fm.fuse_gates(circ)
+    assert len(fused) < len(circ)
+    psi = rng.standard_normal(d ** L) + 1j * rng.standard_normal(d ** L)
+    a = apply_dense(circ, psi, L, d)
+    b = apply_dense(fused, psi, L, d)
+    assert np.linalg.norm(a - b) < 1e-12 * np.linalg.norm(a)
