@@ -213,9 +213,10 @@ def exact_timeevolution(h, t, psi, ishermitian=True, tol=1e-12, krylovdim=30,
                         precision="fp64"):
     """exact_timeevolution(h, t, psi; ishermitian) (exactdiag.jl:44-61):
     exponentiate of ac_prime at the centre.  A complex t promotes the state to
-    complex128."""
-    if not ishermitian:
-        raise NotImplementedError("non-Hermitian exact time evolution (Arnoldi) is not built")
+    complex128.  Both values of ishermitian take the same solver: fmpt_exponentiate is an
+    Arnoldi exponential (full two-pass Gram-Schmidt, exponential of the Hessenberg
+    matrix), the reference's Arnoldi() driver, which its Lanczos() driver for Hermitian h
+    matches up to rounding."""
     t = complex(t)
     if t.imag != 0.0:
         psi = psi.astype(np.complex128)

@@ -78,6 +78,39 @@ def test_eigsolve_highest_and_projected():
     assert np.abs(np.asarray(nxt) - E[1:3]).max() < 1e-9
 
 
+def test_exact_time_evolution_non_hermitian():
+    """ishermitian=False (the reference's Arnoldi driver) on a non-Hermitian H: TFI with
+    complex fields h_i + i g_i, against the dense matrix exponential, for a real and an
+    imaginary time.  Non-Hermitian exact diagonalisation stays unbuilt and says so."""
+    from finitemptools_gb300.utilities import MPOHamiltonian, SchurMPOTensor, spin_half_matrices
+    L = 8
+    rng = np.random.default_rng(11)
+    hc = 1.0 + 0.2 * rng.standard_normal(L) + 0.3j * rng.standard_normal(L)
+    p = spin_half_matrices()
+    data = []
+    for hi in hc:
+        O_ = [[0] * 3 for _ in range(3)]
+        O_[0][0] = np.eye(2)
+        O_[0][1] = -p["z"]
+        O_[0][2] = -hi * p["x"]
+        O_[1][2] = p["z"]
+        O_[2][2] = np.eye(2)
+        data.append(SchurMPOTensor(O_))
+    mpo = FiniteMPO(MPOHamiltonian(data), L)
+    terms = [(-1.0, {i: ed.SZ, i + 1: ed.SZ}) for i in range(1, L)]
+    terms += [(-hc[i - 1], {i: ed.SX}) for i in range(1, L + 1)]
+    H = ed.dense_from_terms(L, 2, terms)
+    assert np.abs(H - H.conj().T).max() > 0.1
+    st = O.randommps(L, 2, 3, rng, dtype=np.complex128)
+    ex = fm.ExactFiniteMPS.from_mps(fm.FiniteMPS.from_numpy(st))
+    for t in (0.3, -0.4j):
+        out = fm.exact_timeevolution(mpo, t, ex, ishermitian=False)
+        ref = ed.exact_evolution(H, O.mps_to_dense(st), t)
+        assert np.linalg.norm(_dense(out) - ref) < 1e-9 * np.linalg.norm(ref)
+    with pytest.raises(NotImplementedError):
+        fm.exact_diagonalization(mpo, ishermitian=False)
+
+
 def test_exact_mps_and_time_evolution():
     L, t = 9, -0.4j
     rng = np.random.default_rng(5)
