@@ -978,7 +978,7 @@ def main():
                "d2h_bytes_per_step": x.size * 8,
                "path": "fmpt_ac2_prime_host through the C ABI: pinned host x/L/R in, y out"}
 
-    # ---- every precision form at every size (config table), rank 0 only
+    # ---- every precision form at every size (D = 256 .. 2048), rank 0 only
     table = None
     if rank == 0 and not args.no_table:
         table = []

@@ -384,7 +384,7 @@ int op_tc_prepare(fmpt_op* op) {
   st->cplx = op->dtype == FMPT_C128;
   if (st->cplx && op->kind != 2) {
     // the MPO step of the embedding acts on the real and imaginary planes alike: it needs
-    // real coefficients (true for the spin and fermion MPOs of the configs)
+    // real coefficients (true for the spin and fermion MPOs of the utilities module)
     const MidSchedule& cs = op->sched;
     MidSchedule& rs = st->rsched;
     rs.nw_in = cs.nw_in; rs.nw_out = cs.nw_out; rs.p_in = cs.p_in; rs.p_out = cs.p_out;

@@ -1,7 +1,7 @@
 """Parity of the plain FP64 device path against the CPU oracle.
 
-Bar (BASELINE the benchmark spec): H_eff*x within 1e-12 relative (Frobenius) of the
-oracle; sweep energies within 1e-10.  Environment updates, SVD, QR/LQ and
+Bar: H_eff*x within 1e-12 relative (Frobenius) of the oracle; sweep energies
+within 1e-10.  Environment updates, SVD, QR/LQ and
 the Krylov solvers are checked at the same level.  Shapes include odd and
 tiny bond dimensions (1, 3, 7, 33) so every tile edge of the kernels runs.
 """

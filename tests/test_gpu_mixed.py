@@ -1,7 +1,7 @@
 """Mixed-precision (tcgen05) contractions against the FP64 oracle.
 
 Each precision form states its error bound against FP64 (relative Frobenius
-norm of H_eff*x), the numbers BASELINE config 2 asks for:
+norm of H_eff*x), the bounds of the mixed-precision H_eff*x workload:
   3xTF32 (hi/lo split, FP32 accumulation)  < 2e-6
   TF32   (FP32 accumulation)               < 3e-3
   BF16   (FP32 accumulation)               < 2e-2
