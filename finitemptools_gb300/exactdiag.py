@@ -181,23 +181,82 @@ def init_h_center(h, psi, precision="fp64"):
     return left, right, Ws[mid - 1]
 
 
+_ORDER = {"SR": lambda v: v.real, "LR": lambda v: -v.real, "LM": lambda v: -np.abs(v),
+          "SM": lambda v: np.abs(v), "SI": lambda v: v.imag, "LI": lambda v: -v.imag}
+
+
+def _arnoldi_eigsolve(op, x0, num, which, krylovdim, maxiter, tol):
+    """eigsolve(f, x0, num, which, Arnoldi()) for a non-Hermitian f (exactdiag.jl:25-28):
+    explicitly restarted Arnoldi on the device vectors (two-pass Gram-Schmidt through
+    device dots and axpys).  The krylovdim x krylovdim Hessenberg eigenproblem is solved on
+    the host, as KrylovKit solves its small dense problem; the restart vector is the sum of
+    the wanted Ritz vectors.  Returns (values, vectors, info) like HeffOp.eigsolve."""
+    from .auxiliary import axpy, dot, norm, scal
+    if which not in _ORDER:
+        raise ValueError("which must be one of %s" % sorted(_ORDER))
+    m = max(num + 1, int(krylovdim))
+    x = scal(1.0 / norm(x0), x0.copy())
+    applies = 0
+    for it in range(int(maxiter)):
+        V = [x]
+        H = np.zeros((m + 1, m), dtype=np.complex128)
+        k = m
+        for j in range(m):
+            w = op(V[j])
+            applies += 1
+            for _ in range(2):
+                for i in range(j + 1):
+                    c = dot(V[i], w)
+                    H[i, j] += c
+                    axpy(-c, V[i], w)
+            b = norm(w)
+            H[j + 1, j] = b
+            if b <= 1e-14 * max(1.0, np.abs(H[:j + 2, :j + 1]).max()):
+                k = j + 1                              # invariant subspace
+                break
+            V.append(scal(1.0 / b, w))
+        ev, Y = np.linalg.eig(H[:k, :k])
+        idx = np.argsort(_ORDER[which](ev), kind="stable")[:num]
+        res = np.abs(H[k, k - 1]) * np.abs(Y[k - 1, idx]) if k < len(V) else np.zeros(len(idx))
+        vecs = []
+        for i in idx:
+            u = scal(complex(Y[0, i]), V[0].copy())
+            for q in range(1, k):
+                axpy(complex(Y[q, i]), V[q], u)
+            vecs.append(scal(1.0 / norm(u), u))
+        done = np.all(res <= tol * np.maximum(1.0, np.abs(ev[idx]))) or k < m
+        if done or it == int(maxiter) - 1:
+            info = {"converged": int(np.sum(res <= tol * np.maximum(1.0, np.abs(ev[idx])))),
+                    "residuals": [float(r) for r in res], "applies": applies}
+            return [complex(v) for v in ev[idx]], vecs, info
+        x = vecs[0].copy()
+        for u in vecs[1:]:
+            axpy(1.0, u, x)
+        x = scal(1.0 / norm(x), x)
+
+
 def exact_diagonalization(h, len=None, ishermitian=True, num=1, which="SR", dtype=None,
                           rng=None, handle=None, krylovdim=30, maxiter=100, tol=1e-12,
                           precision="fp64"):
     """exact_diagonalization(h; sector, len, ishermitian, num, which)
     (exactdiag.jl:23-42): eigsolve of ac_prime at the centre of a random
-    ExactFiniteMPS.  Returns (values, states)."""
-    if not ishermitian:
-        raise NotImplementedError("non-Hermitian exact diagonalisation (Arnoldi) is not built")
+    ExactFiniteMPS, by thick-restart Lanczos for Hermitian h and by restarted Arnoldi
+    (complex vectors, complex eigenvalues) otherwise.  Returns (values, states)."""
     n_sites = len if len is not None else _default_len(h)
     Ws, _ = _sites(h, n_sites)
     physdims = [W.shape[1] for W in Ws]
-    cplx = any(np.iscomplexobj(W) for W in Ws)
+    cplx = any(np.iscomplexobj(W) for W in Ws) or not ishermitian
     dt = np.dtype(dtype) if dtype is not None else np.dtype(np.complex128 if cplx else np.float64)
+    if not ishermitian and dt != np.complex128:
+        raise TypeError("non-Hermitian exact diagonalisation needs complex128 states")
     psi = ExactFiniteMPS.random(physdims, dt, rng, handle)
     left, right, Wc = init_h_center(h, psi, precision)
     op = HeffOp("ac", left, right, W1=Wc, precision=precision, dtype=dt)
-    vals, vecs, info = op.eigsolve(psi[psi.center], num, which, krylovdim, maxiter, tol)
+    if ishermitian:
+        vals, vecs, info = op.eigsolve(psi[psi.center], num, which, krylovdim, maxiter, tol)
+    else:
+        vals, vecs, info = _arnoldi_eigsolve(op, psi[psi.center], num, which, krylovdim,
+                                             maxiter, tol)
     if info["converged"] < num:
         import warnings
         warnings.warn("only %d converged." % info["converged"])
