@@ -434,7 +434,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 // TMA brings 32 KB (48 KB for a one-CTA 128 x 256 tile) and per K=16 step the MMA reads
 // 8 KB of shared memory (12 KB): the one-CTA tile asks the shared memory for about 1.5x
 // the bandwidth the tensor core's rate leaves it, the pair stays within it, and the
-// 32 KB stage leaves room for 6 stages.
+// 32 KB stage leaves room for 6 stages.  TF32 slices are 32 elements of the same 128
+// bytes; 3xTF32 stages hold hi and lo planes (64 KB, 3 stages) and take three MMAs per
+// K step.
 //
 // Barriers: full[s] lives in the even CTA; its producer arms it with both CTAs' bytes and
 // both CTAs' loads (.cta_group::2) complete on it.  empty[s] and acc_full[b] live in both
