@@ -22,7 +22,8 @@ from .device import DeviceTensor, to_host_buffer
 from .mps import canonicalize_
 
 __all__ = ["QuantumGate", "QuantumCircuit", "apply_", "bond_evolution", "bond_evolution3",
-           "bond_evolution4", "swap_gate", "move_", "trotter_propagator", "fuse_gates"]
+           "bond_evolution4", "swap_gate", "move_", "trotter_propagator", "fuse_gates",
+           "compute_step_size", "TEBDStepper", "HomogeneousTEBDCache", "make_step_"]
 
 
 class QuantumGate:
@@ -426,3 +427,45 @@ def trotter_propagator(L, dims, bonds, sites=None, tspan=(0.0, 0.01), order=2, s
     for i in range(1, nsteps + 1):
         c.extend(_propagator_impl(terms, ti + i * dt, ti + (i - 1) * dt, p))
     return c
+
+
+# ---------------------------------------------------------------- TEBD time stepping
+def compute_step_size(t, dt):
+    """compute_step_size (algorithms/timeevo.jl:3-9): n = round(|t / dt|) steps (at least
+    one) of size t / n."""
+    n = int(round(abs(t / dt))) or 1
+    return n, t / n
+
+
+class TEBDStepper:
+    """TEBDStepper (algorithms/timeevo.jl:13-33): the span tspan cut into n steps of
+    size stepsize (adjusted to divide it), the Trotter order and the truncation."""
+
+    def __init__(self, stepsize, tspan=None, order=2, trunc=None):
+        ti, tf = tspan if tspan is not None else (0.0, stepsize)
+        self.n, self.stepsize = compute_step_size(tf - ti, stepsize)
+        self.tspan = (ti, tf)
+        self.order = int(order)
+        self.trunc = trunc if trunc is not None else default_truncation()
+
+    @property
+    def delta(self):
+        return self.tspan[1] - self.tspan[0]
+
+
+class HomogeneousTEBDCache:
+    """HomogeousTEBDCache (algorithms/timeevo.jl:88-99) for a constant Hamiltonian given
+    as bond matrices {(i, i+1): h} and site matrices {i: h}: the circuit of n Trotter steps
+    of size stepsize, fused once (fuse_gates of the repeated one-step circuit)."""
+
+    def __init__(self, L, dims, bonds, sites, stepper):
+        one = trotter_propagator(L, dims, bonds, sites, tspan=(0.0, stepper.stepsize),
+                                 order=stepper.order, stepsize=stepper.stepsize)
+        self.circuit = fuse_gates(QuantumCircuit(list(one) * stepper.n))
+        self.stepper = stepper
+
+
+def make_step_(cache, psi, svd="gesvd"):
+    """make_step! (algorithms/timeevo.jl:117-121): the cached circuit applied to psi with
+    the stepper's truncation; returns the truncation error of every gate."""
+    return apply_(cache.circuit, psi, trunc=cache.stepper.trunc, svd=svd)
