@@ -1,6 +1,6 @@
 """fuse_gates (circuit/gate_fusion.jl:357-400) on the host: the fused circuit applies
 the same operator (checked on dense state vectors through the oracle's dense_apply), with
-the gates the reference's absorption order leaves."""
+the gates the reference's absorption order leaves.  The TEBD stepper's step count."""
 
 import numpy as np
 import pytest
@@ -80,3 +80,14 @@ def test_fuse_trotter_circuit_merges_the_half_steps():
     a = apply_dense(circ, psi, L, d)
     b = apply_dense(fused, psi, L, d)
     assert np.linalg.norm(a - b) < 1e-12 * np.linalg.norm(a)
+
+
+def test_tebd_stepper_step_count():
+    """compute_step_size / TEBDStepper (algorithms/timeevo.jl:3-33): the span is cut into
+    round(|span / stepsize|) steps, at least one, and the stepsize adjusted to divide it."""
+    st = fm.TEBDStepper(stepsize=0.03, tspan=(0.0, 0.1))
+    assert st.n == 3 and abs(st.stepsize - 0.1 / 3) < 1e-15 and st.delta == 0.1
+    st = fm.TEBDStepper(stepsize=1.0, tspan=(0.0, 0.2))
+    assert st.n == 1 and st.stepsize == 0.2
+    st = fm.TEBDStepper(stepsize=-0.05j)
+    assert st.n == 1 and st.tspan == (0.0, -0.05j)
