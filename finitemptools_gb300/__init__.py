@@ -17,8 +17,9 @@ from .derivatives import HeffOp, ac2_prime, ac_prime, c_prime, exponentiate  # n
 from .derivatives import simple_lanczos_solver  # noqa: F401
 from .device import DeviceTensor, Handle, default_handle  # noqa: F401
 from .expansion import OptimalExpansion, default_expansion  # noqa: F401
-from .tebd import (HomogeneousTEBDCache, QuantumCircuit, QuantumGate, TEBDStepper,  # noqa: F401
-                   apply_, bond_evolution, fuse_gates, make_step_, move_, trotter_propagator)
+from .tebd import (HomogeneousTEBDCache, InhomogeneousTEBDCache, QuantumCircuit,  # noqa: F401
+                   QuantumGate, TEBDStepper, apply_, bond_evolution, fuse_gates, make_step_,
+                   move_, trotter_propagator)
 from .exactdiag import (ExactFiniteMPS, exact_diagonalization, exact_timeevolution,  # noqa: F401
                         init_h_center, max_bond_dimensions)
 from .excited import (ProjectedExpectationCache, c2_proj, c_proj, init_cstorage_right,  # noqa: F401

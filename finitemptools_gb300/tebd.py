@@ -23,7 +23,8 @@ from .mps import canonicalize_
 
 __all__ = ["QuantumGate", "QuantumCircuit", "apply_", "bond_evolution", "bond_evolution3",
            "bond_evolution4", "swap_gate", "move_", "trotter_propagator", "fuse_gates",
-           "compute_step_size", "TEBDStepper", "HomogeneousTEBDCache", "make_step_"]
+           "compute_step_size", "TEBDStepper", "HomogeneousTEBDCache",
+           "InhomogeneousTEBDCache", "make_step_"]
 
 
 class QuantumGate:
@@ -359,39 +360,52 @@ def apply_(gates, psi, trunc=None, svd="gesvd"):
 
 
 # ------------------------------------------------------------ Trotter circuits
+def _term_at(h, t):
+    """A term's matrix at time t: h(t) for a time-dependent term, h itself otherwise."""
+    return np.asarray(h(t) if callable(h) else h)
+
+
 def _absorb_one_bodies(L, dims, bonds, sites):
     """_absorb_one_bodies (operators/quantumoperator.jl:221-258) on matrices:
     a one-body term of site i < L joins bond (i, i+1) as h (x) 1, the last
-    site's joins (L-1, L) as 1 (x) h (first site fastest)."""
-    out = {k: np.asarray(v) for k, v in bonds.items()}
+    site's joins (L-1, L) as 1 (x) h (first site fastest).  Terms may be
+    functions of time; a sum with one of them is one too."""
+    out = {k: (v if callable(v) else np.asarray(v)) for k, v in bonds.items()}
     for i, h in sites.items():
-        h = np.asarray(h)
         if i < L:
-            key, m = (i, i + 1), np.kron(np.eye(dims[i]), h)
+            key, emb = (i, i + 1), (lambda m, e=np.eye(dims[i]): np.kron(e, m))
         else:
-            key, m = (i - 1, i), np.kron(h, np.eye(dims[i - 2]))
-        out[key] = out[key] + m if key in out else m
+            key, emb = (i - 1, i), (lambda m, e=np.eye(dims[i - 2]): np.kron(m, e))
+        if callable(h) or callable(out.get(key)):
+            prev = out.get(key)
+            out[key] = (lambda t, h=h, prev=prev, emb=emb:
+                        emb(_term_at(h, t)) + (_term_at(prev, t) if prev is not None else 0.0))
+        else:
+            m = emb(np.asarray(h))
+            out[key] = out[key] + m if key in out else m
     return out
 
 
-def _expm_circuit(terms, dt):
-    """_expm(ham, dt) (operators/quantumoperator.jl:198-219): one gate exp(dt h)
+def _expm_circuit(terms, t, dt):
+    """_expm(ham, t, dt) (operators/quantumoperator.jl:198-219): one gate exp(dt h(t))
     per term."""
     import scipy.linalg
-    return QuantumCircuit(QuantumGate(k, scipy.linalg.expm(dt * np.asarray(h)))
+    return QuantumCircuit(QuantumGate(k, scipy.linalg.expm(dt * _term_at(h, t)))
                           for k, h in sorted(terms.items()))
 
 
 def _propagator_2order(terms, tf, ti):
-    """propagator_2order (tebd.jl:131-140): even/odd nearest-neighbour splitting
-    (split_nn_ham, :24-38) or the symmetric generic form."""
+    """propagator_2order (tebd.jl:99-140): even/odd nearest-neighbour splitting
+    (split_nn_ham, :24-38) or the symmetric generic form, the terms taken at the midpoint
+    ti + dt/2."""
     dt = tf - ti
+    tm = ti + dt / 2
     if all(len(k) == 2 and k[1] == k[0] + 1 for k in terms):
         even = {k: v for k, v in terms.items() if k[0] % 2 == 0}
         odd = {k: v for k, v in terms.items() if k[0] % 2 != 0}
-        half = _expm_circuit(even, dt / 2)
-        return QuantumCircuit(list(half) + list(_expm_circuit(odd, dt)) + list(half))
-    tmp = _expm_circuit(terms, dt / 2)
+        half = _expm_circuit(even, tm, dt / 2)
+        return QuantumCircuit(list(half) + list(_expm_circuit(odd, tm, dt)) + list(half))
+    tmp = _expm_circuit(terms, tm, dt / 2)
     return QuantumCircuit(list(tmp) + list(reversed(tmp)))
 
 
@@ -413,8 +427,9 @@ def _propagator_impl(terms, tf, ti, order):
 
 def trotter_propagator(L, dims, bonds, sites=None, tspan=(0.0, 0.01), order=2, stepsize=0.01):
     """trotter_propagator(ham, tspan; order, stepsize) (tebd.jl:171-193) for a
-    time-independent Hamiltonian given as bond matrices {(i, i+1): h} and site
-    matrices {i: h} (fused index first site fastest); gates are exp(dt h)."""
+    Hamiltonian given as bond terms {(i, i+1): h} and site terms {i: h} (fused index
+    first site fastest), each a matrix or a function of t returning one; gates are
+    exp(dt h(t)) with t the midpoint of their second-order step (tebd.jl:99-119)."""
     terms = _absorb_one_bodies(L, dims, bonds, sites or {})
     p = order // 2
     if 2 * p != order:
@@ -462,6 +477,18 @@ class HomogeneousTEBDCache:
         one = trotter_propagator(L, dims, bonds, sites, tspan=(0.0, stepper.stepsize),
                                  order=stepper.order, stepsize=stepper.stepsize)
         self.circuit = fuse_gates(QuantumCircuit(list(one) * stepper.n))
+        self.stepper = stepper
+
+
+class InhomogeneousTEBDCache:
+    """InhomogenousTEBDCache (algorithms/timeevo.jl:124-140) for a time-dependent
+    Hamiltonian (bond and site terms may be functions of t): the fused Trotter circuit of
+    the whole span tspan."""
+
+    def __init__(self, L, dims, bonds, sites, stepper):
+        self.circuit = fuse_gates(trotter_propagator(L, dims, bonds, sites,
+                                                     tspan=stepper.tspan, order=stepper.order,
+                                                     stepsize=stepper.stepsize))
         self.stepper = stepper
 
 

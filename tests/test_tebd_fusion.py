@@ -91,3 +91,62 @@ def test_tebd_stepper_step_count():
     assert st.n == 1 and st.stepsize == 0.2
     st = fm.TEBDStepper(stepsize=-0.05j)
     assert st.n == 1 and st.tspan == (0.0, -0.05j)
+
+
+def test_time_dependent_trotter_and_inhomogeneous_cache():
+    """Bond and site terms as functions of t (the reference takes each second-order step's
+    terms at its midpoint, tebd.jl:99-119): constant functions give the constant circuit
+    bit for bit, and a ramped field h(t) = h0 + a t follows the time-ordered evolution
+    (a product of 4000 midpoint exponentials) to the Trotter error.  The inhomogeneous
+    cache is the fused circuit of the whole span."""
+    import scipy.linalg
+    L, d = 5, 2
+    X = np.array([[0.0, 1.0], [1.0, 0.0]])
+    Z = np.diag([1.0, -1.0])
+    bonds = {(i, i + 1): -np.kron(Z, Z) for i in range(1, L)}
+    c0 = fm.trotter_propagator(L, [d] * L, bonds, {i: -0.7 * X for i in range(1, L + 1)},
+                               tspan=(0.0, 0.2), order=2, stepsize=0.05)
+    c1 = fm.trotter_propagator(L, [d] * L, bonds,
+                               {i: (lambda t: -0.7 * X) for i in range(1, L + 1)},
+                               tspan=(0.0, 0.2), order=2, stepsize=0.05)
+    assert len(c0) == len(c1)
+    assert all(a.positions == b.positions and np.array_equal(a.op, b.op) for a, b in zip(c0, c1))
+
+    def field(t):
+        return -(0.7 + 1.5 * t) * X
+
+    sites = {i: field for i in range(1, L + 1)}
+    T = 0.4
+    stepper = fm.TEBDStepper(stepsize=0.01, tspan=(0.0, T), order=2)
+    cache = fm.InhomogeneousTEBDCache(L, [d] * L, bonds, sites, stepper)
+    circ = fm.trotter_propagator(L, [d] * L, bonds, sites, tspan=(0.0, T), order=2,
+                                 stepsize=0.01)
+    assert len(cache.circuit) < len(circ)
+
+    def dense_H(t):
+        H = np.zeros((d ** L, d ** L))
+        for i in range(1, L):
+            H += kron_sites(L, {i: -Z, i + 1: Z})
+        for i in range(1, L + 1):
+            H += kron_sites(L, {i: field(t)})
+        return H
+
+    rng = np.random.default_rng(8)
+    psi = rng.standard_normal(d ** L)
+    psi /= np.linalg.norm(psi)
+    ref = psi.copy()
+    n = 4000
+    for k in range(n):
+        ref = scipy.linalg.expm((T / n) * dense_H((k + 0.5) * T / n)) @ ref
+    a = apply_dense(cache.circuit, psi, L, d)
+    b = apply_dense(circ, psi, L, d)
+    assert np.linalg.norm(a - b) < 1e-12 * np.linalg.norm(b)
+    assert np.linalg.norm(a - ref) < 1e-3 * np.linalg.norm(ref)
+
+
+def kron_sites(L, ops):
+    """The operator with ops[i] on site i (1-based), first site fastest."""
+    m = np.ones((1, 1))
+    for i in range(L, 0, -1):
+        m = np.kron(m, ops.get(i, np.eye(2)))
+    return m
