@@ -827,7 +827,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--D", type=int, default=2048)
-    ap.add_argument("--precision", default="bf16", choices=["fp64", "tf32x3", "tf32", "bf16"])
+    ap.add_argument("--precision", default="fp64_tc",
+                    choices=["fp64_tc", "fp64", "tf32x3", "tf32", "bf16"])
     ap.add_argument("--no-table", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-dmrg", action="store_true")
@@ -986,7 +987,7 @@ def main():
             xt, Lt, Rt, Wt = workload(Dt, seed=7)
             xdt, Ldt, Rdt = DT.from_numpy(xt, h), DT.from_numpy(Lt, h), DT.from_numpy(Rt, h)
             ref = None
-            for p in ("fp64", "tf32x3", "tf32", "bf16"):
+            for p in ("fp64", "fp64_tc", "tf32x3", "tf32", "bf16"):
                 opt = fm.HeffOp("ac2", Ldt, Rdt, W1=Wt, W2=Wt, precision=p)
                 yt = opt(xdt)
                 reps = 2 if (p == "fp64" and Dt >= 1024) else 5
@@ -1039,7 +1040,8 @@ def main():
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": tot_ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": prec, "data": "synthetic",
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if prec in ("fp64", "fp64_tc") else prec, "data": "synthetic",
             "config": config_dict(args, prec), "clocks": clocks, "e2e": e2e,
             "gpu_launches": n_launch, "roofline": roof, "cpu_baseline": cpu,
             "per_dtype": table, "dmrg": dmrg, "u1": u1, "tdvp_gradient": tgrad,

@@ -20,7 +20,7 @@ dptr = c_void_p        # device pointer
 hptr = c_void_p        # host pointer
 
 F64, C128 = 0, 1
-PREC = {"fp64": 0, "tf32x3": 1, "tf32": 2, "bf16": 3}
+PREC = {"fp64": 0, "tf32x3": 1, "tf32": 2, "bf16": 3, "fp64_tc": 4}
 TRANS = {"N": 0, "T": 1, "C": 2, "R": 3}
 
 
@@ -89,6 +89,7 @@ SIGNATURES = {
     "fmpt_op_set_projectors": (c_int, [c_void_p, c_int, P(c_void_p)]),
     "fmpt_set_svd_method": (c_int, [c_void_p, c_int]),
     "fmpt_set_tc_tile": (c_int, [c_void_p, c_int]),
+    "fmpt_set_f64_engine": (c_int, [c_void_p, c_int]),
     "fmpt_ac2_prime_host": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p,
                                     c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_int,
                                     c_int, c_int, c_int]),

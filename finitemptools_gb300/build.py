@@ -47,7 +47,7 @@ def _digest(paths):
 def build(force=False, verbose=False):
     """Compile and link libfmpt.so; returns its path."""
     srcs = _sources()
-    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".h")]
+    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     headers.append(os.path.join(INCLUDE, "fmpt.h"))
     stamp = os.path.join(BUILD_DIR, "stamp")
     dig = _digest(srcs + sorted(headers))

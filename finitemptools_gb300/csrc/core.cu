@@ -348,6 +348,7 @@ int fmpt_destroy(fmpt_handle* h) {
   for (auto& kv : h->arnoldi_exec) cudaGraphExecDestroy(kv.second);
   if (h->gemm_ws) cudaFree(h->gemm_ws);
   if (h->tc_ws) cudaFree(h->tc_ws);
+  if (h->oz_ws) cudaFree(h->oz_ws);
   if (h->gstatus) cudaFree(h->gstatus);
   if (h->pinned) cudaFreeHost(h->pinned);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
@@ -384,6 +385,13 @@ int fmpt_set_tc_tile(fmpt_handle* h, int mode) {
   if (!h) return FMPT_ERR_ARG;
   if (mode < 0 || mode > 1) return set_error(h, FMPT_ERR_ARG, "tc tile mode must be 0 or 1");
   h->tc_tile = mode;
+  return FMPT_OK;
+}
+
+int fmpt_set_f64_engine(fmpt_handle* h, int mode) {
+  if (!h) return FMPT_ERR_ARG;
+  if (mode < 0 || mode > 1) return set_error(h, FMPT_ERR_ARG, "f64 engine mode must be 0 or 1");
+  h->f64_tc = mode;
   return FMPT_OK;
 }
 

@@ -234,6 +234,12 @@ int gemm_f64(fmpt_handle* h, const GemmArgs& g) {
     return set_error(h, FMPT_ERR_SHAPE, "gemm: negative extent");
   if (g.m == 0 || g.n == 0) return FMPT_OK;
   if (g.k == 0 && g.beta[0] == 1.0 && g.beta[1] == 0.0) return FMPT_OK;
+  if (g.k > 0 && !g.nosplit && gemm_f64_ozaki_possible(h, g)) {
+    const int st = gemm_f64_ozaki(h, g);
+    // FMPT_ERR_UNSUPPORTED: nothing launched (no cluster fits, or its workspace would have
+    // to grow inside a stream capture); the CUDA-core kernel runs instead
+    if (st != FMPT_ERR_UNSUPPORTED) return st;
+  }
   return g.cplx ? launch<true>(h, g) : launch<false>(h, g);
 }
 

@@ -456,7 +456,8 @@ int gp_check_status(fmpt_handle* h) {
   if (v != 0) {
     FMPT_CUDA(h, cudaMemsetAsync(h->gstatus, 0, sizeof(int), h->stream));
     return set_error(h, FMPT_ERR_TIMEOUT,
-                     "grouped block-sparse launch: a grid barrier timed out (results invalid)");
+                     "a bounded device wait timed out (grouped block-sparse launch or FP64 "
+                     "tensor-core GEMM; results invalid)");
   }
   return FMPT_OK;
 }

@@ -120,6 +120,12 @@ int set_error(fmpt_handle* h, int status, const char* fmt, ...) {
 int schedule_ac2(fmpt_handle* h, int cplx, const double* W1, const double* W2, int d1, int d2,
                  int wl, int wm, int wr, MidSchedule& s) {
   if (!W1 || !W2) return set_error(h, FMPT_ERR_ARG, "ac2: null MPO tensor");
+  schedule_ac2_host(cplx, W1, W2, d1, d2, wl, wm, wr, s);
+  return mid_upload(h, s);
+}
+
+void schedule_ac2_host(int cplx, const double* W1, const double* W2, int d1, int d2, int wl,
+                       int wm, int wr, MidSchedule& s) {
   const int P = d1 * d2;
   const int64_t n1 = (int64_t)wl * d1 * wm * d1, n2 = (int64_t)wm * d2 * wr * d2;
   std::vector<C2> O((size_t)wl * wr * P * P, C2{0, 0});
@@ -141,7 +147,6 @@ int schedule_ac2(fmpt_handle* h, int cplx, const double* W1, const double* W2, i
               }
           }
   build_schedule(cplx, wl, wr, P, P, O, s);
-  return mid_upload(h, s);
 }
 
 int schedule_ac(fmpt_handle* h, int cplx, const double* W, int d, int wl, int wr,
@@ -236,6 +241,12 @@ static GemmArgs gemm_args(int cplx, int ta, int tb, int m, int n, int k, const d
 
 int op_apply_fp64(fmpt_op* op, const double* x, double* y) {
   fmpt_handle* h = op->h;
+  // FP64_TC: the GEMMs go to the tensor-core FP64 engine wherever it is faster
+  const int eng = op->precision == FMPT_PREC_FP64_TC ? 1 : 0;
+  auto gemm_f64 = [&](fmpt_handle* hh, GemmArgs g) {
+    g.engine = eng;
+    return fmpt::gemm_f64(hh, g);
+  };
   const int cp = op->dtype == FMPT_C128;
   const int Dl = op->Dl, Dr = op->Dr;
   const size_t es = sizeof(double) * (cp ? 2 : 1);
@@ -285,7 +296,7 @@ static int check_dtype_prec(fmpt_handle* h, int dtype, int precision) {
   if (!h) return FMPT_ERR_ARG;
   if (dtype != FMPT_F64 && dtype != FMPT_C128)
     return set_error(h, FMPT_ERR_ARG, "unknown dtype %d", dtype);
-  if (precision < FMPT_PREC_FP64 || precision > FMPT_PREC_BF16)
+  if (precision < FMPT_PREC_FP64 || precision > FMPT_PREC_FP64_TC)
     return set_error(h, FMPT_ERR_ARG, "unknown precision %d", precision);
   return FMPT_OK;
 }
@@ -302,7 +313,7 @@ static int make_op(fmpt_handle* h, int kind, int dtype, int precision, const dou
   op->h = h; op->kind = kind; op->dtype = dtype; op->precision = precision;
   op->Dl = Dl; op->Dr = Dr; op->d1 = d1; op->d2 = d2; op->wl = wl; op->wm = wm; op->wr = wr;
   op->hleft = hleft; op->hright = hright;
-  op->defer_right = defer_right && precision != FMPT_PREC_FP64 && dtype == FMPT_F64 && kind == 0;
+  op->defer_right = defer_right && !prec_is_f64(precision) && dtype == FMPT_F64 && kind == 0;
   const int cp = dtype == FMPT_C128;
   int st = FMPT_OK;
   if (kind == 0) {
@@ -315,7 +326,7 @@ static int make_op(fmpt_handle* h, int kind, int dtype, int precision, const dou
   } else {
     op->n = (int64_t)Dl * Dr;
   }
-  if (st == FMPT_OK && precision != FMPT_PREC_FP64) st = op_tc_prepare(op);
+  if (st == FMPT_OK && !prec_is_f64(precision)) st = op_tc_prepare(op);
   if (st != FMPT_OK) {
     fmpt_op_destroy(op);
     return st;
@@ -348,7 +359,7 @@ int fmpt_op_apply(fmpt_op* op, const double* x, double* y) {
   if (!x || !y) return set_error(op->h, FMPT_ERR_ARG, "op_apply: null vector");
   if (op->u1) {
     FMPT_TRY(op_u1_apply(op, x, y));
-  } else if (op->precision != FMPT_PREC_FP64) {
+  } else if (!prec_is_f64(op->precision)) {
     FMPT_TRY(op_tc_apply(op, x, y));
   } else {
     FMPT_TRY(op_apply_fp64(op, x, y));
@@ -398,7 +409,7 @@ int fmpt_ac2_prime_host(fmpt_handle* h, int dtype, int precision, const double* 
   FMPT_TRY(dR.alloc(h, bR));
   FMPT_TRY(dy.alloc(h, bx));
   cudaStream_t ms = h->stream;
-  const bool pipeline = precision != FMPT_PREC_FP64 && dtype == FMPT_F64;
+  const bool pipeline = !prec_is_f64(precision) && dtype == FMPT_F64;
   if (!pipeline) {
     FMPT_CUDA(h, cudaMemcpyAsync(dx.p, x, bx, cudaMemcpyHostToDevice, ms));
     FMPT_CUDA(h, cudaMemcpyAsync(dL.p, hleft, bL, cudaMemcpyHostToDevice, ms));
@@ -502,10 +513,15 @@ int fmpt_updateleft(fmpt_handle* h, int dtype, int precision, const double* hold
     return set_error(h, FMPT_ERR_SHAPE, "updateleft: non-positive dimension");
   if (!W && wl != wr) return set_error(h, FMPT_ERR_SHAPE, "overlap update needs wl == wr");
   const int cp = dtype == FMPT_C128;
-  if (precision != FMPT_PREC_FP64) {
+  if (!prec_is_f64(precision)) {
     if (cp) return set_error(h, FMPT_ERR_UNSUPPORTED, "mixed precision: complex environments");
     return env_update_tc(h, false, precision, hold, A, W, B, hnew, Dl, d, Dr, wl, wr);
   }
+  const int eng = precision == FMPT_PREC_FP64_TC ? 1 : 0;
+  auto gemm_f64 = [&](fmpt_handle* hh, GemmArgs g) {
+    g.engine = eng;
+    return fmpt::gemm_f64(hh, g);
+  };
   MidSchedule s;
   FMPT_TRY(schedule_env(h, cp, W, d, wl, wr, false, s));
   const int64_t nT = (int64_t)Dl * wl * d * Dr, nU = (int64_t)Dl * d * wr * Dr;
@@ -538,10 +554,15 @@ int fmpt_updateright(fmpt_handle* h, int dtype, int precision, const double* hol
     return set_error(h, FMPT_ERR_SHAPE, "updateright: non-positive dimension");
   if (!W && wl != wr) return set_error(h, FMPT_ERR_SHAPE, "overlap update needs wl == wr");
   const int cp = dtype == FMPT_C128;
-  if (precision != FMPT_PREC_FP64) {
+  if (!prec_is_f64(precision)) {
     if (cp) return set_error(h, FMPT_ERR_UNSUPPORTED, "mixed precision: complex environments");
     return env_update_tc(h, true, precision, hold, A, W, B, hnew, Dl, d, Dr, wl, wr);
   }
+  const int eng = precision == FMPT_PREC_FP64_TC ? 1 : 0;
+  auto gemm_f64 = [&](fmpt_handle* hh, GemmArgs g) {
+    g.engine = eng;
+    return fmpt::gemm_f64(hh, g);
+  };
   MidSchedule s;
   FMPT_TRY(schedule_env(h, cp, W, d, wl, wr, true, s));
   const int64_t nT = (int64_t)Dl * d * Dr * wr, nU = (int64_t)wl * Dl * d * Dr;

@@ -46,6 +46,12 @@ struct fmpt_handle {
   // partial tiles and arrival counters of the BF16 pair GEMM's K-split last round
   void* tc_ws = nullptr;
   size_t tc_ws_bytes = 0;
+  // FP64 GEMMs on the BF16 tensor cores (Ozaki digit planes, exponents, split pieces):
+  // f64_tc 1 routes every FP64 GEMM of this handle there when its cost model says it is
+  // faster than the CUDA-core kernel (fmpt_set_f64_engine)
+  int f64_tc = 0;
+  void* oz_ws = nullptr;
+  size_t oz_ws_bytes = 0;
   // executable graphs of the captured Arnoldi basis, one per operator structure
   std::map<std::string, cudaGraphExec_t> arnoldi_exec;
   cudaGraphExec_t lanczos_exec = nullptr;   // reused through cudaGraphExecUpdate
@@ -132,8 +138,19 @@ struct GemmArgs {
   int batch;                // batched over blockIdx.z with the strides below
   int64_t strideA, strideB, strideC;
   int nosplit;              // 1: never split K (no workspace allocation)
+  int engine;               // 0: the handle's FP64 engine, 1: tensor cores where faster
 };
 int gemm_f64(fmpt_handle* h, const GemmArgs& g);
+// the Ozaki-scheme FP64 GEMM on the BF16 tensor cores (ozaki.cu): whether it applies to g
+// (engine requested, shape large enough to win), and the call itself
+int gemm_f64_ozaki_possible(fmpt_handle* h, const GemmArgs& g);
+int gemm_f64_ozaki(fmpt_handle* h, const GemmArgs& g);
+// the handle's device status word (1: a bounded device wait timed out), read and cleared by
+// gp_check_status / fmpt_synchronize
+int gp_status_word(fmpt_handle* h, int** out);
+inline bool prec_is_f64(int precision) {
+  return precision == FMPT_PREC_FP64 || precision == FMPT_PREC_FP64_TC;
+}
 
 // -------- block-sparse MPO "middle" contraction (heff.cu)
 // out[o1, o2, wo, so] = sum_{blocks (wi -> wo)} sum_si coef[so, si] in[o1, o2, wi, si]
@@ -157,6 +174,9 @@ int mid_apply(fmpt_handle* h, const MidSchedule& s, const double* in, int64_t pl
 // Schedules from dense host MPO tensors (W[wl, s_out, wr, s_in]).
 int schedule_ac2(fmpt_handle* h, int cplx, const double* W1, const double* W2, int d1, int d2,
                  int wl, int wm, int wr, MidSchedule& s);
+// the host part of schedule_ac2: fills s.blk_win / s.wout_start / s.coef, uploads nothing
+void schedule_ac2_host(int cplx, const double* W1, const double* W2, int d1, int d2, int wl,
+                       int wm, int wr, MidSchedule& s);
 int schedule_ac(fmpt_handle* h, int cplx, const double* W, int d, int wl, int wr, MidSchedule& s);
 // updateright maps the right index w2 (input) to the left index w (output)
 int schedule_env(fmpt_handle* h, int cplx, const double* W, int d, int wl, int wr, bool right,

@@ -1073,7 +1073,7 @@ int fmpt_lanczos_ground(fmpt_op* op, const double* x0, int kmax, double btol, in
                                h->stream));
   FMPT_CUDA(h, cudaStreamSynchronize(h->stream));
   *eigval = h->pinned[0];
-  if (op->precision != FMPT_PREC_FP64) FMPT_TRY(op_tc_check(op));
+  if (!prec_is_f64(op->precision)) FMPT_TRY(op_tc_check(op));
   if (op->u1) FMPT_TRY(gp_check_status(op->h));
   if (info) *info = inf;
   if (niter) *niter = k;
@@ -1185,7 +1185,7 @@ int fmpt_exponentiate(fmpt_op* op, double t_re, double t_im, const double* x, do
                                h->stream));
   scale_by<<<G, KT, 0, h->stream>>>(nr, xout, acc.d());
   FMPT_LAUNCHED(h);
-  if (op->precision != FMPT_PREC_FP64) FMPT_TRY(op_tc_check(op));
+  if (!prec_is_f64(op->precision)) FMPT_TRY(op_tc_check(op));
   if (op->u1) FMPT_TRY(gp_check_status(op->h));
   if (info) *info = steps;
   return FMPT_OK;
@@ -1274,7 +1274,7 @@ int fmpt_expm_nodes(fmpt_op* op, double t_re, double t_im, const double* x, int 
       e = std::max(e, hlast * std::hypot(h->pinned[2 * q], h->pinned[2 * q + 1]));
   }
   if (err_est) *err_est = e;
-  if (op->precision != FMPT_PREC_FP64) FMPT_TRY(op_tc_check(op));
+  if (!prec_is_f64(op->precision)) FMPT_TRY(op_tc_check(op));
   if (op->u1) FMPT_TRY(gp_check_status(op->h));
   return FMPT_OK;
 }

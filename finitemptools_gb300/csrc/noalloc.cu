@@ -1,17 +1,18 @@
 // Allocation-free variant of the plain FP64 two-site H_eff*x.
 //
-// Who needs it: callers that must not allocate device memory while they
-// run -- code issuing work inside a CUDA stream capture (cudaMalloc is not
-// capturable), applications whose own memory manager owns all device memory,
-// or drivers that run with a fixed memory budget.  The ordinary
-// fmpt_ac2_prime takes its intermediates (T1, T3) and its MPO block table
-// from the stream-ordered pool; this entry point takes them from one
+// Who needs it: callers that must not allocate device memory while they run --
+// applications whose own memory manager owns all device memory (a framework's caching
+// allocator, an embedding host that hands the library a fixed arena), and drivers that
+// run under a fixed memory budget, where a pool allocation in the middle of a solve can
+// fail or stall.  The ordinary fmpt_ac2_prime takes its intermediates (T1, T3) and its
+// MPO block table from the stream-ordered pool; this entry point takes them from one
 // file-scope device array instead, so the call itself allocates nothing.
 //
-// The array is FMPT_NOALLOC_SCRATCH_BYTES (64 MiB) and every GPU that loads
-// the library holds it until the process exits.  All calls share it and it
-// keeps the last call's contents; calls that overlap on the GPU (two streams,
-// two host threads) race on it, so the caller must serialise them.
+// The array is FMPT_NOALLOC_SCRATCH_BYTES (64 MiB) and every GPU that loads the library
+// holds it until the process exits.  All calls share it and it keeps the last call's
+// contents; calls that overlap on the GPU (two streams, two host threads) race on it, so
+// the caller must serialise them.
+#include <algorithm>
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -52,7 +53,27 @@ int scratch_for_current_device(fmpt_handle* h, double** out) {
   return FMPT_OK;
 }
 
-struct Cplx { double r, i; };
+// A piece of the block table passed by value to table_put.
+constexpr int kChunkWords = 960;   // 3840 bytes: within the classic 4 KB parameter space
+struct TableChunk {
+  uint32_t w[kChunkWords];
+};
+
+__global__ void table_put(TableChunk c, int n, uint32_t* __restrict__ dst) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = c.w[i];
+}
+
+// n 32-bit words from host memory to dst (scratch) through kernel parameters
+int upload_words(fmpt_handle* h, const uint32_t* src, size_t n, uint32_t* dst) {
+  for (size_t o = 0; o < n; o += kChunkWords) {
+    const int k = (int)std::min<size_t>(kChunkWords, n - o);
+    TableChunk c;
+    std::memcpy(c.w, src + o, (size_t)k * sizeof(uint32_t));
+    table_put<<<1, 256, 0, h->stream>>>(c, k, dst + o);
+    FMPT_LAUNCHED(h);
+  }
+  return FMPT_OK;
+}
 
 }  // namespace
 }  // namespace fmpt
@@ -75,44 +96,12 @@ extern "C" int fmpt_ac2_prime_noalloc(fmpt_handle* h, int dtype, const double* x
   if (P > 16)
     return set_error(h, FMPT_ERR_UNSUPPORTED, "noalloc: physical dimension product %d > 16", P);
 
-  // ---- MPO block table of the two-site MPO (host), same rule as the pooled path:
-  // O[w -> w2][s', s] = sum_m W1[w, s1', m, s1] W2[m, s2', w2, s2]
-  const int64_t n1 = (int64_t)wl * d1 * wm * d1, n2 = (int64_t)wm * d2 * wr * d2;
-  std::vector<Cplx> O((size_t)wl * wr * P * P, Cplx{0, 0});
-  for (int w = 0; w < wl; w++)
-    for (int w2 = 0; w2 < wr; w2++)
-      for (int m = 0; m < wm; m++)
-        for (int a1 = 0; a1 < d1; a1++)
-          for (int b1 = 0; b1 < d1; b1++) {
-            const int64_t i1 = w + (int64_t)wl * (a1 + d1 * (m + (int64_t)wm * b1));
-            const Cplx u{W1[i1], cp ? W1[n1 + i1] : 0.0};
-            if (u.r == 0.0 && u.i == 0.0) continue;
-            for (int a2 = 0; a2 < d2; a2++)
-              for (int b2 = 0; b2 < d2; b2++) {
-                const int64_t i2 = m + (int64_t)wm * (a2 + d2 * (w2 + (int64_t)wr * b2));
-                const Cplx v{W2[i2], cp ? W2[n2 + i2] : 0.0};
-                if (v.r == 0.0 && v.i == 0.0) continue;
-                Cplx& o = O[(((size_t)w * wr + w2) * P + a1 + d1 * a2) * P + b1 + d1 * b2];
-                o.r += u.r * v.r - u.i * v.i;
-                o.i += u.r * v.i + u.i * v.r;
-              }
-          }
-  std::vector<int> win, wstart(wr + 1, 0);
-  std::vector<double> coef;
-  for (int wo = 0; wo < wr; wo++) {
-    wstart[wo] = (int)win.size();
-    for (int wi = 0; wi < wl; wi++) {
-      const Cplx* blk = &O[((size_t)wi * wr + wo) * P * P];
-      bool nz = false;
-      for (int q = 0; q < P * P; q++) nz |= (blk[q].r != 0.0 || blk[q].i != 0.0);
-      if (!nz) continue;
-      win.push_back(wi);
-      for (int q = 0; q < P * P; q++) coef.push_back(blk[q].r);
-      if (cp)
-        for (int q = 0; q < P * P; q++) coef.push_back(blk[q].i);
-    }
-  }
-  wstart[wr] = (int)win.size();
+  // ---- MPO block table of the two-site MPO (host): the builder of fmpt_ac2_prime
+  MidSchedule sched;
+  schedule_ac2_host(cp, W1, W2, d1, d2, wl, wm, wr, sched);
+  const std::vector<int>& win = sched.blk_win;
+  const std::vector<int>& wstart = sched.wout_start;
+  const std::vector<double>& coef = sched.coef;
 
   // ---- scratch layout (doubles): [ table | T1 | T3 ], every part 256-byte aligned
   auto up32 = [](size_t n) { return (n + 31) / 32 * 32; };
@@ -133,21 +122,16 @@ extern "C" int fmpt_ac2_prime_noalloc(fmpt_handle* h, int dtype, const double* x
   double* d_coef = base + t_int;
   double* T1 = d_coef + t_coef;
   double* T3 = T1 + s1;
-  // The table is the only part that must hold defined values before the
-  // kernels run; T1 and T3 are written in full (GEMM with beta = 0, every
-  // output block of the MPO step) before they are read, so nothing is cleared.
-  // Pageable-source copies return once the source is staged: the host
-  // vectors may go out of scope afterwards.
-  if (!win.empty())
-    FMPT_CUDA(h, cudaMemcpyAsync(d_win, win.data(), win.size() * sizeof(int),
-                                 cudaMemcpyHostToDevice, h->stream));
-  FMPT_CUDA(h, cudaMemcpyAsync(d_wstart, wstart.data(), wstart.size() * sizeof(int),
-                               cudaMemcpyHostToDevice, h->stream));
-  if (!coef.empty())
-    FMPT_CUDA(h, cudaMemcpyAsync(d_coef, coef.data(), coef.size() * sizeof(double),
-                                 cudaMemcpyHostToDevice, h->stream));
-  MidSchedule sched;
-  sched.nw_in = wl; sched.nw_out = wr; sched.p_in = P; sched.p_out = P; sched.cplx = cp;
+  // The table is the only part that must hold defined values before the kernels run; T1
+  // and T3 are written in full (GEMM with beta = 0, every output block of the MPO step)
+  // before they are read, so nothing is cleared.  The table reaches the device as kernel
+  // parameters (by value, in pieces of TableChunk), not through a host-memory copy.
+  FMPT_TRY(upload_words(h, reinterpret_cast<const uint32_t*>(win.data()), win.size(),
+                        reinterpret_cast<uint32_t*>(d_win)));
+  FMPT_TRY(upload_words(h, reinterpret_cast<const uint32_t*>(wstart.data()), wstart.size(),
+                        reinterpret_cast<uint32_t*>(d_wstart)));
+  FMPT_TRY(upload_words(h, reinterpret_cast<const uint32_t*>(coef.data()), coef.size() * 2,
+                        reinterpret_cast<uint32_t*>(d_coef)));
   sched.d_win = d_win; sched.d_wstart = d_wstart; sched.d_coef = d_coef;
 
   // ---- the three steps of the plain form (the same kernels as fmpt_ac2_prime)

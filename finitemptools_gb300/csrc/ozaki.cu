@@ -1,0 +1,725 @@
+// FP64-accurate GEMM on the BF16 tensor cores (Ozaki scheme).
+//
+// GB300 runs FP64 on the CUDA cores at about 2 DFMA per clock per SM (~1.2 TFLOP/s for
+// the whole chip) while its BF16 tensor cores run three orders of magnitude faster.  The
+// plain-FP64 contractions therefore go through the error-free splitting of Ozaki, Ogita,
+// Oishi and Rump (Numer. Algorithms 59, 2012):
+//
+//   1. every row r of op(A) (and every column n of op(B)) gets an exponent e with
+//      max |row| < 2^e, and its entries become NS = 9 balanced base-64 digits,
+//        X(r, k) = sum_i sigma_i(r, k) 2^(e_r - 6 i),   sigma_i integer, |sigma_i| <= 64,
+//      exact to 2^(e_r - 54) (54 bits: every FP64 entry within 2^-1 of its row maximum is
+//      represented exactly); the digits are computed with integer arithmetic on the FP64
+//      bit pattern (no FP64 instruction), and each one is an exact BF16 value;
+//   2. the digit planes are multiplied on the tensor cores (tcgen05.mma kind::f16, BF16 x
+//      BF16 -> FP32).  All products sigma_i tau_j with the same level l = i + j carry the
+//      same scale 2^(e_r + e_n - 6 l), so they share one TMEM accumulator; the 45 products
+//      with l <= NS + 1 are formed (the rest lie below 2^-54 of the row and column maxima);
+//   3. a level accumulator is an integer sum.  Its terms are bounded by 64 * 64 (l = 2) up to
+//      2 * 64 * 32 + (l - 3) * 32 * 32 (l > 2), so over a K-chunk of KC = 1024 it stays below
+//      2^24 and FP32 accumulation is exact.  After each (chunk, level) the epilogue warps add
+//      the accumulator, scaled by 2^(e_r + e_n - 6 l) (built in the FP64 exponent field with
+//      integer operations), into the FP64 output.
+//
+// The result is op(A) op(B) to about 2^-53 relative to max|row| * max|column| per term:
+// the accuracy class of an FP64 GEMM even for rows whose entries span a few decades
+// (8 digits, 48 bits, measured 6e-13 on rows spanning e^+-3), at 45 BF16 MMAs per FP64
+// multiply-add.  Complex operands use the real embedding [Re -Im; Im Re] x [Re; Im].
+//
+// Kernels: oz_slice (FP64 operand -> exponents + 8 K-major BF16 digit planes, one pass
+// for the row maxima and one for the digits over a 32-row strip), oz_gemm_pair (the CTA
+// pair tcgen05 kernel of tc_gemm.cu with the (chunk, level, product) sequence and the
+// FP64 epilogue), oz_reduce (sums split pieces in a fixed order, applies alpha / beta).
+#include <algorithm>
+#include <cmath>
+
+#include "tc_ptx.cuh"
+
+namespace fmpt {
+namespace oz {
+
+using namespace tc;
+
+constexpr int NS = 9;                 // digits per entry
+constexpr int SB = 6;                 // bits per digit
+constexpr int NLEV = NS;              // levels 2 .. NS + 1
+constexpr int NPROD = NS * (NS + 1) / 2;
+constexpr int STAGES = 6;
+constexpr int KELEMS = 64;            // BF16 elements per 128-byte K slice
+constexpr int KC_SLICES = 16;         // K slices per exactness chunk (KC = 1024)
+constexpr int E_BAD = 1 << 20;        // exponent of a row or column holding Inf / NaN
+constexpr int TILE = 256;             // pair tile edge
+
+// Level sets of the pieces a tile's work is cut into (variant v: 1, 3 or 5 pieces; level l
+// holds l - 1 digit products): the order the kernel visits the levels of a piece, and the
+// piece boundaries in it.  Long and short groups alternate, so the epilogue's drain of one
+// level overlaps the MMAs of the next.
+constexpr int NVAR = 3;
+__constant__ int kOrder[NVAR][NLEV] = {{10, 2, 6, 9, 3, 5, 8, 4, 7},
+                                       {10, 2, 6, 9, 3, 5, 8, 4, 7},    // 15, 14, 16 products
+                                       {10, 2, 9, 3, 8, 4, 7, 5, 6}};   // 10, 10, 10, 10, 5
+__constant__ int kSetStart[NVAR][6] = {{0, 9}, {0, 3, 6, 9}, {0, 2, 4, 6, 8, 9}};
+constexpr int kVarPieces[NVAR] = {1, 3, 5};
+constexpr int kVarMaxProducts[NVAR] = {45, 16, 10};
+static_assert(kVarMaxProducts[0] == NPROD, "one piece holds every digit product");
+
+// ------------------------------------------------------------ digit planes
+// op(X)(r, c) of a GEMM operand, real index space: X[r * sr + c * sc] (+ batch stride).
+// Complex operands are embedded as real matrices with doubled extents: the A side as
+// rows [Re, -Im] over [Im, Re], the B side (rows = output columns) as [Re, Im].
+struct SliceSrc {
+  const double* p;
+  int64_t plane;        // offset of the imaginary plane
+  int64_t sr, sc;       // element strides of row and column index
+  int64_t bstride;      // batch stride
+  int rows, cols;       // real extents of op(X)
+  int cplx, role, conj; // role 0: A side, 1: B side
+};
+
+__device__ __forceinline__ uint64_t src_bits(const SliceSrc& s, int z, int r2, int c2) {
+  int r = r2, c = c2, hr = 0, hc = 0;
+  if (s.cplx) {
+    if (s.role == 0 && r >= s.rows) { r -= s.rows; hr = 1; }
+    if (c >= s.cols) { c -= s.cols; hc = 1; }
+  }
+  // the imaginary part sits at (hr, hc) = (0, 1) with a minus sign and at (1, 0) on the
+  // A side, at hc = 1 on the B side; conj flips its sign once more
+  bool im = false, neg = false;
+  if (s.cplx) {
+    if (s.role == 0) {
+      im = hr != hc;
+      neg = hr == 0 && hc == 1;
+    } else {
+      im = hc == 1;
+    }
+    if (im && s.conj) neg = !neg;
+  }
+  const double* b = s.p + (int64_t)z * s.bstride + (int64_t)r * s.sr + (int64_t)c * s.sc;
+  uint64_t v = (uint64_t)__double_as_longlong(__ldg(b + (im ? s.plane : 0)));
+  if (neg) v ^= 0x8000000000000000ull;
+  return v;
+}
+
+// bf16 bits of an integer |k| <= 64
+__device__ __forceinline__ uint32_t int_bf16(int k) {
+  if (k == 0) return 0u;
+  const uint32_t s = k < 0 ? 0x8000u : 0u;
+  const uint32_t a = (uint32_t)(k < 0 ? -k : k);
+  const int p = 31 - __clz(a);                                  // a in [2^p, 2^(p+1))
+  return s | ((uint32_t)(127 + p) << 7) | ((a << (7 - p)) & 0x7fu);
+}
+
+// One block: 32 rows of one batch entry.  Pass 1: row maxima of |X| on the bit patterns
+// (the order of non-negative IEEE doubles is that of their bits).  Pass 2: digits.
+// S[(z NS + i) rows_out + r][ldk] (K-major BF16 planes), E[z rows_out + r].
+__global__ void __launch_bounds__(256) oz_slice(SliceSrc src, int rows_out, int k_out, int ldk,
+                                                uint16_t* __restrict__ S, int* __restrict__ E) {
+  __shared__ uint64_t tile[32][65];
+  const int r0 = blockIdx.x * 32, z = blockIdx.y;
+  const int t = threadIdx.x, rr = t >> 3, part = t & 7;
+  const bool rowfast = src.sr == 1;
+  auto load = [&](int c0) {
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      const int e = t + 256 * q;
+      int lr, lc;
+      if (rowfast) { lr = e & 31; lc = e >> 5; } else { lc = e & 63; lr = e >> 6; }
+      const int r = r0 + lr, c = c0 + lc;
+      tile[lr][lc] = (r < rows_out && c < k_out) ? src_bits(src, z, r, c) : 0ull;
+    }
+  };
+  uint64_t mx = 0;
+  for (int c0 = 0; c0 < k_out; c0 += 64) {
+    load(c0);
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      const uint64_t a = tile[rr][part * 8 + q] & 0x7fffffffffffffffull;
+      mx = a > mx ? a : mx;
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int o = 1; o < 8; o <<= 1) {
+    const uint64_t y = __shfl_xor_sync(0xffffffffu, mx, o);
+    mx = y > mx ? y : mx;
+  }
+  const int exm = (int)(mx >> 52);
+  const bool bad = exm == 0x7ff;
+  // max |row| = f 2^e with f in [0.5, 1): e = exm - 1022 for normal numbers; the
+  // subnormal exponent field 0 behaves as 1 with no implicit bit (then max < 2^-1021)
+  const int e = mx == 0 ? 0 : (exm == 0 ? -1021 : exm - 1022);
+  const int r = r0 + rr;
+  if (part == 0 && r < rows_out) E[(int64_t)z * rows_out + r] = bad ? E_BAD : e;
+  const int64_t plane_stride = (int64_t)rows_out * ldk;
+  uint16_t* out = S + ((int64_t)z * NS * rows_out + r) * ldk;
+  for (int c0 = 0; c0 < ldk; c0 += 64) {
+    load(c0);
+    __syncthreads();
+    const int cb = c0 + part * 8;
+    if (r < rows_out && cb < ldk) {
+      uint32_t pk[NS][4];
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        const uint64_t bits = bad ? 0ull : tile[rr][part * 8 + q];
+        const int ex = (int)((bits >> 52) & 0x7ff);
+        int64_t M = (int64_t)(bits & 0xfffffffffffffull);
+        if (ex) M |= (int64_t)1 << 52;
+        // N = X 2^(54 - e) as an integer: |N| < 2^54; shift = max(ex, 1) - 1075 + 54 - e
+        const int sh = (ex ? ex : 1) - 1021 - e;
+        int64_t N;
+        if (sh >= 0) N = M << sh;                         // sh <= 1
+        else N = sh <= -63 ? 0 : (M >> (-sh));
+        if (bits >> 63) N = -N;
+#pragma unroll
+        for (int i = 0; i < NS; i++) {
+          const int s = 54 - SB * (i + 1);
+          int64_t d;
+          if (s > 0) {
+            d = (N + ((int64_t)1 << (s - 1))) >> s;   // nearest, ties up
+            N -= d << s;
+          } else {
+            d = N;                                    // the last digit takes the rest
+          }
+          const uint32_t b = int_bf16((int)d);
+          if (q & 1) pk[i][q >> 1] |= b << 16;
+          else pk[i][q >> 1] = b;
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < NS; i++)
+        *reinterpret_cast<uint4*>(out + i * plane_stride + cb) =
+            make_uint4(pk[i][0], pk[i][1], pk[i][2], pk[i][3]);
+    }
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------ GEMM kernel
+struct OzEpi {
+  double* C;            // direct: output; split: workspace tiles [item][256 cols][256 rows]
+  int64_t ldc, strideC, planeC;
+  int M, N, mh;         // rows >= mh of the real embedding go to the imaginary plane
+  const int* ea;        // [batch][M] row exponents
+  const int* eb;        // [batch][N] column exponents
+  double alpha;         // direct mode only
+  int* err;
+  int nfast;
+  int split;            // pieces per tile: S level sets x Q chunk ranges (1: direct)
+  int var, S, Q;        // level-set variant (kOrder / kSetStart), S = its piece count
+};
+
+// x 2^E of an FP32 integer value (|v| < 2^25), built in the exponent field
+__device__ __forceinline__ double scaled(uint32_t u, int E) {
+  if ((u << 1) == 0) return 0.0;
+  if (E >= -1000 && E <= 990) {
+    const uint32_t hi = (u & 0x80000000u) | ((((u >> 23) & 0xffu) + (uint32_t)(896 + E)) << 20) |
+                        ((u & 0x7fffffu) >> 3);
+    return __hiloint2double((int)hi, (int)(u << 29));
+  }
+  return ldexp((double)__uint_as_float(u), E);
+}
+
+// the levels of piece lp of variant v: kOrder[v][l0 .. l0 + nl)
+__device__ __forceinline__ void piece_levels(int v, int lp, int& l0, int& nl) {
+  l0 = kSetStart[v][lp];
+  nl = kSetStart[v][lp + 1] - l0;
+}
+
+template <bool SPLIT>
+__device__ __forceinline__ void drain(uint32_t tbase, int row, int rloc, int n0, int z,
+                                      int level, bool first, bool last, const OzEpi& ep,
+                                      double* wtile) {
+  const bool live = row < ep.M;
+  double* crow;
+  int64_t ld;
+  if (SPLIT) {
+    crow = wtile + rloc;
+    ld = TILE;
+  } else {
+    crow = ep.C + (int64_t)z * ep.strideC + (row < ep.mh ? (int64_t)row : ep.planeC + row - ep.mh);
+    ld = ep.ldc;
+  }
+  const int er = live ? __ldg(ep.ea + (int64_t)z * ep.M + row) : 0;
+  const int lane = threadIdx.x & 31;
+#pragma unroll 1
+  for (int c0 = 0; c0 < TILE; c0 += 32) {
+    uint32_t r[32];
+    tmem_ld32_async(tbase + c0, r);
+    const int nb = n0 + c0;
+    const int ec = nb + lane < ep.N ? __ldg(ep.eb + (int64_t)z * ep.N + nb + lane) : 0;
+    const int lim = SPLIT ? 32 : min(32, ep.N - nb);
+    double old[32];
+    if (!first && live) {
+#pragma unroll
+      for (int j = 0; j < 32; j++) old[j] = j < lim ? crow[(int64_t)(SPLIT ? c0 + j : nb + j) * ld] : 0.0;
+    }
+    tmem_wait_ld(r);
+#pragma unroll
+    for (int j = 0; j < 32; j++) {
+      const int ecj = __shfl_sync(0xffffffffu, ec, j);
+      if (!live || j >= lim) continue;
+      double v;
+      if (er >= E_BAD || ecj >= E_BAD)
+        v = __longlong_as_double(0x7ff8000000000000ll);
+      else
+        v = scaled(r[j], er + ecj - SB * level);
+      if (!first) v += old[j];
+      if (!SPLIT && last && ep.alpha != 1.0) v *= ep.alpha;
+      crow[(int64_t)(SPLIT ? c0 + j : nb + j) * ld] = v;
+    }
+  }
+}
+
+// Persistent over work items (tile, piece); cluster c of two CTAs takes items c, c + ncl..
+// Per item the producer and the MMA issuer walk the same sequence:
+//   for chunk in the piece's chunk range, for level in its level set, for i in 1..level-1
+//   (j = level - i), for the chunk's K slices: A digit plane i-1, B digit plane j-1.
+// Each (chunk, level) group accumulates in one TMEM buffer (two, alternating) and is
+// drained by the epilogue warps into the FP64 output.
+__global__ void __launch_bounds__(NTHREADS, 1)
+    oz_gemm_pair(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
+                 int K, int tiles_m2, int tiles_n, int batch, OzEpi ep) {
+  constexpr int A_BYTES = BM * 128, B_BYTES = 128 * 128;
+  constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
+  constexpr int TMEM_COLS = 256;
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                             ~uintptr_t(1023));
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);
+  uint64_t* acc_full = bars + 2 * STAGES;
+  uint64_t* acc_empty = bars + 2 * STAGES + 2;
+  uint64_t* drainb = bars + 2 * STAGES + 4;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 5);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const uint32_t rank = cluster_rank();
+  const bool lead = rank == 0;
+  const int cl = blockIdx.x >> 1, ncl = gridDim.x >> 1;
+  const int nk = (K + KELEMS - 1) / KELEMS;
+  const int nch = (nk + KC_SLICES - 1) / KC_SLICES;
+  const int units = tiles_m2 * tiles_n * batch;
+  const int num_items = units * ep.split;
+  auto stageA = [&](int s) { return smem + s * STAGE_BYTES; };
+  auto stageB = [&](int s) { return stageA(s) + A_BYTES; };
+  // item -> tile unit u, level set [l0, l0 + nl) of kOrder[ep.var], chunks [c0, c1)
+  auto item_of = [&](int item, int& u, int& l0, int& nl, int& c0, int& c1) {
+    u = item / ep.split;
+    const int p = item - u * ep.split;
+    const int lp = p % ep.S, cq = p / ep.S;
+    piece_levels(ep.var, lp, l0, nl);
+    c0 = (int)((int64_t)cq * nch / ep.Q);
+    c1 = (int)((int64_t)(cq + 1) * nch / ep.Q);
+  };
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; s++) {
+      mbar_init(smem_u32(&bars[s]), 1);
+      mbar_init(smem_u32(&bars[STAGES + s]), 1);
+    }
+    for (int b = 0; b < 2; b++) {
+      mbar_init(smem_u32(&acc_full[b]), 1);
+      mbar_init(smem_u32(&acc_empty[b]), 8);
+    }
+    mbar_init(smem_u32(drainb), 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&mapA)) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&mapB)) : "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "r"(2 * TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  cluster_sync();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      int it = 0, last = -1;
+      bool stop = false;
+      for (int item = cl; item < num_items && !stop && !*abort_flag; item += ncl) {
+        int u, l0, nl, c0, c1, mt2, nt, z;
+        item_of(item, u, l0, nl, c0, c1);
+        tile_coords(u, tiles_m2, tiles_n, ep.nfast, mt2, nt, z);
+        const int m0 = min(mt2 * 2 * BM + (int)rank * BM, ep.M - 1);
+        const int n0 = min(nt * TILE + (int)rank * 128, ep.N - 1);
+        for (int c = c0; c < c1 && !stop; c++) {
+          const int kb0 = c * KC_SLICES, kb1 = min(kb0 + KC_SLICES, nk);
+          for (int li = 0; li < nl && !stop; li++) {
+            const int level = kOrder[ep.var][l0 + li];
+            for (int i = 1; i < level && !stop; i++) {
+              const int za = z * NS + i - 1, zb = z * NS + (level - i) - 1;
+              for (int kb = kb0; kb < kb1; kb++, it++) {
+                const int s = it % STAGES;
+                const uint32_t ph = (it / STAGES) & 1;
+                if (!mbar_wait(smem_u32(&bars[STAGES + s]), ph ^ 1, abort_flag, ep.err)) {
+                  stop = true;
+                  break;
+                }
+                const uint32_t full = smem_u32(&bars[s]);
+                if (lead) mbar_expect_tx(full, 2 * STAGE_BYTES);
+                const uint32_t full_lead = cluster_addr(full, 0);
+                const int kc = kb * KELEMS;
+                tma_load_3d_pair(smem_u32(stageA(s)), &mapA, full_lead, kc, m0, za);
+                tma_load_3d_pair(smem_u32(stageB(s)), &mapB, full_lead, kc, n0, zb);
+                last = it;
+              }
+            }
+          }
+        }
+      }
+      if (*abort_flag && last >= 0) {
+        const unsigned long long t0 = globaltimer();
+        if (lead) {
+          for (int j = max(0, last - STAGES + 1); j <= last; j++) {
+            const uint32_t bar = smem_u32(&bars[j % STAGES]);
+            while (!mbar_try(bar, (j / STAGES) & 1) && globaltimer() - t0 < WAIT_NS) {
+            }
+          }
+        } else {
+          while (globaltimer() - t0 < 1000000ull) {
+          }
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0 && lead) {
+      constexpr uint32_t idesc = make_idesc(BF16, 2 * BM, TILE);
+      int it = 0, local = 0;
+      bool stop = false;
+      for (int item = cl; item < num_items && !stop && !*abort_flag; item += ncl) {
+        int u, l0, nl, c0, c1;
+        item_of(item, u, l0, nl, c0, c1);
+        for (int c = c0; c < c1 && !stop; c++) {
+          const int kb0 = c * KC_SLICES, kb1 = min(kb0 + KC_SLICES, nk);
+          for (int li = 0; li < nl && !stop; li++, local++) {
+            const int level = kOrder[ep.var][l0 + li];
+            const int buf = local & 1;
+            const uint32_t use = (uint32_t)(local >> 1);
+            if (!mbar_wait(smem_u32(&acc_empty[buf]), (use & 1) ^ 1, abort_flag, ep.err)) {
+              stop = true;
+              break;
+            }
+            tc_fence_after();
+            const uint32_t tacc = tmem + buf * TMEM_COLS;
+            for (int i = 1; i < level && !stop; i++) {
+              for (int kb = kb0; kb < kb1; kb++, it++) {
+                const int s = it % STAGES;
+                const uint32_t ph = (it / STAGES) & 1;
+                if (!mbar_wait(smem_u32(&bars[s]), ph, abort_flag, ep.err)) {
+                  stop = true;
+                  break;
+                }
+                tc_fence_after();
+                const uint32_t a0 = smem_u32(stageA(s)), b0 = smem_u32(stageB(s));
+#pragma unroll
+                for (int ks = 0; ks < 4; ks++) {
+                  const uint32_t acc = (i > 1 || kb > kb0 || ks > 0) ? 1u : 0u;
+                  mma_pair<BF16>(tacc, smem_desc(a0 + ks * 32), smem_desc(b0 + ks * 32), idesc, acc);
+                }
+                mma_commit_pair(smem_u32(&bars[STAGES + s]), 3);
+              }
+            }
+            if (!stop) mma_commit_pair(smem_u32(&acc_full[buf]), 3);
+          }
+        }
+      }
+    }
+  } else {
+    const int q = warp & 3;
+    int local = 0;
+    bool stop = false;
+    for (int item = cl; item < num_items && !stop; item += ncl) {
+      int u, l0, nl, c0, c1, mt2, nt, z;
+      item_of(item, u, l0, nl, c0, c1);
+      tile_coords(u, tiles_m2, tiles_n, ep.nfast, mt2, nt, z);
+      const int rloc = (int)rank * BM + 32 * q + lane;
+      const int row = mt2 * 2 * BM + rloc;
+      double* wtile = ep.split > 1 || ep.mh < 0 ? ep.C + (int64_t)item * TILE * TILE : nullptr;
+      for (int c = c0; c < c1 && !stop; c++) {
+        for (int li = 0; li < nl; li++, local++) {
+          const int level = kOrder[ep.var][l0 + li];
+          const int buf = local & 1;
+          const uint32_t use = (uint32_t)(local >> 1);
+          const bool ok = mbar_wait(smem_u32(&acc_full[buf]), use & 1, abort_flag, ep.err);
+          if (!ok || *abort_flag) {
+            stop = true;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t tbase = tmem + buf * TMEM_COLS + ((uint32_t)(32 * q) << 16);
+          const bool first = c == c0 && li == 0;
+          const bool lastg = c == c1 - 1 && li == nl - 1;
+          if (wtile)
+            drain<true>(tbase, row, rloc, nt * TILE, z, level, first, lastg, ep, wtile);
+          else
+            drain<false>(tbase, row, rloc, nt * TILE, z, level, first, lastg, ep, nullptr);
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive_cluster(cluster_addr(smem_u32(&acc_empty[buf]), 0));
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1 && lead) {
+    tc_fence_after();
+    if (lane == 0) {
+      mma_commit_pair(smem_u32(drainb), 1);
+      const unsigned long long t0 = globaltimer();
+      while (!mbar_try(smem_u32(drainb), 0) && globaltimer() - t0 < WAIT_NS) {
+      }
+    }
+    __syncwarp();
+  }
+  cluster_sync();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(2 * TMEM_COLS)
+                 : "memory");
+  }
+}
+
+// C = alpha (sum of the pieces, in piece order) + beta C.  ws holds the pieces of tile
+// unit u at items u * split + p, each [256 columns][256 rows] of the real embedding.
+struct RedArgs {
+  const double* ws;
+  double* C;
+  int64_t ldc, strideC, planeC;
+  int m, n, batch, cplx, split, tiles_m2, tiles_n, nfast;
+  double alpha[2], beta[2];
+};
+
+__device__ __forceinline__ double ws_sum(const RedArgs& a, int z, int r, int c) {
+  // unit index of the tile holding (r, c) under the kernel's tile order
+  const int mt2 = r / TILE, nt = c / TILE;
+  const int per = a.tiles_m2 * a.tiles_n;
+  const int u = z * per + (a.nfast ? mt2 * a.tiles_n + nt : nt * a.tiles_m2 + mt2);
+  const double* w = a.ws + ((int64_t)u * a.split) * TILE * TILE + (int64_t)(c % TILE) * TILE + r % TILE;
+  double s = 0.0;
+  for (int p = 0; p < a.split; p++) s += w[(int64_t)p * TILE * TILE];
+  return s;
+}
+
+__global__ void oz_reduce(RedArgs a) {
+  const int64_t mn = (int64_t)a.m * a.n;
+  const int64_t total = mn * a.batch;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int z = (int)(t / mn);
+    const int64_t rem = t - z * mn;
+    const int r = (int)(rem % a.m), c = (int)(rem / a.m);
+    double* C = a.C + z * a.strideC;
+    const int64_t idx = (int64_t)r + (int64_t)c * a.ldc;
+    const bool has_beta = a.beta[0] != 0.0 || a.beta[1] != 0.0;
+    if (a.cplx) {
+      const double sr = ws_sum(a, z, r, c), si = ws_sum(a, z, r + a.m, c);
+      double re = a.alpha[0] * sr - a.alpha[1] * si;
+      double im = a.alpha[0] * si + a.alpha[1] * sr;
+      if (has_beta) {
+        const double cr = C[idx], ci = C[a.planeC + idx];
+        re += a.beta[0] * cr - a.beta[1] * ci;
+        im += a.beta[0] * ci + a.beta[1] * cr;
+      }
+      C[idx] = re;
+      C[a.planeC + idx] = im;
+    } else {
+      double v = a.alpha[0] * ws_sum(a, z, r, c);
+      if (has_beta) v += a.beta[0] * C[idx];
+      C[idx] = v;
+    }
+  }
+}
+
+// ------------------------------------------------------------ host side
+constexpr int SMEM = STAGES * (BM * 128 + 128 * 128) + 1024 + 256;
+static_assert(SMEM <= 227 * 1024, "shared memory");
+
+struct Plan {
+  int var = 0, S = 1, Q = 1;
+  double t_oz = 0.0;
+};
+
+}  // namespace oz
+
+// estimated device seconds of the digit GEMM with the piece split (S level sets, Q chunk
+// ranges) on `cl` resident clusters, against the CUDA-core FP64 kernel
+static oz::Plan oz_plan(int64_t M2, int64_t N, int64_t K2, int batch, int cl) {
+  using namespace oz;
+  const int64_t tiles = ((M2 + TILE - 1) / TILE) * ((N + TILE - 1) / TILE) * batch;
+  const int64_t nk = (K2 + KELEMS - 1) / KELEMS;
+  const int nch = (int)((nk + KC_SLICES - 1) / KC_SLICES);
+  // one digit product of a pair tile: 256 x 256 x K on two SMs at ~1.75 PFLOP/s / 76 pairs
+  const double prod_s = 2.0 * TILE * TILE * (double)(nk * KELEMS) / (1.75e15 / 76.0);
+  Plan best;
+  best.t_oz = 1e30;
+  for (int v = 0; v < NVAR; v++)
+    for (int Q = 1; Q <= std::min(nch, 8); Q *= 2) {
+      const int S = kVarPieces[v];
+      const int64_t items = tiles * S * Q;
+      const int64_t rounds = (items + cl - 1) / cl;
+      // an item: its level set's products over 1/Q of the K chunks
+      double t = rounds * prod_s * kVarMaxProducts[v] / Q;
+      if (S * Q > 1) t += (double)items * TILE * TILE * 8.0 * 2.0 / 5e12 + 4e-6;   // reduce
+      if (t < best.t_oz * 0.97) {
+        best.t_oz = t;
+        best.var = v;
+        best.S = S;
+        best.Q = Q;
+      }
+    }
+  // digit planes: read FP64 twice, write 16 B per element; launch overheads
+  best.t_oz += (double)(M2 + N) * K2 * batch * 32.0 / 5e12 + 15e-6;
+  return best;
+}
+
+int gemm_f64_ozaki_possible(fmpt_handle* h, const GemmArgs& g) {
+  if (!h->f64_tc && !g.engine) return 0;
+  if (g.m < 32 || g.n < 32 || g.k < 16) return 0;
+  const int cp = g.cplx ? 2 : 1;
+  const double flops = 2.0 * g.m * g.n * (double)g.k * g.batch * cp * cp;
+  const double t_simt = flops / 1.1e12;
+  oz::Plan p = oz_plan((int64_t)g.m * cp, g.n, (int64_t)g.k * cp, g.batch,
+                       std::max(1, h->sm_count / 2));
+  return p.t_oz < t_simt ? 1 : 0;
+}
+
+int gemm_f64_ozaki(fmpt_handle* h, const GemmArgs& g) {
+  using namespace oz;
+  const int cp = g.cplx ? 1 : 0;
+  const int M2 = g.m * (cp ? 2 : 1), K2 = g.k * (cp ? 2 : 1), N = g.n;
+  const int ldk = (K2 + 7) / 8 * 8;
+  const int batch = g.batch;
+  if ((int64_t)batch * NS > INT32_MAX / 2) return set_error(h, FMPT_ERR_SHAPE, "ozaki: batch");
+  // workspace: digit planes of A and B, exponents, then the split pieces
+  const size_t planesA = (size_t)batch * NS * M2 * ldk * 2, planesB = (size_t)batch * NS * N * ldk * 2;
+  const size_t expA = (size_t)batch * M2 * 4, expB = (size_t)batch * N * 4;
+  auto al = [](size_t b) { return (b + 255) / 256 * 256; };
+  const int tiles_m2 = (M2 + TILE - 1) / TILE, tiles_n = (N + TILE - 1) / TILE;
+  const int64_t units = (int64_t)tiles_m2 * tiles_n * batch;
+  if (units > INT32_MAX / 64) return set_error(h, FMPT_ERR_SHAPE, "ozaki: too many tiles");
+  // resident clusters of the kernel
+  static int clusters = -1;
+  cudaLaunchConfig_t cfg{};
+  cfg.blockDim = dim3(NTHREADS);
+  cfg.dynamicSmemBytes = SMEM;
+  cfg.stream = h->stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = 2;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (clusters < 0) {
+    FMPT_CUDA(h, cudaFuncSetAttribute(oz_gemm_pair, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM));
+    cfg.gridDim = dim3(2 * std::max(1, h->sm_count / 2));
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, oz_gemm_pair, &cfg) != cudaSuccess) {
+      (void)cudaGetLastError();
+      n = 0;
+    }
+    clusters = n;
+  }
+  if (clusters <= 0) return set_error(h, FMPT_ERR_UNSUPPORTED, "ozaki: no 2-CTA cluster fits");
+  const Plan plan = oz_plan(M2, N, K2, batch, clusters);
+  const int split = plan.S * plan.Q;
+  const bool direct = split == 1 && g.beta[0] == 0.0 && g.beta[1] == 0.0 && g.alpha[1] == 0.0;
+  const size_t wsb = direct ? 0 : (size_t)units * split * TILE * TILE * sizeof(double);
+  const size_t need = al(planesA) + al(planesB) + al(expA) + al(expB) + wsb;
+  FMPT_TRY(grow_buffer(h, &h->oz_ws, &h->oz_ws_bytes, need));
+  char* base = static_cast<char*>(h->oz_ws);
+  uint16_t* SA = reinterpret_cast<uint16_t*>(base);
+  uint16_t* SBp = reinterpret_cast<uint16_t*>(base + al(planesA));
+  int* EA = reinterpret_cast<int*>(base + al(planesA) + al(planesB));
+  int* EB = reinterpret_cast<int*>(base + al(planesA) + al(planesB) + al(expA));
+  double* WS = reinterpret_cast<double*>(base + al(planesA) + al(planesB) + al(expA) + al(expB));
+
+  // digit planes (A side: op(A), m x k; B side: op(B)^T, n x k)
+  SliceSrc sa{}, sb{};
+  sa.p = g.A; sa.plane = g.planeA; sa.bstride = g.strideA; sa.rows = g.m; sa.cols = g.k;
+  sa.cplx = cp; sa.role = 0; sa.conj = (g.ta == FMPT_C || g.ta == FMPT_R);
+  if (g.ta == FMPT_N || g.ta == FMPT_R) { sa.sr = 1; sa.sc = g.lda; } else { sa.sr = g.lda; sa.sc = 1; }
+  sb.p = g.B; sb.plane = g.planeB; sb.bstride = g.strideB; sb.rows = g.n; sb.cols = g.k;
+  sb.cplx = cp; sb.role = 1; sb.conj = (g.tb == FMPT_C || g.tb == FMPT_R);
+  // op(B)(c, n) = B[c + n ldb] (N, R) or B[n + c ldb] (T, C)
+  if (g.tb == FMPT_N || g.tb == FMPT_R) { sb.sr = g.ldb; sb.sc = 1; } else { sb.sr = 1; sb.sc = g.ldb; }
+  {
+    ProfScope prof(h, FMPT_K_CONVERT);
+    oz_slice<<<dim3((M2 + 31) / 32, batch), 256, 0, h->stream>>>(sa, M2, K2, ldk, SA, EA);
+    FMPT_LAUNCHED(h);
+    oz_slice<<<dim3((N + 31) / 32, batch), 256, 0, h->stream>>>(sb, N, K2, ldk, SBp, EB);
+    FMPT_LAUNCHED(h);
+  }
+  CUtensorMap ma, mb;
+  FMPT_TRY(make_map(h, &ma, SA, BF16, K2, M2, ldk, (int64_t)batch * NS, (int64_t)M2 * ldk, BM));
+  FMPT_TRY(make_map(h, &mb, SBp, BF16, K2, N, ldk, (int64_t)batch * NS, (int64_t)N * ldk, 128));
+
+  OzEpi ep{};
+  ep.M = M2;
+  ep.N = N;
+  ep.ea = EA;
+  ep.eb = EB;
+  FMPT_TRY(gp_status_word(h, &ep.err));
+  ep.nfast = M2 > N ? 1 : 0;
+  ep.split = split;
+  ep.var = plan.var;
+  ep.S = plan.S;
+  ep.Q = plan.Q;
+  if (direct) {
+    ep.C = g.C;
+    ep.ldc = g.ldc;
+    ep.strideC = g.strideC;
+    ep.planeC = g.planeC;
+    ep.mh = cp ? g.m : INT32_MAX;
+    ep.alpha = g.alpha[0];
+  } else {
+    ep.C = WS;
+    ep.mh = -1;        // workspace tiles
+    ep.alpha = 1.0;
+  }
+  const int64_t items = units * split;
+  cfg.gridDim = dim3((unsigned)(2 * std::min<int64_t>(items, clusters)));
+  {
+    ProfScope prof(h, FMPT_K_TC_GEMM);
+    FMPT_CUDA(h, cudaLaunchKernelEx(&cfg, oz_gemm_pair, ma, mb, K2, tiles_m2, tiles_n, batch, ep));
+    FMPT_LAUNCHED(h);
+  }
+  if (!direct) {
+    RedArgs ra{};
+    ra.ws = WS;
+    ra.C = g.C;
+    ra.ldc = g.ldc;
+    ra.strideC = g.strideC;
+    ra.planeC = g.planeC;
+    ra.m = g.m;
+    ra.n = g.n;
+    ra.batch = batch;
+    ra.cplx = cp;
+    ra.split = split;
+    ra.tiles_m2 = tiles_m2;
+    ra.tiles_n = tiles_n;
+    ra.nfast = ep.nfast;
+    ra.alpha[0] = g.alpha[0];
+    ra.alpha[1] = g.alpha[1];
+    ra.beta[0] = g.beta[0];
+    ra.beta[1] = g.beta[1];
+    const int64_t total = (int64_t)g.m * g.n * batch;
+    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((total + 255) / 256, 8LL * h->sm_count));
+    oz_reduce<<<blocks, 256, 0, h->stream>>>(ra);
+    FMPT_LAUNCHED(h);
+  }
+  return FMPT_OK;
+}
+
+}  // namespace fmpt

@@ -23,175 +23,10 @@
 #include <cmath>
 #include <cstring>
 
-#include "internal.h"
+#include "tc_ptx.cuh"
 
 namespace fmpt {
 namespace tc {
-
-constexpr int BM = 128;
-constexpr int NTHREADS = 192;
-constexpr unsigned long long WAIT_NS = 2000000000ull;
-
-enum Mode { TF32 = 0, TF32X3 = 1, BF16 = 2 };
-
-// --------------------------------------------------------------- PTX helpers
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ unsigned long long globaltimer() {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
-               : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(bar), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-// bounded wait; false (and the abort flag set) when it gave up
-__device__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag,
-                          int* err) {
-  if (mbar_try(bar, parity)) return true;
-  const unsigned long long t0 = globaltimer();
-  while (true) {
-    if (mbar_try(bar, parity)) return true;
-    if (*abort_flag) return false;
-    if (globaltimer() - t0 > WAIT_NS) {
-      *abort_flag = 1;
-      atomicExch(err, 1);
-      return false;
-    }
-  }
-}
-
-__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, uint32_t bar,
-                                            int c0, int c1, int c2) {
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
-      " [%0], [%1, {%3, %4, %5}], [%2];" ::"r"(dst),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(bar), "r"(c0), "r"(c1), "r"(c2)
-      : "memory");
-}
-
-__device__ __forceinline__ void tc_fence_before() {
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-}
-__device__ __forceinline__ void tc_fence_after() {
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-}
-
-// K-major operand tile, 128-byte rows, 128-byte swizzle, 8-row groups 1024 B apart
-__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
-  uint64_t d = 0;
-  d |= (uint64_t)((addr >> 4) & 0x3FFF);          // start address
-  d |= (uint64_t)1 << 16;                         // leading byte offset (unused for SW128 K-major)
-  d |= (uint64_t)(1024 >> 4) << 32;               // stride byte offset: 8 rows x 128 B
-  d |= (uint64_t)1 << 46;                         // descriptor version (sm_100 family)
-  d |= (uint64_t)2 << 61;                         // SWIZZLE_128B
-  return d;
-}
-
-// instruction descriptor: D=F32, A/B format, K-major A and B, N, M
-__host__ __device__ constexpr uint32_t make_idesc(int mode, int M, int N) {
-  return (1u << 4) |                                      // D format F32
-         ((mode == BF16 ? 1u : 2u) << 7) |               // A: BF16 (kind::f16) / TF32
-         ((mode == BF16 ? 1u : 2u) << 10) |              // B
-         ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
-}
-
-template <int MODE>
-__device__ __forceinline__ void mma(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc,
-                                    uint32_t accum) {
-  if (MODE == BF16) {
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
-        "l"(a), "l"(b), "r"(idesc), "r"(accum));
-  } else {
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
-        "l"(a), "l"(b), "r"(idesc), "r"(accum));
-  }
-}
-
-__device__ __forceinline__ void mma_commit(uint32_t bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                   bar)
-               : "memory");
-}
-
-struct EpiArgs {
-  void* C;            // float or double
-  int64_t ldc;        // column stride (elements)
-  int64_t strideC;    // batch stride (elements)
-  int M, N;
-  int* err;
-  int nfast;          // tile order: 0 = M index fastest, 1 = N index fastest
-};
-
-// tile -> (mt, nt, z).  M index fastest: the CTAs running together share B tiles; N
-// index fastest when A is the larger operand: they share A tiles, so A streams from DRAM
-// once while the smaller B is reused from L2 (at D=2048 this cut GEMM 2's DRAM reads from
-// 707 MB, 3.4x its 210 MB of operands, to 334 MB: A is streamed once and partly evicts B).
-__device__ __forceinline__ void tile_coords(int tile, int tiles_m, int tiles_n, int nfast,
-                                            int& mt, int& nt, int& z) {
-  const int per = tiles_m * tiles_n;
-  z = tile / per;
-  const int r = tile - z * per;
-  if (nfast) {
-    nt = r % tiles_n;
-    mt = r / tiles_n;
-  } else {
-    mt = r % tiles_m;
-    nt = r / tiles_m;
-  }
-}
-
-__device__ __forceinline__ void tmem_ld32_async(uint32_t taddr, uint32_t (&r)[32]) {
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
-      "%11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, "
-      "%28, %29, %30, %31}, [%32];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
-        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
-        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-      : "r"(taddr));
-}
-
-// waits for this thread's TMEM loads; the registers of the load in flight are in-out
-// operands, so no use of them is scheduled before the wait
-__device__ __forceinline__ void tmem_wait_ld(uint32_t (&r)[32]) {
-  asm volatile("tcgen05.wait::ld.sync.aligned;"
-               : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]),
-                 "+r"(r[6]), "+r"(r[7]), "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]),
-                 "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15]), "+r"(r[16]), "+r"(r[17]),
-                 "+r"(r[18]), "+r"(r[19]), "+r"(r[20]), "+r"(r[21]), "+r"(r[22]), "+r"(r[23]),
-                 "+r"(r[24]), "+r"(r[25]), "+r"(r[26]), "+r"(r[27]), "+r"(r[28]), "+r"(r[29]),
-                 "+r"(r[30]), "+r"(r[31])
-               :
-               : "memory");
-}
 
 template <int OUT>
 __device__ __forceinline__ void store_cols(void* base, int64_t ldc, int n_base, int n_lim,
@@ -455,64 +290,6 @@ struct PairCfg {
   static_assert(SMEM <= 227 * 1024, "shared memory");
   static_assert((2 * STAGES + 5) * 8 + 8 <= 256, "barrier area");
 };
-
-__device__ __forceinline__ uint32_t cluster_rank() {
-  uint32_t r;
-  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
-  return r;
-}
-
-// shared::cluster address of this CTA's shared-memory offset `a` in CTA `rank`
-__device__ __forceinline__ uint32_t cluster_addr(uint32_t a, uint32_t rank) {
-  uint32_t d;
-  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(rank));
-  return d;
-}
-
-__device__ __forceinline__ void cluster_sync() {
-  asm volatile("barrier.cluster.arrive.release;\n\tbarrier.cluster.wait.acquire;" ::: "memory");
-}
-
-// tile load into this CTA's shared memory, completing on an mbarrier of either CTA
-__device__ __forceinline__ void tma_load_3d_pair(uint32_t dst, const CUtensorMap* map,
-                                                 uint32_t bar_cluster, int c0, int c1, int c2) {
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes.cta_group::2"
-      " [%0], [%1, {%3, %4, %5}], [%2];" ::"r"(dst),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(bar_cluster), "r"(c0), "r"(c1), "r"(c2)
-      : "memory");
-}
-
-template <int MODE>
-__device__ __forceinline__ void mma_pair(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc,
-                                         uint32_t accum) {
-  if (MODE == BF16) {
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
-        "l"(a), "l"(b), "r"(idesc), "r"(accum));
-  } else {
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::2.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
-        "l"(a), "l"(b), "r"(idesc), "r"(accum));
-  }
-}
-
-// arrive on the mbarrier at this offset in every CTA of `mask` once the issuing
-// thread's MMAs have completed
-__device__ __forceinline__ void mma_commit_pair(uint32_t bar, uint16_t mask) {
-  asm volatile(
-      "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64"
-      " [%0], %1;" ::"r"(bar),
-      "h"(mask)
-      : "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive_cluster(uint32_t bar_cluster) {
-  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(bar_cluster)
-               : "memory");
-}
 
 // Work items of the pair kernel.  Items [0, full) are whole tiles (units).  When the last
 // round of tiles would leave clusters idle, the `tail` units after them are each cut into
@@ -810,7 +587,6 @@ EncodeTiledFn encode_fn(fmpt_handle* h) {
   return fn;
 }
 
-// 3-D K-major operand map: dims {K, rows, batch}, box {K slice of 128 B, box_rows, 1}
 int make_map(fmpt_handle* h, CUtensorMap* map, const void* base, int mode, int64_t K,
              int64_t rows, int64_t ld, int64_t batch, int64_t bstride, int box_rows) {
   EncodeTiledFn fn = encode_fn(h);

@@ -44,6 +44,14 @@ class Handle:
             raise ValueError("tc tile must be 'pair' or 'single'")
         self.check(lib().fmpt_set_tc_tile(self.ptr, codes[tile]))
 
+    def set_f64_engine(self, engine="cuda_cores"):
+        """Engine of this handle's FP64 GEMMs: "cuda_cores" (default) or "tensor_cores"
+        (the Ozaki-scheme FP64 GEMM on the BF16 tensor cores wherever it is faster)."""
+        codes = {"cuda_cores": 0, "tensor_cores": 1}
+        if engine not in codes:
+            raise ValueError("f64 engine must be 'cuda_cores' or 'tensor_cores'")
+        self.check(lib().fmpt_set_f64_engine(self.ptr, codes[engine]))
+
     def set_graphs(self, on=True):
         """CUDA-graph Krylov solves for block-sparse operators (default on)."""
         self.check(lib().fmpt_set_graphs(self.ptr, 1 if on else 0))

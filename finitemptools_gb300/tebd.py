@@ -474,6 +474,9 @@ class HomogeneousTEBDCache:
     of size stepsize, fused once (fuse_gates of the repeated one-step circuit)."""
 
     def __init__(self, L, dims, bonds, sites, stepper):
+        # the reference refuses a time-dependent Hamiltonian here (timeevo.jl:90)
+        if any(callable(v) for v in list(dict(bonds).values()) + list(dict(sites).values())):
+            raise ValueError("const hamiltonian expected.")
         one = trotter_propagator(L, dims, bonds, sites, tspan=(0.0, stepper.stepsize),
                                  order=stepper.order, stepsize=stepper.stepsize)
         self.circuit = fuse_gates(QuantumCircuit(list(one) * stepper.n))

@@ -51,9 +51,21 @@ enum fmpt_status {
 enum fmpt_dtype { FMPT_F64 = 0, FMPT_C128 = 1 };
 
 /* Arithmetic of the contractions (H_eff*x and environment updates).
- * FP64 is the plain form; the others run on tcgen05 tensor cores with FP32
- * accumulation (3xTF32 = hi/lo split products). */
-enum fmpt_precision { FMPT_PREC_FP64 = 0, FMPT_PREC_TF32X3 = 1, FMPT_PREC_TF32 = 2, FMPT_PREC_BF16 = 3 };
+ * FP64 is the plain form (CUDA-core FMA, or the handle's FP64 engine, see
+ * fmpt_set_f64_engine).  FP64_TC is the same FP64 contraction with every GEMM
+ * large enough to gain run on the BF16 tensor cores by the Ozaki scheme: each
+ * FP64 operand row becomes 8 exact base-64 digit planes, the 36 digit products
+ * up to 48 bits run as tcgen05 MMAs whose FP32 sums are exact, and the partial
+ * results are added in FP64 (Frobenius-relative error ~1e-14 on random data,
+ * the accuracy class of an FP64 GEMM).  TF32, 3xTF32 and BF16 run on tcgen05
+ * with FP32 accumulation (3xTF32 = hi/lo split products). */
+enum fmpt_precision {
+  FMPT_PREC_FP64 = 0,
+  FMPT_PREC_TF32X3 = 1,
+  FMPT_PREC_TF32 = 2,
+  FMPT_PREC_BF16 = 3,
+  FMPT_PREC_FP64_TC = 4
+};
 
 enum fmpt_trans { FMPT_N = 0, FMPT_T = 1, FMPT_C = 2, FMPT_R = 3 /* conj, no transpose */ };
 
@@ -95,6 +107,14 @@ int fmpt_set_tuning(fmpt_handle* h, int mode);
  * 3xTF32); mode 1: always the one-CTA tile.  Both accumulate in FP32 over the
  * same K slices; the last bits may differ.  No counterpart in the reference. */
 int fmpt_set_tc_tile(fmpt_handle* h, int mode);
+/* FP64 engine of every FP64 GEMM this handle runs without a precision argument
+ * of its own (FP64 H_eff*x and environment updates, the density-matrix split's
+ * Gram matrix, the Krylov solvers' Ritz combinations, fmpt_gemm): mode 0
+ * (default) the CUDA cores; mode 1 the BF16 tensor cores by the Ozaki scheme of
+ * FMPT_PREC_FP64_TC wherever a cost model of the two kernels says it is faster
+ * (large GEMMs; small ones stay on the CUDA cores).  No counterpart in the
+ * reference. */
+int fmpt_set_f64_engine(fmpt_handle* h, int mode);
 /* Number of cached tuning decisions and of timed tunings so far. */
 int fmpt_tuning_info(fmpt_handle* h, int* entries, int64_t* timed);
 /* Output tile edge (32 or 64) a block-sparse operator runs with (0: dense op). */
@@ -260,22 +280,26 @@ int fmpt_exponentiate(fmpt_op* op, double t_re, double t_im, const double* x, do
 
 /* ------------------------------------------ allocation-free H_eff * x
  * No counterpart in the reference.  The plain FP64 two-site H_eff*x of
- * fmpt_ac2_prime (same arguments, same result) for callers that cannot
- * allocate device memory while they run: work recorded under stream
- * capture, applications whose own allocator owns the device memory, fixed
- * memory budgets.  Instead of pool memory it uses one file-scope device
- * array of FMPT_NOALLOC_SCRATCH_BYTES, held by every GPU that loads the
- * library until the process exits; it calls no cudaMalloc/cudaFree and no
- * allocating library routine.
+ * fmpt_ac2_prime (same arguments; the result equals fmpt_ac2_prime's to FP64
+ * rounding -- the summation order of the GEMMs may differ) for callers that
+ * cannot allocate device memory while they run: applications whose own memory
+ * manager owns the device memory (a framework's caching allocator, a host that
+ * hands the library a fixed arena) and runs under a fixed memory budget, where
+ * a pool allocation in the middle of a solve may fail.  Instead of pool memory
+ * it uses one file-scope device array of FMPT_NOALLOC_SCRATCH_BYTES, held by
+ * every GPU that loads the library until the process exits; it calls no
+ * cudaMalloc/cudaFree and no allocating library routine, and its MPO block
+ * table reaches the device as kernel parameters.
  *   - Scratch need: 8*(Dl*wl*P*Dr + Dl*P*wr*Dr) bytes (x2 for C128), P = d1*d2,
  *     plus a small block table; larger problems return FMPT_ERR_SHAPE with
  *     the sizes in fmpt_last_error (use fmpt_ac2_prime for them).
  *   - The first call on a device resolves the array's device address
  *     (cudaGetSymbolAddress, with that device current); make that first call
  *     before any stream capture.
- *   - All calls share the array: calls that overlap on the GPU race on it.
- *     Issue them on one stream (or serialise them).
- *   - FP64 forms only (dtype F64 or C128); precision is always FMPT_PREC_FP64. */
+ *   - All calls share the array, which keeps the last call's contents: calls
+ *     that overlap on the GPU race on it.  Issue them on one stream (or
+ *     serialise them).
+ *   - FP64 forms only (dtype F64 or C128), always on the CUDA cores. */
 #define FMPT_NOALLOC_SCRATCH_BYTES (64u * 1024u * 1024u)
 int fmpt_ac2_prime_noalloc(fmpt_handle* h, int dtype, const double* x, const double* W1_host,
                            const double* W2_host, const double* hleft, const double* hright,

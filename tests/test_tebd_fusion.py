@@ -93,6 +93,23 @@ def test_tebd_stepper_step_count():
     assert st.n == 1 and st.tspan == (0.0, -0.05j)
 
 
+def test_homogeneous_cache_refuses_time_dependent_terms():
+    """HomogeousTEBDCache takes a constant Hamiltonian only (timeevo.jl:90 throws
+    ArgumentError("const hamiltonian expected.")): a term given as a function of t is
+    refused instead of being frozen at the first step."""
+    X = np.array([[0.0, 1.0], [1.0, 0.0]])
+    ZZ = np.kron(np.diag([-1.0, 1.0]), np.diag([-1.0, 1.0]))
+    L = 4
+    stepper = fm.TEBDStepper(stepsize=0.05, tspan=(0.0, 0.2), order=2)
+    bonds = {(i, i + 1): -ZZ for i in range(1, L)}
+    with pytest.raises(ValueError, match="const hamiltonian expected"):
+        fm.HomogeneousTEBDCache(L, [2] * L, bonds, {1: (lambda t: t * X)}, stepper)
+    with pytest.raises(ValueError, match="const hamiltonian expected"):
+        fm.HomogeneousTEBDCache(L, [2] * L, {(1, 2): (lambda t: -ZZ)}, {}, stepper)
+    cache = fm.HomogeneousTEBDCache(L, [2] * L, bonds, {1: -0.5 * X}, stepper)
+    assert len(cache.circuit) > 0
+
+
 def test_time_dependent_trotter_and_inhomogeneous_cache():
     """Bond and site terms as functions of t (the reference takes each second-order step's
     terms at its midpoint, tebd.jl:99-119): constant functions give the constant circuit

@@ -1,7 +1,7 @@
 """The allocation-free two-site H_eff*x (fmpt_ac2_prime_noalloc).
 
-Callers that cannot allocate device memory while they run (stream capture,
-an application-owned allocator, a fixed memory budget) use this entry point:
+Callers that cannot allocate device memory while they run (a host whose own
+allocator owns the device memory, a fixed memory budget) use this entry point:
 its scratch is a static device array inside libfmpt, so the call allocates
 nothing.  This file is collected last so that a failure here leaves every
 other test already run.  It calls the C ABI directly (ctypes), compares two
@@ -56,6 +56,46 @@ def test_noalloc_matches_pooled_entry_point_twice():
         assert st == 0, lib.fmpt_last_error(h)
         y0 = _get(lib, h, py0, x.size)
         y1 = _get(lib, h, py1, x.size)
+        assert np.linalg.norm(y1 - y0) <= 1e-12 * np.linalg.norm(y0), call
+        for p in (px, pL, pR, py0, py1):
+            lib.fmpt_free(h, p)
+    lib.fmpt_destroy(h)
+
+
+def test_noalloc_complex_matches_pooled_entry_point_twice():
+    """C128: complex W (imaginary planes of both MPO tensors, complex block coefficients)
+    and split-plane x / L / R, whose T1 / T3 take twice the scratch."""
+    lib = _native.lib()
+    h = ctypes.c_void_p()
+    assert lib.fmpt_create(0, ctypes.byref(h)) == 0
+    rng = np.random.default_rng(7)
+    w = 4
+    for call, (Dl, Dr) in enumerate([(24, 36), (40, 40)]):
+        W1 = (rng.standard_normal((w, 2, w, 2)) + 1j * rng.standard_normal((w, 2, w, 2)))
+        W2 = (rng.standard_normal((w, 2, w, 2)) + 1j * rng.standard_normal((w, 2, w, 2)))
+        W1 *= rng.random((w, 1, w, 1)) < 0.6
+        W2 *= rng.random((w, 1, w, 1)) < 0.6
+
+        def planes(a):
+            f = np.asarray(a).ravel(order="F")
+            return np.ascontiguousarray(np.concatenate([f.real, f.imag]))
+
+        hW1, hW2 = planes(W1), planes(W2)
+        x = rng.standard_normal((Dl, 2, 2, Dr)) + 1j * rng.standard_normal((Dl, 2, 2, Dr))
+        L = rng.standard_normal((Dl, w, Dl)) + 1j * rng.standard_normal((Dl, w, Dl))
+        R = rng.standard_normal((Dr, w, Dr)) + 1j * rng.standard_normal((Dr, w, Dr))
+        px, pL, pR = _buf(lib, h, planes(x)), _buf(lib, h, planes(L)), _buf(lib, h, planes(R))
+        py0, py1 = ctypes.c_void_p(), ctypes.c_void_p()
+        assert lib.fmpt_malloc(h, x.size * 16, ctypes.byref(py0)) == 0
+        assert lib.fmpt_malloc(h, x.size * 16, ctypes.byref(py1)) == 0
+        st = lib.fmpt_ac2_prime(h, 1, 0, px, hW1.ctypes.data, hW2.ctypes.data, pL, pR, py0,
+                                Dl, 2, 2, Dr, w, w, w)
+        assert st == 0, lib.fmpt_last_error(h)
+        st = lib.fmpt_ac2_prime_noalloc(h, 1, px, hW1.ctypes.data, hW2.ctypes.data, pL, pR,
+                                        py1, Dl, 2, 2, Dr, w, w, w)
+        assert st == 0, lib.fmpt_last_error(h)
+        y0 = _get(lib, h, py0, 2 * x.size)
+        y1 = _get(lib, h, py1, 2 * x.size)
         assert np.linalg.norm(y1 - y0) <= 1e-12 * np.linalg.norm(y0), call
         for p in (px, pL, pR, py0, py1):
             lib.fmpt_free(h, p)
