@@ -48,6 +48,7 @@ NCU_TRAFFIC = {("bf16", 2048): {"bytes_per_launch": (88.77e6 + 134.09e6 + 334.29
                                 "algorithmic_operand_bytes": {"gemm1": 76.0e6, "gemm2": 210.0e6}}}
 UNIT = "TFLOP/s"
 W_MPO, D_PHYS = 5, 2
+OZ_PRODUCTS = 45          # BF16 digit products per FP64 multiply-add of the fp64_tc GEMM
 
 
 def flops_ac2(D, w=W_MPO, d=D_PHYS):
@@ -215,7 +216,70 @@ def cpu_dmrg_sweeps(mpo, e_ed, e_gpu, budget_s=40.0):
             "note": "numpy/OpenBLAS with all host threads; E is the last Ritz value"}
 
 
-def dmrg_section(h, fm, budget_s=150.0):
+def config3_j1j2(h, fm, run, full=False, L=100, window=20):
+    """J1-J2 L=100 (J1=1, J2=0.3), cutoff 1e-9, D ramp 64 -> 256 -> 1024 from a seeded D=16
+    state.  (At J2=0.5 the ground state is an exact dimer product and keeps D<=3, so the
+    D=1024 stage runs at J2=0.3.)
+      mixed: 3xTF32 contractions and environment updates, FP64 Lanczos reorthogonalisation,
+             the FP64 density-matrix split with tail refinement;
+      fp64:  the plain form -- FP64-accurate contractions (the tensor-core FP64 engine) and
+             the reference's SVD split (gesvd).
+    Always: the mixed ramp with two D=1024 sweeps (the second one timed: sweep_s_mixed) and,
+    from that converged state, the same window of `window` consecutive centre bonds run in
+    both forms (state restored in between): window_s_mixed / window_s_fp64.
+    full=True adds the plain form's own ramp from the same start (64, 256, then one D=1024
+    sweep, timed: sweep_s_fp64) and the relative difference of the two FP64-evaluated
+    ground-state energies."""
+    import time as _t
+    from finitemptools_gb300 import algorithms as A
+    hj = fm.j1j2_heisenberg_mpo(1.0, 0.3)
+    mpo = fm.FiniteMPO(hj, L)
+    alg_mx = fm.DMRG2(eig_maxiter=30, eig_tol=1e-12, trunc=fm.MPSTruncation(1024, 1e-9),
+                      precision="tf32x3", reorth=True, svd="dm")
+    alg_64 = fm.DMRG2(eig_maxiter=30, eig_tol=1e-12, trunc=fm.MPSTruncation(1024, 1e-9),
+                      precision="fp64_tc", svd="gesvd")
+    env, tmx = run(L, hj, [(64, 1), (256, 1), (1024, 2)], "tf32x3", "dm", True, 1e-9, 16, 5)
+    E_mx = float(fm.expectation(env.mps, mpo))
+    res = {"J2": 0.3, "cutoff": 1e-9, "ramp_sweeps_s_mixed": tmx, "sweep_s_mixed": tmx[-1],
+           "Dmax_mixed": fm.bond_dimension(env.mps), "E_mixed_fp64_eval": E_mx}
+    # the window: left-sweep bond bodies at sites s0 .. s0+window-1 from the converged state
+    s0 = L // 2 - window // 2
+    env.precision = alg_mx.env_precision
+    for site in range(1, s0):
+        A._dmrg2_bond_left(env, site, alg_mx)
+    keep_mps = {i: env.mps[i].copy() for i in range(s0, s0 + window + 1)}
+    keep_env = {i: env.hstorage[i] for i in range(s0 + 1, s0 + window + 1)}
+    shapes = [list(env.mps[i].shape) for i in range(s0, s0 + window)]
+    times = {}
+    for name, alg in (("mixed", alg_mx), ("fp64", alg_64)):
+        env.precision = alg.env_precision
+        h.synchronize()
+        t0 = _t.perf_counter()
+        for site in range(s0, s0 + window):
+            A._dmrg2_bond_left(env, site, alg)
+        h.synchronize()
+        times[name] = _t.perf_counter() - t0
+        for i, v in keep_mps.items():
+            env.mps[i] = v.copy()
+        for i, v in keep_env.items():
+            env.hstorage[i] = v
+    res.update({"window_sites": [s0, s0 + window - 1], "window_site_shapes": shapes,
+                "window_s_mixed": times["mixed"], "window_s_fp64": times["fp64"],
+                "window_speedup_fp64_over_mixed": times["fp64"] / times["mixed"]})
+    del env, keep_mps, keep_env
+    if full:
+        env64, t64 = run(L, hj, [(64, 1), (256, 1), (1024, 1)], "fp64_tc", "gesvd", False, 1e-9,
+                         16, 5)
+        E_64 = float(fm.expectation(env64.mps, mpo))
+        res.update({"ramp_sweeps_s_fp64": t64, "sweep_s_fp64": t64[-1],
+                    "Dmax_fp64": fm.bond_dimension(env64.mps), "E_fp64": E_64,
+                    "dE_rel_mixed_vs_fp64": abs(E_mx - E_64) / abs(E_64),
+                    "sweep_speedup_fp64_over_mixed": t64[-1] / tmx[-1]})
+        del env64
+    return res
+
+
+def dmrg_section(h, fm, budget_s=150.0, full3=False, only3=False):
     """DMRG sweep seconds, plain FP64 vs the mixed form (3xTF32 contractions and
     environment updates, FP64 Lanczos reorthogonalisation, FP64 density-matrix
     split), each energy evaluated in FP64 as <psi|H|psi> of the final state.
@@ -253,6 +317,8 @@ def dmrg_section(h, fm, budget_s=150.0):
                 times.append(_t.perf_counter() - t0)
         return env, times
 
+    if only3:
+        return config3_j1j2(h, fm, run, full=True)
     hx = fm.heisenberg_xxz_mpo(1.0, 1.0, 0.0)
     env64, t64 = run(20, hx, [(64, 4)], "fp64", "gesvd", False, 1e-10, 8, 20)
     envmx, tmx = run(20, hx, [(64, 4)], "tf32x3", "dm", True, 1e-10, 8, 20)
@@ -294,87 +360,7 @@ def dmrg_section(h, fm, budget_s=150.0):
     out["xxz_L20_D64_dmrg1s"] = res1
     if _t.perf_counter() - t_start > budget_s:
         return out
-    hj = fm.j1j2_heisenberg_mpo(1.0, 0.3)
-    env, tramp = run(100, hj, [(64, 1), (256, 1), (1024, 1)], "tf32x3", "dm", True, 1e-9, 16, 5)
-    alg_mx = fm.DMRG2(eig_maxiter=30, eig_tol=1e-12, trunc=fm.MPSTruncation(1024, 1e-9),
-                      precision="tf32x3", reorth=True, svd="dm")
-    h.synchronize()
-    t0 = _t.perf_counter()
-    fm.sweep_(env, alg_mx)
-    h.synchronize()
-    t_mixed = _t.perf_counter() - t0
-    E = float(fm.expectation(env.mps, fm.FiniteMPO(hj, 100)))
-    Dmax = fm.bond_dimension(env.mps)
-    # the centre bond (left-sweep bond body) in both forms on the same tensors: advance the
-    # mixed left sweep to site 49 so that its left environment is current, then time the
-    # bond three times per form, restoring the two site tensors and the environment after
-    # every call
-    alg_64 = fm.DMRG2(eig_maxiter=30, eig_tol=1e-12, trunc=fm.MPSTruncation(1024, 1e-9))
-    env.precision = alg_mx.env_precision
-    for site in range(1, 49):
-        A._dmrg2_bond_left(env, site, alg_mx)
-    site = 49
-    bonds = []
-    for rep in range(3):          # rep 0 warms both forms up and is not reported
-        tb = {}
-        for name, alg in (("mixed", alg_mx), ("fp64", alg_64)):
-            saved = [env.mps[site].copy(), env.mps[site + 1].copy()]
-            saved_env = env.hstorage[site + 1]
-            env.precision = alg.env_precision
-            h.synchronize()
-            t0 = _t.perf_counter()
-            A._dmrg2_bond_left(env, site, alg)
-            h.synchronize()
-            tb[name] = _t.perf_counter() - t0
-            env.mps[site], env.mps[site + 1] = saved
-            env.hstorage[site + 1] = saved_env
-        if rep > 0:
-            bonds.append({"site": site, "D": list(env.mps[site].shape), "s_mixed": tb["mixed"],
-                          "s_fp64": tb["fp64"]})
-    ratio = sum(b["s_fp64"] for b in bonds) / sum(b["s_mixed"] for b in bonds)
-    del env
-    # the same bond body at a true D=1024: the ground state above keeps only the
-    # singular values the density-matrix split resolves (about 1e-6 sigma_max), so
-    # time one centre bond of a random (flat-spectrum) D=1024 state, both forms
-    # on the same tensors (L=24, J1-J2 w=8; environments built in the mixed form)
-    rng = np.random.default_rng(1024)
-    psi_r = fm.randommps(24, 2, 1024, rng, handle=h)
-    # iid N(0,1) entries scaled by 1/sqrt(D*d) on the side the environments are built
-    # from, so that both transfer maps keep the identity on average (no overflow)
-    for i in range(1, 25):
-        Dl_i, d_i, Dr_i = psi_r[i].shape
-        scal(1.0 / np.sqrt((Dl_i if i <= 12 else Dr_i) * d_i), psi_r[i])
-    env_r = fm.environments(fm.FiniteMPO(hj, 24), psi_r, "tf32x3")
-    for site in range(1, 12):
-        fm.updateleft_(env_r, site)
-    bond1024 = []
-    for rep in range(3):          # rep 0 warms both forms up and is not reported
-        tb = {}
-        for name, alg in (("mixed", alg_mx), ("fp64", alg_64)):
-            saved = [env_r.mps[12].copy(), env_r.mps[13].copy()]
-            saved_env = env_r.hstorage[13]
-            env_r.precision = alg.env_precision
-            h.synchronize()
-            t0 = _t.perf_counter()
-            A._dmrg2_bond_left(env_r, 12, alg)
-            h.synchronize()
-            tb[name] = _t.perf_counter() - t0
-            env_r.mps[12], env_r.mps[13] = saved
-            env_r.hstorage[13] = saved_env
-        if rep > 0:
-            bond1024.append({"site": 12, "D": list(env_r.mps[12].shape), "s_mixed": tb["mixed"],
-                             "s_fp64": tb["fp64"]})
-    ratio1024 = sum(b["s_fp64"] for b in bond1024) / sum(b["s_mixed"] for b in bond1024)
-    del env_r, psi_r
-    out["j1j2_L100_J2_0.3_D1024"] = {
-        "ramp_sweeps_s_mixed": tramp, "sweep_s_mixed": t_mixed, "Dmax": Dmax,
-        "E_mixed_fp64_eval": E, "centre_bonds": bonds, "bond_speedup_fp64_over_mixed": ratio,
-        "sweep_s_fp64_extrapolated": t_mixed * ratio,
-        "bond_D1024_random_state": bond1024, "bond_speedup_fp64_over_mixed_D1024": ratio1024,
-        "note": "FP64 sweep time = timed mixed sweep x (FP64 / mixed time of the centre bond); "
-                "the ground state keeps D = Dmax at cutoff 1e-9 (the density-matrix split "
-                "resolves sigma down to ~1e-6 sigma_max), so the D=1024 bond is timed on a "
-                "random flat-spectrum state"}
+    out["j1j2_L100_J2_0.3_D1024"] = config3_j1j2(h, fm, run, full=full3)
     if _t.perf_counter() - t_start > budget_s:
         return out
     # XX chain (Delta = 0), L=200, D=256, against the free-fermion closed form
@@ -835,6 +821,9 @@ def main():
     ap.add_argument("--no-u1", action="store_true")
     ap.add_argument("--no-grad", action="store_true")
     ap.add_argument("--no-next", action="store_true")
+    ap.add_argument("--config3", action="store_true",
+                    help="only the J1-J2 L=100 D=1024 mixed-vs-FP64 comparison with both forms' "
+                         "full ramps (sweep times and energies of both), printed as JSON")
     ap.add_argument("--ed-heff", type=int, default=0, metavar="L",
                     help="time the exact-diagonalisation operator of an L-site XXZ chain alone")
     ap.add_argument("--u1-heff", type=int, default=0, metavar="D",
@@ -867,6 +856,10 @@ def main():
     h = fm.Handle(local)
     h.set_stream(stream.cuda_stream)
 
+    if args.config3:
+        res = dmrg_section(h, fm, full3=True, only3=True)
+        print(json.dumps({"config3": res}), flush=True)
+        return
     D, prec = args.D, args.precision
     x, L, R, W = workload(D)
     xd, Ld, Rd = DT.from_numpy(x, h), DT.from_numpy(L, h), DT.from_numpy(R, h)
@@ -920,6 +913,11 @@ def main():
         pass
     if prec == "bf16":
         peak, peak_note = peaks.get("bf16_tflops", 1900.0), "bf16_tflops (burst) of measured"
+    elif prec == "fp64_tc":
+        # the FP64-accurate GEMM forms 45 BF16 digit products per FP64 multiply-add: the FP64
+        # rate it can reach is the measured BF16 peak / 45
+        peak = peaks.get("bf16_tflops", 1900.0) / OZ_PRODUCTS
+        peak_note = "bf16_tflops (burst) of measured / %d digit products" % OZ_PRODUCTS
     elif prec in ("tf32", "tf32x3"):
         peak = peaks.get("bf16_tflops", 1900.0) / 2
         peak_note = "half of measured bf16_tflops (dense TF32 rate is half of BF16)"
@@ -931,7 +929,9 @@ def main():
         achieved = per_launch / (tc_ms / tc_n / 1e3) / 1e12
         if prec == "tf32x3":
             achieved *= 1.0          # algorithmic flops only (3 products are not credited)
-        roof = {"bound": "tensor", "kernel": "tc_gemm (tcgen05 %s)" % prec,
+        kname = ("oz_gemm_pair (tcgen05 BF16 digit products of the FP64-accurate GEMM)"
+                 if prec == "fp64_tc" else "tc_gemm (tcgen05 %s)" % prec)
+        roof = {"bound": "tensor", "kernel": kname,
                 "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": achieved / peak if peak else None, "peak_source": peak_note,
                 "traffic": NCU_TRAFFIC.get((prec, D)), "launches": tc_n,
@@ -939,6 +939,10 @@ def main():
                 "share_of_step": tc_ms / tot_ms if tot_ms else None,
                 "other_kernels_ms_per_step": {"mpo_step": mid_ms / args.steps,
                                               "convert": cv_ms / args.steps}}
+        if prec == "fp64_tc":
+            roof["bf16_mma_tflops"] = achieved * OZ_PRODUCTS
+            roof["unit_note"] = ("achieved: algorithmic FP64 flops (2 w d^2 D^3 per launch) per "
+                                 "second; bf16_mma_tflops: the digit-product MMA work per second")
         if prec == "bf16" and rank == 0:
             roof["cublas_same_shapes"] = cublas_same_shapes(D, stream)
 

@@ -90,6 +90,7 @@ SIGNATURES = {
     "fmpt_set_svd_method": (c_int, [c_void_p, c_int]),
     "fmpt_set_tc_tile": (c_int, [c_void_p, c_int]),
     "fmpt_set_f64_engine": (c_int, [c_void_p, c_int]),
+    "fmpt_set_wait_test": (c_int, [c_void_p, c_int64, c_int]),
     "fmpt_ac2_prime_host": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p,
                                     c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_int,
                                     c_int, c_int, c_int]),

@@ -395,6 +395,15 @@ int fmpt_set_f64_engine(fmpt_handle* h, int mode) {
   return FMPT_OK;
 }
 
+int fmpt_set_wait_test(fmpt_handle* h, int64_t timeout_ns, int hold) {
+  if (!h) return FMPT_ERR_ARG;
+  if (timeout_ns < 0 || timeout_ns > 10000000000LL || hold < 0 || hold > 1)
+    return set_error(h, FMPT_ERR_ARG, "wait test: timeout 0..1e10 ns, hold 0 or 1");
+  h->wait_test_ns = timeout_ns;
+  h->wait_test_hold = hold;
+  return FMPT_OK;
+}
+
 int fmpt_set_graphs(fmpt_handle* h, int on) {
   if (!h) return FMPT_ERR_ARG;
   h->graphs = on != 0;

@@ -43,6 +43,9 @@ struct GKArgs {
   int* ctl;        // [0, GP_MAX_PHASES) tile counters, then barrier count, then abort flag
   int* status;     // handle status word (1 = a bounded wait gave up)
   const int* gate; // nonzero at launch: return at once (nullptr: always run)
+  uint64_t wait_ns;   // bound of every barrier wait
+  int hold;           // arrivals the barriers wait for beyond the grid (0; > 0 only to test
+                      // the bounded wait: the barrier then gives up after wait_ns)
 };
 
 __device__ __forceinline__ int64_t op_index(int t, int r, int c, int64_t ld) {
@@ -72,9 +75,9 @@ __device__ bool grid_barrier(const GKArgs& a, int target, int* s_flag) {
     atomicAdd(bar, 1);
     int ok = 1;
     const uint64_t t0 = global_ns();
-    while (ld_acquire(bar) < target) {
+    while (ld_acquire(bar) < target + a.hold) {
       if (ld_acquire(abort_flag)) { ok = 0; break; }
-      if (global_ns() - t0 > kBarrierTimeoutNs) {
+      if (global_ns() - t0 > a.wait_ns) {
         atomicExch(abort_flag, 1);
         atomicExch(a.status, 1);
         ok = 0;
@@ -494,6 +497,8 @@ int gp_run(fmpt_handle* h, const GroupedProgram& g, double* const* slots, int ns
   a.tile_prob = g.d_tile_prob; a.tile_mn = g.d_tile_mn;
   a.ctl = g.d_ctl;
   a.gate = gate;
+  a.wait_ns = h->wait_test_ns > 0 ? (uint64_t)h->wait_test_ns : kBarrierTimeoutNs;
+  a.hold = h->wait_test_hold;
   FMPT_TRY(gp_status_word(h, &a.status));
   FMPT_CUDA(h, cudaMemsetAsync(g.d_ctl, 0, (GP_MAX_PHASES + 2) * sizeof(int), h->stream));
   ProfScope prof(h, FMPT_K_GROUPED);

@@ -73,6 +73,50 @@ __global__ void mid_kernel(const double* __restrict__ in, int64_t plane_in, MidS
   }
 }
 
+// Sparse form of the block step: for each output (wo, q) the list of its nonzero terms
+// (wi, s, coefficient), in block order then s -- the order in which mid_kernel adds them,
+// so that both give the same sums.  It does only the nonzero multiply-adds (the two-site
+// blocks are Kronecker products of single-site operators, mostly zeros), which is what
+// bounds the step on GB300's FP64 pipe.  Passed by value.
+struct MidSparse {
+  int n_out;                          // nw_out * p_out
+  short start[MS_MAX_OUT + 1];
+  short idx[MS_MAX_T];                // wi * 16 + s
+  double c[MS_MAX_T];                 // real coefficients; complex: re, im pairs
+};
+
+template <bool CPLX>
+__global__ void mid_sparse_kernel(const double* __restrict__ in, int64_t plane_in, MidStrides si,
+                                  double* __restrict__ out, int64_t plane_out, MidStrides so,
+                                  int n1, int n2, int p_out, const __grid_constant__ MidSparse ms) {
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)n1 * n2) return;
+  const int o1 = (int)(t % n1), o2 = (int)(t / n1);
+  const double* ib = in + o1 * si.o1 + o2 * si.o2;
+  double* ob = out + o1 * so.o1 + o2 * so.o2;
+  for (int o = 0; o < ms.n_out; o++) {
+    const int wo = o / p_out, q = o - wo * p_out;
+    double ar = 0.0, ai = 0.0;
+    for (int e = ms.start[o]; e < ms.start[o + 1]; e++) {
+      const int ix = ms.idx[e];
+      const int64_t off = (ix >> 4) * si.w + (ix & 15) * si.s;
+      const double vr = ib[off];
+      if (CPLX) {
+        const double vi = ib[plane_in + off];
+        const double cr = ms.c[2 * e], ci = ms.c[2 * e + 1];
+        ar = fma(cr, vr, ar);
+        ar = fma(-ci, vi, ar);
+        ai = fma(cr, vi, ai);
+        ai = fma(ci, vr, ai);
+      } else {
+        ar = fma(ms.c[e], vr, ar);
+      }
+    }
+    ob[wo * so.w + q * so.s] = ar;
+    if (CPLX) ob[plane_out + wo * so.w + q * so.s] = ai;
+  }
+}
+
 // host-side complex helpers for schedule construction
 struct C2 { double r, i; };
 inline C2 cmul(C2 a, C2 b) { return {a.r * b.r - a.i * b.i, a.r * b.i + a.i * b.r}; }
@@ -101,6 +145,35 @@ void build_schedule(int cplx, int nw_in, int nw_out, int p_in, int p_out,
     }
   }
   s.wout_start[nw_out] = (int)s.blk_win.size();
+  // the sparse term lists (left empty when they do not fit MidSparse)
+  s.sp_start.clear();
+  s.sp_idx.clear();
+  s.sp_coef.clear();
+  const int cap = cplx ? MS_MAX_T / 2 : MS_MAX_T;
+  bool fits = nw_out * p_out <= MS_MAX_OUT && p_in <= 16;
+  std::vector<int> st, ix;
+  std::vector<double> cf;
+  for (int wo = 0; wo < nw_out && fits; wo++)
+    for (int q = 0; q < p_out && fits; q++) {
+      st.push_back((int)ix.size());
+      for (int b = s.wout_start[wo]; b < s.wout_start[wo + 1]; b++) {
+        const double* cb = &s.coef[(size_t)b * csz * (cplx ? 2 : 1)];
+        for (int si = 0; si < p_in; si++) {
+          const double cr = cb[q * p_in + si], ci = cplx ? cb[csz + q * p_in + si] : 0.0;
+          if (cr == 0.0 && ci == 0.0) continue;
+          ix.push_back(s.blk_win[b] * 16 + si);
+          cf.push_back(cr);
+          if (cplx) cf.push_back(ci);
+        }
+      }
+      if ((int)ix.size() > cap) fits = false;
+    }
+  if (fits) {
+    st.push_back((int)ix.size());
+    s.sp_start = st;
+    s.sp_idx = ix;
+    s.sp_coef = cf;
+  }
 }
 
 }  // namespace
@@ -213,6 +286,21 @@ int mid_apply(fmpt_handle* h, const MidSchedule& s, const double* in, int64_t pl
   int P = std::max(s.p_in, s.p_out);
   if (P > 16) return set_error(h, FMPT_ERR_UNSUPPORTED, "physical dimension product %d > 16", P);
   ProfScope prof(h, FMPT_K_MPO_STEP);
+  if (!s.sp_start.empty()) {
+    MidSparse ms;
+    ms.n_out = (int)s.sp_start.size() - 1;
+    for (size_t i = 0; i < s.sp_start.size(); i++) ms.start[i] = (short)s.sp_start[i];
+    for (size_t i = 0; i < s.sp_idx.size(); i++) ms.idx[i] = (short)s.sp_idx[i];
+    for (size_t i = 0; i < s.sp_coef.size(); i++) ms.c[i] = s.sp_coef[i];
+    if (s.cplx)
+      mid_sparse_kernel<true><<<(unsigned)blocks, threads, 0, h->stream>>>(
+          in, plane_in, si, out, plane_out, so, n1, n2, s.p_out, ms);
+    else
+      mid_sparse_kernel<false><<<(unsigned)blocks, threads, 0, h->stream>>>(
+          in, plane_in, si, out, plane_out, so, n1, n2, s.p_out, ms);
+    FMPT_LAUNCHED(h);
+    return FMPT_OK;
+  }
 #define MIDL(MP, CP)                                                                          \
   mid_kernel<MP, CP><<<(unsigned)blocks, threads, 0, h->stream>>>(                            \
       in, plane_in, si, out, plane_out, so, n1, n2, s.nw_out, s.p_in, s.p_out, s.d_win,       \
@@ -241,10 +329,14 @@ static GemmArgs gemm_args(int cplx, int ta, int tb, int m, int n, int k, const d
 
 int op_apply_fp64(fmpt_op* op, const double* x, double* y) {
   fmpt_handle* h = op->h;
-  // FP64_TC: the GEMMs go to the tensor-core FP64 engine wherever it is faster
+  // FP64_TC: the GEMMs go to the tensor-core FP64 engine wherever it is faster; the digit
+  // planes of the environments (A of the first GEMM, B of the second) are kept in the
+  // operator, since they do not change while it lives
   const int eng = op->precision == FMPT_PREC_FP64_TC ? 1 : 0;
   auto gemm_f64 = [&](fmpt_handle* hh, GemmArgs g) {
     g.engine = eng;
+    if (eng && g.A == op->hleft) g.cacheA = &op->oz_left;
+    if (eng && g.B == op->hright) g.cacheB = &op->oz_right;
     return fmpt::gemm_f64(hh, g);
   };
   const int cp = op->dtype == FMPT_C128;
@@ -372,6 +464,8 @@ int64_t fmpt_op_size(fmpt_op* op) { return op ? op->n : -1; }
 int fmpt_op_destroy(fmpt_op* op) {
   if (!op) return FMPT_OK;
   mid_free(op->h, op->sched);
+  oz_cache_free(op->h, op->oz_left);
+  oz_cache_free(op->h, op->oz_right);
   op_tc_free(op);
   op_u1_free(op);
   if (op->proj_part) cudaFreeAsync(op->proj_part, op->h->stream);

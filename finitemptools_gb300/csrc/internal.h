@@ -50,6 +50,10 @@ struct fmpt_handle {
   // f64_tc 1 routes every FP64 GEMM of this handle there when its cost model says it is
   // faster than the CUDA-core kernel (fmpt_set_f64_engine)
   int f64_tc = 0;
+  // failure-detection test hook (fmpt_set_wait_test): bound of the grouped kernel's barrier
+  // waits (0: 2 s) and extra arrivals they wait for (0 in normal use)
+  int64_t wait_test_ns = 0;
+  int wait_test_hold = 0;
   void* oz_ws = nullptr;
   size_t oz_ws_bytes = 0;
   // executable graphs of the captured Arnoldi basis, one per operator structure
@@ -125,6 +129,18 @@ struct ProfScope {
   ~ProfScope();
 };
 
+// Digit planes and exponents of one FP64 GEMM operand for the tensor-core FP64 engine,
+// kept across calls by an owner whose operand does not change between them (a prepared
+// operator's environments): built on first use, reused while src and shape match.
+struct OzCache {
+  const double* src = nullptr;
+  int64_t key[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  void* buf = nullptr;
+  size_t bytes = 0;
+  bool valid = false;
+};
+void oz_cache_free(fmpt_handle* h, OzCache& c);
+
 // -------- generic FP64 / split-complex GEMM (gemm_f64.cu)
 // C = alpha op(A) op(B) + beta C ; planes: element offsets between re and im planes.
 struct GemmArgs {
@@ -139,6 +155,8 @@ struct GemmArgs {
   int64_t strideA, strideB, strideC;
   int nosplit;              // 1: never split K (no workspace allocation)
   int engine;               // 0: the handle's FP64 engine, 1: tensor cores where faster
+  OzCache* cacheA;          // optional digit-plane caches of A / B (tensor-core engine)
+  OzCache* cacheB;
 };
 int gemm_f64(fmpt_handle* h, const GemmArgs& g);
 // the Ozaki-scheme FP64 GEMM on the BF16 tensor cores (ozaki.cu): whether it applies to g
@@ -154,11 +172,16 @@ inline bool prec_is_f64(int precision) {
 
 // -------- block-sparse MPO "middle" contraction (heff.cu)
 // out[o1, o2, wo, so] = sum_{blocks (wi -> wo)} sum_si coef[so, si] in[o1, o2, wi, si]
+constexpr int MS_MAX_OUT = 128, MS_MAX_T = 512;   // sparse MPO-step table capacity
 struct MidSchedule {
   int nw_in = 0, nw_out = 0, p_in = 0, p_out = 0, cplx = 0;
   std::vector<int> blk_win;      // per block: input w
   std::vector<int> wout_start;   // nw_out + 1 prefix offsets into the blocks (sorted by wo)
   std::vector<double> coef;      // per block: p_out x p_in (row-major so, si), re then im if cplx
+  // the nonzero terms per output (wo, so): prefix offsets, wi * 16 + si, coefficients (re, im
+  // pairs if cplx); empty when they exceed the by-value table of the sparse kernel
+  std::vector<int> sp_start, sp_idx;
+  std::vector<double> sp_coef;
   // device copies
   int* d_win = nullptr;
   int* d_wstart = nullptr;
@@ -270,6 +293,8 @@ struct fmpt_op {
   bool defer_right = false;  // mixed precision: the right environment is converted later
   // FP64 intermediates of one application (T1/T3 or T), grown outside stream capture only
   double* scratch = nullptr;
+  // digit planes of the environments for the tensor-core FP64 engine (FP64_TC operators)
+  fmpt::OzCache oz_left, oz_right;
   size_t scratch_bytes = 0;
   // projectors of the excited-state sweeps: after every application
   // y -= dot(y, p) p for each p in order (device vectors of n elements, not owned)

@@ -276,6 +276,75 @@ int fmpt_svd_trunc(fmpt_handle* h, int dtype, const double* M, int m, int n, int
   return FMPT_OK;
 }
 
+namespace fmpt {
+namespace {
+
+// Hermitian eigendecomposition of an r x r split-plane matrix H (lower triangle used):
+// eigenvalues ascending into W (device), eigenvectors (columns, split planes) into V.
+int eigh_split(fmpt_handle* h, int cp, int r, const double* H, double* W, double* V) {
+  DevBuf inter, work, dinfo;
+  double* A = V;
+  if (cp) {
+    FMPT_TRY(inter.alloc(h, (size_t)r * r * 2 * sizeof(double)));
+    FMPT_TRY(copy_mat(h, 1, r, r, H, r, (int64_t)r * r, 0, 0, inter.d(), r, -1));
+    A = inter.d();
+  } else if (H != V) {
+    FMPT_CUDA(h, cudaMemcpyAsync(V, H, (size_t)r * r * sizeof(double), cudaMemcpyDeviceToDevice,
+                                 h->stream));
+  }
+  FMPT_TRY(dinfo.alloc(h, sizeof(int)));
+  int lwork = 0;
+  if (cp)
+    FMPT_SOLVER(h, cusolverDnZheevd_bufferSize(h->solver, CUSOLVER_EIG_MODE_VECTOR,
+                                               CUBLAS_FILL_MODE_LOWER, r, (cuDoubleComplex*)A, r,
+                                               W, &lwork));
+  else
+    FMPT_SOLVER(h, cusolverDnDsyevd_bufferSize(h->solver, CUSOLVER_EIG_MODE_VECTOR,
+                                               CUBLAS_FILL_MODE_LOWER, r, A, r, W, &lwork));
+  FMPT_TRY(work.alloc(h, (size_t)std::max(lwork, 1) * sizeof(double) * (cp ? 2 : 1)));
+  if (cp)
+    FMPT_SOLVER(h, cusolverDnZheevd(h->solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, r,
+                                    (cuDoubleComplex*)A, r, W, (cuDoubleComplex*)work.p, lwork,
+                                    (int*)dinfo.p));
+  else
+    FMPT_SOLVER(h, cusolverDnDsyevd(h->solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, r,
+                                    A, r, W, work.d(), lwork, (int*)dinfo.p));
+  int info = 0;
+  FMPT_TRY(read_info(h, (const int*)dinfo.p, &info));
+  if (info != 0) return set_error(h, FMPT_ERR_CUSOLVER, "syevd/heevd info %d", info);
+  if (cp) FMPT_TRY(copy_mat(h, 1, r, r, A, r, -1, 0, 0, V, r, (int64_t)r * r));
+  return FMPT_OK;
+}
+
+// dst column j = src column idx[j] (r rows, split planes with the given plane strides)
+__global__ void gather_cols(int cp, int r, int k, const double* __restrict__ src, int64_t splane,
+                            const int* __restrict__ idx, double* __restrict__ dst,
+                            int64_t dplane) {
+  const int64_t tot = (int64_t)r * k;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < tot;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(t % r), j = (int)(t / r);
+    const int64_t s = (int64_t)idx[j] * r + i;
+    dst[t] = src[s];
+    if (cp) dst[dplane + t] = src[splane + s];
+  }
+}
+
+GemmArgs gemm_plain(int cp, int ta, int tb, int m, int n, int k, const double* A, int64_t lda,
+                    int64_t pA, const double* B, int64_t ldb, int64_t pB, double* C, int64_t ldc,
+                    int64_t pC) {
+  GemmArgs g{};
+  g.cplx = cp; g.ta = ta; g.tb = tb; g.m = m; g.n = n; g.k = k;
+  g.alpha[0] = 1.0; g.batch = 1;
+  g.A = A; g.lda = lda; g.planeA = pA;
+  g.B = B; g.ldb = ldb; g.planeB = pB;
+  g.C = C; g.ldc = ldc; g.planeC = pC;
+  return g;
+}
+
+}  // namespace
+}  // namespace fmpt
+
 int fmpt_dm_split(fmpt_handle* h, int dtype, const double* M, int m, int n, int maxD,
                   double eps, int side, double* Aout, double* S, double* Bout, int* kout,
                   double* errout) {
@@ -284,60 +353,104 @@ int fmpt_dm_split(fmpt_handle* h, int dtype, const double* M, int m, int n, int 
   if (side != 0 && side != 1) return set_error(h, FMPT_ERR_ARG, "dm_split: side must be 0 or 1");
   const int cp = dtype == FMPT_C128;
   const bool left = side == 0;
-  const int r = left ? m : n;
-  const int64_t planeM = (int64_t)m * n;
-  // rho = M M^H (left) or M^H M (right), split planes, FP64 GEMM
-  DevBuf rho, W, rhoI, work, dinfo;
-  FMPT_TRY(rho.alloc(h, (size_t)r * r * sizeof(double) * (cp ? 2 : 1)));
-  {
-    GemmArgs g{};
-    g.cplx = cp; g.alpha[0] = 1.0; g.batch = 1;
-    g.m = r; g.n = r; g.k = left ? n : m;
-    g.A = M; g.lda = m; g.planeA = planeM;
-    g.B = M; g.ldb = m; g.planeB = planeM;
-    g.C = rho.d(); g.ldc = r; g.planeC = (int64_t)r * r;
-    if (left) { g.ta = FMPT_N; g.tb = FMPT_C; } else { g.ta = FMPT_C; g.tb = FMPT_N; }
-    FMPT_TRY(gemm_f64(h, g));
-  }
+  // X = op(M): M (left, r = m rows of length c = n) or M^H (right, r = n, c = m)
+  const int r = left ? m : n, c = left ? n : m;
+  const int xop = left ? FMPT_N : FMPT_C;
+  const int64_t planeM = (int64_t)m * n, pr = (int64_t)r * r;
+  // pass 1: rho = X X^H, U diag(lam) U^H (FP64 GEMM + cuSOLVER syevd/heevd)
+  DevBuf rho, U, W;
+  FMPT_TRY(rho.alloc(h, (size_t)pr * sizeof(double) * (cp ? 2 : 1)));
+  FMPT_TRY(U.alloc(h, (size_t)pr * sizeof(double) * (cp ? 2 : 1)));
   FMPT_TRY(W.alloc(h, (size_t)r * sizeof(double)));
-  FMPT_TRY(dinfo.alloc(h, sizeof(int)));
-  double* A = rho.d();
-  if (cp) {
-    FMPT_TRY(rhoI.alloc(h, (size_t)r * r * 2 * sizeof(double)));
-    FMPT_TRY(copy_mat(h, 1, r, r, rho.d(), r, (int64_t)r * r, 0, 0, rhoI.d(), r, -1));
-    A = rhoI.d();
-  }
-  int lwork = 0;
-  if (cp)
-    FMPT_SOLVER(h, cusolverDnZheevd_bufferSize(h->solver, CUSOLVER_EIG_MODE_VECTOR,
-                                               CUBLAS_FILL_MODE_LOWER, r, (cuDoubleComplex*)A, r,
-                                               W.d(), &lwork));
-  else
-    FMPT_SOLVER(h, cusolverDnDsyevd_bufferSize(h->solver, CUSOLVER_EIG_MODE_VECTOR,
-                                               CUBLAS_FILL_MODE_LOWER, r, A, r, W.d(), &lwork));
-  FMPT_TRY(work.alloc(h, (size_t)std::max(lwork, 1) * sizeof(double) * (cp ? 2 : 1)));
-  if (cp)
-    FMPT_SOLVER(h, cusolverDnZheevd(h->solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, r,
-                                    (cuDoubleComplex*)A, r, W.d(), (cuDoubleComplex*)work.p, lwork,
-                                    (int*)dinfo.p));
-  else
-    FMPT_SOLVER(h, cusolverDnDsyevd(h->solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, r,
-                                    A, r, W.d(), work.d(), lwork, (int*)dinfo.p));
-  int info = 0;
-  FMPT_TRY(read_info(h, (const int*)dinfo.p, &info));
-  if (info != 0) return set_error(h, FMPT_ERR_CUSOLVER, "syevd/heevd info %d", info);
-  // sigma (descending) on the host; the rank is at most min(m, n)
-  std::vector<double> lam(r), s(r);
+  FMPT_TRY(gemm_f64(h, gemm_plain(cp, xop, left ? FMPT_C : FMPT_N, r, r, c, M, m, planeM, M, m,
+                                  planeM, rho.d(), r, pr)));
+  FMPT_TRY(eigh_split(h, cp, r, rho.d(), W.d(), U.d()));
+  std::vector<double> lam(r);
   FMPT_CUDA(h, cudaMemcpyAsync(lam.data(), W.d(), r * sizeof(double), cudaMemcpyDeviceToHost,
                                h->stream));
   FMPT_CUDA(h, cudaStreamSynchronize(h->stream));
-  // eigenvalues below the eigensolver's noise floor (~ r eps lambda_max) are
-  // exact zeros: their square roots (~1e-8 sigma_max) would be junk directions
   const int rank_max = std::min(m, n);
-  const double floor_ = 4.0 * r * 2.220446049250313e-16 * std::max(lam[r - 1], 0.0);
+  const double epsm = 2.220446049250313e-16;
+  // Squaring the matrix leaves an eigenvalue lam resolved only to ~ r eps lam_max, i.e. a
+  // singular value to ~ sqrt(r eps) sigma_max.  Refinement passes resolve the tail: the
+  // columns [0, t) of U (ascending lam) whose lam is below TAU times the largest of the
+  // pass are rotated again, by the eigenvectors of the Gram matrix of their rows of
+  // U^H X -- rows from which the components along the resolved rows have been projected
+  // out -- so that the next pass resolves lam relative to the tail's own largest value.
+  const double TAU = 1e-8;
+  const int MAXPASS = 4;
+  int t = r;                                          // unresolved prefix of U's columns
+  double floor_ = 4.0 * r * epsm * std::max(lam[r - 1], 0.0);
+  for (int pass = 1; pass < MAXPASS && t > 0; pass++) {
+    const double top = std::max(lam[t - 1], 0.0);
+    const double thr = TAU * top;
+    int tn = 0;
+    while (tn < t && lam[tn] < thr) tn++;
+    if (tn == 0) break;
+    const int nres = r - tn;
+    // nothing below the resolved set can be kept: the bond is full, or the tail lies
+    // below the cutoff eps ||sigma||_2
+    double nrm2 = 0.0;
+    for (int i = tn; i < r; i++) nrm2 += std::max(lam[i], 0.0);
+    if (std::min(nres, rank_max) >= maxD) break;
+    if (std::sqrt(thr) < 0.25 * eps * std::sqrt(nrm2)) break;
+    if (top <= 0.0) break;
+    // rows of the resolved directions, normalised: Qr = diag(lam)^-1/2 U_res^H X
+    DevBuf Qr, Bt, G, inv, Gt, Wt, Vt, Ut;
+    const int64_t pq = (int64_t)nres * c, pb = (int64_t)tn * c;
+    FMPT_TRY(Qr.alloc(h, (size_t)pq * sizeof(double) * (cp ? 2 : 1)));
+    FMPT_TRY(Bt.alloc(h, (size_t)pb * sizeof(double) * (cp ? 2 : 1)));
+    const double* Ures = U.d() + (int64_t)tn * r;
+    FMPT_TRY(gemm_f64(h, gemm_plain(cp, FMPT_C, xop, nres, c, r, Ures, r, pr, M, m, planeM,
+                                    Qr.d(), nres, pq)));
+    std::vector<double> sc(nres);
+    for (int i = 0; i < nres; i++) sc[i] = lam[tn + i] > 0.0 ? 1.0 / std::sqrt(lam[tn + i]) : 0.0;
+    FMPT_TRY(inv.alloc(h, (size_t)nres * sizeof(double)));
+    FMPT_CUDA(h, cudaMemcpyAsync(inv.d(), sc.data(), nres * sizeof(double), cudaMemcpyHostToDevice,
+                                 h->stream));
+    FMPT_TRY(fmpt_scale_dim(h, dtype, 0, nres, c, inv.d(), Qr.d()));
+    // tail rows Bt = U_tail^H X, minus their components along the resolved rows (twice)
+    FMPT_TRY(gemm_f64(h, gemm_plain(cp, FMPT_C, xop, tn, c, r, U.d(), r, pr, M, m, planeM,
+                                    Bt.d(), tn, pb)));
+    FMPT_TRY(G.alloc(h, (size_t)tn * nres * sizeof(double) * (cp ? 2 : 1)));
+    for (int rep = 0; rep < 2; rep++) {
+      FMPT_TRY(gemm_f64(h, gemm_plain(cp, FMPT_N, FMPT_C, tn, nres, c, Bt.d(), tn, pb, Qr.d(),
+                                      nres, pq, G.d(), tn, (int64_t)tn * nres)));
+      GemmArgs g = gemm_plain(cp, FMPT_N, FMPT_N, tn, c, nres, G.d(), tn, (int64_t)tn * nres,
+                              Qr.d(), nres, pq, Bt.d(), tn, pb);
+      g.alpha[0] = -1.0;
+      g.beta[0] = 1.0;
+      FMPT_TRY(gemm_f64(h, g));
+    }
+    // Gram of the tail rows, its eigenvectors rotate the tail columns of U
+    const int64_t pt = (int64_t)tn * tn;
+    FMPT_TRY(Gt.alloc(h, (size_t)pt * sizeof(double) * (cp ? 2 : 1)));
+    FMPT_TRY(Wt.alloc(h, (size_t)tn * sizeof(double)));
+    FMPT_TRY(Vt.alloc(h, (size_t)pt * sizeof(double) * (cp ? 2 : 1)));
+    FMPT_TRY(gemm_f64(h, gemm_plain(cp, FMPT_N, FMPT_C, tn, tn, c, Bt.d(), tn, pb, Bt.d(), tn, pb,
+                                    Gt.d(), tn, pt)));
+    FMPT_TRY(eigh_split(h, cp, tn, Gt.d(), Wt.d(), Vt.d()));
+    FMPT_TRY(Ut.alloc(h, (size_t)r * tn * sizeof(double) * (cp ? 2 : 1)));
+    FMPT_TRY(gemm_f64(h, gemm_plain(cp, FMPT_N, FMPT_N, r, tn, tn, U.d(), r, pr, Vt.d(), tn, pt,
+                                    Ut.d(), r, (int64_t)r * tn)));
+    FMPT_TRY(copy_mat(h, cp, r, tn, Ut.d(), r, (int64_t)r * tn, 0, 0, U.d(), r, pr));
+    FMPT_CUDA(h, cudaMemcpyAsync(lam.data(), Wt.d(), tn * sizeof(double), cudaMemcpyDeviceToHost,
+                                 h->stream));
+    FMPT_CUDA(h, cudaStreamSynchronize(h->stream));
+    floor_ = 4.0 * tn * epsm * std::max(lam[tn - 1], 0.0);
+    t = tn;
+  }
+  // sigma descending: the resolved columns [t, r) and the prefix [0, t) above its pass's
+  // noise floor (below it an eigenvalue is rounding noise and counts as an exact zero)
+  std::vector<int> order(r);
+  for (int i = 0; i < r; i++) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return lam[a] > lam[b]; });
+  std::vector<double> s(r);
   for (int i = 0; i < r; i++) {
-    const double l = lam[r - 1 - i];
-    s[i] = (i < rank_max && l > floor_) ? std::sqrt(l) : 0.0;
+    const int j = order[i];
+    const double l = lam[j];
+    const bool ok = j >= t ? l > 0.0 : l > floor_;
+    s[i] = (i < rank_max && ok) ? std::sqrt(l) : 0.0;
   }
   double nrm = 0.0;
   for (double v : s) nrm += v * v;
@@ -355,12 +468,19 @@ int fmpt_dm_split(fmpt_handle* h, int dtype, const double* M, int m, int n, int 
   *kout = k;
   if (errout) *errout = std::sqrt(e1 + e2);
   FMPT_CUDA(h, cudaMemcpyAsync(S, s.data(), k * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-  // Q (r x k, split planes): eigenvectors of the k largest eigenvalues, descending;
-  // one copy with a negative column stride starting at the last column
-  DevBuf Q;
+  // Q (r x k, split planes): the columns of the k largest, descending
+  DevBuf Q, didx;
   FMPT_TRY(Q.alloc(h, (size_t)r * k * sizeof(double) * (cp ? 2 : 1)));
-  FMPT_TRY(copy_mat(h, cp, r, k, A + (size_t)(r - 1) * r * (cp ? 2 : 1), -(int64_t)r,
-                    cp ? -1 : 0, 0, 0, Q.d(), r, (int64_t)r * k));
+  FMPT_TRY(didx.alloc(h, (size_t)k * sizeof(int)));
+  FMPT_CUDA(h, cudaMemcpyAsync(didx.p, order.data(), k * sizeof(int), cudaMemcpyHostToDevice,
+                               h->stream));
+  {
+    const int64_t tot = (int64_t)r * k;
+    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((tot + 255) / 256, 8LL * h->sm_count));
+    gather_cols<<<blocks, 256, 0, h->stream>>>(cp, r, k, U.d(), pr, (const int*)didx.p, Q.d(),
+                                               (int64_t)r * k);
+    FMPT_LAUNCHED(h);
+  }
   GemmArgs g{};
   g.cplx = cp; g.alpha[0] = 1.0; g.batch = 1;
   if (left) {
@@ -381,7 +501,7 @@ int fmpt_dm_split(fmpt_handle* h, int dtype, const double* M, int m, int n, int 
     g.C = Aout; g.ldc = m; g.planeC = (int64_t)m * k;
     FMPT_TRY(gemm_f64(h, g));
   }
-  // the host vector s must stay alive until its async copy finishes
+  // the host vectors must stay alive until their async copies finish
   FMPT_CUDA(h, cudaStreamSynchronize(h->stream));
   return FMPT_OK;
 }

@@ -15,10 +15,11 @@
 //      BF16 -> FP32).  All products sigma_i tau_j with the same level l = i + j carry the
 //      same scale 2^(e_r + e_n - 6 l), so they share one TMEM accumulator; the 45 products
 //      with l <= NS + 1 are formed (the rest lie below 2^-54 of the row and column maxima);
-//   3. a level accumulator is an integer sum.  Its terms are bounded by 64 * 64 (l = 2) up to
-//      2 * 64 * 32 + (l - 3) * 32 * 32 (l > 2), so over a K-chunk of KC = 1024 it stays below
-//      2^24 and FP32 accumulation is exact.  After each (chunk, level) the epilogue warps add
-//      the accumulator, scaled by 2^(e_r + e_n - 6 l) (built in the FP64 exponent field with
+//   3. a level accumulator is an integer sum.  Its terms per k are bounded by 64 * 64
+//      (l = 2), 2 * 64 * 32 + (l - 3) * 32 * 32 (l > 2), so over a K-chunk of up to
+//      2^24 / bound(l) (4096 at l <= 3 down to 1472 at l = 10) it stays below 2^24 and FP32
+//      accumulation is exact.  After each (level, chunk) the epilogue warps add the
+//      accumulator, scaled by 2^(e_r + e_n - 6 l) (built in the FP64 exponent field with
 //      integer operations), into the FP64 output.
 //
 // The result is op(A) op(B) to about 2^-53 relative to max|row| * max|column| per term:
@@ -26,8 +27,8 @@
 // (8 digits, 48 bits, measured 6e-13 on rows spanning e^+-3), at 45 BF16 MMAs per FP64
 // multiply-add.  Complex operands use the real embedding [Re -Im; Im Re] x [Re; Im].
 //
-// Kernels: oz_slice (FP64 operand -> exponents + 8 K-major BF16 digit planes, one pass
-// for the row maxima and one for the digits over a 32-row strip), oz_gemm_pair (the CTA
+// Kernels: oz_rowmax / oz_digits (FP64 operand -> row exponents + 9 K-major BF16 digit
+// planes, gridded over 32-row strips and 512-column K chunks), oz_gemm_pair (the CTA
 // pair tcgen05 kernel of tc_gemm.cu with the (chunk, level, product) sequence and the
 // FP64 epilogue), oz_reduce (sums split pieces in a fixed order, applies alpha / beta).
 #include <algorithm>
@@ -46,7 +47,7 @@ constexpr int NLEV = NS;              // levels 2 .. NS + 1
 constexpr int NPROD = NS * (NS + 1) / 2;
 constexpr int STAGES = 6;
 constexpr int KELEMS = 64;            // BF16 elements per 128-byte K slice
-constexpr int KC_SLICES = 16;         // K slices per exactness chunk (KC = 1024)
+constexpr int GH = 8;                 // tile rows per group of the tile order
 constexpr int E_BAD = 1 << 20;        // exponent of a row or column holding Inf / NaN
 constexpr int TILE = 256;             // pair tile edge
 
@@ -109,52 +110,74 @@ __device__ __forceinline__ uint32_t int_bf16(int k) {
   return s | ((uint32_t)(127 + p) << 7) | ((a << (7 - p)) & 0x7fu);
 }
 
-// One block: 32 rows of one batch entry.  Pass 1: row maxima of |X| on the bit patterns
-// (the order of non-negative IEEE doubles is that of their bits).  Pass 2: digits.
-// S[(z NS + i) rows_out + r][ldk] (K-major BF16 planes), E[z rows_out + r].
-__global__ void __launch_bounds__(256) oz_slice(SliceSrc src, int rows_out, int k_out, int ldk,
-                                                uint16_t* __restrict__ S, int* __restrict__ E) {
-  __shared__ uint64_t tile[32][65];
-  const int r0 = blockIdx.x * 32, z = blockIdx.y;
-  const int t = threadIdx.x, rr = t >> 3, part = t & 7;
+constexpr int SL_ROWS = 32;           // rows of a slicing block
+constexpr int SL_KCH = 512;           // K columns of a slicing block (8 tiles of 64)
+
+// 32 x 64 tile of op(X) bit patterns into shared memory, coalesced along whichever index
+// is contiguous in the source; zeros outside the operand
+__device__ __forceinline__ void load_tile(const SliceSrc& src, int z, int r0, int c0, int rows_out,
+                                          int k_out, uint64_t (&tile)[SL_ROWS][65]) {
+  const int t = threadIdx.x;
   const bool rowfast = src.sr == 1;
-  auto load = [&](int c0) {
 #pragma unroll
-    for (int q = 0; q < 8; q++) {
-      const int e = t + 256 * q;
-      int lr, lc;
-      if (rowfast) { lr = e & 31; lc = e >> 5; } else { lc = e & 63; lr = e >> 6; }
-      const int r = r0 + lr, c = c0 + lc;
-      tile[lr][lc] = (r < rows_out && c < k_out) ? src_bits(src, z, r, c) : 0ull;
-    }
-  };
-  uint64_t mx = 0;
-  for (int c0 = 0; c0 < k_out; c0 += 64) {
-    load(c0);
+  for (int q = 0; q < 8; q++) {
+    const int e = t + 256 * q;
+    int lr, lc;
+    if (rowfast) { lr = e & 31; lc = e >> 5; } else { lc = e & 63; lr = e >> 6; }
+    const int r = r0 + lr, c = c0 + lc;
+    tile[lr][lc] = (r < rows_out && c < k_out) ? src_bits(src, z, r, c) : 0ull;
+  }
+}
+
+// Row maxima of |X| on the bit patterns (non-negative IEEE doubles order as their bits):
+// block (strip, K chunk, batch) reduces its 32 x SL_KCH part and folds it into mx with an
+// atomic max (mx zeroed beforehand).
+__global__ void __launch_bounds__(256) oz_rowmax(SliceSrc src, int rows_out, int k_out,
+                                                 unsigned long long* __restrict__ mx) {
+  __shared__ uint64_t tile[SL_ROWS][65];
+  const int r0 = blockIdx.x * SL_ROWS, kc0 = blockIdx.y * SL_KCH, z = blockIdx.z;
+  const int t = threadIdx.x, rr = t >> 3, part = t & 7;
+  uint64_t m = 0;
+  for (int c0 = kc0; c0 < min(kc0 + SL_KCH, k_out); c0 += 64) {
+    load_tile(src, z, r0, c0, rows_out, k_out, tile);
     __syncthreads();
 #pragma unroll
     for (int q = 0; q < 8; q++) {
       const uint64_t a = tile[rr][part * 8 + q] & 0x7fffffffffffffffull;
-      mx = a > mx ? a : mx;
+      m = a > m ? a : m;
     }
     __syncthreads();
   }
 #pragma unroll
   for (int o = 1; o < 8; o <<= 1) {
-    const uint64_t y = __shfl_xor_sync(0xffffffffu, mx, o);
-    mx = y > mx ? y : mx;
+    const uint64_t y = __shfl_xor_sync(0xffffffffu, m, o);
+    m = y > m ? y : m;
   }
+  const int r = r0 + rr;
+  if (part == 0 && r < rows_out && m != 0) atomicMax(mx + (int64_t)z * rows_out + r, m);
+}
+
+// Digits: block (strip, K chunk, batch) writes NS BF16 planes of its 32 x SL_KCH part
+// (zeros in the padding up to ldk); the chunk-0 blocks write the row exponents.
+// S[(z NS + i) rows_out + r][ldk] (K-major), E[z rows_out + r].
+__global__ void __launch_bounds__(256) oz_digits(SliceSrc src, int rows_out, int k_out, int ldk,
+                                                 const unsigned long long* __restrict__ mxa,
+                                                 uint16_t* __restrict__ S, int* __restrict__ E) {
+  __shared__ uint64_t tile[SL_ROWS][65];
+  const int r0 = blockIdx.x * SL_ROWS, kc0 = blockIdx.y * SL_KCH, z = blockIdx.z;
+  const int t = threadIdx.x, rr = t >> 3, part = t & 7;
+  const int r = r0 + rr;
+  const uint64_t mx = r < rows_out ? mxa[(int64_t)z * rows_out + r] : 0ull;
   const int exm = (int)(mx >> 52);
   const bool bad = exm == 0x7ff;
   // max |row| = f 2^e with f in [0.5, 1): e = exm - 1022 for normal numbers; the
   // subnormal exponent field 0 behaves as 1 with no implicit bit (then max < 2^-1021)
   const int e = mx == 0 ? 0 : (exm == 0 ? -1021 : exm - 1022);
-  const int r = r0 + rr;
-  if (part == 0 && r < rows_out) E[(int64_t)z * rows_out + r] = bad ? E_BAD : e;
+  if (blockIdx.y == 0 && part == 0 && r < rows_out) E[(int64_t)z * rows_out + r] = bad ? E_BAD : e;
   const int64_t plane_stride = (int64_t)rows_out * ldk;
   uint16_t* out = S + ((int64_t)z * NS * rows_out + r) * ldk;
-  for (int c0 = 0; c0 < ldk; c0 += 64) {
-    load(c0);
+  for (int c0 = kc0; c0 < min(kc0 + SL_KCH, ldk); c0 += 64) {
+    load_tile(src, z, r0, c0, rows_out, k_out, tile);
     __syncthreads();
     const int cb = c0 + part * 8;
     if (r < rows_out && cb < ldk) {
@@ -218,6 +241,34 @@ __device__ __forceinline__ double scaled(uint32_t u, int E) {
     return __hiloint2double((int)hi, (int)(u << 29));
   }
   return ldexp((double)__uint_as_float(u), E);
+}
+
+// K slices (of KELEMS) per exactness chunk of a level: the longest run of K over which the
+// level's integer sum stays below 2^24 (per-k bound 4096 for l <= 3, 4096 + (l - 3) 1024)
+__host__ __device__ constexpr int level_chunk_slices(int level) {
+  return (1 << 24) / (level <= 3 ? 4096 : 4096 + (level - 3) * 1024) / KELEMS;
+}
+static_assert(level_chunk_slices(2) == 64 && level_chunk_slices(10) == 23, "chunk lengths");
+
+// tile unit -> (mt2, nt, z): groups of GH tile rows, column by column inside a group, so the
+// clusters running at the same time share the digit planes of few A row blocks and few B
+// column blocks in L2
+__host__ __device__ inline void oz_tile(int u, int tiles_m2, int tiles_n, int& mt2, int& nt,
+                                        int& z) {
+  const int per = tiles_m2 * tiles_n;
+  z = u / per;
+  const int r = u - z * per;
+  const int g = r / (GH * tiles_n);
+  const int rows = min(GH, tiles_m2 - g * GH);
+  const int idx = r - g * GH * tiles_n;
+  mt2 = g * GH + idx % rows;
+  nt = idx / rows;
+}
+
+__host__ __device__ inline int oz_unit(int mt2, int nt, int z, int tiles_m2, int tiles_n) {
+  const int g = mt2 / GH;
+  const int rows = min(GH, tiles_m2 - g * GH);
+  return z * tiles_m2 * tiles_n + g * GH * tiles_n + nt * rows + (mt2 - g * GH);
 }
 
 // the levels of piece lp of variant v: kOrder[v][l0 .. l0 + nl)
@@ -298,19 +349,18 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   const bool lead = rank == 0;
   const int cl = blockIdx.x >> 1, ncl = gridDim.x >> 1;
   const int nk = (K + KELEMS - 1) / KELEMS;
-  const int nch = (nk + KC_SLICES - 1) / KC_SLICES;
   const int units = tiles_m2 * tiles_n * batch;
   const int num_items = units * ep.split;
   auto stageA = [&](int s) { return smem + s * STAGE_BYTES; };
   auto stageB = [&](int s) { return stageA(s) + A_BYTES; };
-  // item -> tile unit u, level set [l0, l0 + nl) of kOrder[ep.var], chunks [c0, c1)
-  auto item_of = [&](int item, int& u, int& l0, int& nl, int& c0, int& c1) {
+  // item -> tile unit u, level set [l0, l0 + nl) of kOrder[ep.var], K slices [k0, k1)
+  auto item_of = [&](int item, int& u, int& l0, int& nl, int& k0, int& k1) {
     u = item / ep.split;
     const int p = item - u * ep.split;
     const int lp = p % ep.S, cq = p / ep.S;
     piece_levels(ep.var, lp, l0, nl);
-    c0 = (int)((int64_t)cq * nch / ep.Q);
-    c1 = (int)((int64_t)(cq + 1) * nch / ep.Q);
+    k0 = (int)((int64_t)cq * nk / ep.Q);
+    k1 = (int)((int64_t)(cq + 1) * nk / ep.Q);
   };
 
   if (threadIdx.x == 0) {
@@ -346,15 +396,16 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       int it = 0, last = -1;
       bool stop = false;
       for (int item = cl; item < num_items && !stop && !*abort_flag; item += ncl) {
-        int u, l0, nl, c0, c1, mt2, nt, z;
-        item_of(item, u, l0, nl, c0, c1);
-        tile_coords(u, tiles_m2, tiles_n, ep.nfast, mt2, nt, z);
+        int u, l0, nl, k0, k1, mt2, nt, z;
+        item_of(item, u, l0, nl, k0, k1);
+        oz_tile(u, tiles_m2, tiles_n, mt2, nt, z);
         const int m0 = min(mt2 * 2 * BM + (int)rank * BM, ep.M - 1);
         const int n0 = min(nt * TILE + (int)rank * 128, ep.N - 1);
-        for (int c = c0; c < c1 && !stop; c++) {
-          const int kb0 = c * KC_SLICES, kb1 = min(kb0 + KC_SLICES, nk);
-          for (int li = 0; li < nl && !stop; li++) {
-            const int level = kOrder[ep.var][l0 + li];
+        for (int li = 0; li < nl && !stop; li++) {
+          const int level = kOrder[ep.var][l0 + li];
+          const int kcs = level_chunk_slices(level);
+          for (int kb0 = k0; kb0 < k1 && !stop; kb0 += kcs) {
+            const int kb1 = min(kb0 + kcs, k1);
             for (int i = 1; i < level && !stop; i++) {
               const int za = z * NS + i - 1, zb = z * NS + (level - i) - 1;
               for (int kb = kb0; kb < kb1; kb++, it++) {
@@ -396,12 +447,13 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       int it = 0, local = 0;
       bool stop = false;
       for (int item = cl; item < num_items && !stop && !*abort_flag; item += ncl) {
-        int u, l0, nl, c0, c1;
-        item_of(item, u, l0, nl, c0, c1);
-        for (int c = c0; c < c1 && !stop; c++) {
-          const int kb0 = c * KC_SLICES, kb1 = min(kb0 + KC_SLICES, nk);
-          for (int li = 0; li < nl && !stop; li++, local++) {
-            const int level = kOrder[ep.var][l0 + li];
+        int u, l0, nl, k0, k1;
+        item_of(item, u, l0, nl, k0, k1);
+        for (int li = 0; li < nl && !stop; li++) {
+          const int level = kOrder[ep.var][l0 + li];
+          const int kcs = level_chunk_slices(level);
+          for (int kb0 = k0; kb0 < k1 && !stop; kb0 += kcs, local++) {
+            const int kb1 = min(kb0 + kcs, k1);
             const int buf = local & 1;
             const uint32_t use = (uint32_t)(local >> 1);
             if (!mbar_wait(smem_u32(&acc_empty[buf]), (use & 1) ^ 1, abort_flag, ep.err)) {
@@ -438,15 +490,16 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     int local = 0;
     bool stop = false;
     for (int item = cl; item < num_items && !stop; item += ncl) {
-      int u, l0, nl, c0, c1, mt2, nt, z;
-      item_of(item, u, l0, nl, c0, c1);
-      tile_coords(u, tiles_m2, tiles_n, ep.nfast, mt2, nt, z);
+      int u, l0, nl, k0, k1, mt2, nt, z;
+      item_of(item, u, l0, nl, k0, k1);
+      oz_tile(u, tiles_m2, tiles_n, mt2, nt, z);
       const int rloc = (int)rank * BM + 32 * q + lane;
       const int row = mt2 * 2 * BM + rloc;
       double* wtile = ep.split > 1 || ep.mh < 0 ? ep.C + (int64_t)item * TILE * TILE : nullptr;
-      for (int c = c0; c < c1 && !stop; c++) {
-        for (int li = 0; li < nl; li++, local++) {
-          const int level = kOrder[ep.var][l0 + li];
+      for (int li = 0; li < nl && !stop; li++) {
+        const int level = kOrder[ep.var][l0 + li];
+        const int kcs = level_chunk_slices(level);
+        for (int kb0 = k0; kb0 < k1; kb0 += kcs, local++) {
           const int buf = local & 1;
           const uint32_t use = (uint32_t)(local >> 1);
           const bool ok = mbar_wait(smem_u32(&acc_full[buf]), use & 1, abort_flag, ep.err);
@@ -456,8 +509,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           }
           tc_fence_after();
           const uint32_t tbase = tmem + buf * TMEM_COLS + ((uint32_t)(32 * q) << 16);
-          const bool first = c == c0 && li == 0;
-          const bool lastg = c == c1 - 1 && li == nl - 1;
+          const bool first = li == 0 && kb0 == k0;
+          const bool lastg = li == nl - 1 && kb0 + kcs >= k1;
           if (wtile)
             drain<true>(tbase, row, rloc, nt * TILE, z, level, first, lastg, ep, wtile);
           else
@@ -504,7 +557,8 @@ __device__ __forceinline__ double ws_sum(const RedArgs& a, int z, int r, int c) 
   // unit index of the tile holding (r, c) under the kernel's tile order
   const int mt2 = r / TILE, nt = c / TILE;
   const int per = a.tiles_m2 * a.tiles_n;
-  const int u = z * per + (a.nfast ? mt2 * a.tiles_n + nt : nt * a.tiles_m2 + mt2);
+  (void)per;
+  const int u = oz_unit(mt2, nt, z, a.tiles_m2, a.tiles_n);
   const double* w = a.ws + ((int64_t)u * a.split) * TILE * TILE + (int64_t)(c % TILE) * TILE + r % TILE;
   double s = 0.0;
   for (int p = 0; p < a.split; p++) s += w[(int64_t)p * TILE * TILE];
@@ -558,7 +612,7 @@ static oz::Plan oz_plan(int64_t M2, int64_t N, int64_t K2, int batch, int cl) {
   using namespace oz;
   const int64_t tiles = ((M2 + TILE - 1) / TILE) * ((N + TILE - 1) / TILE) * batch;
   const int64_t nk = (K2 + KELEMS - 1) / KELEMS;
-  const int nch = (int)((nk + KC_SLICES - 1) / KC_SLICES);
+  const int nch = (int)nk;          // Q splits the K slices
   // one digit product of a pair tile: 256 x 256 x K on two SMs at ~1.75 PFLOP/s / 76 pairs
   const double prod_s = 2.0 * TILE * TILE * (double)(nk * KELEMS) / (1.75e15 / 76.0);
   Plan best;
@@ -636,14 +690,39 @@ int gemm_f64_ozaki(fmpt_handle* h, const GemmArgs& g) {
   const int split = plan.S * plan.Q;
   const bool direct = split == 1 && g.beta[0] == 0.0 && g.beta[1] == 0.0 && g.alpha[1] == 0.0;
   const size_t wsb = direct ? 0 : (size_t)units * split * TILE * TILE * sizeof(double);
-  const size_t need = al(planesA) + al(planesB) + al(expA) + al(expB) + wsb;
+  const size_t mxb = (size_t)batch * (M2 + N) * sizeof(uint64_t);
+  // an operand with a cache keeps its planes there (built once while its key holds)
+  const int64_t keyA[8] = {M2, K2, ldk, g.ta, cp, batch, g.lda, g.strideA};
+  const int64_t keyB[8] = {N, K2, ldk, g.tb, cp, batch, g.ldb, g.strideB};
+  auto cache_hit = [](const OzCache* c, const double* src, const int64_t* key) {
+    if (!c || !c->valid || c->src != src) return false;
+    for (int i = 0; i < 8; i++)
+      if (c->key[i] != key[i]) return false;
+    return true;
+  };
+  const bool hitA = cache_hit(g.cacheA, g.A, keyA), hitB = cache_hit(g.cacheB, g.B, keyB);
+  const bool inA = g.cacheA != nullptr, inB = g.cacheB != nullptr;
+  const size_t need = (inA ? 0 : al(planesA) + al(expA)) + (inB ? 0 : al(planesB) + al(expB)) +
+                      al(mxb) + wsb;
   FMPT_TRY(grow_buffer(h, &h->oz_ws, &h->oz_ws_bytes, need));
+  for (int side = 0; side < 2; side++) {
+    OzCache* c = side == 0 ? g.cacheA : g.cacheB;
+    if (!c || (side == 0 ? hitA : hitB)) continue;
+    const size_t want = side == 0 ? al(planesA) + al(expA) : al(planesB) + al(expB);
+    c->valid = false;
+    FMPT_TRY(grow_buffer(h, &c->buf, &c->bytes, want));
+  }
   char* base = static_cast<char*>(h->oz_ws);
-  uint16_t* SA = reinterpret_cast<uint16_t*>(base);
-  uint16_t* SBp = reinterpret_cast<uint16_t*>(base + al(planesA));
-  int* EA = reinterpret_cast<int*>(base + al(planesA) + al(planesB));
-  int* EB = reinterpret_cast<int*>(base + al(planesA) + al(planesB) + al(expA));
-  double* WS = reinterpret_cast<double*>(base + al(planesA) + al(planesB) + al(expA) + al(expB));
+  char* pa = inA ? static_cast<char*>(g.cacheA->buf) : base;
+  if (!inA) base += al(planesA) + al(expA);
+  char* pb = inB ? static_cast<char*>(g.cacheB->buf) : base;
+  if (!inB) base += al(planesB) + al(expB);
+  uint16_t* SA = reinterpret_cast<uint16_t*>(pa);
+  int* EA = reinterpret_cast<int*>(pa + al(planesA));
+  uint16_t* SBp = reinterpret_cast<uint16_t*>(pb);
+  int* EB = reinterpret_cast<int*>(pb + al(planesB));
+  unsigned long long* MX = reinterpret_cast<unsigned long long*>(base);
+  double* WS = reinterpret_cast<double*>(base + al(mxb));
 
   // digit planes (A side: op(A), m x k; B side: op(B)^T, n x k)
   SliceSrc sa{}, sb{};
@@ -656,10 +735,28 @@ int gemm_f64_ozaki(fmpt_handle* h, const GemmArgs& g) {
   if (g.tb == FMPT_N || g.tb == FMPT_R) { sb.sr = g.ldb; sb.sc = 1; } else { sb.sr = 1; sb.sc = g.ldb; }
   {
     ProfScope prof(h, FMPT_K_CONVERT);
-    oz_slice<<<dim3((M2 + 31) / 32, batch), 256, 0, h->stream>>>(sa, M2, K2, ldk, SA, EA);
-    FMPT_LAUNCHED(h);
-    oz_slice<<<dim3((N + 31) / 32, batch), 256, 0, h->stream>>>(sb, N, K2, ldk, SBp, EB);
-    FMPT_LAUNCHED(h);
+    FMPT_CUDA(h, cudaMemsetAsync(MX, 0, (size_t)batch * (M2 + N) * sizeof(uint64_t), h->stream));
+    const unsigned kch = (unsigned)((ldk + SL_KCH - 1) / SL_KCH);
+    const dim3 ga((M2 + SL_ROWS - 1) / SL_ROWS, kch, batch), gb((N + SL_ROWS - 1) / SL_ROWS, kch, batch);
+    if (!hitA) {
+      oz_rowmax<<<ga, 256, 0, h->stream>>>(sa, M2, K2, MX);
+      FMPT_LAUNCHED(h);
+      oz_digits<<<ga, 256, 0, h->stream>>>(sa, M2, K2, ldk, MX, SA, EA);
+      FMPT_LAUNCHED(h);
+    }
+    if (!hitB) {
+      oz_rowmax<<<gb, 256, 0, h->stream>>>(sb, N, K2, MX + (size_t)batch * M2);
+      FMPT_LAUNCHED(h);
+      oz_digits<<<gb, 256, 0, h->stream>>>(sb, N, K2, ldk, MX + (size_t)batch * M2, SBp, EB);
+      FMPT_LAUNCHED(h);
+    }
+  }
+  for (int side = 0; side < 2; side++) {
+    OzCache* c = side == 0 ? g.cacheA : g.cacheB;
+    if (!c || (side == 0 ? hitA : hitB)) continue;
+    c->src = side == 0 ? g.A : g.B;
+    for (int i = 0; i < 8; i++) c->key[i] = side == 0 ? keyA[i] : keyB[i];
+    c->valid = true;
   }
   CUtensorMap ma, mb;
   FMPT_TRY(make_map(h, &ma, SA, BF16, K2, M2, ldk, (int64_t)batch * NS, (int64_t)M2 * ldk, BM));
@@ -720,6 +817,14 @@ int gemm_f64_ozaki(fmpt_handle* h, const GemmArgs& g) {
     FMPT_LAUNCHED(h);
   }
   return FMPT_OK;
+}
+
+void oz_cache_free(fmpt_handle* h, OzCache& c) {
+  if (c.buf) cudaFreeAsync(c.buf, h->stream);
+  c.buf = nullptr;
+  c.bytes = 0;
+  c.valid = false;
+  c.src = nullptr;
 }
 
 }  // namespace fmpt

@@ -52,6 +52,11 @@ class Handle:
             raise ValueError("f64 engine must be 'cuda_cores' or 'tensor_cores'")
         self.check(lib().fmpt_set_f64_engine(self.ptr, codes[engine]))
 
+    def set_wait_test(self, timeout_s=0.0, hold=False):
+        """Failure-detection test hook: bound of the grouped kernel's grid-barrier waits
+        (0: the default 2 s); hold=True makes them wait for an arrival that never comes."""
+        self.check(lib().fmpt_set_wait_test(self.ptr, int(timeout_s * 1e9), 1 if hold else 0))
+
     def set_graphs(self, on=True):
         """CUDA-graph Krylov solves for block-sparse operators (default on)."""
         self.check(lib().fmpt_set_graphs(self.ptr, 1 if on else 0))

@@ -115,6 +115,13 @@ int fmpt_set_tc_tile(fmpt_handle* h, int mode);
  * (large GEMMs; small ones stay on the CUDA cores).  No counterpart in the
  * reference. */
 int fmpt_set_f64_engine(fmpt_handle* h, int mode);
+/* Failure-detection test hook of the grouped block-sparse kernel (no counterpart in the
+ * reference).  Every grid barrier of a grouped launch waits at most timeout_ns (0: the
+ * default 2 s); then the launch sets the handle's status word and returns, and the next
+ * fmpt_synchronize (or solver) reports FMPT_ERR_TIMEOUT while the context stays usable.
+ * hold = 1 makes the barriers wait for one arrival that never comes, so that a test can
+ * run the wait out; hold = 0 is normal operation.  No other kernel is affected. */
+int fmpt_set_wait_test(fmpt_handle* h, int64_t timeout_ns, int hold);
 /* Number of cached tuning decisions and of timed tunings so far. */
 int fmpt_tuning_info(fmpt_handle* h, int* entries, int64_t* timed);
 /* Output tile edge (32 or 64) a block-sparse operator runs with (0: dense op). */

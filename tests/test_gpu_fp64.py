@@ -396,3 +396,36 @@ def test_exponentiate_graph_equals_direct(prec, cplx):
     h.set_graphs(True)
     for a, b in zip(outs[False], outs[True]):
         assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("cplx", [False, True])
+@pytest.mark.parametrize("side", [0, 1])
+@pytest.mark.parametrize("m,n,eps", [(300, 256, 1e-10), (256, 384, 1e-9)])
+def test_dm_split_resolves_graded_spectrum(cplx, side, m, n, eps):
+    """A spectrum logspace(0, -12): squaring resolves sigma only to ~1e-7 sigma_max, so the
+    split refines its tail (rotations by the eigenvectors of the tail rows' Gram matrix,
+    after projecting out the resolved rows).  The kept count equals the MPSTruncation rule
+    (truncation.jl:27-47) on the exact singular values, the kept sigma match them to 1e-7
+    relative (1e-8 above 1e-4 sigma_max), and the product is the rank-k truncation of M."""
+    from finitemptools_gb300.auxiliary import dm_split
+    rng = np.random.default_rng(m + n + 10 * side + cplx)
+    r = min(m, n)
+    U0, _ = np.linalg.qr(rnd(rng, (m, r), cplx))
+    V0, _ = np.linalg.qr(rnd(rng, (n, r), cplx))
+    s0 = np.logspace(0, -12, r)
+    M = (U0 * s0) @ V0.conj().T
+    tr = fm.MPSTruncation(r, eps)
+    k_ref, err_ref = O.mps_truncate(s0, tr)
+    A, S, B, err = dm_split(DT.from_numpy(M), m, n, tr, side)
+    An, Sn, Bn = A.numpy(), S.numpy(), B.numpy()
+    assert Sn.shape[0] == k_ref
+    relerr = np.abs(Sn / s0[:k_ref] - 1.0)
+    assert relerr.max() < 1e-7, relerr.max()
+    assert relerr[s0[:k_ref] > 1e-4].max() < 1e-8
+    if side == 0:
+        assert np.allclose(An.conj().T @ An, np.eye(k_ref), atol=1e-12)
+    else:
+        assert np.allclose(Bn @ Bn.conj().T, np.eye(k_ref), atol=1e-12)
+    Mk = (U0[:, :k_ref] * s0[:k_ref]) @ V0[:, :k_ref].conj().T
+    assert rel(An @ Bn, Mk) < 1e-10
+    assert abs(err - err_ref) < 1e-12

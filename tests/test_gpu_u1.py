@@ -352,3 +352,34 @@ def test_u1_rejects_bad_input():
         fm.U1HeffOp(dL, dR, bad, Ws[4], sp(Vl), sp(Vr), QP, QP, qw[3], qw[4], qw[5])
     with pytest.raises(fm.FMPTError):   # wrong channel charges
         fm.U1HeffOp(dL, dR, Ws[3], Ws[4], sp(Vl), sp(Vr), QP, QP, qw[3], [0, 0, 0, 0, 0], qw[5])
+
+
+def test_grouped_barrier_timeout_is_reported_and_context_survives():
+    """Failure detection without a GPU fault: the grouped launch's grid barrier is made to
+    wait for an arrival that never comes (fmpt_set_wait_test hold), gives up after its
+    0.2 s bound, sets the status word and returns; fmpt_synchronize reports
+    FMPT_ERR_TIMEOUT, and after the hook is cleared the same operator gives the right
+    result again on the same context."""
+    from finitemptools_gb300._native import FMPTError
+    L, N, D, site = 10, 5, 20, 5
+    Ws, qw, mps, legs, Lm, Rm = _bond(L, N, D, site, 77)
+    Vl, Vr = legs[site - 1], legs[site + 1]
+    W1, W2 = Ws[site - 1], Ws[site]
+    X = np.tensordot(mps[site - 1], mps[site], axes=([2], [0]))
+    ref = OU.pack2(O.ac2_prime(X, W1, W2, Lm, Rm), Vl, Vr, list(QP), list(QP))
+    h = fm.default_handle()
+    dL, dR = DT.from_numpy(Lm), DT.from_numpy(Rm)
+    op = fm.U1HeffOp(dL, dR, W1, W2, sp(Vl), sp(Vr), QP, QP, qw[site - 1], qw[site],
+                     qw[site + 1])
+    x = DT.from_numpy(OU.pack2(X, Vl, Vr, list(QP), list(QP)))
+    assert rel(op(x).numpy(), ref) < 1e-13          # built, tuned and correct
+    h.set_wait_test(0.2, hold=True)
+    try:
+        op(x)
+        with pytest.raises(FMPTError) as ei:
+            h.synchronize()
+        assert ei.value.status == -5
+    finally:
+        h.set_wait_test(0.0, hold=False)
+    h.synchronize()                                  # the status word was cleared
+    assert rel(op(x).numpy(), ref) < 1e-13
