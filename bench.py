@@ -10,14 +10,19 @@ inside a Lanczos solve).  Algorithmic flops per step: F2 = 4 w d^2 D^3 +
 4 w^2 d^3 D^2 (the reference's dense pairwise order, derivatives.jl:21).
 
 Arms:
-  default            this library (libfmpt) at --precision (default bf16,
-                     FP32 accumulation); also reports every precision form
-                     (fp64, tf32x3, tf32, bf16) at D in {256..2048} with its
-                     relative Frobenius error against the FP64 form.
+  default            this library (libfmpt) at --precision (default fp64_tc: the
+                     FP64-accurate form, FP64 products emulated exactly on the
+                     BF16 tensor cores by the Ozaki scheme); also reports every
+                     precision form (fp64, fp64_tc, tf32x3, tf32, bf16) at D in
+                     {256..2048} with its relative Frobenius error against the
+                     plain FP64 form, and the DMRG, U(1), TDVP1 and gradient
+                     sections beside the hot path.
   --impl reference   the reference's algorithm on the host cores: the numpy
                      restatement of ac2_prime in the reference's pairwise
                      order (OpenBLAS, all host threads).  The reference itself
                      is Julia and cannot run on this machine.
+  --config3          the J1-J2 L=100 D=1024 mixed-vs-FP64 DMRG comparison, both ramps.
+  --config5          the differentiable TDVP1 run as configured (100 steps).
 
 Multi-GPU: the path does not shard (each sweep is sequential over bonds), so
 --gpus N under torchrun runs N independent replicas; value = all replicas'
@@ -375,37 +380,6 @@ def dmrg_section(h, fm, budget_s=150.0, full3=False, only3=False):
     del envx
     if _t.perf_counter() - t_start > budget_s:
         return out
-    # one-site TDVP trajectory: TFI L=40, h_i = 1 + 0.1 N(0,1), complex128, D=64,
-    # dt=0.05 (stepsize -0.05i), Krylov dimension 20; <Z_20> after the timed steps
-    # (the same trajectory with the contractions in 3xTF32: complex data on the tensor
-    # cores through the real embedding, FP64 Krylov, QR and environment updates)
-    L = 40
-    Z = np.diag([-1.0, 1.0])
-    nsteps = 10
-    res = {}
-    for prec in ("fp64", "tf32x3"):
-        rng = np.random.default_rng(40)
-        hs = 1.0 + 0.1 * rng.standard_normal(L)
-        htfi = fm.tfi_mpo(hs)
-        psi = fm.randommps(L, 2, 64, rng, dtype=np.complex128, handle=h)
-        fm.canonicalize_(psi, normalize=True)
-        envt = fm.environments(fm.FiniteMPO(htfi, L), psi)
-        alg = fm.TDVP1(stepsize=-0.05j, D=64, exptol=1e-8, krylovdim=20, precision=prec)
-        fm.sweep_(envt, alg)                             # first step (bond growth, warm-up)
-        h.synchronize()
-        t0 = _t.perf_counter()
-        for _ in range(nsteps):
-            fm.sweep_(envt, alg)
-        h.synchronize()
-        res[prec] = ((_t.perf_counter() - t0) / nsteps,
-                     float(np.real(fm.expectation_local(envt.mps, 20, Z))))
-        del envt, psi
-    tstep = res["fp64"][0]
-    out["tdvp1_tfi_L40_D64"] = {"s_per_step_fp64_complex": tstep, "steps_timed": nsteps,
-                                "s_per_step_tf32x3_complex": res["tf32x3"][0],
-                                "Z20_after_%d_steps" % (nsteps + 1): res["fp64"][1],
-                                "Z20_tf32x3_minus_fp64": res["tf32x3"][1] - res["fp64"][1],
-                                "note": "100 steps extrapolate to %.1f s" % (100 * tstep)}
     return out
 
 
@@ -669,22 +643,84 @@ def next_rows_section(h, fm):
     return out
 
 
-def tdvp_grad_section(h, fm, nsteps=5):
-    """Config 5 (differentiable TDVP1), reduced length: TFI L=40,
-    h_i = 1 + 0.1 N(0,1) (seed 40), random normalised complex MPS D=64, dt=0.05
-    (stepsize -0.05i), Krylov dimension 20, exptol 1e-8; gradient of <Z_20>(T)
-    with respect to all 40 h_i by the device adjoint (checkpoint every 10
-    steps), checked against central differences (step 1e-5, FP64 device
-    forward) for h_20 and h_21."""
-    import time as _t
-    from finitemptools_gb300 import adjoint as AD
-    L, D = 40, 64
-    rng = np.random.default_rng(40)
+def _tfi_start(fm, h, L=40, D=64, seed=40):
+    """TFI chain h_i = 1 + 0.1 N(0,1) (seeded) and a random normalised complex MPS, D=64."""
+    rng = np.random.default_rng(seed)
     hs = 1.0 + 0.1 * rng.standard_normal(L)
     psi = fm.randommps(L, 2, D, rng, dtype=np.complex128, handle=h)
     fm.canonicalize_(psi, normalize=True)
+    return hs, psi
+
+
+def tdvp_section(h, fm, nsteps=5):
+    """One-site TDVP (algorithms/tdvp.jl:19-69): TFI L=40, complex128, D=64, dt=0.05
+    (stepsize -0.05i), Krylov dimension 20, exptol 1e-8.  After one warm-up step, nsteps
+    timed steps in the plain FP64 form and in the 3xTF32 form (complex data on the
+    tensor cores through the real embedding; FP64 Krylov, QR and environment updates).
+    CPU baseline: the oracle's tdvp1_sweep (numpy, the reference's algorithm step for
+    step, all host threads) for ONE step from the state after the warm-up step, and the
+    device's FP64 step from that same state; <Z_20> of both after that step."""
+    import time as _t
+    import oracle as O
+    from finitemptools_gb300.utilities import FiniteMPO
+    L, Z = 40, np.diag([-1.0, 1.0])
+    res = {}
+    start = None
+    for prec in ("fp64", "tf32x3"):
+        hs, psi = _tfi_start(fm, h)
+        envt = fm.environments(fm.FiniteMPO(fm.tfi_mpo(hs), L), psi)
+        alg = fm.TDVP1(stepsize=-0.05j, D=64, exptol=1e-8, krylovdim=20, precision=prec)
+        fm.sweep_(envt, alg)                             # first step (bond growth, warm-up)
+        if prec == "fp64":
+            start = [A.numpy() for A in envt.mps]
+            h.synchronize()
+            t0 = _t.perf_counter()
+            fm.sweep_(envt, alg)
+            h.synchronize()
+            t_one = _t.perf_counter() - t0
+            z_one = float(np.real(fm.expectation_local(envt.mps, 20, Z)))
+        h.synchronize()
+        t0 = _t.perf_counter()
+        for _ in range(nsteps):
+            fm.sweep_(envt, alg)
+        h.synchronize()
+        res[prec] = ((_t.perf_counter() - t0) / nsteps,
+                     float(np.real(fm.expectation_local(envt.mps, 20, Z))))
+        del envt, psi
+    env_o = O.environments(FiniteMPO(fm.tfi_mpo(hs), L), [A.copy() for A in start])
+    t0 = _t.perf_counter()
+    O.tdvp1_sweep(env_o, -0.05j, D=64, exptol=1e-8, krylovdim=20)
+    t_cpu = _t.perf_counter() - t0
+    z_cpu = float(np.real(O.single_site_expectation(env_o.mps, 20, Z)))
+    return {"s_per_step_fp64_complex": res["fp64"][0], "steps_timed": nsteps,
+            "s_per_step_tf32x3_complex": res["tf32x3"][0],
+            "Z20_after_%d_steps_fp64" % (nsteps + 2): res["fp64"][1],
+            "Z20_tf32x3_minus_fp64": res["tf32x3"][1] - res["fp64"][1],
+            "cpu_reference": {"s_per_step": t_cpu, "threads": os.cpu_count(),
+                              "speedup_gpu_fp64_over_cpu": t_cpu / t_one,
+                              "gpu_fp64_s_same_step": t_one,
+                              "Z20_cpu": z_cpu, "Z20_gpu_fp64": z_one,
+                              "dZ20_gpu_vs_cpu": abs(z_one - z_cpu),
+                              "note": "one step of the oracle's tdvp1_sweep (numpy/OpenBLAS, "
+                                      "all host threads) and of the device FP64 form from the "
+                                      "same state (after one warm-up step)"}}
+
+
+def tdvp_grad_section(h, fm, nsteps=5, checkpoint=2, fd_sites=(20, 21, 1, 40),
+                      mixed=True):
+    """Config 5 (differentiable TDVP1): TFI L=40, h_i = 1 + 0.1 N(0,1) (seed 40), random
+    normalised complex MPS D=64, dt=0.05 (stepsize -0.05i), Krylov dimension 20, exptol
+    1e-8; gradient of <Z_20>(T) with respect to all 40 h_i by the device adjoint (MPS
+    checkpoints every `checkpoint` steps, blocks recomputed in the reverse pass), checked
+    against central differences (step 1e-5, FP64 device forward) on the fields
+    `fd_sites` (1-based).  mixed: the same value and gradient with the Krylov
+    exponentials of forward and adjoint in 3xTF32, and their errors against FP64."""
+    import time as _t
+    from finitemptools_gb300 import adjoint as AD
+    L = 40
+    hs, psi = _tfi_start(fm, h)
     Z = np.diag([-1.0, 1.0])
-    alg = fm.TDVP1(stepsize=-0.05j, D=D, exptol=1e-8, krylovdim=20)
+    alg = fm.TDVP1(stepsize=-0.05j, D=64, exptol=1e-8, krylovdim=20)
 
     def forward(hv):
         env = fm.environments(fm.tfi_mpo(hv), fm.FiniteMPS([A.copy() for A in psi.data]))
@@ -698,24 +734,38 @@ def tdvp_grad_section(h, fm, nsteps=5):
     h.synchronize()
     t_fwd = _t.perf_counter() - t0
     t0 = _t.perf_counter()
-    val, g = AD.tfi_field_gradient(hs, psi, -0.05j, nsteps, 20, Z, checkpoint=10, exptol=1e-8,
-                                   krylovdim=20)
+    val, g = AD.tfi_field_gradient(hs, psi, -0.05j, nsteps, 20, Z, checkpoint=checkpoint,
+                                   exptol=1e-8, krylovdim=20)
     h.synchronize()
     t_grad = _t.perf_counter() - t0
     checks = {}
-    for i in (19, 20):
+    for site in fd_sites:
+        i = site - 1
         hp, hm = hs.copy(), hs.copy()
         hp[i] += 1e-5
         hm[i] -= 1e-5
         fd = (forward(hp) - forward(hm)) / 2e-5
-        checks["h_%d" % (i + 1)] = {"adjoint": float(g[i]), "central_fd": fd,
-                                    "rel_err": abs(g[i] - fd) / max(abs(fd), 1e-300)}
-    return {"steps": nsteps, "value_Z20": val, "value_forward_only": v0,
-            "grad_norm": float(np.linalg.norm(g)), "grad": [float(x) for x in g],
-            "s_forward": t_fwd, "s_value_and_gradient": t_grad,
-            "gradient_over_forward": t_grad / t_fwd, "fd_checks": checks,
-            "note": "100 steps (the full config) extrapolate to %.0f s for value+gradient"
-                    % (100 * t_grad / nsteps)}
+        checks["h_%d" % site] = {"adjoint": float(g[i]), "central_fd": fd,
+                                 "abs_err": abs(g[i] - fd),
+                                 "rel_err": abs(g[i] - fd) / max(abs(fd), 1e-300)}
+    out = {"steps": nsteps, "checkpoint": checkpoint, "blocks": -(-nsteps // checkpoint),
+           "value_Z20": val, "value_forward_only": v0,
+           "grad_norm": float(np.linalg.norm(g)), "grad": [float(x) for x in g],
+           "s_forward": t_fwd, "s_value_and_gradient": t_grad,
+           "gradient_over_forward": t_grad / t_fwd, "fd_checks": checks,
+           "fd_max_abs_err_over_grad_norm": max(c["abs_err"] for c in checks.values()) /
+           float(np.linalg.norm(g))}
+    if mixed:
+        h.synchronize()
+        t0 = _t.perf_counter()
+        v32, g32 = AD.tfi_field_gradient(hs, psi, -0.05j, nsteps, 20, Z, checkpoint=checkpoint,
+                                         exptol=1e-8, krylovdim=20, precision="tf32x3")
+        h.synchronize()
+        out["tf32x3"] = {"s_value_and_gradient": _t.perf_counter() - t0,
+                         "value_minus_fp64": v32 - val,
+                         "grad_rel_err_vs_fp64": float(np.linalg.norm(g32 - g) /
+                                                       np.linalg.norm(g))}
+    return out
 
 
 def ed_heff_case(args):
@@ -824,6 +874,10 @@ def main():
     ap.add_argument("--config3", action="store_true",
                     help="only the J1-J2 L=100 D=1024 mixed-vs-FP64 comparison with both forms' "
                          "full ramps (sweep times and energies of both), printed as JSON")
+    ap.add_argument("--config5", action="store_true",
+                    help="only the differentiable TDVP1 run as configured: TFI L=40, D=64, "
+                         "100 steps, checkpoint every 10, gradient of <Z_20> with respect to "
+                         "all 40 fields, central differences on h_20, h_21, h_1, h_40")
     ap.add_argument("--ed-heff", type=int, default=0, metavar="L",
                     help="time the exact-diagonalisation operator of an L-site XXZ chain alone")
     ap.add_argument("--u1-heff", type=int, default=0, metavar="D",
@@ -859,6 +913,11 @@ def main():
     if args.config3:
         res = dmrg_section(h, fm, full3=True, only3=True)
         print(json.dumps({"config3": res}), flush=True)
+        return
+    if args.config5:
+        res = tdvp_grad_section(h, fm, nsteps=100, checkpoint=10, fd_sites=(20, 21, 1, 40),
+                                mixed=False)
+        print(json.dumps({"config5": res}), flush=True)
         return
     D, prec = args.D, args.precision
     x, L, R, W = workload(D)
@@ -1028,8 +1087,9 @@ def main():
     u1 = None
     if rank == 0 and not args.no_u1:
         u1 = u1_section(h, fm)
-    tgrad = None
+    tdvp = tgrad = None
     if rank == 0 and not args.no_grad:
+        tdvp = tdvp_section(h, fm)
         tgrad = tdvp_grad_section(h, fm)
 
     nxt = None
@@ -1048,7 +1108,7 @@ def main():
             "dtype": "f64" if prec in ("fp64", "fp64_tc") else prec, "data": "synthetic",
             "config": config_dict(args, prec), "clocks": clocks, "e2e": e2e,
             "gpu_launches": n_launch, "roofline": roof, "cpu_baseline": cpu,
-            "per_dtype": table, "dmrg": dmrg, "u1": u1, "tdvp_gradient": tgrad,
+            "per_dtype": table, "dmrg": dmrg, "u1": u1, "tdvp1": tdvp, "tdvp_gradient": tgrad,
             "next_rows": nxt,
         }
         print(json.dumps(line), flush=True)

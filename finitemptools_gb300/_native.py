@@ -99,6 +99,10 @@ SIGNATURES = {
                               dptr, P(c_double), P(c_int), P(c_int)]),
     "fmpt_lanczos_ground": (c_int, [c_void_p, dptr, c_int, c_double, c_int, P(c_double), dptr,
                                     P(c_int), P(c_int)]),
+    "fmpt_dmrg2_sweep": (c_int, [c_void_p, c_int, c_int, c_int, c_int, P(c_int), P(c_int),
+                                 P(c_void_p), P(c_int64), P(c_void_p), P(c_int64), P(c_void_p),
+                                 P(c_int), P(c_void_p), c_int, c_double, c_int, c_double, c_int,
+                                 c_int, P(c_double), P(c_double)]),
     "fmpt_exponentiate": (c_int, [c_void_p, c_double, c_double, dptr, dptr, c_int, c_double,
                                   P(c_int)]),
     "fmpt_svd_trunc": (c_int, [c_void_p, c_int, dptr, c_int, c_int, c_int, c_double, dptr, dptr,

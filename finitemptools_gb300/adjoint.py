@@ -34,10 +34,12 @@ from .auxiliary import axpy, gemm, leftorth, rightorth, scal
 from .derivatives import HeffOp, ac_prime
 from .device import DeviceTensor
 from .envs import _mpo_tensors, l_LL, r_RR
+from .utilities import MPOHamiltonian
 from .transfer import updateleft, updateright
 
-__all__ = ["tdvp1_gradient", "tfi_field_gradient", "expm_nodes", "wgrad", "qr_adjoint",
-           "gl_nodes"]
+__all__ = ["tdvp1_gradient", "tdvp1_forward", "tdvp1_backward", "tfi_field_gradient",
+           "TDVP1Observable", "tdvp1_observable", "tfi_observable", "tfi_mpo_torch",
+           "expm_nodes", "wgrad", "qr_adjoint", "gl_nodes"]
 
 
 def gl_nodes(n=8):
@@ -147,9 +149,12 @@ def _c_adjoint(a, C, Le, Re):
     return Lb, Rb
 
 
-def _expo_backward(kind, t, x, ybar, W, Le, Re, krylovdim, nodes):
-    """Cotangents (xbar, Lbar, Wbar, Rbar) of y = exp(t H) x (H Hermitian)."""
-    op = HeffOp(kind, Le, Re, W1=W if kind == "ac" else None, dtype=np.complex128)
+def _expo_backward(run, kind, t, x, ybar, W, Le, Re, nodes):
+    """Cotangents (xbar, Lbar, Wbar, Rbar) of y = exp(t H) x (H Hermitian).  The
+    exponentials run in the run's arithmetic; the contractions that pair the
+    quadrature vectors stay FP64."""
+    krylovdim = run.krylovdim
+    op = run.op(kind, Le, Re, W)
     s, w = nodes
     bs, _ = expm_nodes(op, t, x, 1.0 - s, krylovdim)
     as_, _ = expm_nodes(op, np.conj(t), ybar, np.concatenate([s, [1.0]]), krylovdim)
@@ -209,11 +214,22 @@ def _lq_backward(Lm, Q3, Lb, Qb3):
 
 # -------------------------------------------------------------- TDVP1 tape
 class _Run:
-    def __init__(self, Ws, dt, exptol, krylovdim):
+    def __init__(self, Ws, dt, exptol, krylovdim, precision="fp64"):
         self.Ws = Ws
         self.dt = dt
         self.exptol = exptol
         self.krylovdim = krylovdim
+        self.precision = precision
+
+    def op(self, kind, Le, Re, W=None):
+        """H_eff of one site ("ac", MPO tensor W) or one bond ("c") in the run's
+        arithmetic.  The tensor-core forms embed complex states as real GEMMs and
+        need a real MPO, so a real-valued W is handed over as real."""
+        if kind != "ac":
+            W = None
+        elif self.precision != "fp64" and not np.any(np.imag(W)):
+            W = np.ascontiguousarray(np.real(W))
+        return HeffOp(kind, Le, Re, W1=W, precision=self.precision, dtype=np.complex128)
 
 
 def _init_envs(run, mps, tape=None):
@@ -238,7 +254,7 @@ def _step(run, mps, hs, rec=None):
     tol2, tol1 = run.exptol / abs(dt / 2), run.exptol / abs(dt)
     for s in range(L - 1):
         x = mps[s]
-        op = HeffOp("ac", hs[s], hs[s + 1], W1=Ws[s], dtype=np.complex128)
+        op = run.op("ac", hs[s], hs[s + 1], Ws[s])
         tmp = op.exponentiate(dt / 2, x, tol2, run.krylovdim)
         del op
         Dl, d, Dr = x.shape
@@ -246,7 +262,7 @@ def _step(run, mps, hs, rec=None):
         k = Q.shape[1]
         Q3 = Q.view_as((Dl, d, k))
         hnew = updateleft(hs[s], Q3, Ws[s], Q3)
-        opc = HeffOp("c", hnew, hs[s + 1], dtype=np.complex128)
+        opc = run.op("c", hnew, hs[s + 1])
         v = opc.exponentiate(-dt / 2, R, tol2, run.krylovdim)
         del opc
         B = mps[s + 1]
@@ -260,7 +276,7 @@ def _step(run, mps, hs, rec=None):
     x = mps[s]
     if rec is not None:
         rec.append({"kind": "last", "s": s, "x": x, "Le": hs[s], "Re": hs[s + 1]})
-    op = HeffOp("ac", hs[s], hs[s + 1], W1=Ws[s], dtype=np.complex128)
+    op = run.op("ac", hs[s], hs[s + 1], Ws[s])
     mps[s] = op.exponentiate(dt, x, tol1, run.krylovdim)
     del op
     for s in range(L - 2, -1, -1):
@@ -272,7 +288,7 @@ def _step(run, mps, hs, rec=None):
         hold = hs[s + 2]
         hnew = updateright(hold, Q3, Ws[s + 1], Q3)
         Lc = hs[s + 1]
-        opc = HeffOp("c", Lc, hnew, dtype=np.complex128)
+        opc = run.op("c", Lc, hnew)
         v = opc.exponentiate(-dt / 2, Lm, tol2, run.krylovdim)
         del opc
         A = mps[s]
@@ -282,7 +298,7 @@ def _step(run, mps, hs, rec=None):
                         "Le": hs[s], "hnew": hnew, "v": v, "A": A, "Av": Av})
         mps[s + 1] = Q3
         hs[s + 1] = hnew
-        op = HeffOp("ac", hs[s], hnew, W1=Ws[s], dtype=np.complex128)
+        op = run.op("ac", hs[s], hnew, Ws[s])
         mps[s] = op.exponentiate(dt / 2, Av, tol2, run.krylovdim)
         del op
 
@@ -326,7 +342,7 @@ def _observable_backward(mps, site, Op):
 def _reverse_block(run, rec, init_tape, mb, Wb, nodes):
     """Reverse one recomputed block: mb (site cotangents at the block end) ->
     cotangents at the block start; Wbar accumulated into Wb."""
-    Ws, dt, kd = run.Ws, run.dt, run.krylovdim
+    Ws, dt = run.Ws, run.dt
     L = len(Ws)
     hb = [None] * (L + 1)
 
@@ -341,8 +357,8 @@ def _reverse_block(run, rec, init_tape, mb, Wb, nodes):
     for r in reversed(rec):
         s = r["s"]
         if r["kind"] == "right":
-            xb, lb, wb, rb = _expo_backward("ac", dt / 2, r["Av"], mb[s], Ws[s], r["Le"],
-                                            r["hnew"], kd, nodes)
+            xb, lb, wb, rb = _expo_backward(run, "ac", dt / 2, r["Av"], mb[s], Ws[s], r["Le"],
+                                            r["hnew"], nodes)
             Wb[s] = _acc(Wb[s], wb)
             add(s, lb)
             add(s + 1, rb)
@@ -353,8 +369,8 @@ def _reverse_block(run, rec, init_tape, mb, Wb, nodes):
             mb[s] = gemm(Cm, v, (Dl, d, k), Dl * d, k, rr, tb="C")             # Avbar v^H
             vb = gemm(A, Cm, (k, rr), k, rr, Dl * d, ta="C", lda=Dl * d)      # A^H Avbar
             hnb = pop(s + 1)
-            Lmb, lb2, _, rb2 = _expo_backward("c", -dt / 2, r["Lm"], vb, None, r["Lc"],
-                                              r["hnew"], kd, nodes)
+            Lmb, lb2, _, rb2 = _expo_backward(run, "c", -dt / 2, r["Lm"], vb, None, r["Lc"],
+                                              r["hnew"], nodes)
             add(s + 1, lb2)
             hnb = _acc(hnb, rb2)
             W1 = Ws[s + 1]
@@ -367,8 +383,8 @@ def _reverse_block(run, rec, init_tape, mb, Wb, nodes):
                 axpy(1.0, mb[s + 1], Qb)
             mb[s + 1] = _lq_backward(r["Lm"], r["Q"], Lmb, Qb)
         elif r["kind"] == "last":
-            xb, lb, wb, rb = _expo_backward("ac", dt, r["x"], mb[s], Ws[s], r["Le"], r["Re"], kd,
-                                            nodes)
+            xb, lb, wb, rb = _expo_backward(run, "ac", dt, r["x"], mb[s], Ws[s], r["Le"],
+                                            r["Re"], nodes)
             mb[s] = xb
             Wb[s] = _acc(Wb[s], wb)
             add(s, lb)
@@ -382,8 +398,8 @@ def _reverse_block(run, rec, init_tape, mb, Wb, nodes):
             mb[s + 1] = gemm(v, Cm, B.shape, Dlb, B.shape[1] * B.shape[2], k, ta="C")
             Qb = mb[s]
             mb[s] = None
-            Rb, lb, _, rb = _expo_backward("c", -dt / 2, r["R"], vb, None, r["hnew"], r["Re"], kd,
-                                           nodes)
+            Rb, lb, _, rb = _expo_backward(run, "c", -dt / 2, r["R"], vb, None, r["hnew"],
+                                           r["Re"], nodes)
             hnb = _acc(hnb, lb)
             add(s + 1, rb)
             hold_b, Ab, wb, Bb = _updateleft_backward(hnb, r["Le"], r["Q"], Ws[s], r["Q"])
@@ -392,8 +408,8 @@ def _reverse_block(run, rec, init_tape, mb, Wb, nodes):
             axpy(1.0, Ab, Qb)
             axpy(1.0, Bb, Qb)
             tmpb = _qr_backward(r["Q"], r["R"], Qb, Rb)
-            xb, lb, wb, rb = _expo_backward("ac", dt / 2, r["x"], tmpb, Ws[s], r["Le"], r["Re"],
-                                            kd, nodes)
+            xb, lb, wb, rb = _expo_backward(run, "ac", dt / 2, r["x"], tmpb, Ws[s], r["Le"],
+                                            r["Re"], nodes)
             mb[s] = xb
             Wb[s] = _acc(Wb[s], wb)
             add(s, lb)
@@ -411,18 +427,37 @@ def _reverse_block(run, rec, init_tape, mb, Wb, nodes):
     return mb
 
 
-def tdvp1_gradient(mpo, psi0, stepsize, nsteps, site, Op, checkpoint=10, exptol=1e-12,
-                   krylovdim=30, quad_nodes=8):
-    """Value and MPO-tensor gradient of Re <Op_site>(T) (``site`` 1-based) after
-    ``nsteps`` TDVP1 sweeps of size ``stepsize`` (real time: -1j*dt) from psi0
-    (a complex FiniteMPS, not modified).  Returns (value, [Wbar_i] as numpy
-    arrays, one per site).  Only every ``checkpoint``-th MPS is kept; each
-    block is recomputed and reversed in turn."""
+class TDVP1Tape:
+    """What the reverse pass of a TDVP1 trajectory needs: the run (MPO tensors,
+    step, tolerances, arithmetic), the MPS every ``checkpoint`` steps and the
+    final state.  Held by TDVP1Observable between forward and backward."""
+
+    def __init__(self, run, checkpoints, nsteps, final_mps, site, Op):
+        self.run, self.checkpoints, self.nsteps = run, checkpoints, nsteps
+        self.final_mps, self.site, self.Op = final_mps, site, Op
+
+
+def tdvp1_forward(mpo, psi0, stepsize, nsteps, site, Op, checkpoint=10, exptol=1e-12,
+                  krylovdim=30, precision="fp64"):
+    """Re <Op_site>(T) (``site`` 1-based) after ``nsteps`` TDVP1 sweeps of size
+    ``stepsize`` (real time: -1j*dt) from psi0 (a complex FiniteMPS, not
+    modified), and the tape for tdvp1_backward.  ``mpo`` is an MPOHamiltonian or
+    a list of dense site tensors W[wl, s_out, wr, s_in]: bulk Schur grids (the
+    environments close them with the boundary vectors l_LL / r_RR) or a strict
+    FiniteMPO (first and last MPO bonds 1, where those vectors are [1]).  ``precision`` is the
+    arithmetic of the Krylov exponentials (forward and adjoint); "fp64" is the
+    reference's, the tensor-core forms ("tf32x3", ...) need a real MPO."""
+    if checkpoint < 1:
+        raise ValueError("checkpoint must be >= 1")
     L = len(psi0)
-    Ws, _ = _mpo_tensors(mpo, L)
+    if isinstance(mpo, MPOHamiltonian):
+        Ws, _ = _mpo_tensors(mpo, L)
+    else:
+        Ws = list(mpo)
+        if len(Ws) != L:
+            raise ValueError("DimensionMismatch: MPO length %d vs MPS length %d" % (len(Ws), L))
     Ws = [np.asarray(W, dtype=np.complex128) for W in Ws]
-    run = _Run(Ws, complex(stepsize), exptol, krylovdim)
-    nodes = gl_nodes(quad_nodes)
+    run = _Run(Ws, complex(stepsize), exptol, krylovdim, precision)
     mps = [psi0[i].copy() for i in range(1, L + 1)]
     checkpoints = []
     hs = _init_envs(run, mps)
@@ -430,12 +465,24 @@ def tdvp1_gradient(mpo, psi0, stepsize, nsteps, site, Op, checkpoint=10, exptol=
         if step % checkpoint == 0:
             checkpoints.append((step, [A.copy() for A in mps]))
         _step(run, mps, hs)
-    value, mb = _observable_backward(mps, site - 1, Op)
     del hs
+    n1, n0 = _observable(mps, site - 1, Op)
+    return float(np.real(n1 / n0)), TDVP1Tape(run, checkpoints, nsteps, mps, site, Op)
+
+
+def tdvp1_backward(tape, quad_nodes=8):
+    """Gradient of tdvp1_forward's value with respect to every MPO site tensor
+    (numpy arrays, zbar = dL/dRe W + i dL/dIm W).  Each checkpoint block is
+    recomputed from its MPS, taped and reversed, last block first."""
+    run = tape.run
+    L = len(run.Ws)
+    nodes = gl_nodes(quad_nodes)
+    _, mb = _observable_backward(tape.final_mps, tape.site - 1, tape.Op)
     Wb = [None] * L
-    for k in range(len(checkpoints) - 1, -1, -1):
-        start, snap = checkpoints[k]
-        stop = checkpoints[k + 1][0] if k + 1 < len(checkpoints) else nsteps
+    cps = tape.checkpoints
+    for k in range(len(cps) - 1, -1, -1):
+        start, snap = cps[k]
+        stop = cps[k + 1][0] if k + 1 < len(cps) else tape.nsteps
         mps = [A.copy() for A in snap]
         init_tape = []
         hs = _init_envs(run, mps, init_tape)
@@ -444,9 +491,27 @@ def tdvp1_gradient(mpo, psi0, stepsize, nsteps, site, Op, checkpoint=10, exptol=
             _step(run, mps, hs, rec)
         mb = _reverse_block(run, rec, init_tape, mb, Wb, nodes)
         del rec, init_tape, hs
-    out = [np.zeros(W.shape, dtype=np.complex128) if g is None else g.numpy() for W, g in
-           zip(Ws, Wb)]
-    return value, out
+    return [np.zeros(W.shape, dtype=np.complex128) if g is None else g.numpy() for W, g in
+            zip(run.Ws, Wb)]
+
+
+def tdvp1_gradient(mpo, psi0, stepsize, nsteps, site, Op, checkpoint=10, exptol=1e-12,
+                   krylovdim=30, quad_nodes=8, precision="fp64"):
+    """Value and MPO-tensor gradient of Re <Op_site>(T) (``site`` 1-based) after
+    ``nsteps`` TDVP1 sweeps of size ``stepsize`` (real time: -1j*dt) from psi0
+    (a complex FiniteMPS, not modified).  Returns (value, [Wbar_i] as numpy
+    arrays, one per site).  Only every ``checkpoint``-th MPS is kept; each
+    block is recomputed and reversed in turn."""
+    value, tape = tdvp1_forward(mpo, psi0, stepsize, nsteps, site, Op, checkpoint, exptol,
+                                krylovdim, precision)
+    return value, tdvp1_backward(tape, quad_nodes)
+
+
+def _field_grad(Wb):
+    """dL/dh_i from the site-tensor cotangents of the TFI MPO (utilities.tfi_mpo):
+    W[0, :, 2, :] = -h X, so dL/dh = Re sum conj(Wbar[0, :, 2, :]) * (-X)."""
+    X = np.array([[0.0, 1.0], [1.0, 0.0]])
+    return np.array([np.real(np.sum(np.conj(g[0, :, 2, :]) * (-X))) for g in Wb])
 
 
 def tfi_field_gradient(h_fields, psi0, stepsize, nsteps, site, Op=None, **kw):
@@ -455,7 +520,86 @@ def tfi_field_gradient(h_fields, psi0, stepsize, nsteps, site, Op=None, **kw):
     from .utilities import tfi_mpo
     Op = np.diag([-1.0, 1.0]) if Op is None else Op
     value, Wb = tdvp1_gradient(tfi_mpo(h_fields), psi0, stepsize, nsteps, site, Op, **kw)
-    X = np.array([[0.0, 1.0], [1.0, 0.0]])
-    # W[0, :, 2, :] = -h X  ->  dL/dh = Re sum conj(Wbar[0, :, 2, :]) * (-X)
-    grad = np.array([np.real(np.sum(np.conj(g[0, :, 2, :]) * (-X))) for g in Wb])
-    return value, grad
+    return value, _field_grad(Wb)
+
+
+# ------------------------------------------------------------ autograd boundary
+def _torch():
+    import torch
+    return torch
+
+
+def _make_function():
+    torch = _torch()
+
+    class TDVP1Observable(torch.autograd.Function):
+        """Re <Op_site>(T) after a TDVP1 trajectory as a differentiable function of
+        the MPO site tensors (complex128 torch tensors W[wl, s_out, wr, s_in], one
+        per site).  forward runs the trajectory on the device and keeps only the
+        checkpoints; backward runs the reverse pass (tdvp1_backward) and returns
+        g * Wbar per site, Wbar = dL/dRe W + i dL/dIm W (torch's convention for a
+        real loss of complex leaves).  The counterpart of a ChainRulesCore rrule
+        around the reference's TDVP1 sweeps (algorithms/tdvp.jl:19-69)."""
+
+        @staticmethod
+        def forward(ctx, psi0, stepsize, nsteps, site, Op, opts, *Ws):
+            mpo = [W.detach().cpu().numpy().astype(np.complex128) for W in Ws]
+            value, tape = tdvp1_forward(mpo, psi0, stepsize, nsteps, site, Op,
+                                        opts.get("checkpoint", 10), opts.get("exptol", 1e-12),
+                                        opts.get("krylovdim", 30),
+                                        opts.get("precision", "fp64"))
+            ctx.tape = tape
+            ctx.quad_nodes = opts.get("quad_nodes", 8)
+            ctx.devices = [W.device for W in Ws]
+            return torch.tensor(value, dtype=torch.float64)
+
+        @staticmethod
+        def backward(ctx, g):
+            Wb = tdvp1_backward(ctx.tape, ctx.quad_nodes)
+            ctx.tape = None
+            grads = tuple(g.to(dev) * torch.from_numpy(w).to(dev)
+                          for w, dev in zip(Wb, ctx.devices))
+            return (None,) * 6 + grads
+
+    return TDVP1Observable
+
+
+_FUNCTION = None
+
+
+def TDVP1Observable():
+    """The torch.autograd.Function class (built on first use, so that importing
+    this module does not import torch)."""
+    global _FUNCTION
+    if _FUNCTION is None:
+        _FUNCTION = _make_function()
+    return _FUNCTION
+
+
+def tdvp1_observable(Ws, psi0, stepsize, nsteps, site, Op, **opts):
+    """Differentiable Re <Op_site>(T): ``Ws`` a list of complex torch tensors
+    (MPO site tensors, requires_grad as wanted).  Options: checkpoint, exptol,
+    krylovdim, quad_nodes, precision."""
+    return TDVP1Observable().apply(psi0, stepsize, nsteps, site, Op, dict(opts), *Ws)
+
+
+def tfi_mpo_torch(h):
+    """The TFI site tensors of utilities.tfi_mpo (w=3 Schur grid of
+    -sum Z Z - sum h_i X, boundary vectors applied by the environments) as
+    W_i = W(h=0) + h_i * dW/dh, built with torch ops from a real tensor of
+    fields so that autograd carries dL/dW back to dL/dh."""
+    torch = _torch()
+    from .utilities import tfi_mpo
+    w0 = np.asarray(tfi_mpo([0.0]).site_tensors(1)[0], dtype=np.complex128)
+    w1 = np.asarray(tfi_mpo([1.0]).site_tensors(1)[0], dtype=np.complex128)
+    base = torch.from_numpy(w0).to(h.device)
+    field = torch.from_numpy(w1 - w0).to(h.device)
+    hc = h.to(torch.complex128)
+    return [base + hc[i] * field for i in range(h.shape[0])]
+
+
+def tfi_observable(h, psi0, stepsize, nsteps, site, Op=None, **opts):
+    """Differentiable Re <Op_site>(T) (default Op = Z) of the TFI chain with
+    fields ``h`` (a real torch tensor): loss.backward() fills h.grad."""
+    Op = np.diag([-1.0, 1.0]) if Op is None else Op
+    return tdvp1_observable(tfi_mpo_torch(h), psi0, stepsize, nsteps, site, Op, **opts)

@@ -8,14 +8,18 @@ Functions ending in ``_`` mutate their first argument like the reference's
 environments and the Krylov vectors on the GPU; only scalars come back.
 """
 
+import ctypes
+
 import numpy as np
 
+from ._native import C128, F64, PREC, lib
 from .auxiliary import (MPSTruncation, default_truncation, dm_split, dot, gemm, leftorth, norm,
                         rightorth, scal, scale_cols, scale_rows, stable_tsvd)
 from .derivatives import HeffOp
-from .device import DeviceTensor
+from .device import DeviceTensor, to_host_mpo
 from .envs import ExpectationCache, environments, increase_bond_env_, updateleft_, updateright_
 from .excited import project_, projectors1, projectors2
+from .mps import max_bond_dimensions
 from .transfer import updateleft, updateright
 from .expansion import (DMRG1S, TDVP1S, TDVP2, dmrg1s_leftsweep_, dmrg1s_rightsweep_,
                         tdvp1s_sweep_, tdvp2_sweep_)
@@ -23,7 +27,7 @@ from .u1 import U1ExpectationCache, U1FiniteMPS, u1_expectation, u1_leftsweep_, 
 from .utilities import MPOHamiltonian
 
 __all__ = ["Defaults", "DMRG1", "DMRG2", "DMRG1S", "TDVP1", "TDVP2", "TDVP1S", "leftsweep_",
-           "rightsweep_", "sweep_",
+           "rightsweep_", "sweep_", "dmrg2_sweep_device_",
            "compute_", "ground_state_", "expectation", "expectation_local"]
 
 
@@ -44,7 +48,10 @@ class DMRG2:
 
     def __init__(self, maxiter=Defaults.maxiter, tol=Defaults.tol, eig_maxiter=10,
                  eig_tol=Defaults.dmrg_eig_tol, verbosity=Defaults.verbosity, trunc=None,
-                 precision="fp64", reorth=False, svd="gesvd", env_precision=None):
+                 precision="fp64", reorth=False, svd="gesvd", env_precision=None,
+                 driver="python"):
+        if driver not in ("python", "device"):
+            raise ValueError("driver must be 'python' or 'device'")
         self.maxiter, self.tol = maxiter, tol
         self.eig_maxiter, self.eig_tol = eig_maxiter, eig_tol
         self.verbosity = verbosity
@@ -53,6 +60,9 @@ class DMRG2:
         self.svd = svd          # "gesvd" (reference semantics) or "dm" (density matrix)
         # arithmetic of the environment updates (defaults to the contractions')
         self.env_precision = env_precision or precision
+        # "python": the bond loop below; "device": one fmpt_dmrg2_sweep call per sweep
+        # (same library calls per bond, no Python between bonds; plain caches only)
+        self.driver = driver
 
 
 class DMRG1:
@@ -134,6 +144,69 @@ def _dmrg2_bond_left(m, site, alg):
     if alg.verbosity > 2:
         print("bond %d (left): E=%.15g lanczos k=%d info=%d D=%d" % (site, E, k, info, kk))
     return E, delta
+
+
+def _grown(t, cap, dtype):
+    """t itself when its buffer holds ``cap`` elements, else a copy in a buffer that does."""
+    if t is not None and t.capacity >= cap * (16 if dtype == np.complex128 else 8):
+        return t
+    big = DeviceTensor((cap,), dtype, t.h)
+    if t is not None:
+        t.h.check(lib().fmpt_memcpy_d2d(t.h.ptr, big.ptr, t.ptr, t.nbytes))
+    return big
+
+
+def dmrg2_sweep_device_(m, alg):
+    """sweep!(m, DMRG2) (dmrgexcited.jl:219-223) as ONE fmpt_dmrg2_sweep call: the
+    left and right bond loops of leftsweep_/rightsweep_ run inside the library on
+    the device-resident chain, with the same calls per bond (so the same Ritz
+    values, tensors and environments).  Site tensors and environments are moved
+    into buffers sized for the largest bonds the truncation allows, then viewed
+    with their new shapes (no copy back).  Returns (energies, delta)."""
+    if getattr(m, "cstorages", None) or isinstance(m, U1ExpectationCache):
+        raise NotImplementedError("device sweep: plain dense ExpectationCache only")
+    mps, hs = m.mps, m.hstorage
+    h = mps.handle
+    L = len(mps)
+    dt = m.dtype
+    m.precision = alg.env_precision
+    phys = [mps[i].shape[1] for i in range(1, L + 1)]
+    bond = [mps[1].shape[0]] + [mps[i].shape[2] for i in range(1, L + 1)]
+    wb = [m.mpo[1].shape[0]] + [m.mpo[i].shape[2] for i in range(1, L + 1)]
+    vmax = max_bond_dimensions(phys, alg.trunc.D)
+    cb = [max(bond[b], vmax[b]) for b in range(L + 1)]
+    site_cap = [cb[i] * phys[i] * cb[i + 1] for i in range(L)]
+    env_cap = [cb[b] * wb[b] * cb[b] for b in range(L + 1)]
+    for i in range(L):
+        mps[i + 1] = _grown(mps[i + 1], site_cap[i], dt)
+    for b in range(L + 1):
+        hs[b + 1] = _grown(hs[b + 1], env_cap[b], dt)
+    for b in range(1, L):
+        mps.s[b + 1] = _grown(mps.s[b + 1] if mps.s[b + 1] is not None else
+                              DeviceTensor((1,), np.float64, h), cb[b], np.float64)
+    Wbufs = [to_host_mpo(W, dt) for W in m.mpo]
+    arr = ctypes.c_void_p * L
+    earr = ctypes.c_void_p * (L + 1)
+    c_bond = (ctypes.c_int * (L + 1))(*bond)
+    energies = (ctypes.c_double * max(1, 2 * L - 3))()
+    delta = ctypes.c_double()
+    h.check(lib().fmpt_dmrg2_sweep(
+        h.ptr, C128 if dt == np.complex128 else F64, PREC[alg.precision],
+        PREC[alg.env_precision], L, (ctypes.c_int * L)(*phys), c_bond,
+        arr(*[mps[i + 1].ptr for i in range(L)]), (ctypes.c_int64 * L)(*site_cap),
+        earr(*[hs[b + 1].ptr for b in range(L + 1)]), (ctypes.c_int64 * (L + 1))(*env_cap),
+        arr(*[w.ctypes.data for w in Wbufs]), (ctypes.c_int * (L + 1))(*wb),
+        earr(*([None] + [mps.s[b + 1].ptr for b in range(1, L)] + [None])),
+        int(alg.trunc.D), float(alg.trunc.eps), int(alg.eig_maxiter), float(alg.eig_tol),
+        1 if alg.reorth else 0, 1 if alg.svd == "dm" else 0, energies, ctypes.byref(delta)))
+    bond = list(c_bond)
+    for i in range(L):
+        mps[i + 1].view_as((bond[i], phys[i], bond[i + 1]))
+    for b in range(L + 1):
+        hs[b + 1].view_as((bond[b], wb[b], bond[b]))
+    for b in range(1, L):
+        mps.s[b + 1].view_as((bond[b],))
+    return list(energies)[:2 * L - 3], delta.value
 
 
 def leftsweep_(m, alg):
@@ -352,6 +425,8 @@ def sweep_(m, alg):
     if isinstance(alg, TDVP1S):
         tdvp1s_sweep_(m, alg)
         return None
+    if isinstance(alg, DMRG2) and alg.driver == "device":
+        return dmrg2_sweep_device_(m, alg)
     E1, d1 = leftsweep_(m, alg)
     E2, d2 = rightsweep_(m, alg)
     return E1 + E2, max(d1, d2)

@@ -254,6 +254,31 @@ int fmpt_op_set_projectors(fmpt_op* op, int nproj, const double* const* p);
 int fmpt_lanczos_ground(fmpt_op* op, const double* x0, int kmax, double btol, int reorth,
                         double* eigval, double* xout, int* info, int* niter);
 
+/* One whole DMRG2 sweep: sweep!(m, DMRG2) (algorithms/dmrgexcited.jl:219-223),
+ * i.e. leftsweep! over the bonds (1,2) .. (L-2,L-1) then rightsweep! over
+ * (L-1,L) .. (1,2) (algorithms/dmrg.jl:89-144).  Each bond: two-site product,
+ * fmpt_lanczos_ground on the ac2 operator (eig_maxiter, eig_tol, reorth), the
+ * MPSTruncation split (split 0: fmpt_svd_trunc, 1: fmpt_dm_split; maxD, eps),
+ * normalize!(s), the fidelity |1 - |<usv, x2>||, and updateleft!/updateright!
+ * in env_precision.  The chain stays in caller-owned device buffers:
+ *   sites[i]  A_i [bond[i], phys[i], bond[i+1]], capacity site_cap[i] elements;
+ *   envs[b]   h_b [bond[b], wbond[b], bond[b]] (envs[0] = l_LL, envs[L] =
+ *             r_RR, envs[b] the environment left of site b), capacity env_cap[b];
+ *   W_host[i] the HOST MPO tensor of site i [wbond[i], phys[i], wbond[i+1], phys[i]];
+ *   svals[b]  optional (NULL, or NULL entries): receives s of bond b on the
+ *             right sweep (psi.s[b+1] in the reference's 1-based numbering).
+ * bond (HOST, L+1 entries, bond[0] = bond[L] = 1 for a finite chain) is updated
+ * bond by bond.  energies (HOST) gets the 2L-3 Ritz values in sweep order and
+ * delta (HOST) the largest fidelity delta.  A kept rank that does not fit a
+ * buffer returns FMPT_ERR_SHAPE before that bond writes anything (the bonds
+ * before it are complete).  No projectors (plain ExpectationCache only). */
+int fmpt_dmrg2_sweep(fmpt_handle* h, int dtype, int precision, int env_precision, int L,
+                     const int* phys, int* bond, double* const* sites, const int64_t* site_cap,
+                     double* const* envs, const int64_t* env_cap, const double* const* W_host,
+                     const int* wbond, double* const* svals, int maxD, double eps,
+                     int eig_maxiter, double eig_tol, int reorth, int split, double* energies,
+                     double* delta);
+
 /* TEBD gate action (the bondmpo contraction of bond_evolution,
  * circuit/apply_gates.jl:11-50): y[a, p', b] = sum_p G[p', p] x[a, p, b] for a
  * device tensor x [Dl, P, Dr] whose middle index fuses the physical indices of
