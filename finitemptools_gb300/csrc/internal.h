@@ -37,6 +37,9 @@ struct fmpt_handle {
   std::vector<cudaEvent_t> aux_event;   // [0] fork, [1 + i] join of aux stream i
   // CUDA graphs for the Krylov solvers of block-sparse operators (fmpt_set_graphs)
   bool graphs = true;
+  // Krylov exponentials: one cooperative launch per Arnoldi orthogonalisation step
+  // (fmpt_set_fused_krylov; the seven separate launches give bit-identical results)
+  int fused_gs = 1;
   int svd_method = 0;          // 0 gesvd (bidiagonalisation), 1 gesvdp (polar decomposition)
   int tc_tile = 0;             // tcgen05 GEMM tile: 0 CTA pair where it applies, 1 one CTA
   // split-K workspace of the FP64 GEMM, grown outside stream capture only (stream-ordered

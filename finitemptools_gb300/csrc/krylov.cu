@@ -1,14 +1,16 @@
 // Krylov solvers on device-resident vectors: the reference's plain Lanczos
 // for the lowest eigenpair and a Krylov exponential for TDVP.
 //
-// Vectors stay in HBM for the whole solve; only the scalars that steer the
-// host loop (beta for the stopping test, the first column of the small
-// exponential for the step-size control) come back to the host.  All
-// reductions are deterministic two-level sums (warp shuffles inside a block,
-// a fixed-order sum over the block partials, recomputed by every consumer
-// block so that no separate finalisation launch is needed).
+// Vectors stay in HBM for the whole solve; only the small matrices and scalars
+// that steer the host loop come back to the host (beta for the Lanczos stopping
+// test; the Krylov exponential's Hessenberg matrix, whose small exponential and
+// step-size control run on the host).  All reductions are deterministic
+// two-level sums (warp shuffles inside a block, a fixed-order sum over the block
+// partials, recomputed by every consumer block so that no separate
+// finalisation launch is needed).
 #include <algorithm>
 #include <cmath>
+#include <complex>
 #include <vector>
 
 #include "internal.h"
@@ -22,6 +24,32 @@ __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
+}
+
+// Warp sums of K values at once (K a power of two <= 32).  GB300 issues an FP64 warp
+// instruction at about 2 lanes per clock per SM, so the adds of a reduction cost more than
+// the shuffles: plain xor-sums take 5 K adds per lane, this takes K - 1 + (5 - log2 K).
+// Recursive halving: at each butterfly step (lane offsets 16, 8, ...) a lane keeps one half
+// of its values, the partner lane the other half, and each adds the partner's copy of the
+// half it keeps; then a plain xor-sum over the remaining lane bits.  a[0] ends up holding
+// the warp sum of value (lane >> (5 - log2 K)); the order of the adds is fixed.
+template <int K>
+__device__ __forceinline__ void warp_sum_many(double (&a)[K]) {
+  const int lane = threadIdx.x & 31;
+  int o = 16;
+#pragma unroll
+  for (int cnt = K; cnt > 1; cnt >>= 1, o >>= 1) {
+    const int half = cnt >> 1;
+    const bool upper = (lane & o) != 0;
+#pragma unroll
+    for (int i = 0; i < half; i++) {
+      const double send = upper ? a[i] : a[i + half];
+      const double keep = upper ? a[i + half] : a[i];
+      a[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+    }
+  }
+#pragma unroll
+  for (; o > 0; o >>= 1) a[0] += __shfl_xor_sync(0xffffffffu, a[0], o);
 }
 
 __device__ double block_sum(double v) {
@@ -108,10 +136,12 @@ __global__ void lanczos_scale(int64_t n, double* __restrict__ y, const double* _
 // shared-memory pass per chunk -- instead of one full block reduction per vector.  Fixed
 // summation order throughout (deterministic).
 constexpr int MD_CH = 8;
-__global__ void multidot_partial(int cplx, int64_t n, int j, const double* __restrict__ V,
-                                 int64_t vstride, const double* __restrict__ z,
-                                 double* __restrict__ part, const int* gate = nullptr) {
-  if (gate && *gate) return;
+template <int CH = MD_CH>
+__device__ __forceinline__ void multidot_body(int cplx, int64_t n, int j,
+                                              const double* __restrict__ V, int64_t vstride,
+                                              const double* __restrict__ z,
+                                              double* __restrict__ part) {
+  constexpr int MD_CH = CH;       // vectors per pass over z (the sums do not depend on it)
   __shared__ double red[KT / 32][2 * MD_CH];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (int i0 = 0; i0 < j; i0 += MD_CH) {
@@ -138,17 +168,16 @@ __global__ void multidot_partial(int cplx, int64_t n, int j, const double* __res
         }
       }
     }
+    double v[2 * MD_CH];
 #pragma unroll
     for (int c = 0; c < MD_CH; c++) {
-      sr[c] = warp_sum(sr[c]);
-      si[c] = warp_sum(si[c]);
+      v[2 * c] = sr[c];
+      v[2 * c + 1] = si[c];
     }
-    if (lane == 0) {
-#pragma unroll
-      for (int c = 0; c < MD_CH; c++) {
-        red[wid][2 * c] = sr[c];
-        red[wid][2 * c + 1] = si[c];
-      }
+    warp_sum_many<2 * MD_CH>(v);
+    {
+      constexpr int sh = MD_CH == 16 ? 0 : (MD_CH == 8 ? 1 : (MD_CH == 4 ? 2 : 3));
+      if ((lane & ((1 << sh) - 1)) == 0) red[wid][lane >> sh] = v[0];
     }
     __syncthreads();
     if (threadIdx.x < 2 * MD_CH) {
@@ -161,44 +190,90 @@ __global__ void multidot_partial(int cplx, int64_t n, int j, const double* __res
   }
 }
 
+__global__ void multidot_partial(int cplx, int64_t n, int j, const double* __restrict__ V,
+                                 int64_t vstride, const double* __restrict__ z,
+                                 double* __restrict__ part, const int* gate = nullptr) {
+  if (gate && *gate) return;
+  multidot_body<>(cplx, n, j, V, vstride, z, part);
+}
+
 // coef[i] (re, im) = sum over the G partials, one warp per value (lanes stride over the
 // partials in a fixed order, then a shuffle sum); launched with one block of KT threads
+// Coefficients t0 .. t0 + 63 (t = 2 i + re/im) of the sums over the G partials [G][j][2]:
+// warp w takes t = t0 + w + 8 u (u < 8); a lane adds its partials g = lane, lane + 32, ...
+// in g order, then the warp sums its 8 values with warp_sum_many.  out[t] = the sum
+// (accum[t] += it when given).  QMAX > 0: at most QMAX partials per lane, loads unrolled.
+template <int QMAX>
+__device__ __forceinline__ void coef_group(int j, int G, const double* __restrict__ part, int t0,
+                                           double* out, double* accum) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  double acc[8];
+#pragma unroll
+  for (int u = 0; u < 8; u++) {
+    const int t = t0 + wid + 8 * u;
+    double sum = 0.0;
+    if (t < 2 * j) {
+      const int i = t >> 1, comp = t & 1;
+      if (QMAX > 0) {
+#pragma unroll
+        for (int q = 0; q < QMAX; q++) {
+          const int g = lane + 32 * q;
+          if (g < G) sum += part[((int64_t)g * j + i) * 2 + comp];
+        }
+      } else {
+        for (int g = lane; g < G; g += 32) sum += part[((int64_t)g * j + i) * 2 + comp];
+      }
+    }
+    acc[u] = sum;
+  }
+  warp_sum_many<8>(acc);
+  const int t = t0 + wid + 8 * (lane >> 2);
+  if ((lane & 3) == 0 && t < 2 * j) {
+    out[t] = acc[0];
+    if (accum) accum[t] += acc[0];
+  }
+}
+
+// coef[t] = the sums (accum[t] += them when given); launched with one block of KT threads
 __global__ void multidot_finalize(int j, int G, const double* __restrict__ part,
                                   double* __restrict__ coef, double* __restrict__ accum,
                                   const int* gate = nullptr) {
   if (gate && *gate) return;
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-  for (int t = wid; t < 2 * j; t += nwarp) {
-    const int i = t >> 1, comp = t & 1;
-    double s = 0.0;
-    for (int g = lane; g < G; g += 32) s += part[((int64_t)g * j + i) * 2 + comp];
-    s = warp_sum(s);
-    if (lane == 0) {
-      coef[t] = s;
-      if (accum) accum[t] += s;
-    }
-  }
+  for (int t0 = 0; t0 < 2 * j; t0 += 64) coef_group<0>(j, G, part, t0, coef, accum);
 }
 
-// z -= sum_i coef_i V_i ; part = partial |z|^2
-__global__ void multi_axpy_sub(int cplx, int64_t n, int j, const double* __restrict__ V,
-                               int64_t vstride, const double* __restrict__ coef,
-                               double* __restrict__ z, double* __restrict__ part,
-                               const int* gate = nullptr) {
-  if (gate && *gate) return;
+__device__ __forceinline__ void multi_axpy_body(int cplx, int64_t n, int j,
+                                                const double* __restrict__ V, int64_t vstride,
+                                                const double* __restrict__ coef,
+                                                double* __restrict__ z, double* __restrict__ part) {
   double s = 0.0;
   for (int64_t e = (int64_t)blockIdx.x * KT + threadIdx.x; e < n; e += (int64_t)gridDim.x * KT) {
     double zr = z[e], zi = cplx ? z[n + e] : 0.0;
-    for (int i = 0; i < j; i++) {
-      const double* v = V + (int64_t)i * vstride;
-      double cr = coef[2 * i], ci = coef[2 * i + 1];
-      double vr = v[e];
-      if (cplx) {
-        double vi = v[n + e];
-        zr -= cr * vr - ci * vi;
-        zi -= cr * vi + ci * vr;
-      } else {
-        zr -= cr * vr;
+    // MD_CH vectors' elements are loaded together (their L2 latencies overlap), then
+    // subtracted in vector order
+    for (int i0 = 0; i0 < j; i0 += MD_CH) {
+      double vr[MD_CH], vi[MD_CH];
+#pragma unroll
+      for (int c = 0; c < MD_CH; c++) {
+        vr[c] = 0.0;
+        vi[c] = 0.0;
+        if (i0 + c < j) {
+          const double* v = V + (int64_t)(i0 + c) * vstride;
+          vr[c] = v[e];
+          if (cplx) vi[c] = v[n + e];
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < MD_CH; c++) {
+        if (i0 + c < j) {
+          const double cr = coef[2 * (i0 + c)], ci = coef[2 * (i0 + c) + 1];
+          if (cplx) {
+            zr -= cr * vr[c] - ci * vi[c];
+            zi -= cr * vi[c] + ci * vr[c];
+          } else {
+            zr -= cr * vr[c];
+          }
+        }
       }
     }
     z[e] = zr;
@@ -208,6 +283,14 @@ __global__ void multi_axpy_sub(int cplx, int64_t n, int j, const double* __restr
   }
   s = block_sum(s);
   if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+__global__ void multi_axpy_sub(int cplx, int64_t n, int j, const double* __restrict__ V,
+                               int64_t vstride, const double* __restrict__ coef,
+                               double* __restrict__ z, double* __restrict__ part,
+                               const int* gate = nullptr) {
+  if (gate && *gate) return;
+  multi_axpy_body(cplx, n, j, V, vstride, coef, z, part);
 }
 
 // out = sum_i c_i V_i (c complex when cplx, real otherwise); scale multiplies
@@ -242,12 +325,14 @@ __global__ void combine_basis(int cplx, int64_t n, int j, const double* __restri
 // norm before it is sqrt(s^2 + sum_i |H[i][j]|^2).  If s is below 1e-12 of
 // that (the Krylov space is exhausted: happy breakdown) the next basis vector
 // and H[j+1][j] are zero, otherwise V_{j+1} = z / s and H[j+1][j] = s.
-__global__ void arnoldi_normalize(int64_t n_real, const double* __restrict__ z,
-                                  const double* __restrict__ part, int G,
-                                  double* __restrict__ Hcol, int j, double* __restrict__ vnext) {
+__device__ __forceinline__ void arnoldi_normalize_body(int64_t n_real,
+                                                       const double* __restrict__ z,
+                                                       const double* __restrict__ part, int G,
+                                                       const double* hc, double* __restrict__ Hcol,
+                                                       int j, double* __restrict__ vnext) {
   const double s = sqrt(sum_parts(part, G));
   double ref = s * s;
-  for (int i = 0; i <= j; i++) ref += Hcol[2 * i] * Hcol[2 * i] + Hcol[2 * i + 1] * Hcol[2 * i + 1];
+  for (int i = 0; i <= j; i++) ref += hc[2 * i] * hc[2 * i] + hc[2 * i + 1] * hc[2 * i + 1];
   const bool breakdown = !(s > 1e-12 * sqrt(ref));
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     Hcol[2 * (j + 1)] = breakdown ? 0.0 : s;
@@ -257,6 +342,108 @@ __global__ void arnoldi_normalize(int64_t n_real, const double* __restrict__ z,
   for (int64_t e = (int64_t)blockIdx.x * KT + threadIdx.x; e < n_real;
        e += (int64_t)gridDim.x * KT)
     vnext[e] = z[e] * inv;
+}
+
+__global__ void arnoldi_normalize(int64_t n_real, const double* __restrict__ z,
+                                  const double* __restrict__ part, int G,
+                                  double* __restrict__ Hcol, int j, double* __restrict__ vnext) {
+  arnoldi_normalize_body(n_real, z, part, G, Hcol, Hcol, j, vnext);
+}
+
+// ---- the whole orthogonalisation step of one Arnoldi vector as ONE cooperative launch:
+// pass 1 (partial dots, barrier, coefficients, z -= V c), pass 2 (the same), barrier,
+// normalisation.  Every block computes the coefficients itself in the summation order of
+// multidot_finalize (coef_group), so the results are bit-identical to the seven separate
+// launches.  The
+// grid barriers are bounded (2 s on %globaltimer): a timeout sets the abort flag and the
+// handle's status word and every block returns.
+struct CoopBar {
+  int* count;        // arrivals (zeroed before each launch, in stream order)
+  int* abort_flag;
+  int* status;       // handle status word
+  uint64_t wait_ns;
+  int hold;          // arrivals waited for beyond the grid: 0, or 1 only to test the bound
+};
+
+__device__ __forceinline__ int ld_acquire_i(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ uint64_t now_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ bool coop_barrier(const CoopBar& b, int target) {
+  __shared__ int ok_s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(b.count, 1);
+    int ok = 1;
+    const uint64_t t0 = now_ns();
+    while (ld_acquire_i(b.count) < target + b.hold) {
+      // this launch gave up, or an earlier one of the same solve did (the status word
+      // stays set until the host reads it)
+      if (ld_acquire_i(b.abort_flag) || ld_acquire_i(b.status)) { ok = 0; break; }
+      if (now_ns() - t0 > b.wait_ns) {
+        atomicExch(b.abort_flag, 1);
+        atomicExch(b.status, 1);
+        ok = 0;
+        break;
+      }
+      __nanosleep(64);
+    }
+    __threadfence();
+    ok_s = ok;
+  }
+  __syncthreads();
+  return ok_s != 0;
+}
+
+template <int QMAX>
+__global__ void __launch_bounds__(KT) arnoldi_gs_fused(int cplx, int64_t n, int j,
+                                                       const double* __restrict__ V,
+                                                       int64_t vstride, double* __restrict__ z,
+                                                       double* __restrict__ partA,
+                                                       double* __restrict__ partB,
+                                                       double* __restrict__ partN,
+                                                       double* __restrict__ Hcol,
+                                                       double* __restrict__ vnext, CoopBar bar) {
+  __shared__ double c1[64], c2[64], hc[64];
+  const int G = gridDim.x, jj = j + 1;
+  // pass 1
+  multidot_body<16>(cplx, n, jj, V, vstride, z, partA);
+  if (!coop_barrier(bar, G)) return;
+  coef_group<QMAX>(jj, G, partA, 0, c1, nullptr);     // 2 jj <= 62 values: one group
+  __syncthreads();
+  multi_axpy_body(cplx, n, jj, V, vstride, c1, z, partN);
+  // pass 2 (each thread reads back only the elements it has just written)
+  multidot_body<16>(cplx, n, jj, V, vstride, z, partB);
+  if (!coop_barrier(bar, 2 * G)) return;
+  coef_group<QMAX>(jj, G, partB, 0, c2, nullptr);
+  __syncthreads();
+  for (int t = threadIdx.x; t < 2 * jj; t += KT) {
+    hc[t] = (0.0 + c1[t]) + c2[t];    // the accumulation order of Hcol in the separate form
+    if (blockIdx.x == 0) Hcol[t] = hc[t];
+  }
+  __syncthreads();
+  multi_axpy_body(cplx, n, jj, V, vstride, c2, z, partN);
+  if (!coop_barrier(bar, 3 * G)) return;
+  arnoldi_normalize_body(n * (cplx ? 2 : 1), z, partN, G, hc, Hcol, j, vnext);
+}
+
+// the kernel instance for a grid of G blocks (partials per lane: G / 32 rounded up)
+using GsKernel = void (*)(int, int64_t, int, const double*, int64_t, double*, double*, double*,
+                          double*, double*, double*, CoopBar);
+GsKernel gs_kernel_for(int G) {
+  if (G <= 64) return arnoldi_gs_fused<2>;
+  if (G <= 160) return arnoldi_gs_fused<5>;
+  if (G <= 320) return arnoldi_gs_fused<10>;
+  return arnoldi_gs_fused<19>;                 // G <= 608 = 4 blocks x 152 SMs
 }
 
 // acc *= v (device scalars)
@@ -388,65 +575,110 @@ __global__ void lanczos_close(int64_t n, const double* __restrict__ y,
     vnext[i] = y[i] / b;
 }
 
-// E = exp(H) for a small complex matrix (m <= 32, column-major, re/im pairs)
-// by Taylor scaling and squaring (Moler & Van Loan, method 3): scale so that
-// the 1-norm is <= 1/2, sum 20 Taylor terms, square back.
-__global__ void small_expm(int m, const double* __restrict__ H, double* __restrict__ E) {
-  __shared__ double Ar[32][33], Ai[32][33], Pr[32][33], Pi[32][33], Sr[32][33], Si[32][33];
-  __shared__ int s_sq;
-  const int r = threadIdx.x, c = threadIdx.y;
-  const bool in = (r < m && c < m);
-  Ar[r][c] = in ? H[2 * (r + c * m)] : 0.0;
-  Ai[r][c] = in ? H[2 * (r + c * m) + 1] : 0.0;
-  __syncthreads();
-  if (r == 0 && c == 0) {
-    double nrm = 0.0;
-    for (int j = 0; j < m; j++) {
-      double col = 0.0;
-      for (int i = 0; i < m; i++) col += hypot(Ar[i][j], Ai[i][j]);
-      nrm = fmax(nrm, col);
+// exp(A) e_1 for the small complex matrix A = t * H_m of a Krylov exponential (m <= 31,
+// column-major (re, im) pairs), on the host: the m x m problem is a few hundred thousand
+// flops, which a host core runs in tens of microseconds while one SM's FP64 pipe (about
+// 2 DFMA per clock) needs a millisecond -- and the step-size control reads the result on
+// the host anyway.  Taylor scaling and squaring (Moler & Van Loan, method 3): s halvings
+// bring ||A||_1 to <= 1, where the degree-kDeg Taylor polynomial T is exact to rounding
+// (remainder < e / 19! ~ 2e-17); exp(A) e_1 = T(A / 2^s)^(2^s) e_1, applied to the vector
+// when 2^s applications of T cost less than s squarings of the matrix, else by squaring.
+constexpr int kDeg = 18;
+constexpr double kTheta = 1.0;     // ||A / 2^s||_1 <= 1: the Taylor remainder is < 1 / 19!
+using cplx = std::complex<double>;
+
+// y = a x for an m x m complex matrix in split planes (ar, ai column-major) whose column c
+// is zero below row rows[c] - 1 (an upper Hessenberg matrix has rows[c] = c + 2); plain
+// double arithmetic (std::complex products take a slow special-value path without
+// fast-math)
+void cmatvec(int m, const double* ar, const double* ai, const int* rows, const double* xr,
+             const double* xi, double* yr, double* yi) {
+  for (int r = 0; r < m; r++) { yr[r] = 0.0; yi[r] = 0.0; }
+  for (int c = 0; c < m; c++) {
+    const double br = xr[c], bi = xi[c];
+    const double* cr = ar + (size_t)m * c;
+    const double* ci = ai + (size_t)m * c;
+    const int nr = rows[c];
+    for (int r = 0; r < nr; r++) {
+      yr[r] += cr[r] * br - ci[r] * bi;
+      yi[r] += cr[r] * bi + ci[r] * br;
     }
-    int s = 0;
-    while (nrm > 0.5 && s < 60) { nrm *= 0.5; s++; }
-    s_sq = s;
-  }
-  __syncthreads();
-  const double sc = ldexp(1.0, -s_sq);
-  Ar[r][c] *= sc;
-  Ai[r][c] *= sc;
-  const double id = (r == c && in) ? 1.0 : 0.0;
-  Pr[r][c] = id; Pi[r][c] = 0.0;
-  Sr[r][c] = id; Si[r][c] = 0.0;
-  __syncthreads();
-  for (int t = 1; t <= 20; t++) {
-    double nr = 0.0, ni = 0.0;
-    for (int q = 0; q < m; q++) {
-      nr += Pr[r][q] * Ar[q][c] - Pi[r][q] * Ai[q][c];
-      ni += Pr[r][q] * Ai[q][c] + Pi[r][q] * Ar[q][c];
-    }
-    __syncthreads();
-    Pr[r][c] = nr / t;
-    Pi[r][c] = ni / t;
-    Sr[r][c] += Pr[r][c];
-    Si[r][c] += Pi[r][c];
-    __syncthreads();
-  }
-  for (int t = 0; t < s_sq; t++) {
-    double nr = 0.0, ni = 0.0;
-    for (int q = 0; q < m; q++) {
-      nr += Sr[r][q] * Sr[q][c] - Si[r][q] * Si[q][c];
-      ni += Sr[r][q] * Si[q][c] + Si[r][q] * Sr[q][c];
-    }
-    __syncthreads();
-    Sr[r][c] = nr;
-    Si[r][c] = ni;
-    __syncthreads();
-  }
-  if (in) {
-    E[2 * (r + c * m)] = Sr[r][c];
-    E[2 * (r + c * m) + 1] = Si[r][c];
   }
 }
+
+void host_expm_col(int m, const double* A, std::vector<cplx>& out) {
+  const size_t mm = (size_t)m * m;
+  std::vector<double> ar(mm), ai(mm);
+  std::vector<int> rows(m, 0), full(m, m);
+  double nrm = 0.0;
+  for (int c = 0; c < m; c++) {
+    double col = 0.0;
+    for (int r = 0; r < m; r++) {
+      const size_t e = r + (size_t)m * c;
+      ar[e] = A[2 * e];
+      ai[e] = A[2 * e + 1];
+      col += std::hypot(ar[e], ai[e]);
+      if (ar[e] != 0.0 || ai[e] != 0.0) rows[c] = r + 1;
+    }
+    nrm = std::max(nrm, col);
+  }
+  int sq = 0;
+  while (nrm > kTheta && sq < 60) { nrm *= 0.5; sq++; }
+  const double sc = std::ldexp(1.0, -sq);
+  for (size_t e = 0; e < mm; e++) { ar[e] *= sc; ai[e] *= sc; }
+  out.assign(m, cplx(0.0, 0.0));
+  const bool by_vector = sq < 20 && (double)(1 << sq) * kDeg < (double)(kDeg + sq) * m;
+  if (by_vector) {
+    // Horner: T(A) w = w + A (w + A / 2 (w + ... (w + A w / kDeg)))
+    std::vector<double> wr(m, 0.0), wi(m, 0.0), ur(m), ui(m), tr(m), ti(m);
+    wr[0] = 1.0;
+    for (int round = 0; round < (1 << sq); round++) {
+      ur = wr;
+      ui = wi;
+      for (int k = kDeg; k >= 1; k--) {
+        cmatvec(m, ar.data(), ai.data(), rows.data(), ur.data(), ui.data(), tr.data(),
+                ti.data());
+        const double inv = 1.0 / (double)k;
+        for (int r = 0; r < m; r++) {
+          ur[r] = wr[r] + tr[r] * inv;
+          ui[r] = wi[r] + ti[r] * inv;
+        }
+      }
+      wr.swap(ur);
+      wi.swap(ui);
+    }
+    for (int r = 0; r < m; r++) out[r] = cplx(wr[r], wi[r]);
+    return;
+  }
+  // matrix form: E = T(A) by the powers A^k / k!, then s squarings; column 0 out
+  std::vector<double> er(mm, 0.0), ei(mm, 0.0), pr(mm, 0.0), pi(mm, 0.0), qr(mm), qi(mm);
+  for (int r = 0; r < m; r++) { er[r + (size_t)m * r] = 1.0; pr[r + (size_t)m * r] = 1.0; }
+  // Z = X Y, column by column as matrix-vector products
+  auto matmul = [&](const std::vector<double>& xr, const std::vector<double>& xi,
+                    const std::vector<double>& yr, const std::vector<double>& yi,
+                    std::vector<double>& zr, std::vector<double>& zi) {
+    for (int c = 0; c < m; c++)
+      cmatvec(m, xr.data(), xi.data(), full.data(), yr.data() + (size_t)m * c,
+              yi.data() + (size_t)m * c, zr.data() + (size_t)m * c, zi.data() + (size_t)m * c);
+  };
+  for (int k = 1; k <= kDeg; k++) {
+    matmul(pr, pi, ar, ai, qr, qi);
+    const double inv = 1.0 / (double)k;
+    for (size_t e = 0; e < mm; e++) {
+      pr[e] = qr[e] * inv;
+      pi[e] = qi[e] * inv;
+      er[e] += pr[e];
+      ei[e] += pi[e];
+    }
+  }
+  for (int t = 0; t < sq; t++) {
+    matmul(er, ei, er, ei, qr, qi);
+    er.swap(qr);
+    ei.swap(qi);
+  }
+  for (int r = 0; r < m; r++) out[r] = cplx(er[r], ei[r]);
+}
+
 
 int grid_for(fmpt_handle* h, int64_t n) {
   int64_t g = (n + KT - 1) / KT;
@@ -844,6 +1076,54 @@ int op_project(fmpt_op* op, double* y, const int* gate) {
   return FMPT_OK;
 }
 
+// Workspace of the fused orthogonalisation step (arnoldi_gs_fused): the pass-2 partials
+// (pass 1 uses the caller's partM), the barrier words and the status word.
+struct GsWork {
+  double* partB;
+  int* bar;
+  int* status;
+  uint64_t wait_ns;
+  int hold;
+};
+
+// Whether G blocks of arnoldi_gs_fused are co-resident on this device (the cooperative
+// launch needs it); measured once per device.
+bool gs_fused_fits(fmpt_handle* h, int G) {
+  static int occ[64] = {};
+  static bool done[64] = {};
+  const int dev = h->device;
+  if (dev < 0 || dev >= 64) return false;
+  if (!done[dev]) {
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, arnoldi_gs_fused<19>, KT, 0) !=
+        cudaSuccess) {
+      cudaGetLastError();
+      b = 0;
+    }
+    occ[dev] = b;
+    done[dev] = true;
+  }
+  return (int64_t)occ[dev] * h->sm_count >= G;
+}
+
+// Set up the fused step's workspace in `buf` (allocated here) when it applies: enabled on
+// the handle (fmpt_set_fused_krylov), a co-resident grid and a Krylov space of at most 31
+// vectors.  gs stays null otherwise (the separate launches run).
+int gs_setup(fmpt_op* op, int G, int M, DevBuf& buf, GsWork& w, const GsWork** gs) {
+  fmpt_handle* h = op->h;
+  *gs = nullptr;
+  if (!h->fused_gs || M > 31 || !gs_fused_fits(h, G)) return FMPT_OK;
+  const size_t nb = (size_t)G * (M + 1) * 2 * sizeof(double);
+  FMPT_TRY(buf.alloc(h, nb + 16 * sizeof(int)));
+  w.partB = buf.d();
+  w.bar = reinterpret_cast<int*>(static_cast<char*>(buf.p) + nb);
+  FMPT_TRY(gp_status_word(h, &w.status));
+  w.wait_ns = h->wait_test_ns > 0 ? (uint64_t)h->wait_test_ns : 2000000000ull;
+  w.hold = h->wait_test_hold;
+  *gs = &w;
+  return FMPT_OK;
+}
+
 // The Arnoldi basis V_1..V_M of fmpt_exponentiate / fmpt_expm_nodes (two-pass classical
 // Gram-Schmidt; the columns of H into Hdev), device launches only.  With graphs enabled the
 // launches are captured into one CUDA graph per operator structure and replayed: the
@@ -853,7 +1133,8 @@ int op_project(fmpt_op* op, double* y, const int* gate) {
 // fresh operator among them, whose scratch is sized outside capture -- runs the same
 // launches directly.
 int arnoldi_basis(fmpt_op* op, int cp, int64_t n, int64_t nr, int G, int M, int ldh, double* V,
-                  double* z, double* part, double* partM, double* coef, DevBuf& Hdev) {
+                  double* z, double* part, double* partM, double* coef, DevBuf& Hdev,
+                  const GsWork* gs) {
   fmpt_handle* h = op->h;
   cudaStream_t st = h->stream;
   auto record = [&]() -> int {
@@ -862,6 +1143,23 @@ int arnoldi_basis(fmpt_op* op, int cp, int64_t n, int64_t nr, int G, int M, int 
       double* Hcol = Hdev.d() + (size_t)2 * ldh * j;
       double* vj = V + (int64_t)j * nr;
       FMPT_TRY(fmpt_op_apply(op, vj, z));
+      if (gs) {
+        FMPT_CUDA(h, cudaMemsetAsync(gs->bar, 0, 2 * sizeof(int), st));
+        CoopBar bar{gs->bar, gs->bar + 1, gs->status, gs->wait_ns, gs->hold};
+        cudaLaunchConfig_t cfg{};
+        cfg.gridDim = dim3(G);
+        cfg.blockDim = dim3(KT);
+        cfg.stream = st;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeCooperative;
+        attr[0].val.cooperative = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        FMPT_CUDA(h, cudaLaunchKernelEx(&cfg, gs_kernel_for(G), cp, n, j, (const double*)V, nr,
+                                        z, partM, gs->partB, part, Hcol, vj + nr, bar));
+        FMPT_LAUNCHED(h);
+        continue;
+      }
       for (int pass = 0; pass < 2; pass++) {
         multidot_partial<<<G, KT, 0, st>>>(cp, n, j + 1, V, nr, z, partM);
         FMPT_LAUNCHED(h);
@@ -894,8 +1192,8 @@ int arnoldi_basis(fmpt_op* op, int cp, int64_t n, int64_t nr, int G, int M, int 
     return record();
   }
   char key[96];
-  std::snprintf(key, sizeof(key), "k%d p%d c%d u%d q%zu M%d", op->kind, op->precision, cp,
-                op->u1 ? 1 : 0, op->proj.size(), M);
+  std::snprintf(key, sizeof(key), "k%d p%d c%d u%d q%zu M%d g%d", op->kind, op->precision, cp,
+                op->u1 ? 1 : 0, op->proj.size(), M, gs ? 1 : 0);
   cudaGraphExec_t& ex = h->arnoldi_exec[key];
   bool ready = false;
   if (ex) {
@@ -1096,18 +1394,22 @@ int fmpt_exponentiate(fmpt_op* op, double t_re, double t_im, const double* x, do
   // the Krylov space cannot be larger than the vector space
   const int M = (int)std::min<int64_t>(krylovdim, n);
   const int ldh = M + 1;
-  DevBuf Vb, zb, part, partM, coef, Hdev, Hd, Ed, nrm, acc;
+  DevBuf Vb, zb, part, partM, coef, Hdev, Ed, nrm, acc;
   FMPT_TRY(Vb.alloc(h, (size_t)(M + 1) * nr * sizeof(double)));
   FMPT_TRY(zb.alloc(h, (size_t)nr * sizeof(double)));
   FMPT_TRY(part.alloc(h, (size_t)G * sizeof(double)));
   FMPT_TRY(partM.alloc(h, (size_t)G * (M + 1) * 2 * sizeof(double)));
   FMPT_TRY(coef.alloc(h, (size_t)(M + 1) * 2 * sizeof(double)));
   FMPT_TRY(Hdev.alloc(h, (size_t)ldh * M * 2 * sizeof(double)));
-  FMPT_TRY(Hd.alloc(h, (size_t)32 * 32 * 2 * sizeof(double)));
-  FMPT_TRY(Ed.alloc(h, (size_t)32 * 32 * 2 * sizeof(double)));
+  FMPT_TRY(Ed.alloc(h, (size_t)M * 2 * sizeof(double)));
+  std::vector<double> colbuf((size_t)2 * M);
   FMPT_TRY(nrm.alloc(h, 2 * sizeof(double)));
   FMPT_TRY(acc.alloc(h, 2 * sizeof(double)));
   FMPT_TRY(ensure_pinned(h, (size_t)ldh * M * 2 + 8));
+  DevBuf gsbuf;
+  GsWork gsw{};
+  const GsWork* gs = nullptr;
+  FMPT_TRY(gs_setup(op, G, M, gsbuf, gsw, &gs));
   double* V = Vb.d();
   auto V_ = [&](int i) { return V + (int64_t)i * nr; };
   const double tabs = std::hypot(t_re, t_im);
@@ -1131,10 +1433,11 @@ int fmpt_exponentiate(fmpt_op* op, double t_re, double t_im, const double* x, do
     if (++steps > 1000) return set_error(h, FMPT_ERR_NOCONV, "exponentiate: too many steps");
     // ---- Arnoldi (two-pass classical Gram-Schmidt) entirely on the device
     FMPT_TRY(arnoldi_basis(op, cp, n, nr, G, M, ldh, V, zb.d(), part.d(), partM.d(), coef.d(),
-                           Hdev));
+                           Hdev, gs));
     FMPT_CUDA(h, cudaMemcpyAsync(h->pinned, Hdev.p, Hdev.bytes, cudaMemcpyDeviceToHost,
                                  h->stream));
     FMPT_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (gs) FMPT_TRY(gp_check_status(h));     // a fused step that gave up left H invalid
     std::copy(h->pinned, h->pinned + Hh.size(), Hh.begin());
     for (double v : Hh)
       if (!std::isfinite(v)) return set_error(h, FMPT_ERR_NONFINITE, "exponentiate: NaN");
@@ -1145,7 +1448,7 @@ int fmpt_exponentiate(fmpt_op* op, double t_re, double t_im, const double* x, do
       if (Hh[2 * (j + 1 + (size_t)ldh * j)] == 0.0) { m = j + 1; happy = true; break; }
     dtau = happy ? (tabs - tau_done) : std::min(dtau, tabs - tau_done);
     Hs.assign((size_t)m * m * 2, 0.0);
-    double err = 0.0;
+    std::vector<cplx> col;
     for (int tries = 0; tries < 200; tries++) {
       const double fr = sg_r * dtau, fi = sg_i * dtau;
       for (int c = 0; c < m; c++)
@@ -1154,20 +1457,21 @@ int fmpt_exponentiate(fmpt_op* op, double t_re, double t_im, const double* x, do
           Hs[2 * (r + (size_t)m * c)] = fr * hr - fi * hi;
           Hs[2 * (r + (size_t)m * c) + 1] = fr * hi + fi * hr;
         }
-      FMPT_CUDA(h, cudaMemcpyAsync(Hd.d(), Hs.data(), Hs.size() * sizeof(double),
-                                   cudaMemcpyHostToDevice, h->stream));
-      small_expm<<<1, dim3(32, 32), 0, h->stream>>>(m, Hd.d(), Ed.d());
-      FMPT_LAUNCHED(h);
+      host_expm_col(m, Hs.data(), col);
       if (happy) break;
-      // error estimate |h_{m+1,m} dtau [exp(dtau H)]_{m,1}| needs the last entry only
-      FMPT_CUDA(h, cudaMemcpyAsync(h->pinned, Ed.d() + 2 * (m - 1), 2 * sizeof(double),
-                                   cudaMemcpyDeviceToHost, h->stream));
-      FMPT_CUDA(h, cudaStreamSynchronize(h->stream));
+      // error estimate |h_{m+1,m} dtau [exp(dtau H)]_{m,1}|
       const double hlast = Hh[2 * (m + (size_t)ldh * (m - 1))];
-      err = std::abs(hlast * dtau) * std::hypot(h->pinned[0], h->pinned[1]);
+      const double err = std::abs(hlast * dtau) * std::abs(col[m - 1]);
       if (err <= 0.9 * tol * dtau) break;
       dtau *= 0.5;
     }
+    // pageable source: the copy has left colbuf when cudaMemcpyAsync returns
+    for (int r = 0; r < m; r++) {
+      colbuf[2 * r] = col[r].real();
+      colbuf[2 * r + 1] = col[r].imag();
+    }
+    FMPT_CUDA(h, cudaMemcpyAsync(Ed.d(), colbuf.data(), (size_t)2 * m * sizeof(double),
+                                 cudaMemcpyHostToDevice, h->stream));
     // w = sum_i E[i, 0] V_i, renormalised into V_0; acc *= ||w||
     combine_basis<<<G, KT, 0, h->stream>>>(cp, n, m, V, nr, Ed.d(), 2, 1.0, 0, zb.d());
     FMPT_LAUNCHED(h);
@@ -1186,7 +1490,7 @@ int fmpt_exponentiate(fmpt_op* op, double t_re, double t_im, const double* x, do
   scale_by<<<G, KT, 0, h->stream>>>(nr, xout, acc.d());
   FMPT_LAUNCHED(h);
   if (!prec_is_f64(op->precision)) FMPT_TRY(op_tc_check(op));
-  if (op->u1) FMPT_TRY(gp_check_status(op->h));
+  if (op->u1 || gs) FMPT_TRY(gp_check_status(op->h));
   if (info) *info = steps;
   return FMPT_OK;
 }
@@ -1211,17 +1515,20 @@ int fmpt_expm_nodes(fmpt_op* op, double t_re, double t_im, const double* x, int 
   const int G = grid_for(h, nr);
   const int M = (int)std::min<int64_t>(krylovdim, n);
   const int ldh = M + 1;
-  DevBuf Vb, zb, part, partM, coef, Hdev, Hd, Ed, acc;
+  DevBuf Vb, zb, part, partM, coef, Hdev, Ed, acc;
   FMPT_TRY(Vb.alloc(h, (size_t)(M + 1) * nr * sizeof(double)));
   FMPT_TRY(zb.alloc(h, (size_t)nr * sizeof(double)));
   FMPT_TRY(part.alloc(h, (size_t)G * sizeof(double)));
   FMPT_TRY(partM.alloc(h, (size_t)G * (M + 1) * 2 * sizeof(double)));
   FMPT_TRY(coef.alloc(h, (size_t)(M + 1) * 2 * sizeof(double)));
   FMPT_TRY(Hdev.alloc(h, (size_t)ldh * M * 2 * sizeof(double)));
-  FMPT_TRY(Hd.alloc(h, (size_t)nnodes * 32 * 32 * 2 * sizeof(double)));
-  FMPT_TRY(Ed.alloc(h, (size_t)nnodes * 32 * 32 * 2 * sizeof(double)));
+  FMPT_TRY(Ed.alloc(h, (size_t)nnodes * M * 2 * sizeof(double)));
   FMPT_TRY(acc.alloc(h, 2 * sizeof(double)));
-  FMPT_TRY(ensure_pinned(h, (size_t)ldh * M * 2 + 2 * nnodes + 8));
+  FMPT_TRY(ensure_pinned(h, (size_t)ldh * M * 2 + 8));
+  DevBuf gsbuf;
+  GsWork gsw{};
+  const GsWork* gs = nullptr;
+  FMPT_TRY(gs_setup(op, G, M, gsbuf, gsw, &gs));
   double* V = Vb.d();
   auto V_ = [&](int i) { return V + (int64_t)i * nr; };
   rdot_partial<<<G, KT, 0, h->stream>>>(nr, x, x, part.d());
@@ -1229,10 +1536,11 @@ int fmpt_expm_nodes(fmpt_op* op, double t_re, double t_im, const double* x, int 
   normalize_from_parts<<<G, KT, 0, h->stream>>>(nr, x, V_(0), part.d(), G, acc.d());
   FMPT_LAUNCHED(h);
   FMPT_TRY(arnoldi_basis(op, cp, n, nr, G, M, ldh, V, zb.d(), part.d(), partM.d(), coef.d(),
-                         Hdev));
+                         Hdev, gs));
   std::vector<double> Hh((size_t)ldh * M * 2);
   FMPT_CUDA(h, cudaMemcpyAsync(h->pinned, Hdev.p, Hdev.bytes, cudaMemcpyDeviceToHost, h->stream));
   FMPT_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (gs) FMPT_TRY(gp_check_status(h));       // a fused step that gave up left H invalid
   std::copy(h->pinned, h->pinned + Hh.size(), Hh.begin());
   for (double v : Hh)
     if (!std::isfinite(v)) return set_error(h, FMPT_ERR_NONFINITE, "expm_nodes: NaN");
@@ -1240,42 +1548,40 @@ int fmpt_expm_nodes(fmpt_op* op, double t_re, double t_im, const double* x, int 
   bool happy = M == n;
   for (int j = 0; j < M; j++)
     if (Hh[2 * (j + 1 + (size_t)ldh * j)] == 0.0) { m = j + 1; happy = true; break; }
-  std::vector<double> Hs((size_t)nnodes * 32 * 32 * 2, 0.0);
+  // every node's exp(s_q t H_m) e_1 on the host, uploaded in one copy (pageable source:
+  // the copy has left it when cudaMemcpyAsync returns)
+  std::vector<double> Hs((size_t)m * m * 2), cols((size_t)nnodes * m * 2);
+  std::vector<cplx> col;
+  double e = 0.0;
+  const double hlast = happy ? 0.0 : std::abs(Hh[2 * (m + (size_t)ldh * (m - 1))]);
   for (int q = 0; q < nnodes; q++) {
     const double fr = nodes[q] * t_re, fi = nodes[q] * t_im;
-    double* Hq = Hs.data() + (size_t)q * 32 * 32 * 2;
     for (int c = 0; c < m; c++)
       for (int r = 0; r < m; r++) {
         const double hr = Hh[2 * (r + (size_t)ldh * c)], hi = Hh[2 * (r + (size_t)ldh * c) + 1];
-        Hq[2 * (r + (size_t)m * c)] = fr * hr - fi * hi;
-        Hq[2 * (r + (size_t)m * c) + 1] = fr * hi + fi * hr;
+        Hs[2 * (r + (size_t)m * c)] = fr * hr - fi * hi;
+        Hs[2 * (r + (size_t)m * c) + 1] = fr * hi + fi * hr;
       }
+    host_expm_col(m, Hs.data(), col);
+    for (int r = 0; r < m; r++) {
+      cols[2 * (r + (size_t)m * q)] = col[r].real();
+      cols[2 * (r + (size_t)m * q) + 1] = col[r].imag();
+    }
+    if (!happy) e = std::max(e, hlast * std::abs(col[m - 1]));
   }
-  FMPT_CUDA(h, cudaMemcpyAsync(Hd.d(), Hs.data(), Hs.size() * sizeof(double),
+  FMPT_CUDA(h, cudaMemcpyAsync(Ed.d(), cols.data(), cols.size() * sizeof(double),
                                cudaMemcpyHostToDevice, h->stream));
   for (int q = 0; q < nnodes; q++) {
-    const double* Hq = Hd.d() + (size_t)q * 32 * 32 * 2;
-    double* Eq = Ed.d() + (size_t)q * 32 * 32 * 2;
-    small_expm<<<1, dim3(32, 32), 0, h->stream>>>(m, Hq, Eq);
-    FMPT_LAUNCHED(h);
     double* oq = out + (int64_t)q * nr;
-    combine_basis<<<G, KT, 0, h->stream>>>(cp, n, m, V, nr, Eq, 2, 1.0, 0, oq);
+    combine_basis<<<G, KT, 0, h->stream>>>(cp, n, m, V, nr, Ed.d() + (size_t)2 * m * q, 2, 1.0,
+                                           0, oq);
     FMPT_LAUNCHED(h);
     scale_by<<<G, KT, 0, h->stream>>>(nr, oq, acc.d());
     FMPT_LAUNCHED(h);
-    FMPT_CUDA(h, cudaMemcpyAsync(h->pinned + 2 * q, Eq + 2 * (m - 1), 2 * sizeof(double),
-                                 cudaMemcpyDeviceToHost, h->stream));
-  }
-  FMPT_CUDA(h, cudaStreamSynchronize(h->stream));
-  double e = 0.0;
-  if (!happy) {
-    const double hlast = std::abs(Hh[2 * (m + (size_t)ldh * (m - 1))]);
-    for (int q = 0; q < nnodes; q++)
-      e = std::max(e, hlast * std::hypot(h->pinned[2 * q], h->pinned[2 * q + 1]));
   }
   if (err_est) *err_est = e;
   if (!prec_is_f64(op->precision)) FMPT_TRY(op_tc_check(op));
-  if (op->u1) FMPT_TRY(gp_check_status(op->h));
+  if (op->u1 || gs) FMPT_TRY(gp_check_status(op->h));
   return FMPT_OK;
 }
 

@@ -53,13 +53,19 @@ class Handle:
         self.check(lib().fmpt_set_f64_engine(self.ptr, codes[engine]))
 
     def set_wait_test(self, timeout_s=0.0, hold=False):
-        """Failure-detection test hook: bound of the grouped kernel's grid-barrier waits
-        (0: the default 2 s); hold=True makes them wait for an arrival that never comes."""
+        """Failure-detection test hook: bound of the grid-barrier waits of the grouped
+        kernel and of the fused Krylov step (0: the default 2 s); hold=True makes them
+        wait for an arrival that never comes."""
         self.check(lib().fmpt_set_wait_test(self.ptr, int(timeout_s * 1e9), 1 if hold else 0))
 
     def set_graphs(self, on=True):
         """CUDA-graph Krylov solves for block-sparse operators (default on)."""
         self.check(lib().fmpt_set_graphs(self.ptr, 1 if on else 0))
+
+    def set_fused_krylov(self, on=True):
+        """One cooperative launch per Arnoldi orthogonalisation step of the Krylov
+        exponentials (default on); off: seven launches, bit-identical results."""
+        self.check(lib().fmpt_set_fused_krylov(self.ptr, 1 if on else 0))
 
     def graph_count(self):
         return int(lib().fmpt_graph_launch_count(self.ptr))

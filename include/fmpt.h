@@ -93,6 +93,12 @@ int fmpt_set_svd_method(fmpt_handle* h, int method);
 int fmpt_set_graphs(fmpt_handle* h, int on);
 /* Number of CUDA graph launches of this handle's solvers. */
 uint64_t fmpt_graph_launch_count(fmpt_handle* h);
+/* Krylov exponentials (fmpt_exponentiate, fmpt_expm_nodes): on (default), each
+ * Arnoldi vector's two-pass Gram-Schmidt orthogonalisation and normalisation
+ * run as ONE cooperative launch with bounded grid barriers instead of seven
+ * launches; off, the seven launches.  Both give bit-identical results.  No
+ * counterpart in the reference. */
+int fmpt_set_fused_krylov(fmpt_handle* h, int on);
 /* Tile autotuner of the grouped block-sparse kernel.  mode 0 (default): the
  * first time a block-sparse operator or environment update of a new work size
  * (kind, half-octave of FLOPs) is built, every kernel variant (32x32 and 64x64
@@ -115,8 +121,9 @@ int fmpt_set_tc_tile(fmpt_handle* h, int mode);
  * (large GEMMs; small ones stay on the CUDA cores).  No counterpart in the
  * reference. */
 int fmpt_set_f64_engine(fmpt_handle* h, int mode);
-/* Failure-detection test hook of the grouped block-sparse kernel (no counterpart in the
- * reference).  Every grid barrier of a grouped launch waits at most timeout_ns (0: the
+/* Failure-detection test hook of the cooperative SIMT launches -- the grouped
+ * block-sparse kernel and the fused Krylov orthogonalisation step (no counterpart in the
+ * reference).  Every grid barrier of those launches waits at most timeout_ns (0: the
  * default 2 s); then the launch sets the handle's status word and returns, and the next
  * fmpt_synchronize (or solver) reports FMPT_ERR_TIMEOUT while the context stays usable.
  * hold = 1 makes the barriers wait for one arrival that never comes, so that a test can

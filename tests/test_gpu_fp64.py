@@ -398,6 +398,76 @@ def test_exponentiate_graph_equals_direct(prec, cplx):
         assert np.array_equal(a, b)
 
 
+@pytest.mark.parametrize("graphs", [False, True])
+@pytest.mark.parametrize("prec,cplx", [("fp64", True), ("fp64", False), ("tf32x3", True)])
+def test_fused_krylov_step_equals_separate_launches(prec, cplx, graphs):
+    """The fused orthogonalisation step (one cooperative launch per Arnoldi vector) gives
+    bit-identical exponentials and quadrature-node vectors to the seven separate launches,
+    with and without graph capture, and the Krylov exponential stays within 1e-10 of the
+    dense matrix exponential."""
+    import scipy.linalg
+    from finitemptools_gb300 import adjoint as AD
+    W = heisenberg_xxz_mpo(1.0, 1.0, 0.2)[1].dense()
+    dt = np.complex128 if cplx else np.float64
+    h = fm.default_handle()
+    r = np.random.default_rng(31)
+    Ln = r.standard_normal((24, 5, 24))
+    Rn = r.standard_normal((20, 5, 20))
+    Ln, Rn = 0.5 * (Ln + Ln.transpose(2, 1, 0)), 0.5 * (Rn + Rn.transpose(2, 1, 0))
+    xn = r.standard_normal((24, 2, 20))
+    L, R, x = (DT.from_numpy(a, dtype=dt) for a in (Ln, Rn, xn))
+    t = -0.05j if cplx else -0.05
+    h.set_graphs(graphs)
+    outs = {}
+    try:
+        for fused in (False, True):
+            h.set_fused_krylov(fused)
+            op = fm.HeffOp("ac", L, R, W1=W, precision=prec, dtype=dt)
+            y1 = op.exponentiate(t, x, 1e-10, 20).numpy()
+            y2 = op.exponentiate(t, x, 1e-10, 20).numpy()
+            vs, err = AD.expm_nodes(op, t, x, np.array([0.25, 1.0]), 20)
+            outs[fused] = [y1, y2] + [v.numpy() for v in vs]
+    finally:
+        h.set_fused_krylov(True)
+        h.set_graphs(True)
+    for a, b in zip(outs[False], outs[True]):
+        assert np.array_equal(a, b)
+    if prec == "fp64":
+        from oracle import tdvp_adjoint as TA
+        Hd = TA._heff("ac", W, Ln, Rn, xn.shape)
+        ref = scipy.linalg.expm(t * Hd) @ xn.ravel(order="F")
+        assert rel(outs[True][0].ravel(order="F"), ref) < 1e-10
+
+
+def test_fused_krylov_barrier_timeout_is_reported_and_context_survives():
+    """Failure detection without a GPU fault on the fused Krylov step: its grid barriers
+    are made to wait for an arrival that never comes (fmpt_set_wait_test hold), give up
+    after the 0.2 s bound, set the status word and return; the exponential reports
+    FMPT_ERR_TIMEOUT, and with the hook cleared the same operator gives the same result
+    as before on the same context."""
+    from finitemptools_gb300._native import FMPTError
+    W = heisenberg_xxz_mpo(1.0, 1.0, 0.0)[1].dense()
+    h = fm.default_handle()
+    r = np.random.default_rng(32)
+    Ln = r.standard_normal((16, 5, 16))
+    Rn = r.standard_normal((16, 5, 16))
+    Ln, Rn = 0.5 * (Ln + Ln.transpose(2, 1, 0)), 0.5 * (Rn + Rn.transpose(2, 1, 0))
+    L, R = DT.from_numpy(Ln, dtype=np.complex128), DT.from_numpy(Rn, dtype=np.complex128)
+    x = DT.from_numpy(r.standard_normal((16, 2, 16)), dtype=np.complex128)
+    op = fm.HeffOp("ac", L, R, W1=W, dtype=np.complex128)
+    ref = op.exponentiate(-0.05j, x, 1e-10, 10).numpy()
+    h.set_wait_test(0.2, hold=True)
+    try:
+        with pytest.raises(FMPTError) as ei:
+            op.exponentiate(-0.05j, x, 1e-10, 10)
+            h.synchronize()
+        assert ei.value.status == -5
+    finally:
+        h.set_wait_test(0.0, hold=False)
+    h.synchronize()
+    assert np.array_equal(op.exponentiate(-0.05j, x, 1e-10, 10).numpy(), ref)
+
+
 @pytest.mark.parametrize("cplx", [False, True])
 @pytest.mark.parametrize("side", [0, 1])
 @pytest.mark.parametrize("m,n,eps", [(300, 256, 1e-10), (256, 384, 1e-9)])
