@@ -232,9 +232,9 @@ def config3_j1j2(h, fm, run, full=False, L=100, window=20):
     Always: the mixed ramp with two D=1024 sweeps (the second one timed: sweep_s_mixed) and,
     from that converged state, the same window of `window` consecutive centre bonds run in
     both forms (state restored in between): window_s_mixed / window_s_fp64.
-    full=True adds the plain form's own ramp from the same start (64, 256, then one D=1024
-    sweep, timed: sweep_s_fp64) and the relative difference of the two FP64-evaluated
-    ground-state energies."""
+    full=True adds the plain form's own ramp from the same start (64, 256, then two D=1024
+    sweeps, the second timed: sweep_s_fp64) and the relative difference of the two
+    FP64-evaluated ground-state energies."""
     import time as _t
     from finitemptools_gb300 import algorithms as A
     hj = fm.j1j2_heisenberg_mpo(1.0, 0.3)
@@ -273,7 +273,8 @@ def config3_j1j2(h, fm, run, full=False, L=100, window=20):
                 "window_speedup_fp64_over_mixed": times["fp64"] / times["mixed"]})
     del env, keep_mps, keep_env
     if full:
-        env64, t64 = run(L, hj, [(64, 1), (256, 1), (1024, 1)], "fp64_tc", "gesvd", False, 1e-9,
+        # the same ramp as the mixed form (one D=1024 sweep only reaches about D=500)
+        env64, t64 = run(L, hj, [(64, 1), (256, 1), (1024, 2)], "fp64_tc", "gesvd", False, 1e-9,
                          16, 5)
         E_64 = float(fm.expectation(env64.mps, mpo))
         res.update({"ramp_sweeps_s_fp64": t64, "sweep_s_fp64": t64[-1],
@@ -403,17 +404,26 @@ def u1_section(h, fm, budget_s=150.0):
         e_ed = json.load(f)["xxz_L20_J1_Jzz1_hz0"]
     hx = fm.heisenberg_xxz_mpo(1.0, 1.0, 0.0)
 
+    profile = []
+
     def sweeps(m, D, n, eps, kmax):
         alg = fm.DMRG2(eig_maxiter=kmax, eig_tol=1e-12, trunc=fm.MPSTruncation(D, eps), svd="dm",
                        verbosity=0)
         ts, Es = [], []
         for _ in range(n):
+            dims0 = m.mps.bond_dimensions()
             h.synchronize()
             t0 = _t.perf_counter()
             E, _ = fm.sweep_(m, alg)
             h.synchronize()
             ts.append(_t.perf_counter() - t0)
             Es.append(E[-1])
+            dims1 = m.mps.bond_dimensions()
+            # the work of a bond grows as D^3: sum of D^3 over the bonds before and after
+            profile.append({"D": D, "s": ts[-1], "Dmax_before": max(dims0),
+                            "Dmax_after": max(dims1),
+                            "sum_D3_before": float(sum(float(d) ** 3 for d in dims0)),
+                            "sum_D3_after": float(sum(float(d) ** 3 for d in dims1))})
         return ts, Es
 
     psi = u1_randommps(20, 10, 8, rng=20, handle=h)
@@ -496,6 +506,7 @@ def u1_section(h, fm, budget_s=150.0):
         "heff_rel_diff_vs_dense": float(np.linalg.norm(yu - yd) / np.linalg.norm(yd)),
         "lanczos10_ms": lz, "heff_cpu_oracle_blocks_ms": cpu_ms,
         "tuning_entries_timed": h.tuning_info(),
+        "sweep_profile": profile[-4:],
         "note": "sweeps: DMRG2 svd=dm (batched density-matrix sector split), eig_maxiter 10, "
                 "cutoff 1e-14"}
     return out

@@ -45,6 +45,7 @@ SIGNATURES = {
     "fmpt_synchronize": (c_int, [c_void_p]),
     "fmpt_set_graphs": (c_int, [c_void_p, c_int]),
     "fmpt_set_fused_krylov": (c_int, [c_void_p, c_int]),
+    "fmpt_set_cluster_qr": (c_int, [c_void_p, c_int]),
     "fmpt_graph_launch_count": (c_uint64, [c_void_p]),
     "fmpt_set_tuning": (c_int, [c_void_p, c_int]),
     "fmpt_tuning_info": (c_int, [c_void_p, P(c_int), P(c_int64)]),

@@ -416,6 +416,12 @@ int fmpt_set_fused_krylov(fmpt_handle* h, int on) {
   return FMPT_OK;
 }
 
+int fmpt_set_cluster_qr(fmpt_handle* h, int on) {
+  if (!h) return FMPT_ERR_ARG;
+  h->cluster_qr = on != 0;
+  return FMPT_OK;
+}
+
 int fmpt_synchronize(fmpt_handle* h) {
   if (!h) return FMPT_ERR_ARG;
   FMPT_CUDA(h, cudaStreamSynchronize(h->stream));

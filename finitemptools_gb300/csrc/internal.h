@@ -40,6 +40,8 @@ struct fmpt_handle {
   // Krylov exponentials: one cooperative launch per Arnoldi orthogonalisation step
   // (fmpt_set_fused_krylov; the seven separate launches give bit-identical results)
   int fused_gs = 1;
+  // thin QR of small tall panels on one thread-block cluster (fmpt_set_cluster_qr)
+  int cluster_qr = 1;
   int svd_method = 0;          // 0 gesvd (bidiagonalisation), 1 gesvdp (polar decomposition)
   int tc_tile = 0;             // tcgen05 GEMM tile: 0 CTA pair where it applies, 1 one CTA
   // split-K workspace of the FP64 GEMM, grown outside stream capture only (stream-ordered
@@ -114,6 +116,10 @@ struct DevBuf {
 };
 
 int ensure_pinned(fmpt_handle* h, size_t n_doubles);
+// Q (m x n) and R (n x n) of a small tall panel (m >= n) on one thread-block cluster;
+// FMPT_ERR_UNSUPPORTED (nothing launched) outside its range (qr_cluster.cu)
+int qr_small_cluster(fmpt_handle* h, int cplx, int m, int n, const double* M, double* Q,
+                     double* R);
 // a device buffer of at least `bytes` held in *buf / *cap (stream-ordered on h->stream);
 // growing it while h->stream is being captured returns FMPT_ERR_UNSUPPORTED
 int grow_buffer(fmpt_handle* h, void** buf, size_t* cap, size_t bytes);

@@ -140,7 +140,7 @@ template <int CH = MD_CH>
 __device__ __forceinline__ void multidot_body(int cplx, int64_t n, int j,
                                               const double* __restrict__ V, int64_t vstride,
                                               const double* __restrict__ z,
-                                              double* __restrict__ part) {
+                                              double* __restrict__ part, int epb = KT) {
   constexpr int MD_CH = CH;       // vectors per pass over z (the sums do not depend on it)
   __shared__ double red[KT / 32][2 * MD_CH];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -151,7 +151,8 @@ __device__ __forceinline__ void multidot_body(int cplx, int64_t n, int j,
       sr[c] = 0.0;
       si[c] = 0.0;
     }
-    for (int64_t e = (int64_t)blockIdx.x * KT + threadIdx.x; e < n; e += (int64_t)gridDim.x * KT) {
+    for (int64_t e = (int64_t)blockIdx.x * epb + threadIdx.x; threadIdx.x < epb && e < n;
+         e += (int64_t)gridDim.x * epb) {
       const double zr = z[e], zi = cplx ? z[n + e] : 0.0;
 #pragma unroll
       for (int c = 0; c < MD_CH; c++) {
@@ -192,9 +193,10 @@ __device__ __forceinline__ void multidot_body(int cplx, int64_t n, int j,
 
 __global__ void multidot_partial(int cplx, int64_t n, int j, const double* __restrict__ V,
                                  int64_t vstride, const double* __restrict__ z,
-                                 double* __restrict__ part, const int* gate = nullptr) {
+                                 double* __restrict__ part, const int* gate = nullptr,
+                                 int epb = KT) {
   if (gate && *gate) return;
-  multidot_body<>(cplx, n, j, V, vstride, z, part);
+  multidot_body<>(cplx, n, j, V, vstride, z, part, epb);
 }
 
 // coef[i] (re, im) = sum over the G partials, one warp per value (lanes stride over the
@@ -245,9 +247,11 @@ __global__ void multidot_finalize(int j, int G, const double* __restrict__ part,
 __device__ __forceinline__ void multi_axpy_body(int cplx, int64_t n, int j,
                                                 const double* __restrict__ V, int64_t vstride,
                                                 const double* __restrict__ coef,
-                                                double* __restrict__ z, double* __restrict__ part) {
+                                                double* __restrict__ z, double* __restrict__ part,
+                                                int epb = KT) {
   double s = 0.0;
-  for (int64_t e = (int64_t)blockIdx.x * KT + threadIdx.x; e < n; e += (int64_t)gridDim.x * KT) {
+  for (int64_t e = (int64_t)blockIdx.x * epb + threadIdx.x; threadIdx.x < epb && e < n;
+       e += (int64_t)gridDim.x * epb) {
     double zr = z[e], zi = cplx ? z[n + e] : 0.0;
     // MD_CH vectors' elements are loaded together (their L2 latencies overlap), then
     // subtracted in vector order
@@ -288,9 +292,9 @@ __device__ __forceinline__ void multi_axpy_body(int cplx, int64_t n, int j,
 __global__ void multi_axpy_sub(int cplx, int64_t n, int j, const double* __restrict__ V,
                                int64_t vstride, const double* __restrict__ coef,
                                double* __restrict__ z, double* __restrict__ part,
-                               const int* gate = nullptr) {
+                               const int* gate = nullptr, int epb = KT) {
   if (gate && *gate) return;
-  multi_axpy_body(cplx, n, j, V, vstride, coef, z, part);
+  multi_axpy_body(cplx, n, j, V, vstride, coef, z, part, epb);
 }
 
 // out = sum_i c_i V_i (c complex when cplx, real otherwise); scale multiplies
@@ -329,7 +333,8 @@ __device__ __forceinline__ void arnoldi_normalize_body(int64_t n_real,
                                                        const double* __restrict__ z,
                                                        const double* __restrict__ part, int G,
                                                        const double* hc, double* __restrict__ Hcol,
-                                                       int j, double* __restrict__ vnext) {
+                                                       int j, double* __restrict__ vnext,
+                                                       int epb = KT) {
   const double s = sqrt(sum_parts(part, G));
   double ref = s * s;
   for (int i = 0; i <= j; i++) ref += hc[2 * i] * hc[2 * i] + hc[2 * i + 1] * hc[2 * i + 1];
@@ -339,15 +344,16 @@ __device__ __forceinline__ void arnoldi_normalize_body(int64_t n_real,
     Hcol[2 * (j + 1) + 1] = 0.0;
   }
   const double inv = breakdown ? 0.0 : 1.0 / s;
-  for (int64_t e = (int64_t)blockIdx.x * KT + threadIdx.x; e < n_real;
-       e += (int64_t)gridDim.x * KT)
+  for (int64_t e = (int64_t)blockIdx.x * epb + threadIdx.x; threadIdx.x < epb && e < n_real;
+       e += (int64_t)gridDim.x * epb)
     vnext[e] = z[e] * inv;
 }
 
 __global__ void arnoldi_normalize(int64_t n_real, const double* __restrict__ z,
                                   const double* __restrict__ part, int G,
-                                  double* __restrict__ Hcol, int j, double* __restrict__ vnext) {
-  arnoldi_normalize_body(n_real, z, part, G, Hcol, Hcol, j, vnext);
+                                  double* __restrict__ Hcol, int j, double* __restrict__ vnext,
+                                  int epb = KT) {
+  arnoldi_normalize_body(n_real, z, part, G, Hcol, Hcol, j, vnext, epb);
 }
 
 // ---- the whole orthogonalisation step of one Arnoldi vector as ONE cooperative launch:
@@ -412,17 +418,18 @@ __global__ void __launch_bounds__(KT) arnoldi_gs_fused(int cplx, int64_t n, int 
                                                        double* __restrict__ partB,
                                                        double* __restrict__ partN,
                                                        double* __restrict__ Hcol,
-                                                       double* __restrict__ vnext, CoopBar bar) {
+                                                       double* __restrict__ vnext, CoopBar bar,
+                                                       int epb) {
   __shared__ double c1[64], c2[64], hc[64];
   const int G = gridDim.x, jj = j + 1;
   // pass 1
-  multidot_body<16>(cplx, n, jj, V, vstride, z, partA);
+  multidot_body<16>(cplx, n, jj, V, vstride, z, partA, epb);
   if (!coop_barrier(bar, G)) return;
   coef_group<QMAX>(jj, G, partA, 0, c1, nullptr);     // 2 jj <= 62 values: one group
   __syncthreads();
-  multi_axpy_body(cplx, n, jj, V, vstride, c1, z, partN);
+  multi_axpy_body(cplx, n, jj, V, vstride, c1, z, partN, epb);
   // pass 2 (each thread reads back only the elements it has just written)
-  multidot_body<16>(cplx, n, jj, V, vstride, z, partB);
+  multidot_body<16>(cplx, n, jj, V, vstride, z, partB, epb);
   if (!coop_barrier(bar, 2 * G)) return;
   coef_group<QMAX>(jj, G, partB, 0, c2, nullptr);
   __syncthreads();
@@ -431,14 +438,14 @@ __global__ void __launch_bounds__(KT) arnoldi_gs_fused(int cplx, int64_t n, int 
     if (blockIdx.x == 0) Hcol[t] = hc[t];
   }
   __syncthreads();
-  multi_axpy_body(cplx, n, jj, V, vstride, c2, z, partN);
+  multi_axpy_body(cplx, n, jj, V, vstride, c2, z, partN, epb);
   if (!coop_barrier(bar, 3 * G)) return;
-  arnoldi_normalize_body(n * (cplx ? 2 : 1), z, partN, G, hc, Hcol, j, vnext);
+  arnoldi_normalize_body(n * (cplx ? 2 : 1), z, partN, G, hc, Hcol, j, vnext, epb);
 }
 
 // the kernel instance for a grid of G blocks (partials per lane: G / 32 rounded up)
 using GsKernel = void (*)(int, int64_t, int, const double*, int64_t, double*, double*, double*,
-                          double*, double*, double*, CoopBar);
+                          double*, double*, double*, CoopBar, int);
 GsKernel gs_kernel_for(int G) {
   if (G <= 64) return arnoldi_gs_fused<2>;
   if (G <= 160) return arnoldi_gs_fused<5>;
@@ -1076,6 +1083,16 @@ int op_project(fmpt_op* op, double* y, const int* gate) {
   return FMPT_OK;
 }
 
+// Grid of the Arnoldi orthogonalisation kernels: EPB_A vector elements (complex elements
+// for complex data) per block and pass, so that a D = 64 vector (8192 elements) spreads its
+// FP64 work over 128 SMs instead of 32; at most two blocks per SM.
+constexpr int EPB_A = 64;
+int arnoldi_grid(fmpt_handle* h, int64_t n) {
+  const int64_t g = (n + EPB_A - 1) / EPB_A;
+  const int64_t cap = 2LL * std::max(1, h->sm_count);
+  return (int)std::max<int64_t>(1, std::min(g, cap));
+}
+
 // Workspace of the fused orthogonalisation step (arnoldi_gs_fused): the pass-2 partials
 // (pass 1 uses the caller's partM), the barrier words and the status word.
 struct GsWork {
@@ -1156,19 +1173,19 @@ int arnoldi_basis(fmpt_op* op, int cp, int64_t n, int64_t nr, int G, int M, int 
         cfg.attrs = attr;
         cfg.numAttrs = 1;
         FMPT_CUDA(h, cudaLaunchKernelEx(&cfg, gs_kernel_for(G), cp, n, j, (const double*)V, nr,
-                                        z, partM, gs->partB, part, Hcol, vj + nr, bar));
+                                        z, partM, gs->partB, part, Hcol, vj + nr, bar, EPB_A));
         FMPT_LAUNCHED(h);
         continue;
       }
       for (int pass = 0; pass < 2; pass++) {
-        multidot_partial<<<G, KT, 0, st>>>(cp, n, j + 1, V, nr, z, partM);
+        multidot_partial<<<G, KT, 0, st>>>(cp, n, j + 1, V, nr, z, partM, nullptr, EPB_A);
         FMPT_LAUNCHED(h);
         multidot_finalize<<<1, KT, 0, st>>>(j + 1, G, partM, coef, Hcol);
         FMPT_LAUNCHED(h);
-        multi_axpy_sub<<<G, KT, 0, st>>>(cp, n, j + 1, V, nr, coef, z, part);
+        multi_axpy_sub<<<G, KT, 0, st>>>(cp, n, j + 1, V, nr, coef, z, part, nullptr, EPB_A);
         FMPT_LAUNCHED(h);
       }
-      arnoldi_normalize<<<G, KT, 0, st>>>(nr, z, part, G, Hcol, j, vj + nr);
+      arnoldi_normalize<<<G, KT, 0, st>>>(nr, z, part, G, Hcol, j, vj + nr, EPB_A);
       FMPT_LAUNCHED(h);
     }
     return FMPT_OK;
@@ -1391,14 +1408,15 @@ int fmpt_exponentiate(fmpt_op* op, double t_re, double t_im, const double* x, do
   const int64_t n = op->n;                     // elements (complex for C128)
   const int64_t nr = n * (cp ? 2 : 1);         // real view
   const int G = grid_for(h, nr);
+  const int Ga = arnoldi_grid(h, n);           // grid of the orthogonalisation kernels
   // the Krylov space cannot be larger than the vector space
   const int M = (int)std::min<int64_t>(krylovdim, n);
   const int ldh = M + 1;
   DevBuf Vb, zb, part, partM, coef, Hdev, Ed, nrm, acc;
   FMPT_TRY(Vb.alloc(h, (size_t)(M + 1) * nr * sizeof(double)));
   FMPT_TRY(zb.alloc(h, (size_t)nr * sizeof(double)));
-  FMPT_TRY(part.alloc(h, (size_t)G * sizeof(double)));
-  FMPT_TRY(partM.alloc(h, (size_t)G * (M + 1) * 2 * sizeof(double)));
+  FMPT_TRY(part.alloc(h, (size_t)std::max(G, Ga) * sizeof(double)));
+  FMPT_TRY(partM.alloc(h, (size_t)Ga * (M + 1) * 2 * sizeof(double)));
   FMPT_TRY(coef.alloc(h, (size_t)(M + 1) * 2 * sizeof(double)));
   FMPT_TRY(Hdev.alloc(h, (size_t)ldh * M * 2 * sizeof(double)));
   FMPT_TRY(Ed.alloc(h, (size_t)M * 2 * sizeof(double)));
@@ -1409,7 +1427,7 @@ int fmpt_exponentiate(fmpt_op* op, double t_re, double t_im, const double* x, do
   DevBuf gsbuf;
   GsWork gsw{};
   const GsWork* gs = nullptr;
-  FMPT_TRY(gs_setup(op, G, M, gsbuf, gsw, &gs));
+  FMPT_TRY(gs_setup(op, Ga, M, gsbuf, gsw, &gs));
   double* V = Vb.d();
   auto V_ = [&](int i) { return V + (int64_t)i * nr; };
   const double tabs = std::hypot(t_re, t_im);
@@ -1432,7 +1450,7 @@ int fmpt_exponentiate(fmpt_op* op, double t_re, double t_im, const double* x, do
   while (tau_done < tabs * (1.0 - 1e-15)) {
     if (++steps > 1000) return set_error(h, FMPT_ERR_NOCONV, "exponentiate: too many steps");
     // ---- Arnoldi (two-pass classical Gram-Schmidt) entirely on the device
-    FMPT_TRY(arnoldi_basis(op, cp, n, nr, G, M, ldh, V, zb.d(), part.d(), partM.d(), coef.d(),
+    FMPT_TRY(arnoldi_basis(op, cp, n, nr, Ga, M, ldh, V, zb.d(), part.d(), partM.d(), coef.d(),
                            Hdev, gs));
     FMPT_CUDA(h, cudaMemcpyAsync(h->pinned, Hdev.p, Hdev.bytes, cudaMemcpyDeviceToHost,
                                  h->stream));
@@ -1513,13 +1531,14 @@ int fmpt_expm_nodes(fmpt_op* op, double t_re, double t_im, const double* x, int 
   const int64_t n = op->n;
   const int64_t nr = n * (cp ? 2 : 1);
   const int G = grid_for(h, nr);
+  const int Ga = arnoldi_grid(h, n);           // grid of the orthogonalisation kernels
   const int M = (int)std::min<int64_t>(krylovdim, n);
   const int ldh = M + 1;
   DevBuf Vb, zb, part, partM, coef, Hdev, Ed, acc;
   FMPT_TRY(Vb.alloc(h, (size_t)(M + 1) * nr * sizeof(double)));
   FMPT_TRY(zb.alloc(h, (size_t)nr * sizeof(double)));
-  FMPT_TRY(part.alloc(h, (size_t)G * sizeof(double)));
-  FMPT_TRY(partM.alloc(h, (size_t)G * (M + 1) * 2 * sizeof(double)));
+  FMPT_TRY(part.alloc(h, (size_t)std::max(G, Ga) * sizeof(double)));
+  FMPT_TRY(partM.alloc(h, (size_t)Ga * (M + 1) * 2 * sizeof(double)));
   FMPT_TRY(coef.alloc(h, (size_t)(M + 1) * 2 * sizeof(double)));
   FMPT_TRY(Hdev.alloc(h, (size_t)ldh * M * 2 * sizeof(double)));
   FMPT_TRY(Ed.alloc(h, (size_t)nnodes * M * 2 * sizeof(double)));
@@ -1528,14 +1547,14 @@ int fmpt_expm_nodes(fmpt_op* op, double t_re, double t_im, const double* x, int 
   DevBuf gsbuf;
   GsWork gsw{};
   const GsWork* gs = nullptr;
-  FMPT_TRY(gs_setup(op, G, M, gsbuf, gsw, &gs));
+  FMPT_TRY(gs_setup(op, Ga, M, gsbuf, gsw, &gs));
   double* V = Vb.d();
   auto V_ = [&](int i) { return V + (int64_t)i * nr; };
   rdot_partial<<<G, KT, 0, h->stream>>>(nr, x, x, part.d());
   FMPT_LAUNCHED(h);
   normalize_from_parts<<<G, KT, 0, h->stream>>>(nr, x, V_(0), part.d(), G, acc.d());
   FMPT_LAUNCHED(h);
-  FMPT_TRY(arnoldi_basis(op, cp, n, nr, G, M, ldh, V, zb.d(), part.d(), partM.d(), coef.d(),
+  FMPT_TRY(arnoldi_basis(op, cp, n, nr, Ga, M, ldh, V, zb.d(), part.d(), partM.d(), coef.d(),
                          Hdev, gs));
   std::vector<double> Hh((size_t)ldh * M * 2);
   FMPT_CUDA(h, cudaMemcpyAsync(h->pinned, Hdev.p, Hdev.bytes, cudaMemcpyDeviceToHost, h->stream));

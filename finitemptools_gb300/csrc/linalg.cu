@@ -512,6 +512,11 @@ int fmpt_qr(fmpt_handle* h, int dtype, const double* M, int m, int n, double* Q,
   const int cp = dtype == FMPT_C128;
   const int r = std::min(m, n);
   const size_t es = sizeof(double) * (cp ? 2 : 1);
+  // small tall panels: one thread-block cluster, LAPACK's conventions (qr_cluster.cu)
+  {
+    const int st = qr_small_cluster(h, cp, m, n, M, Q, R);
+    if (st != FMPT_ERR_UNSUPPORTED) return st;
+  }
   DevBuf A, tau, work, dinfo;
   FMPT_TRY(A.alloc(h, (size_t)m * std::max(n, r) * es));
   FMPT_TRY(tau.alloc(h, (size_t)r * es));

@@ -67,6 +67,11 @@ class Handle:
         exponentials (default on); off: seven launches, bit-identical results."""
         self.check(lib().fmpt_set_fused_krylov(self.ptr, 1 if on else 0))
 
+    def set_cluster_qr(self, on=True):
+        """Thin QR of small tall panels on one thread-block cluster (default on); off:
+        cuSOLVER geqrf + ungqr.  Same LAPACK conventions either way."""
+        self.check(lib().fmpt_set_cluster_qr(self.ptr, 1 if on else 0))
+
     def graph_count(self):
         return int(lib().fmpt_graph_launch_count(self.ptr))
 

@@ -99,6 +99,13 @@ uint64_t fmpt_graph_launch_count(fmpt_handle* h);
  * launches; off, the seven launches.  Both give bit-identical results.  No
  * counterpart in the reference. */
 int fmpt_set_fused_krylov(fmpt_handle* h, int on);
+/* Thin QR (fmpt_qr, fmpt_lq, leftorth!/rightorth) of small tall panels: on
+ * (default), a panel with m >= n and m * ceil(n / 16) <= 4096 (e.g. 128 x 64 at
+ * D = 64) runs as ONE launch on a thread-block cluster of 8 or 16 CTAs, with
+ * LAPACK's Householder conventions (the same Q and R as geqrf/ungqr to
+ * rounding); off, or outside that range, cuSOLVER geqrf + ungqr.  No
+ * counterpart in the reference. */
+int fmpt_set_cluster_qr(fmpt_handle* h, int on);
 /* Tile autotuner of the grouped block-sparse kernel.  mode 0 (default): the
  * first time a block-sparse operator or environment update of a new work size
  * (kind, half-octave of FLOPs) is built, every kernel variant (32x32 and 64x64

@@ -133,7 +133,8 @@ def _workload(D, w, seed):
     return x, L, R
 
 
-@pytest.mark.parametrize("D,model", [(256, "xxz"), (512, "xxz"), (256, "j1j2"), (512, "j1j2")])
+@pytest.mark.parametrize("D,model", [(256, "xxz"), (512, "xxz"), (256, "j1j2"), (512, "j1j2"),
+                                     (1024, "xxz")])
 @pytest.mark.parametrize("prec", ["fp64", "fp64_tc"])
 def test_ac2_prime_oracle_parity_config_sizes(D, model, prec):
     """Two-site H_eff*x at the microbenchmark sizes, Heisenberg (w=5) and J1-J2 (w=8)

@@ -211,6 +211,40 @@ def test_qr_conventions_match_lapack(m, n, cplx, zero_col):
     assert rel(Lm.numpy() @ Q2.numpy(), M) < 1e-13
 
 
+@pytest.mark.parametrize("m,n,cplx", [(128, 64, True), (128, 64, False), (96, 96, True),
+                                       (512, 8, True), (33, 17, False), (200, 150, True),
+                                       (3, 1, True)])
+def test_cluster_qr_equals_cusolver(m, n, cplx):
+    """The thread-block-cluster QR of small tall panels against cuSOLVER geqrf/ungqr on the
+    same input, entry by entry (the same LAPACK reflector conventions; a zero column takes
+    tau = 0 in both).  A rank-deficient panel (a repeated column) has no unique Q past its
+    rank -- rounding noise picks those columns -- so there only Q R = M, the orthonormality
+    of Q and the triangular R with real diagonal are checked."""
+    rng = np.random.default_rng(m + 3 * n)
+    M = rnd(rng, (m, n), cplx)
+    if n >= 4:
+        M[:, n - 1] = 0.0
+    h = fm.default_handle()
+    out = {}
+    try:
+        for on in (False, True):
+            h.set_cluster_qr(on)
+            Q, R = fm.leftorth(DT.from_numpy(M), m, n)
+            Lm, Q2 = fm.rightorth(DT.from_numpy(M.conj().T.copy()), n, m)
+            out[on] = (Q.numpy(), R.numpy(), Lm.numpy(), Q2.numpy())
+    finally:
+        h.set_cluster_qr(True)
+    for a, b in zip(out[False], out[True]):
+        assert np.abs(a - b).max() < 1e-12 * max(1, m) * max(1.0, np.abs(a).max())
+    if n >= 4:
+        M[:, 2] = M[:, 1]                     # rank deficient
+    Q, R = fm.leftorth(DT.from_numpy(M), m, n)
+    Qn, Rn = Q.numpy(), R.numpy()
+    assert rel(Qn @ Rn, M) < 1e-13
+    assert np.allclose(Qn.conj().T @ Qn, np.eye(n), atol=1e-13)
+    assert np.allclose(np.tril(Rn, -1), 0) and np.allclose(np.imag(np.diag(Rn)), 0)
+
+
 @pytest.mark.parametrize("cplx", [False, True])
 def test_exponentiate_matches_exact(cplx):
     import scipy.linalg
