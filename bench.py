@@ -285,6 +285,30 @@ def config3_j1j2(h, fm, run, full=False, L=100, window=20):
     return res
 
 
+def config3_equal_D(h, fm, run, eps=1e-12, L=100):
+    """The config-3 comparison at equal bond dimension.  At cutoff 1e-9 the reference's
+    gesvd truncation keeps about 500 states of the FP64 J1-J2 ground state, while the
+    3xTF32 Ritz vectors carry a noise floor near 1e-7 of their largest singular value that
+    the same cutoff keeps, up to D=1024.  Both forms are therefore run here with cutoff
+    `eps`, which neither reaches, so that both ramps (64 -> 256 -> 1024, two sweeps at
+    1024, from the same seeded D=16 state) end at D=1024; the second D=1024 sweep of each
+    is timed, and the FP64-evaluated energies are compared."""
+    hj = fm.j1j2_heisenberg_mpo(1.0, 0.3)
+    mpo = fm.FiniteMPO(hj, L)
+    envm, tm = run(L, hj, [(64, 1), (256, 1), (1024, 2)], "tf32x3", "dm", True, eps, 16, 5)
+    Em = float(fm.expectation(envm.mps, mpo))
+    Dm = fm.bond_dimension(envm.mps)
+    del envm
+    env64, t64 = run(L, hj, [(64, 1), (256, 1), (1024, 2)], "fp64_tc", "gesvd", False, eps, 16, 5)
+    E64 = float(fm.expectation(env64.mps, mpo))
+    D64 = fm.bond_dimension(env64.mps)
+    del env64
+    return {"cutoff": eps, "J2": 0.3, "ramp_sweeps_s_mixed": tm, "ramp_sweeps_s_fp64": t64,
+            "sweep_s_mixed": tm[-1], "sweep_s_fp64": t64[-1], "Dmax_mixed": Dm, "Dmax_fp64": D64,
+            "sweep_speedup_fp64_over_mixed": t64[-1] / tm[-1], "E_mixed_fp64_eval": Em,
+            "E_fp64": E64, "dE_rel_mixed_vs_fp64": abs(Em - E64) / abs(E64)}
+
+
 def dmrg_section(h, fm, budget_s=150.0, full3=False, only3=False):
     """DMRG sweep seconds, plain FP64 vs the mixed form (3xTF32 contractions and
     environment updates, FP64 Lanczos reorthogonalisation, FP64 density-matrix
@@ -306,7 +330,7 @@ def dmrg_section(h, fm, budget_s=150.0, full3=False, only3=False):
     with open(os.path.join(ROOT, "tests", "golden", "exact_energies.json")) as f:
         e_ed = json.load(f)["xxz_L20_J1_Jzz1_hz0"]
 
-    def run(L, mpo, stages, prec, svd, reorth, eps, D0, seed):
+    def run(L, mpo, stages, prec, svd, reorth, eps, D0, seed, driver="python"):
         rng = np.random.default_rng(seed)
         psi = fm.randommps(L, 2, D0, rng, handle=h)
         fm.canonicalize_(psi, normalize=True)
@@ -314,7 +338,7 @@ def dmrg_section(h, fm, budget_s=150.0, full3=False, only3=False):
         times = []
         for D, n in stages:
             alg = fm.DMRG2(eig_maxiter=30, eig_tol=1e-12, trunc=fm.MPSTruncation(D, eps),
-                           precision=prec, reorth=reorth, svd=svd)
+                           precision=prec, reorth=reorth, svd=svd, driver=driver)
             for _ in range(n):
                 h.synchronize()
                 t0 = _t.perf_counter()
@@ -324,15 +348,24 @@ def dmrg_section(h, fm, budget_s=150.0, full3=False, only3=False):
         return env, times
 
     if only3:
-        return config3_j1j2(h, fm, run, full=True)
+        return {"as_configured": config3_j1j2(h, fm, run, full=True),
+                "equal_D": config3_equal_D(h, fm, run)}
     hx = fm.heisenberg_xxz_mpo(1.0, 1.0, 0.0)
     env64, t64 = run(20, hx, [(64, 4)], "fp64", "gesvd", False, 1e-10, 8, 20)
     envmx, tmx = run(20, hx, [(64, 4)], "tf32x3", "dm", True, 1e-10, 8, 20)
+    # the same FP64 sweeps through the whole-sweep entry point (fmpt_dmrg2_sweep)
+    envdv, tdv = run(20, hx, [(64, 4)], "fp64", "gesvd", False, 1e-10, 8, 20, driver="device")
     E64 = float(fm.expectation(env64.mps, fm.FiniteMPO(hx, 20)))
     Emx = float(fm.expectation(envmx.mps, fm.FiniteMPO(hx, 20)))
+    Edv = float(fm.expectation(envdv.mps, fm.FiniteMPO(hx, 20)))
     out["xxz_L20_D64"] = {"sweep_s_fp64": t64, "sweep_s_mixed": tmx, "E_fp64": E64,
                           "E_mixed_fp64_eval": Emx, "dE_rel_mixed_vs_fp64": abs(Emx - E64) / abs(E64),
-                          "E_ed": e_ed, "dE_rel_fp64_vs_ed": abs(E64 - e_ed) / abs(e_ed)}
+                          "E_ed": e_ed, "dE_rel_fp64_vs_ed": abs(E64 - e_ed) / abs(e_ed),
+                          "sweep_s_fp64_device_driver": tdv,
+                          "ms_per_bond_fp64": [1e3 * t / 37 for t in t64],
+                          "ms_per_bond_fp64_device_driver": [1e3 * t / 37 for t in tdv],
+                          "E_fp64_device_driver_equal": Edv == E64}
+    del envdv
     # the same 4 FP64 sweeps (same seed, start and truncation) by the oracle's DMRG2 on the
     # host cores: the CPU run this workload is checked against
     out["xxz_L20_D64"]["cpu_reference"] = cpu_dmrg_sweeps(hx, e_ed, E64)
@@ -686,7 +719,8 @@ def tdvp_section(h, fm, nsteps=5):
             start = [A.numpy() for A in envt.mps]
             h.synchronize()
             t0 = _t.perf_counter()
-            fm.sweep_(envt, alg)
+        fm.sweep_(envt, alg)                             # second step (fp64: timed alone)
+        if prec == "fp64":
             h.synchronize()
             t_one = _t.perf_counter() - t0
             z_one = float(np.real(fm.expectation_local(envt.mps, 20, Z)))

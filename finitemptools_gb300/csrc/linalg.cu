@@ -353,6 +353,13 @@ int fmpt_dm_split(fmpt_handle* h, int dtype, const double* M, int m, int n, int 
   if (side != 0 && side != 1) return set_error(h, FMPT_ERR_ARG, "dm_split: side must be 0 or 1");
   const int cp = dtype == FMPT_C128;
   const bool left = side == 0;
+  // The split's GEMMs (Gram matrix, refinement projections, the factors) go to the
+  // FP64-accurate tensor-core engine wherever its cost model is faster than the CUDA
+  // cores: FP64-class results at a fraction of the FP64 pipe's time
+  auto split_gemm = [](fmpt_handle* hh, GemmArgs g) {
+    g.engine = 1;
+    return gemm_f64(hh, g);
+  };
   // X = op(M): M (left, r = m rows of length c = n) or M^H (right, r = n, c = m)
   const int r = left ? m : n, c = left ? n : m;
   const int xop = left ? FMPT_N : FMPT_C;
@@ -362,7 +369,7 @@ int fmpt_dm_split(fmpt_handle* h, int dtype, const double* M, int m, int n, int 
   FMPT_TRY(rho.alloc(h, (size_t)pr * sizeof(double) * (cp ? 2 : 1)));
   FMPT_TRY(U.alloc(h, (size_t)pr * sizeof(double) * (cp ? 2 : 1)));
   FMPT_TRY(W.alloc(h, (size_t)r * sizeof(double)));
-  FMPT_TRY(gemm_f64(h, gemm_plain(cp, xop, left ? FMPT_C : FMPT_N, r, r, c, M, m, planeM, M, m,
+  FMPT_TRY(split_gemm(h, gemm_plain(cp, xop, left ? FMPT_C : FMPT_N, r, r, c, M, m, planeM, M, m,
                                   planeM, rho.d(), r, pr)));
   FMPT_TRY(eigh_split(h, cp, r, rho.d(), W.d(), U.d()));
   std::vector<double> lam(r);
@@ -401,7 +408,7 @@ int fmpt_dm_split(fmpt_handle* h, int dtype, const double* M, int m, int n, int 
     FMPT_TRY(Qr.alloc(h, (size_t)pq * sizeof(double) * (cp ? 2 : 1)));
     FMPT_TRY(Bt.alloc(h, (size_t)pb * sizeof(double) * (cp ? 2 : 1)));
     const double* Ures = U.d() + (int64_t)tn * r;
-    FMPT_TRY(gemm_f64(h, gemm_plain(cp, FMPT_C, xop, nres, c, r, Ures, r, pr, M, m, planeM,
+    FMPT_TRY(split_gemm(h, gemm_plain(cp, FMPT_C, xop, nres, c, r, Ures, r, pr, M, m, planeM,
                                     Qr.d(), nres, pq)));
     std::vector<double> sc(nres);
     for (int i = 0; i < nres; i++) sc[i] = lam[tn + i] > 0.0 ? 1.0 / std::sqrt(lam[tn + i]) : 0.0;
@@ -410,28 +417,28 @@ int fmpt_dm_split(fmpt_handle* h, int dtype, const double* M, int m, int n, int 
                                  h->stream));
     FMPT_TRY(fmpt_scale_dim(h, dtype, 0, nres, c, inv.d(), Qr.d()));
     // tail rows Bt = U_tail^H X, minus their components along the resolved rows (twice)
-    FMPT_TRY(gemm_f64(h, gemm_plain(cp, FMPT_C, xop, tn, c, r, U.d(), r, pr, M, m, planeM,
+    FMPT_TRY(split_gemm(h, gemm_plain(cp, FMPT_C, xop, tn, c, r, U.d(), r, pr, M, m, planeM,
                                     Bt.d(), tn, pb)));
     FMPT_TRY(G.alloc(h, (size_t)tn * nres * sizeof(double) * (cp ? 2 : 1)));
     for (int rep = 0; rep < 2; rep++) {
-      FMPT_TRY(gemm_f64(h, gemm_plain(cp, FMPT_N, FMPT_C, tn, nres, c, Bt.d(), tn, pb, Qr.d(),
+      FMPT_TRY(split_gemm(h, gemm_plain(cp, FMPT_N, FMPT_C, tn, nres, c, Bt.d(), tn, pb, Qr.d(),
                                       nres, pq, G.d(), tn, (int64_t)tn * nres)));
       GemmArgs g = gemm_plain(cp, FMPT_N, FMPT_N, tn, c, nres, G.d(), tn, (int64_t)tn * nres,
                               Qr.d(), nres, pq, Bt.d(), tn, pb);
       g.alpha[0] = -1.0;
       g.beta[0] = 1.0;
-      FMPT_TRY(gemm_f64(h, g));
+      FMPT_TRY(split_gemm(h, g));
     }
     // Gram of the tail rows, its eigenvectors rotate the tail columns of U
     const int64_t pt = (int64_t)tn * tn;
     FMPT_TRY(Gt.alloc(h, (size_t)pt * sizeof(double) * (cp ? 2 : 1)));
     FMPT_TRY(Wt.alloc(h, (size_t)tn * sizeof(double)));
     FMPT_TRY(Vt.alloc(h, (size_t)pt * sizeof(double) * (cp ? 2 : 1)));
-    FMPT_TRY(gemm_f64(h, gemm_plain(cp, FMPT_N, FMPT_C, tn, tn, c, Bt.d(), tn, pb, Bt.d(), tn, pb,
+    FMPT_TRY(split_gemm(h, gemm_plain(cp, FMPT_N, FMPT_C, tn, tn, c, Bt.d(), tn, pb, Bt.d(), tn, pb,
                                     Gt.d(), tn, pt)));
     FMPT_TRY(eigh_split(h, cp, tn, Gt.d(), Wt.d(), Vt.d()));
     FMPT_TRY(Ut.alloc(h, (size_t)r * tn * sizeof(double) * (cp ? 2 : 1)));
-    FMPT_TRY(gemm_f64(h, gemm_plain(cp, FMPT_N, FMPT_N, r, tn, tn, U.d(), r, pr, Vt.d(), tn, pt,
+    FMPT_TRY(split_gemm(h, gemm_plain(cp, FMPT_N, FMPT_N, r, tn, tn, U.d(), r, pr, Vt.d(), tn, pt,
                                     Ut.d(), r, (int64_t)r * tn)));
     FMPT_TRY(copy_mat(h, cp, r, tn, Ut.d(), r, (int64_t)r * tn, 0, 0, U.d(), r, pr));
     FMPT_CUDA(h, cudaMemcpyAsync(lam.data(), Wt.d(), tn * sizeof(double), cudaMemcpyDeviceToHost,
@@ -491,7 +498,7 @@ int fmpt_dm_split(fmpt_handle* h, int dtype, const double* M, int m, int n, int 
     g.A = Q.d(); g.lda = m; g.planeA = (int64_t)m * k;
     g.B = M; g.ldb = m; g.planeB = planeM;
     g.C = Bout; g.ldc = k; g.planeC = (int64_t)k * n;
-    FMPT_TRY(gemm_f64(h, g));
+    FMPT_TRY(split_gemm(h, g));
   } else {
     // B = Q^H (k x n);  A = M Q (m x k)
     FMPT_TRY(copy_mat(h, cp, k, n, Q.d(), n, (int64_t)n * k, 1, cp, Bout, k, (int64_t)k * n));
@@ -499,7 +506,7 @@ int fmpt_dm_split(fmpt_handle* h, int dtype, const double* M, int m, int n, int 
     g.A = M; g.lda = m; g.planeA = planeM;
     g.B = Q.d(); g.ldb = n; g.planeB = (int64_t)n * k;
     g.C = Aout; g.ldc = m; g.planeC = (int64_t)m * k;
-    FMPT_TRY(gemm_f64(h, g));
+    FMPT_TRY(split_gemm(h, g));
   }
   // the host vectors must stay alive until their async copies finish
   FMPT_CUDA(h, cudaStreamSynchronize(h->stream));
