@@ -318,8 +318,9 @@ def dmrg_section(h, fm, budget_s=150.0, full3=False, only3=False):
       xxz_L20_D64_dmrg1s: the same chain and start with DMRG1S + OptimalExpansion, FP64,
                6 sweeps.
       j1j2_L100_D1024: J1-J2 L=100, J1=1, J2=0.3, cutoff 1e-9, ramp 64 -> 256 -> 1024 in
-               the mixed form, then one timed mixed sweep at D=1024; the FP64 sweep
-               time is extrapolated from three centre bonds timed in both forms.
+               the mixed form (two sweeps at 1024, the second timed), then the same window
+               of 20 centre bonds run in both forms from that converged state (config3_j1j2).
+               `--config3` adds both forms' full ramps, as configured and at equal D.
                (At J2=0.5 the ground state is an exact dimer product and keeps D<=3,
                so the D=1024 stage runs at J2=0.3.)"""
     import time as _t
