@@ -353,11 +353,16 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   const int num_items = units * ep.split;
   auto stageA = [&](int s) { return smem + s * STAGE_BYTES; };
   auto stageB = [&](int s) { return stageA(s) + A_BYTES; };
-  // item -> tile unit u, level set [l0, l0 + nl) of kOrder[ep.var], K slices [k0, k1)
+  // item -> tile unit u, level set [l0, l0 + nl) of kOrder[ep.var], K slices [k0, k1).
+  // Items run K-range-major: (K range cq, tile unit u, level set lp), so the clusters that
+  // run at one time cover many tiles over ONE K range and read 1/Q of those tiles' digit
+  // planes (a split GEMM 2 at D=2048 reads 30 GB from DRAM per launch instead of 42 GB)
   auto item_of = [&](int item, int& u, int& l0, int& nl, int& k0, int& k1) {
-    u = item / ep.split;
-    const int p = item - u * ep.split;
-    const int lp = p % ep.S, cq = p / ep.S;
+    const int us = units * ep.S;
+    const int cq = item / us;
+    const int rem = item - cq * us;
+    u = rem / ep.S;
+    const int lp = rem - u * ep.S;
     piece_levels(ep.var, lp, l0, nl);
     k0 = (int)((int64_t)cq * nk / ep.Q);
     k1 = (int)((int64_t)(cq + 1) * nk / ep.Q);
@@ -549,19 +554,24 @@ struct RedArgs {
   const double* ws;
   double* C;
   int64_t ldc, strideC, planeC;
-  int m, n, batch, cplx, split, tiles_m2, tiles_n, nfast;
+  int m, n, batch, cplx, split, S, tiles_m2, tiles_n, nfast;
   double alpha[2], beta[2];
 };
 
 __device__ __forceinline__ double ws_sum(const RedArgs& a, int z, int r, int c) {
   // unit index of the tile holding (r, c) under the kernel's tile order
   const int mt2 = r / TILE, nt = c / TILE;
-  const int per = a.tiles_m2 * a.tiles_n;
-  (void)per;
+  const int units = a.tiles_m2 * a.tiles_n * a.batch;
   const int u = oz_unit(mt2, nt, z, a.tiles_m2, a.tiles_n);
-  const double* w = a.ws + ((int64_t)u * a.split) * TILE * TILE + (int64_t)(c % TILE) * TILE + r % TILE;
+  const double* w = a.ws + (int64_t)(c % TILE) * TILE + r % TILE;
+  // piece p = lp + S cq of unit u sits at item (cq units + u) S + lp (K-range-major);
+  // summed in piece order
   double s = 0.0;
-  for (int p = 0; p < a.split; p++) s += w[(int64_t)p * TILE * TILE];
+  for (int p = 0; p < a.split; p++) {
+    const int lp = p % a.S, cq = p / a.S;
+    const int64_t item = ((int64_t)cq * units + u) * a.S + lp;
+    s += w[item * TILE * TILE];
+  }
   return s;
 }
 
@@ -804,6 +814,7 @@ int gemm_f64_ozaki(fmpt_handle* h, const GemmArgs& g) {
     ra.batch = batch;
     ra.cplx = cp;
     ra.split = split;
+    ra.S = plan.S;
     ra.tiles_m2 = tiles_m2;
     ra.tiles_n = tiles_n;
     ra.nfast = ep.nfast;
