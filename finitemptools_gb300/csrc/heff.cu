@@ -356,6 +356,20 @@ int op_apply_fp64(fmpt_op* op, const double* x, double* y) {
                                    (int64_t)Dl * Dr)));
     return FMPT_OK;
   }
+  FMPT_TRY(op_fp64_head(op, x));
+  return op_fp64_tail(op, y);
+}
+
+// One- and two-site FP64 application in two halves, so that a caller can overlap the
+// upload of the right environment with the first half: head = GEMM 1 and the MPO step
+// (reads x and the left environment, writes T1 and T3 in the operator's scratch), tail =
+// GEMM 2 (reads T3 and the right environment, writes y).
+int op_fp64_head(fmpt_op* op, const double* x) {
+  fmpt_handle* h = op->h;
+  const int eng = op->precision == FMPT_PREC_FP64_TC ? 1 : 0;
+  const int cp = op->dtype == FMPT_C128;
+  const int Dl = op->Dl, Dr = op->Dr;
+  const size_t es = sizeof(double) * (cp ? 2 : 1);
   const int P = op->kind == 0 ? op->d1 * op->d2 : op->d1;
   const int wl = op->wl, wr = op->wr;
   const int64_t nx = (int64_t)Dl * P * Dr;
@@ -366,18 +380,33 @@ int op_apply_fp64(fmpt_op* op, const double* x, double* y) {
   double* T1 = op->scratch;
   double* T3 = op->scratch + n1 * (cp ? 2 : 1);
   // 1. T1[(a' w), (s b)] = L[(a' w), a] x[a, (s b)]
-  FMPT_TRY(gemm_f64(h, gemm_args(cp, FMPT_N, FMPT_N, Dl * wl, P * Dr, Dl, op->hleft,
-                                 (int64_t)Dl * wl, (int64_t)Dl * wl * Dl, x, Dl, nx, T1,
-                                 (int64_t)Dl * wl, n1)));
+  GemmArgs g1 = gemm_args(cp, FMPT_N, FMPT_N, Dl * wl, P * Dr, Dl, op->hleft, (int64_t)Dl * wl,
+                          (int64_t)Dl * wl * Dl, x, Dl, nx, T1, (int64_t)Dl * wl, n1);
+  g1.engine = eng;
+  if (eng) g1.cacheA = &op->oz_left;
+  FMPT_TRY(gemm_f64(h, g1));
   // 2. T3[a', s', w2, b] = sum_blocks O[s', s] T1[a', w, s, b]
   MidStrides si{1, (int64_t)Dl * wl * P, Dl, (int64_t)Dl * wl};
   MidStrides so{1, (int64_t)Dl * P * wr, (int64_t)Dl * P, Dl};
-  FMPT_TRY(mid_apply(h, op->sched, T1, n1, si, T3, n3, so, Dl, Dr));
+  return mid_apply(h, op->sched, T1, n1, si, T3, n3, so, Dl, Dr);
+}
+
+int op_fp64_tail(fmpt_op* op, double* y) {
+  fmpt_handle* h = op->h;
+  const int eng = op->precision == FMPT_PREC_FP64_TC ? 1 : 0;
+  const int cp = op->dtype == FMPT_C128;
+  const int Dl = op->Dl, Dr = op->Dr;
+  const int P = op->kind == 0 ? op->d1 * op->d2 : op->d1;
+  const int wl = op->wl, wr = op->wr;
+  const int64_t nx = (int64_t)Dl * P * Dr;
+  const int64_t n1 = (int64_t)Dl * wl * P * Dr, n3 = (int64_t)Dl * P * wr * Dr;
+  const double* T3 = op->scratch + n1 * (cp ? 2 : 1);
   // 3. y[(a' s'), b'] = T3[(a' s'), (w2 b)] R[b', (w2 b)]^T
-  FMPT_TRY(gemm_f64(h, gemm_args(cp, FMPT_N, FMPT_T, Dl * P, Dr, wr * Dr, T3,
-                                 (int64_t)Dl * P, n3, op->hright, Dr, (int64_t)Dr * wr * Dr, y,
-                                 (int64_t)Dl * P, nx)));
-  return FMPT_OK;
+  GemmArgs g2 = gemm_args(cp, FMPT_N, FMPT_T, Dl * P, Dr, wr * Dr, T3, (int64_t)Dl * P, n3,
+                          op->hright, Dr, (int64_t)Dr * wr * Dr, y, (int64_t)Dl * P, nx);
+  g2.engine = eng;
+  if (eng) g2.cacheB = &op->oz_right;
+  return gemm_f64(h, g2);
 }
 
 }  // namespace fmpt
@@ -503,7 +532,44 @@ int fmpt_ac2_prime_host(fmpt_handle* h, int dtype, int precision, const double* 
   FMPT_TRY(dR.alloc(h, bR));
   FMPT_TRY(dy.alloc(h, bx));
   cudaStream_t ms = h->stream;
-  const bool pipeline = !prec_is_f64(precision) && dtype == FMPT_F64;
+  if (prec_is_f64(precision)) {
+    // FP64 forms: the uploads run on a copy stream in the order L, x, R; the main stream
+    // starts GEMM 1 and the MPO step once L and x have arrived, so R's upload overlaps them,
+    // and GEMM 2 once R has
+    FMPT_TRY(aux_fork(h, 1));       // the copies follow the allocations above
+    cudaStream_t as = h->aux_stream[0];
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+    int st = FMPT_OK;
+    auto ok = [&](cudaError_t e) {
+      if (e != cudaSuccess && st == FMPT_OK)
+        st = set_error(h, FMPT_ERR_CUDA, "ac2_prime_host: %s", cudaGetErrorString(e));
+      return st == FMPT_OK;
+    };
+    for (int i = 0; i < 3 && st == FMPT_OK; i++)
+      ok(cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming));
+    if (st == FMPT_OK) {
+      ok(cudaMemcpyAsync(dL.p, hleft, bL, cudaMemcpyHostToDevice, as)) && ok(cudaEventRecord(ev[0], as));
+      ok(cudaMemcpyAsync(dx.p, x, bx, cudaMemcpyHostToDevice, as)) && ok(cudaEventRecord(ev[1], as));
+      ok(cudaMemcpyAsync(dR.p, hright, bR, cudaMemcpyHostToDevice, as)) && ok(cudaEventRecord(ev[2], as));
+    }
+    fmpt_op* op = nullptr;
+    if (st == FMPT_OK)
+      st = make_op(h, 0, dtype, precision, W1, W2, dL.d(), dR.d(), Dl, d1, d2, Dr, wl, wm, wr,
+                   &op);
+    if (st == FMPT_OK && ok(cudaStreamWaitEvent(ms, ev[0], 0)) &&
+        ok(cudaStreamWaitEvent(ms, ev[1], 0)))
+      st = op_fp64_head(op, dx.d());
+    if (st == FMPT_OK && ok(cudaStreamWaitEvent(ms, ev[2], 0))) st = op_fp64_tail(op, dy.d());
+    if (st == FMPT_OK) ok(cudaMemcpyAsync(y, dy.p, bx, cudaMemcpyDeviceToHost, ms));
+    // every queued copy and kernel ends before the buffers are released
+    ok(cudaStreamSynchronize(as));
+    ok(cudaStreamSynchronize(ms));
+    if (op) fmpt_op_destroy(op);
+    for (cudaEvent_t e : ev)
+      if (e) cudaEventDestroy(e);
+    return st;
+  }
+  const bool pipeline = dtype == FMPT_F64;
   if (!pipeline) {
     FMPT_CUDA(h, cudaMemcpyAsync(dx.p, x, bx, cudaMemcpyHostToDevice, ms));
     FMPT_CUDA(h, cudaMemcpyAsync(dL.p, hleft, bL, cudaMemcpyHostToDevice, ms));

@@ -116,6 +116,10 @@ struct DevBuf {
 };
 
 int ensure_pinned(fmpt_handle* h, size_t n_doubles);
+// the FP64 one-/two-site operator application in two halves (heff.cu): head = GEMM 1 and
+// the MPO step into the operator's scratch, tail = GEMM 2 into y
+int op_fp64_head(fmpt_op* op, const double* x);
+int op_fp64_tail(fmpt_op* op, double* y);
 // Q (m x n) and R (n x n) of a small tall panel (m >= n) on one thread-block cluster;
 // FMPT_ERR_UNSUPPORTED (nothing launched) outside its range (qr_cluster.cu)
 int qr_small_cluster(fmpt_handle* h, int cplx, int m, int n, const double* M, double* Q,
