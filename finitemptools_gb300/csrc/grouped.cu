@@ -92,46 +92,58 @@ __device__ bool grid_barrier(const GKArgs& a, int target, int* s_flag) {
   return *s_flag != 0;
 }
 
-// One GTxGT output tile of a GEMM problem: 256 threads on a 16x16 grid, each
-// owning (GT/16)^2 outputs at rows tx + 16 i, columns ty + 16 j.  Every output
-// sums its segments and k in the same order for any GT, so the tile shape
-// never changes the result.
-template <int GT>
+// Tile word: origin in 16-row / 16-column units and extent in 16-wide groups,
+//   bits 0-11 m0 / 16, bits 12-23 n0 / 16, bits 24-27 MI - 1, bits 28-31 NJ - 1.
+// A tile covers (16 MI) x (16 NJ) outputs; the last tile of a block along either
+// dimension is only as many 16-wide groups as the block needs, so a 40-row block
+// takes a 32-row and a 16-row tile instead of two 32-row tiles.
+__host__ __device__ __forceinline__ uint32_t tile_word(int m16, int n16, int mi, int nj) {
+  return (uint32_t)m16 | ((uint32_t)n16 << 12) | ((uint32_t)(mi - 1) << 24) |
+         ((uint32_t)(nj - 1) << 28);
+}
+constexpr int kMaxTile16 = 0xfff;   // largest origin in 16-wide units
+
+// One (16 MI)x(16 NJ) output tile of a GEMM problem: 256 threads on a 16x16 grid,
+// each owning MI x NJ outputs at rows tx + 16 i, columns ty + 16 j.  Every output
+// sums its segments and k in the same order for any tile shape, so the tiling
+// never changes the result.  MI and NJ are compile-time, so a narrow edge tile
+// issues no FP64 work for the rows or columns it does not hold.
+template <int GT, int MI, int NJ>
 __device__ __forceinline__ void gemm_tile(const GKArgs& a, const GPhaseDesc& ph, int t,
                                           double (*As)[GT + 1], double (*Bs)[GT + 1]) {
-  constexpr int TPR = GT / 16;
+  constexpr int TM = 16 * MI, TN = 16 * NJ;
   const GProblem P = a.probs[a.tile_prob[t]];
-  const int mn = a.tile_mn[t];
-  const int m0 = (mn & 0xffff) * GT, n0 = ((unsigned)mn >> 16) * GT;
+  const uint32_t mn = (uint32_t)a.tile_mn[t];
+  const int m0 = (int)(mn & 0xfffu) * 16, n0 = (int)((mn >> 12) & 0xfffu) * 16;
   const int tid = threadIdx.x;
   const int tx = tid % 16, ty = tid / 16;
   const bool a_mfast = (ph.ta == FMPT_N || ph.ta == FMPT_R);
   const bool b_kfast = (ph.tb == FMPT_N || ph.tb == FMPT_R);
   const double* Ab = a.slot[ph.a_slot];
   const double* Bb = a.slot[ph.b_slot];
-  double acc[TPR][TPR];
+  double acc[MI][NJ];
 #pragma unroll
-  for (int i = 0; i < TPR; i++)
+  for (int i = 0; i < MI; i++)
 #pragma unroll
-    for (int j = 0; j < TPR; j++) acc[i][j] = 0.0;
+    for (int j = 0; j < NJ; j++) acc[i][j] = 0.0;
   for (int sg = P.seg0; sg < P.seg1; sg++) {
     const GSegment S = a.segs[sg];
     const double* A = Ab + S.a_off;
     const double* B = Bb + S.b_off;
     for (int k0 = 0; k0 < S.k; k0 += GK) {
 #pragma unroll
-      for (int e = tid; e < GT * GK; e += GNT) {
+      for (int e = tid; e < TM * GK; e += GNT) {
         int mm, kk;
-        if (a_mfast) { mm = e % GT; kk = e / GT; } else { kk = e % GK; mm = e / GK; }
+        if (a_mfast) { mm = e % TM; kk = e / TM; } else { kk = e % GK; mm = e / GK; }
         const int gm = m0 + mm, gk = k0 + kk;
         double v = 0.0;
         if (gm < P.m && gk < S.k) v = S.coef * __ldg(A + op_index(ph.ta, gm, gk, S.lda));
         As[kk][mm] = v;
       }
 #pragma unroll
-      for (int e = tid; e < GT * GK; e += GNT) {
+      for (int e = tid; e < TN * GK; e += GNT) {
         int nn, kk;
-        if (b_kfast) { kk = e % GK; nn = e / GK; } else { nn = e % GT; kk = e / GT; }
+        if (b_kfast) { kk = e % GK; nn = e / GK; } else { nn = e % TN; kk = e / TN; }
         const int gn = n0 + nn, gk = k0 + kk;
         double v = 0.0;
         if (gn < P.n && gk < S.k) v = __ldg(B + op_index(ph.tb, gk, gn, S.ldb));
@@ -140,35 +152,52 @@ __device__ __forceinline__ void gemm_tile(const GKArgs& a, const GPhaseDesc& ph,
       __syncthreads();
 #pragma unroll
       for (int kk = 0; kk < GK; kk++) {
-        double av[TPR], bv[TPR];
+        double av[MI], bv[NJ];
 #pragma unroll
-        for (int i = 0; i < TPR; i++) { av[i] = As[kk][tx + 16 * i]; bv[i] = Bs[kk][ty + 16 * i]; }
+        for (int i = 0; i < MI; i++) av[i] = As[kk][tx + 16 * i];
 #pragma unroll
-        for (int i = 0; i < TPR; i++)
+        for (int j = 0; j < NJ; j++) bv[j] = Bs[kk][ty + 16 * j];
 #pragma unroll
-          for (int j = 0; j < TPR; j++) acc[i][j] = fma(av[i], bv[j], acc[i][j]);
+        for (int i = 0; i < MI; i++)
+#pragma unroll
+          for (int j = 0; j < NJ; j++) acc[i][j] = fma(av[i], bv[j], acc[i][j]);
       }
       __syncthreads();
     }
   }
   double* C = a.slot[ph.c_slot] + P.c_off;
 #pragma unroll
-  for (int i = 0; i < TPR; i++) {
+  for (int i = 0; i < MI; i++) {
     const int r = m0 + tx + 16 * i;
     if (r >= P.m) continue;
 #pragma unroll
-    for (int j = 0; j < TPR; j++) {
+    for (int j = 0; j < NJ; j++) {
       const int c = n0 + ty + 16 * j;
       if (c < P.n) C[r + (int64_t)c * P.ldc] = acc[i][j];
     }
   }
 }
 
+// the tile's extent (MI, NJ) picks the instantiation; uniform over the block
+template <int GT, int MI = 1, int NJ = 1>
+__device__ __forceinline__ void gemm_tile_any(const GKArgs& a, const GPhaseDesc& ph, int t,
+                                              int mi, int nj, double (*As)[GT + 1],
+                                              double (*Bs)[GT + 1]) {
+  constexpr int TPR = GT / 16;
+  if (mi == MI && nj == NJ) {
+    gemm_tile<GT, MI, NJ>(a, ph, t, As, Bs);
+  } else if constexpr (NJ < TPR) {
+    gemm_tile_any<GT, MI, NJ + 1>(a, ph, t, mi, nj, As, Bs);
+  } else if constexpr (MI < TPR) {
+    gemm_tile_any<GT, MI + 1, 1>(a, ph, t, mi, nj, As, Bs);
+  }
+}
+
 template <int GT>
 __device__ __forceinline__ void sum_tile(const GKArgs& a, const GPhaseDesc& ph, int t) {
   const GProblem P = a.probs[a.tile_prob[t]];
-  const int mn = a.tile_mn[t];
-  const int m0 = (mn & 0xffff) * GT, n0 = ((unsigned)mn >> 16) * GT;
+  const uint32_t mn = (uint32_t)a.tile_mn[t];
+  const int m0 = (int)(mn & 0xfffu) * 16, n0 = (int)((mn >> 12) & 0xfffu) * 16;
   const int r = m0 + (threadIdx.x % GT);
   if (r >= P.m) return;
   const double* Ab = a.slot[ph.a_slot];
@@ -203,9 +232,11 @@ __global__ void __launch_bounds__(GNT) grouped_kernel(const GKArgs a) {
       __syncthreads();
       const int t = s_tile;
       if (t >= ntiles) break;
-      if (ph.type == GP_GEMM)
-        gemm_tile<GT>(a, ph, ph.tile0 + t, As, Bs);
-      else
+      if (ph.type == GP_GEMM) {
+        const uint32_t mn = (uint32_t)a.tile_mn[ph.tile0 + t];
+        gemm_tile_any<GT>(a, ph, ph.tile0 + t, (int)((mn >> 24) & 0xfu) + 1,
+                          (int)(mn >> 28) + 1, As, Bs);
+      } else
         sum_tile<GT>(a, ph, ph.tile0 + t);
     }
   }
@@ -339,13 +370,18 @@ int gp_finalize(fmpt_handle* h, GroupedProgram& g) {
       for (int i : order) {
         const GProblem& p = g.probs[i];
         if (p.m <= 0 || p.n <= 0) continue;
-        const int tm = (p.m + GT - 1) / GT, tn = (p.n + GT - 1) / GT;
-        if (tm > 0xffff || tn > 0x7fff)
+        if ((p.m - 1) / 16 > kMaxTile16 || (p.n - 1) / 16 > kMaxTile16)
           return set_error(h, FMPT_ERR_SHAPE, "grouped: block %d x %d too large", p.m, p.n);
-        for (int b = 0; b < tn; b++)
-          for (int a = 0; a < tm; a++) {
+        // GEMM tiles: GT wide, the last one along each dimension cut to the 16-wide
+        // groups the block needs; SUM tiles (memory-bound) stay GT x GT
+        const bool gemm = g.phases[ph].type == GP_GEMM;
+        const int g16m = (p.m + 15) / 16, g16n = (p.n + 15) / 16, TPR = GT / 16;
+        for (int b = 0; b < g16n; b += TPR)
+          for (int a = 0; a < g16m; a += TPR) {
+            const int mi = gemm ? std::min(TPR, g16m - a) : TPR;
+            const int nj = gemm ? std::min(TPR, g16n - b) : TPR;
             g.tile_prob.push_back(i);
-            g.tile_mn.push_back(a | (b << 16));
+            g.tile_mn.push_back((int)tile_word(a, b, mi, nj));
           }
       }
       g.vtile1[v][ph] = (int)g.tile_prob.size();

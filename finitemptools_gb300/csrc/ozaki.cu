@@ -7,10 +7,12 @@
 //
 //   1. every row r of op(A) (and every column n of op(B)) gets an exponent e with
 //      max |row| < 2^e, and its entries become NS = 9 balanced base-64 digits,
-//        X(r, k) = sum_i sigma_i(r, k) 2^(e_r - 6 i),   sigma_i integer, |sigma_i| <= 64,
+//        X(r, k) = sum_i sigma_i(r, k) 2^(e_r - 6 i),   sigma_i integer, |sigma_1| <= 64,
+//        |sigma_i| <= 32 below it,
 //      exact to 2^(e_r - 54) (54 bits: every FP64 entry within 2^-1 of its row maximum is
 //      represented exactly); the digits are computed with integer arithmetic on the FP64
-//      bit pattern (no FP64 instruction), and each one is an exact BF16 value;
+//      bit pattern (no FP64 instruction; each digit's BF16 encoding comes from one exact
+//      FP32 subtraction), and each one is an exact BF16 value;
 //   2. the digit planes are multiplied on the tensor cores (tcgen05.mma kind::f16, BF16 x
 //      BF16 -> FP32).  All products sigma_i tau_j with the same level l = i + j carry the
 //      same scale 2^(e_r + e_n - 6 l), so they share one TMEM accumulator; the 45 products
@@ -101,14 +103,13 @@ __device__ __forceinline__ uint64_t src_bits(const SliceSrc& s, int z, int r2, i
   return v;
 }
 
-// bf16 bits of an integer |k| <= 64
-__device__ __forceinline__ uint32_t int_bf16(int k) {
-  if (k == 0) return 0u;
-  const uint32_t s = k < 0 ? 0x8000u : 0u;
-  const uint32_t a = (uint32_t)(k < 0 ? -k : k);
-  const int p = 31 - __clz(a);                                  // a in [2^p, 2^(p+1))
-  return s | ((uint32_t)(127 + p) << 7) | ((a << (7 - p)) & 0x7fu);
-}
+// Balanced digits by offset binary: with B = 32 (2^42 + 2^36 + ... + 2^0), N + B written in
+// base 64 has digit words u_i in [0, 64) below the top one, and
+//   N = (N + B) >> 48 * 2^48 + sum_{i >= 2} (u_i - 32) 2^(54 - 6 i),
+// so sigma_1 = (N + B) >> 48 (|sigma_1| <= 64 for |N| < 2^54) and sigma_i = u_i - 32 in
+// [-32, 31]: one 64-bit add and bit-field extracts instead of NS rounding divisions.
+constexpr int64_t kDigitBias = 0x820820820820ll;
+static_assert(NS == 9 && SB == 6, "the digit extraction below is written for 9 digits of 6 bits");
 
 constexpr int SL_ROWS = 32;           // rows of a slicing block
 constexpr int SL_KCH = 512;           // K columns of a slicing block (8 tiles of 64)
@@ -183,31 +184,37 @@ __global__ void __launch_bounds__(256) oz_digits(SliceSrc src, int rows_out, int
     if (r < rows_out && cb < ldk) {
       uint32_t pk[NS][4];
 #pragma unroll
-      for (int q = 0; q < 8; q++) {
-        const uint64_t bits = bad ? 0ull : tile[rr][part * 8 + q];
-        const int ex = (int)((bits >> 52) & 0x7ff);
-        int64_t M = (int64_t)(bits & 0xfffffffffffffull);
-        if (ex) M |= (int64_t)1 << 52;
-        // N = X 2^(54 - e) as an integer: |N| < 2^54; shift = max(ex, 1) - 1075 + 54 - e
-        const int sh = (ex ? ex : 1) - 1021 - e;
-        int64_t N;
-        if (sh >= 0) N = M << sh;                         // sh <= 1
-        else N = sh <= -63 ? 0 : (M >> (-sh));
-        if (bits >> 63) N = -N;
+      for (int q = 0; q < 8; q += 2) {
+        uint32_t fb[2][NS];
 #pragma unroll
-        for (int i = 0; i < NS; i++) {
-          const int s = 54 - SB * (i + 1);
-          int64_t d;
-          if (s > 0) {
-            d = (N + ((int64_t)1 << (s - 1))) >> s;   // nearest, ties up
-            N -= d << s;
-          } else {
-            d = N;                                    // the last digit takes the rest
-          }
-          const uint32_t b = int_bf16((int)d);
-          if (q & 1) pk[i][q >> 1] |= b << 16;
-          else pk[i][q >> 1] = b;
+        for (int h2 = 0; h2 < 2; h2++) {
+          const uint64_t bits = bad ? 0ull : tile[rr][part * 8 + q + h2];
+          const int ex = (int)((bits >> 52) & 0x7ff);
+          int64_t N = (int64_t)(bits & 0xfffffffffffffull);
+          if (ex) N |= (int64_t)1 << 52;
+          // N = X 2^(54 - e) as an integer: |N| < 2^54; shift = max(ex, 1) - 1075 + 54 - e
+          const int sh = (ex ? ex : 1) - 1021 - e;
+          if (sh >= 0) N <<= sh;                            // sh <= 1
+          else N = sh <= -63 ? 0 : (N >> (-sh));
+          if (bits >> 63) N = -N;
+          // offset-binary digits of N + kDigitBias: word i >= 1 is bits [s_i, s_i + 6)
+          // minus 32, word 0 the arithmetic top; converted through 2^23 + u in FP32
+          const uint64_t Mo = (uint64_t)(N + kDigitBias);
+          const uint32_t lo = (uint32_t)Mo, hi = (uint32_t)(Mo >> 32);
+          const int d0 = (int)hi >> 16;
+          const uint32_t u[NS - 1] = {(hi >> 10) & 63u, (hi >> 4) & 63u,
+                                      __funnelshift_r(lo, hi, 30) & 63u, (lo >> 24) & 63u,
+                                      (lo >> 18) & 63u, (lo >> 12) & 63u, (lo >> 6) & 63u,
+                                      lo & 63u};
+          fb[h2][0] = __float_as_uint(__uint_as_float(0x4B000000u | (uint32_t)(d0 + 64)) -
+                                      8388672.0f);
+#pragma unroll
+          for (int i = 1; i < NS; i++)
+            fb[h2][i] = __float_as_uint(__uint_as_float(0x4B000000u | u[i - 1]) - 8388640.0f);
         }
+        // two BF16 digits per word: the upper halves of the exact FP32 values
+#pragma unroll
+        for (int i = 0; i < NS; i++) pk[i][q >> 1] = __byte_perm(fb[0][i], fb[1][i], 0x7632);
       }
 #pragma unroll
       for (int i = 0; i < NS; i++)
