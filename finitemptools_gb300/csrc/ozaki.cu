@@ -114,59 +114,87 @@ static_assert(NS == 9 && SB == 6, "the digit extraction below is written for 9 d
 constexpr int SL_ROWS = 32;           // rows of a slicing block
 constexpr int SL_KCH = 512;           // K columns of a slicing block (8 tiles of 64)
 
-// 32 x 64 tile of op(X) bit patterns into shared memory, coalesced along whichever index
-// is contiguous in the source; zeros outside the operand
-__device__ __forceinline__ void load_tile(const SliceSrc& src, int z, int r0, int c0, int rows_out,
-                                          int k_out, uint64_t (&tile)[SL_ROWS][65]) {
+// A 32 x 64 tile of op(X) bit patterns: element e = t + 256 q of thread t (q < 8) is
+// (row, column) = (e & 31, e >> 5) when rows are contiguous in the source and
+// (e >> 6, e & 63) otherwise, so that every warp load is contiguous; zeros outside the
+// operand.  The loads go to registers first, so that a block can fetch its next tile
+// while it works on the current one.
+__device__ __forceinline__ void tile_pos(bool rowfast, int e, int& lr, int& lc) {
+  if (rowfast) { lr = e & 31; lc = e >> 5; } else { lc = e & 63; lr = e >> 6; }
+}
+
+__device__ __forceinline__ void fetch_tile(const SliceSrc& src, int z, int r0, int c0, int rows_out,
+                                           int k_out, uint64_t (&v)[8]) {
   const int t = threadIdx.x;
   const bool rowfast = src.sr == 1;
 #pragma unroll
   for (int q = 0; q < 8; q++) {
-    const int e = t + 256 * q;
     int lr, lc;
-    if (rowfast) { lr = e & 31; lc = e >> 5; } else { lc = e & 63; lr = e >> 6; }
+    tile_pos(rowfast, t + 256 * q, lr, lc);
     const int r = r0 + lr, c = c0 + lc;
-    tile[lr][lc] = (r < rows_out && c < k_out) ? src_bits(src, z, r, c) : 0ull;
+    v[q] = (r < rows_out && c < k_out) ? src_bits(src, z, r, c) : 0ull;
   }
 }
 
 // Row maxima of |X| on the bit patterns (non-negative IEEE doubles order as their bits):
 // block (strip, K chunk, batch) reduces its 32 x SL_KCH part and folds it into mx with an
 // atomic max (mx zeroed beforehand).
-__global__ void __launch_bounds__(256) oz_rowmax(SliceSrc src, int rows_out, int k_out,
+__global__ void __launch_bounds__(256, 4) oz_rowmax(SliceSrc src, int rows_out, int k_out,
                                                  unsigned long long* __restrict__ mx) {
-  __shared__ uint64_t tile[SL_ROWS][65];
+  __shared__ unsigned long long smax[SL_ROWS];
   const int r0 = blockIdx.x * SL_ROWS, kc0 = blockIdx.y * SL_KCH, z = blockIdx.z;
-  const int t = threadIdx.x, rr = t >> 3, part = t & 7;
-  uint64_t m = 0;
-  for (int c0 = kc0; c0 < min(kc0 + SL_KCH, k_out); c0 += 64) {
-    load_tile(src, z, r0, c0, rows_out, k_out, tile);
-    __syncthreads();
+  const int t = threadIdx.x;
+  const bool rowfast = src.sr == 1;
+  if (t < SL_ROWS) smax[t] = 0ull;
+  // rows of this thread's elements: one row (rowfast) or rows (t >> 6) + 4 q
+  uint64_t m[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  const int c1 = min(kc0 + SL_KCH, k_out);
+  uint64_t v[8];
+  if (kc0 < c1) fetch_tile(src, z, r0, kc0, rows_out, k_out, v);
+  for (int c0 = kc0; c0 < c1; c0 += 64) {
+    uint64_t cur[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) cur[q] = v[q] & 0x7fffffffffffffffull;
+    if (c0 + 64 < c1) fetch_tile(src, z, r0, c0 + 64, rows_out, k_out, v);
+#pragma unroll
+    for (int q = 0; q < 8; q++) m[q] = cur[q] > m[q] ? cur[q] : m[q];
+  }
+  __syncthreads();
+  if (rowfast) {
+    uint64_t a = m[0];
+#pragma unroll
+    for (int q = 1; q < 8; q++) a = m[q] > a ? m[q] : a;
+    if (a) atomicMax(&smax[t & 31], (unsigned long long)a);
+  } else {
+    // the 64 threads of a row group share their rows: fold across the warp's halves
 #pragma unroll
     for (int q = 0; q < 8; q++) {
-      const uint64_t a = tile[rr][part * 8 + q] & 0x7fffffffffffffffull;
-      m = a > m ? a : m;
-    }
-    __syncthreads();
-  }
+      uint64_t a = m[q];
 #pragma unroll
-  for (int o = 1; o < 8; o <<= 1) {
-    const uint64_t y = __shfl_xor_sync(0xffffffffu, m, o);
-    m = y > m ? y : m;
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint64_t y = __shfl_xor_sync(0xffffffffu, a, o);
+        a = y > a ? y : a;
+      }
+      if ((t & 31) == 0 && a) atomicMax(&smax[(t >> 6) + 4 * q], (unsigned long long)a);
+    }
   }
-  const int r = r0 + rr;
-  if (part == 0 && r < rows_out && m != 0) atomicMax(mx + (int64_t)z * rows_out + r, m);
+  __syncthreads();
+  const int r = r0 + t;
+  if (t < SL_ROWS && r < rows_out && smax[t] != 0) atomicMax(mx + (int64_t)z * rows_out + r, smax[t]);
 }
 
 // Digits: block (strip, K chunk, batch) writes NS BF16 planes of its 32 x SL_KCH part
 // (zeros in the padding up to ldk); the chunk-0 blocks write the row exponents.
-// S[(z NS + i) rows_out + r][ldk] (K-major), E[z rows_out + r].
-__global__ void __launch_bounds__(256) oz_digits(SliceSrc src, int rows_out, int k_out, int ldk,
+// S[(z NS + i) rows_out + r][ldk] (K-major), E[z rows_out + r].  Each 32 x 64 tile goes
+// through a double-buffered shared tile (one barrier per tile); thread (rr, part) then
+// turns 8 consecutive K entries of row rr into 16-byte stores, one per digit plane.
+__global__ void __launch_bounds__(256, 3) oz_digits(SliceSrc src, int rows_out, int k_out, int ldk,
                                                  const unsigned long long* __restrict__ mxa,
                                                  uint16_t* __restrict__ S, int* __restrict__ E) {
-  __shared__ uint64_t tile[SL_ROWS][65];
+  __shared__ uint64_t tile[2][SL_ROWS][65];
   const int r0 = blockIdx.x * SL_ROWS, kc0 = blockIdx.y * SL_KCH, z = blockIdx.z;
   const int t = threadIdx.x, rr = t >> 3, part = t & 7;
+  const bool rowfast = src.sr == 1;
   const int r = r0 + rr;
   const uint64_t mx = r < rows_out ? mxa[(int64_t)z * rows_out + r] : 0ull;
   const int exm = (int)(mx >> 52);
@@ -177,51 +205,57 @@ __global__ void __launch_bounds__(256) oz_digits(SliceSrc src, int rows_out, int
   if (blockIdx.y == 0 && part == 0 && r < rows_out) E[(int64_t)z * rows_out + r] = bad ? E_BAD : e;
   const int64_t plane_stride = (int64_t)rows_out * ldk;
   uint16_t* out = S + ((int64_t)z * NS * rows_out + r) * ldk;
-  for (int c0 = kc0; c0 < min(kc0 + SL_KCH, ldk); c0 += 64) {
-    load_tile(src, z, r0, c0, rows_out, k_out, tile);
-    __syncthreads();
-    const int cb = c0 + part * 8;
-    if (r < rows_out && cb < ldk) {
-      uint32_t pk[NS][4];
+  const int c1 = min(kc0 + SL_KCH, ldk);
+  uint64_t v[8];
+  if (kc0 < c1) fetch_tile(src, z, r0, kc0, rows_out, k_out, v);
+  int buf = 0;
+  for (int c0 = kc0; c0 < c1; c0 += 64, buf ^= 1) {
 #pragma unroll
-      for (int q = 0; q < 8; q += 2) {
-        uint32_t fb[2][NS];
-#pragma unroll
-        for (int h2 = 0; h2 < 2; h2++) {
-          const uint64_t bits = bad ? 0ull : tile[rr][part * 8 + q + h2];
-          const int ex = (int)((bits >> 52) & 0x7ff);
-          int64_t N = (int64_t)(bits & 0xfffffffffffffull);
-          if (ex) N |= (int64_t)1 << 52;
-          // N = X 2^(54 - e) as an integer: |N| < 2^54; shift = max(ex, 1) - 1075 + 54 - e
-          const int sh = (ex ? ex : 1) - 1021 - e;
-          if (sh >= 0) N <<= sh;                            // sh <= 1
-          else N = sh <= -63 ? 0 : (N >> (-sh));
-          if (bits >> 63) N = -N;
-          // offset-binary digits of N + kDigitBias: word i >= 1 is bits [s_i, s_i + 6)
-          // minus 32, word 0 the arithmetic top; converted through 2^23 + u in FP32
-          const uint64_t Mo = (uint64_t)(N + kDigitBias);
-          const uint32_t lo = (uint32_t)Mo, hi = (uint32_t)(Mo >> 32);
-          const int d0 = (int)hi >> 16;
-          const uint32_t u[NS - 1] = {(hi >> 10) & 63u, (hi >> 4) & 63u,
-                                      __funnelshift_r(lo, hi, 30) & 63u, (lo >> 24) & 63u,
-                                      (lo >> 18) & 63u, (lo >> 12) & 63u, (lo >> 6) & 63u,
-                                      lo & 63u};
-          fb[h2][0] = __float_as_uint(__uint_as_float(0x4B000000u | (uint32_t)(d0 + 64)) -
-                                      8388672.0f);
-#pragma unroll
-          for (int i = 1; i < NS; i++)
-            fb[h2][i] = __float_as_uint(__uint_as_float(0x4B000000u | u[i - 1]) - 8388640.0f);
-        }
-        // two BF16 digits per word: the upper halves of the exact FP32 values
-#pragma unroll
-        for (int i = 0; i < NS; i++) pk[i][q >> 1] = __byte_perm(fb[0][i], fb[1][i], 0x7632);
-      }
-#pragma unroll
-      for (int i = 0; i < NS; i++)
-        *reinterpret_cast<uint4*>(out + i * plane_stride + cb) =
-            make_uint4(pk[i][0], pk[i][1], pk[i][2], pk[i][3]);
+    for (int q = 0; q < 8; q++) {
+      int lr, lc;
+      tile_pos(rowfast, t + 256 * q, lr, lc);
+      tile[buf][lr][lc] = v[q];
     }
     __syncthreads();
+    if (c0 + 64 < c1) fetch_tile(src, z, r0, c0 + 64, rows_out, k_out, v);
+    const int cb = c0 + part * 8;
+    if (r < rows_out && cb < ldk) {
+      // N + kDigitBias of the 8 entries, N = X 2^(54 - e) as an integer (|N| < 2^54)
+      uint64_t Mo[8];
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        const uint64_t bits = bad ? 0ull : tile[buf][rr][part * 8 + q];
+        const int ex = (int)((bits >> 52) & 0x7ff);
+        int64_t N = (int64_t)(bits & 0xfffffffffffffull);
+        if (ex) N |= (int64_t)1 << 52;
+        const int sh = (ex ? ex : 1) - 1021 - e;          // max(ex, 1) - 1075 + 54 - e
+        if (sh >= 0) N <<= sh;                            // sh <= 1
+        else N = sh <= -63 ? 0 : (N >> (-sh));
+        if (bits >> 63) N = -N;
+        Mo[q] = (uint64_t)(N + kDigitBias);
+      }
+      // digit i of each entry: word 0 the arithmetic top of N + kDigitBias, word i >= 1
+      // its bits [54 - 6 (i + 1), + 6) minus 32; the BF16 encoding is the upper half of the
+      // exact FP32 value (2^23 + u) - (2^23 + bias)
+#pragma unroll
+      for (int i = 0; i < NS; i++) {
+        uint32_t fb[8];
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+          if (i == 0) {
+            const int d0 = (int)(uint32_t)(Mo[q] >> 32) >> 16;
+            fb[q] = __float_as_uint(__uint_as_float(0x4B000000u | (uint32_t)(d0 + 64)) -
+                                    8388672.0f);
+          } else {
+            const uint32_t u = (uint32_t)(Mo[q] >> (54 - SB * (i + 1))) & 63u;
+            fb[q] = __float_as_uint(__uint_as_float(0x4B000000u | u) - 8388640.0f);
+          }
+        }
+        *reinterpret_cast<uint4*>(out + i * plane_stride + cb) =
+            make_uint4(__byte_perm(fb[0], fb[1], 0x7632), __byte_perm(fb[2], fb[3], 0x7632),
+                       __byte_perm(fb[4], fb[5], 0x7632), __byte_perm(fb[6], fb[7], 0x7632));
+      }
+    }
   }
 }
 
@@ -238,17 +272,6 @@ struct OzEpi {
   int split;            // pieces per tile: S level sets x Q chunk ranges (1: direct)
   int var, S, Q;        // level-set variant (kOrder / kSetStart), S = its piece count
 };
-
-// x 2^E of an FP32 integer value (|v| < 2^25), built in the exponent field
-__device__ __forceinline__ double scaled(uint32_t u, int E) {
-  if ((u << 1) == 0) return 0.0;
-  if (E >= -1000 && E <= 990) {
-    const uint32_t hi = (u & 0x80000000u) | ((((u >> 23) & 0xffu) + (uint32_t)(896 + E)) << 20) |
-                        ((u & 0x7fffffu) >> 3);
-    return __hiloint2double((int)hi, (int)(u << 29));
-  }
-  return ldexp((double)__uint_as_float(u), E);
-}
 
 // K slices (of KELEMS) per exactness chunk of a level: the longest run of K over which the
 // level's integer sum stays below 2^24 (per-k bound 4096 for l <= 3, 4096 + (l - 3) 1024)
@@ -284,6 +307,19 @@ __device__ __forceinline__ void piece_levels(int v, int lp, int& l0, int& nl) {
   nl = kSetStart[v][lp + 1] - l0;
 }
 
+// x 2^E of an FP32 integer value outside the exponent range of the fast path
+__device__ __noinline__ double scaled_slow(uint32_t u, int E) {
+  if ((u << 1) == 0) return 0.0;
+  return ldexp((double)__uint_as_float(u), E);
+}
+
+// Adds the level accumulator (TMEM lanes of this warp: 32 rows x 256 columns), scaled by
+// 2^(e_r + e_n - 6 level), into the FP64 output tile (first group: stores it).  A chunk of
+// 32 columns whose row and column exponents all lie in (-400, 400), with every row and
+// column inside the output, takes the fast path: the FP64 value is assembled in the
+// exponent field with integer operations and no branch, and the only FP64 instruction is
+// the add.  Other chunks (a ragged edge, Inf/NaN rows or columns, extreme exponents) take
+// the general path.
 template <bool SPLIT>
 __device__ __forceinline__ void drain(uint32_t tbase, int row, int rloc, int n0, int z,
                                       int level, bool first, bool last, const OzEpi& ep,
@@ -299,6 +335,8 @@ __device__ __forceinline__ void drain(uint32_t tbase, int row, int rloc, int n0,
     ld = ep.ldc;
   }
   const int er = live ? __ldg(ep.ea + (int64_t)z * ep.M + row) : 0;
+  const int eb = er - SB * level;
+  const bool scale = !SPLIT && last && ep.alpha != 1.0;
   const int lane = threadIdx.x & 31;
 #pragma unroll 1
   for (int c0 = 0; c0 < TILE; c0 += 32) {
@@ -307,24 +345,53 @@ __device__ __forceinline__ void drain(uint32_t tbase, int row, int rloc, int n0,
     const int nb = n0 + c0;
     const int ec = nb + lane < ep.N ? __ldg(ep.eb + (int64_t)z * ep.N + nb + lane) : 0;
     const int lim = SPLIT ? 32 : min(32, ep.N - nb);
+    double* p = crow + (int64_t)(SPLIT ? c0 : nb) * ld;
     double old[32];
     if (!first && live) {
 #pragma unroll
-      for (int j = 0; j < 32; j++) old[j] = j < lim ? crow[(int64_t)(SPLIT ? c0 + j : nb + j) * ld] : 0.0;
+      for (int j = 0; j < 32; j++) old[j] = j < lim ? p[j * ld] : 0.0;
     }
+    const bool fast =
+        __all_sync(0xffffffffu, live && er > -400 && er < 400 && ec > -400 && ec < 400) &&
+        lim == 32;
     tmem_wait_ld(r);
+    if (fast) {
 #pragma unroll
-    for (int j = 0; j < 32; j++) {
-      const int ecj = __shfl_sync(0xffffffffu, ec, j);
-      if (!live || j >= lim) continue;
-      double v;
-      if (er >= E_BAD || ecj >= E_BAD)
-        v = __longlong_as_double(0x7ff8000000000000ll);
-      else
-        v = scaled(r[j], er + ecj - SB * level);
-      if (!first) v += old[j];
-      if (!SPLIT && last && ep.alpha != 1.0) v *= ep.alpha;
-      crow[(int64_t)(SPLIT ? c0 + j : nb + j) * ld] = v;
+      for (int j = 0; j < 32; j++) {
+        const int E = eb + __shfl_sync(0xffffffffu, ec, j);
+        const uint32_t u = r[j];
+        const uint32_t hi = (u & 0x80000000u) |
+                            ((((u >> 23) & 0xffu) + (uint32_t)(896 + E)) << 20) |
+                            ((u & 0x7fffffu) >> 3);
+        double v = (u << 1) == 0 ? 0.0 : __hiloint2double((int)hi, (int)(u << 29));
+        if (!first) v += old[j];
+        if (scale) v *= ep.alpha;
+        p[j * ld] = v;
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < 32; j++) {
+        const int ecj = __shfl_sync(0xffffffffu, ec, j);
+        if (!live || j >= lim) continue;
+        double v;
+        if (er >= E_BAD || ecj >= E_BAD) {
+          v = __longlong_as_double(0x7ff8000000000000ll);
+        } else {
+          const int E = eb + ecj;
+          const uint32_t u = r[j];
+          if (E >= -1000 && E <= 990) {
+            const uint32_t hi = (u & 0x80000000u) |
+                                ((((u >> 23) & 0xffu) + (uint32_t)(896 + E)) << 20) |
+                                ((u & 0x7fffffu) >> 3);
+            v = (u << 1) == 0 ? 0.0 : __hiloint2double((int)hi, (int)(u << 29));
+          } else {
+            v = scaled_slow(u, E);
+          }
+        }
+        if (!first) v += old[j];
+        if (scale) v *= ep.alpha;
+        p[j * ld] = v;
+      }
     }
   }
 }
