@@ -6,21 +6,25 @@
 // Oishi and Rump (Numer. Algorithms 59, 2012):
 //
 //   1. every row r of op(A) (and every column n of op(B)) gets an exponent e with
-//      max |row| < 2^e, and its entries become NS = 9 balanced base-64 digits,
-//        X(r, k) = sum_i sigma_i(r, k) 2^(e_r - 6 i),   sigma_i integer, |sigma_1| <= 64,
-//        |sigma_i| <= 32 below it,
-//      exact to 2^(e_r - 54) (54 bits: every FP64 entry within 2^-1 of its row maximum is
-//      represented exactly); the digits are computed with integer arithmetic on the FP64
+//      max |row| < 2^(e - 1) (one bit of headroom), and its entries become NS = 9 balanced
+//      base-64 digits,
+//        X(r, k) = sum_i sigma_i(r, k) 2^(e_r - 6 i),   sigma_i integer, |sigma_i| <= 32,
+//      exact to 2^(e_r - 54) (every FP64 entry in the top binade of its row is represented
+//      exactly, smaller ones to 53 bits below the row maximum); the digits are computed with integer arithmetic on the FP64
 //      bit pattern (no FP64 instruction; each digit's BF16 encoding comes from one exact
 //      FP32 subtraction), and each one is an exact BF16 value;
 //   2. the digit planes are multiplied on the tensor cores (tcgen05.mma kind::f16, BF16 x
 //      BF16 -> FP32).  All products sigma_i tau_j with the same level l = i + j carry the
 //      same scale 2^(e_r + e_n - 6 l), so they share one TMEM accumulator; the 45 products
-//      with l <= NS + 1 are formed (the rest lie below 2^-54 of the row and column maxima);
-//   3. a level accumulator is an integer sum.  Its terms per k are bounded by 64 * 64
-//      (l = 2), 2 * 64 * 32 + (l - 3) * 32 * 32 (l > 2), so over a K-chunk of up to
-//      2^24 / bound(l) (4096 at l <= 3 down to 1472 at l = 10) it stays below 2^24 and FP32
-//      accumulation is exact.  After each (level, chunk) the epilogue warps add the
+//      with l <= NS + 1 are formed (the rest lie about 2^-53 below the row and column
+//      maxima);
+//   3. a level accumulator is an integer sum.  Its terms per k are bounded by
+//      (l - 1) * 32 * 32, so over a K-chunk of up to 2^24 / bound(l) (16384 at l = 2 down
+//      to 1820 at l = 10) it stays below 2^24 and FP32 accumulation is exact.  A level's K
+//      range is cut into equal chunks of at most that length.  The one bit of headroom in
+//      the exponent keeps every digit, the leading one included, within 32, which makes
+//      these chunks up to 4x longer than with a leading digit of 64 (fewer epilogue
+//      passes).  After each (level, chunk) the epilogue warps add the
 //      accumulator, scaled by 2^(e_r + e_n - 6 l) (built in the FP64 exponent field with
 //      integer operations), into the FP64 output.
 //
@@ -106,7 +110,7 @@ __device__ __forceinline__ uint64_t src_bits(const SliceSrc& s, int z, int r2, i
 // Balanced digits by offset binary: with B = 32 (2^42 + 2^36 + ... + 2^0), N + B written in
 // base 64 has digit words u_i in [0, 64) below the top one, and
 //   N = (N + B) >> 48 * 2^48 + sum_{i >= 2} (u_i - 32) 2^(54 - 6 i),
-// so sigma_1 = (N + B) >> 48 (|sigma_1| <= 64 for |N| < 2^54) and sigma_i = u_i - 32 in
+// so sigma_1 = (N + B) >> 48 (|sigma_1| <= 32 for |N| < 2^53) and sigma_i = u_i - 32 in
 // [-32, 31]: one 64-bit add and bit-field extracts instead of NS rounding divisions.
 constexpr int64_t kDigitBias = 0x820820820820ll;
 static_assert(NS == 9 && SB == 6, "the digit extraction below is written for 9 digits of 6 bits");
@@ -199,9 +203,10 @@ __global__ void __launch_bounds__(256, 3) oz_digits(SliceSrc src, int rows_out, 
   const uint64_t mx = r < rows_out ? mxa[(int64_t)z * rows_out + r] : 0ull;
   const int exm = (int)(mx >> 52);
   const bool bad = exm == 0x7ff;
-  // max |row| = f 2^e with f in [0.5, 1): e = exm - 1022 for normal numbers; the
-  // subnormal exponent field 0 behaves as 1 with no implicit bit (then max < 2^-1021)
-  const int e = mx == 0 ? 0 : (exm == 0 ? -1021 : exm - 1022);
+  // max |row| = f 2^(e - 1) with f in [0.5, 1): e = exm - 1021 for normal numbers (one
+  // bit of headroom, so that |N| < 2^53 and every digit lies within 32); the subnormal
+  // exponent field 0 behaves as 1 with no implicit bit (then max < 2^-1022)
+  const int e = mx == 0 ? 0 : (exm == 0 ? -1020 : exm - 1021);
   if (blockIdx.y == 0 && part == 0 && r < rows_out) E[(int64_t)z * rows_out + r] = bad ? E_BAD : e;
   const int64_t plane_stride = (int64_t)rows_out * ldk;
   uint16_t* out = S + ((int64_t)z * NS * rows_out + r) * ldk;
@@ -274,11 +279,20 @@ struct OzEpi {
 };
 
 // K slices (of KELEMS) per exactness chunk of a level: the longest run of K over which the
-// level's integer sum stays below 2^24 (per-k bound 4096 for l <= 3, 4096 + (l - 3) 1024)
+// level's integer sum stays below 2^24 (per-k bound (l - 1) 32 32)
 __host__ __device__ constexpr int level_chunk_slices(int level) {
-  return (1 << 24) / (level <= 3 ? 4096 : 4096 + (level - 3) * 1024) / KELEMS;
+  return (1 << 24) / ((level - 1) * 32 * 32) / KELEMS;
 }
-static_assert(level_chunk_slices(2) == 64 && level_chunk_slices(10) == 23, "chunk lengths");
+static_assert(level_chunk_slices(2) == 256 && level_chunk_slices(10) == 28, "chunk lengths");
+
+// chunk ch of nch equal chunks of the K slices [k0, k1) (nch = ceil((k1 - k0) / kcs), so
+// every chunk is at most kcs long and none is a short tail)
+__device__ __forceinline__ int level_chunks(int k0, int k1, int kcs) {
+  return (k1 - k0 + kcs - 1) / kcs;
+}
+__device__ __forceinline__ int chunk_edge(int k0, int k1, int nch, int ch) {
+  return k0 + (int)((int64_t)(k1 - k0) * ch / nch);
+}
 
 // tile unit -> (mt2, nt, z): groups of GH tile rows, column by column inside a group, so the
 // clusters running at the same time share the digit planes of few A row blocks and few B
@@ -482,9 +496,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         const int n0 = min(nt * TILE + (int)rank * 128, ep.N - 1);
         for (int li = 0; li < nl && !stop; li++) {
           const int level = kOrder[ep.var][l0 + li];
-          const int kcs = level_chunk_slices(level);
-          for (int kb0 = k0; kb0 < k1 && !stop; kb0 += kcs) {
-            const int kb1 = min(kb0 + kcs, k1);
+          const int nch = level_chunks(k0, k1, level_chunk_slices(level));
+          for (int ch = 0; ch < nch && !stop; ch++) {
+            const int kb0 = chunk_edge(k0, k1, nch, ch), kb1 = chunk_edge(k0, k1, nch, ch + 1);
             for (int i = 1; i < level && !stop; i++) {
               const int za = z * NS + i - 1, zb = z * NS + (level - i) - 1;
               for (int kb = kb0; kb < kb1; kb++, it++) {
@@ -530,9 +544,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         item_of(item, u, l0, nl, k0, k1);
         for (int li = 0; li < nl && !stop; li++) {
           const int level = kOrder[ep.var][l0 + li];
-          const int kcs = level_chunk_slices(level);
-          for (int kb0 = k0; kb0 < k1 && !stop; kb0 += kcs, local++) {
-            const int kb1 = min(kb0 + kcs, k1);
+          const int nch = level_chunks(k0, k1, level_chunk_slices(level));
+          for (int ch = 0; ch < nch && !stop; ch++, local++) {
+            const int kb0 = chunk_edge(k0, k1, nch, ch), kb1 = chunk_edge(k0, k1, nch, ch + 1);
             const int buf = local & 1;
             const uint32_t use = (uint32_t)(local >> 1);
             if (!mbar_wait(smem_u32(&acc_empty[buf]), (use & 1) ^ 1, abort_flag, ep.err)) {
@@ -577,8 +591,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       double* wtile = ep.split > 1 || ep.mh < 0 ? ep.C + (int64_t)item * TILE * TILE : nullptr;
       for (int li = 0; li < nl && !stop; li++) {
         const int level = kOrder[ep.var][l0 + li];
-        const int kcs = level_chunk_slices(level);
-        for (int kb0 = k0; kb0 < k1; kb0 += kcs, local++) {
+        const int nch = level_chunks(k0, k1, level_chunk_slices(level));
+        for (int ch = 0; ch < nch; ch++, local++) {
           const int buf = local & 1;
           const uint32_t use = (uint32_t)(local >> 1);
           const bool ok = mbar_wait(smem_u32(&acc_full[buf]), use & 1, abort_flag, ep.err);
@@ -588,8 +602,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           }
           tc_fence_after();
           const uint32_t tbase = tmem + buf * TMEM_COLS + ((uint32_t)(32 * q) << 16);
-          const bool first = li == 0 && kb0 == k0;
-          const bool lastg = li == nl - 1 && kb0 + kcs >= k1;
+          const bool first = li == 0 && ch == 0;
+          const bool lastg = li == nl - 1 && ch == nch - 1;
           if (wtile)
             drain<true>(tbase, row, rloc, nt * TILE, z, level, first, lastg, ep, wtile);
           else

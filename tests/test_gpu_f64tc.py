@@ -86,9 +86,9 @@ def test_gemm_alpha_beta_and_small_tile_counts(tc_handle, cplx):
 
 
 def test_gemm_exact_on_integer_grids(tc_handle):
-    """Entries j/64 with |j| <= 63 and all of one sign: every digit sum reaches its largest
-    size, the exact product is a multiple of 2^-12 below 2^12, representable in FP64, and
-    the tensor-core result must equal it bit for bit."""
+    """Entries j/64 with |j| <= 63 and all of one sign: the digit sums grow as large as
+    same-sign entries make them, the exact product is a multiple of 2^-12 below 2^12,
+    representable in FP64, and the tensor-core result must equal it bit for bit."""
     rng = np.random.default_rng(3)
     m, n, k = 768, 640, 2048
     A = rng.integers(1, 64, size=(m, k)) / 64.0
