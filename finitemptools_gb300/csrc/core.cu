@@ -347,6 +347,7 @@ int fmpt_destroy(fmpt_handle* h) {
   if (h->lanczos_exec) cudaGraphExecDestroy(h->lanczos_exec);
   for (auto& kv : h->arnoldi_exec) cudaGraphExecDestroy(kv.second);
   if (h->gemm_ws) cudaFree(h->gemm_ws);
+  if (h->gemm_cnt) cudaFree(h->gemm_cnt);
   if (h->tc_ws) cudaFree(h->tc_ws);
   if (h->oz_ws) cudaFree(h->oz_ws);
   if (h->gstatus) cudaFree(h->gstatus);

@@ -2,12 +2,16 @@
 //
 // GB300's FP64 rate is small (about 2 DFMA per clock per SM), so this kernel
 // is FP64-pipe bound for every shape that matters, and what decides its speed
-// is how many SMs it keeps busy.  Large problems use a 64x64 tile with a 4x4
-// register block per thread.  Small ones (the D <= 128 contractions of TDVP
-// and of the first DMRG bonds) use 32x32 tiles and, when that still leaves
-// SMs idle, split K over the grid: every split writes its partial product to
-// a workspace and a second kernel sums the splits in a fixed order (so the
-// result does not depend on scheduling) and applies alpha/beta.
+// is how evenly it spreads the multiply-adds over the SMs.  Large problems use a
+// 64x64 tile with a 4x4 register block per thread.  Small ones (the D <= 128
+// contractions of TDVP and of the first DMRG bonds) use 32x32 or 16x16 tiles
+// and may split K over the grid; a cost model picks the tile and the split that
+// put the fewest multiply-adds on the busiest SM.  Every split writes its
+// partial product to a workspace; the last split of a tile to finish (an atomic
+// count per tile) sums the tile's partials in split order, so the result does
+// not depend on scheduling, applies alpha/beta and resets the count.  Where no
+// count is available (a stream capture before the counts exist) a second kernel
+// does the same sum.
 #include "internal.h"
 
 namespace fmpt {
@@ -25,7 +29,8 @@ __device__ __forceinline__ int64_t a_index(int t, int r, int c, int64_t ld) {
 // product goes to ws + split * plane_ws (re, then im plane at + m*n).
 template <bool CPLX, int BMN>
 __global__ void __launch_bounds__(NT) gemm_kernel(GemmArgs g, int splits, int kchunk,
-                                                  double* __restrict__ ws) {
+                                                  double* __restrict__ ws,
+                                                  int* __restrict__ tile_cnt) {
   constexpr int TPR = BMN / 16;                // outputs per thread along each dimension
   __shared__ double As[2][BK][BMN + 1];
   __shared__ double Bs[2][BK][BMN + 1];
@@ -118,6 +123,55 @@ __global__ void __launch_bounds__(NT) gemm_kernel(GemmArgs g, int splits, int kc
         if (CPLX) W[mn + idx] = acci[i][j];
       }
     }
+    if (!tile_cnt) return;                 // the reduction kernel sums the splits
+    // the last split of this tile to arrive sums the partials in split order
+    __shared__ int s_last;
+    __threadfence();
+    __syncthreads();
+    const int tile = (blockIdx.y * gridDim.x + blockIdx.x) + (int)(gridDim.x * gridDim.y) * zb;
+    if (tid == 0) {
+      const int prev = atomicAdd(tile_cnt + tile, 1);
+      s_last = prev == splits - 1;
+      if (s_last) tile_cnt[tile] = 0;      // ready for the next launch (stream order)
+    }
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    const bool has_beta = (g.beta[0] != 0.0 || g.beta[1] != 0.0);
+    double* C = g.C + zb * g.strideC;
+#pragma unroll
+    for (int i = 0; i < TPR; i++) {
+      const int gm = m0 + tx + 16 * i;
+      if (gm >= g.m) continue;
+#pragma unroll
+      for (int j = 0; j < TPR; j++) {
+        const int gn = n0 + ty + 16 * j;
+        if (gn >= g.n) continue;
+        const int64_t t = (int64_t)gm + (int64_t)gn * g.m;
+        double sr = 0.0, si = 0.0;
+        for (int q = 0; q < splits; q++) {
+          const double* Wq = ws + (int64_t)q * mn * (CPLX ? 2 : 1);
+          sr += __ldcg(Wq + t);
+          if (CPLX) si += __ldcg(Wq + mn + t);
+        }
+        const int64_t idx = (int64_t)gm + (int64_t)gn * g.ldc;
+        if (CPLX) {
+          double r = g.alpha[0] * sr - g.alpha[1] * si;
+          double im = g.alpha[0] * si + g.alpha[1] * sr;
+          if (has_beta) {
+            const double cr = C[idx], ci = C[g.planeC + idx];
+            r += g.beta[0] * cr - g.beta[1] * ci;
+            im += g.beta[0] * ci + g.beta[1] * cr;
+          }
+          C[idx] = r;
+          C[g.planeC + idx] = im;
+        } else {
+          double r = g.alpha[0] * sr;
+          if (has_beta) r += g.beta[0] * C[idx];
+          C[idx] = r;
+        }
+      }
+    }
     return;
   }
   double* C = g.C + zb * g.strideC;
@@ -183,21 +237,34 @@ __global__ void split_reduce(GemmArgs g, int splits, const double* __restrict__ 
   }
 }
 
+// Per-tile split counters (zeroed once, left zero by every launch): enough for any grid
+// the cost model below may choose with a split.
+constexpr int kMaxSplitTiles = 1 << 14;
+
 template <bool CPLX>
 int launch(fmpt_handle* h, const GemmArgs& g) {
   const int sms = h->sm_count > 0 ? h->sm_count : 1;
-  const int64_t want = 2LL * sms;                      // blocks that keep every SM busy
-  auto tiles = [&](int bmn) {
-    return (int64_t)((g.m + bmn - 1) / bmn) * ((g.n + bmn - 1) / bmn) * g.batch;
-  };
-  int bmn = 64;
-  if (tiles(64) < want) bmn = 32;
-  int splits = 1;
-  const int64_t t = tiles(bmn);
-  if (t < want && g.batch == 1 && g.k >= 4 * BK && !g.nosplit) {
-    const int64_t by_grid = (want + t - 1) / t;
-    const int64_t by_k = g.k / (2 * BK);               // at least 16 k per split
-    splits = (int)std::max<int64_t>(1, std::min<int64_t>(std::min(by_grid, by_k), 64));
+  // (tile edge, splits) with the fewest multiply-adds on the busiest SM; a split adds the
+  // partials' round trip, priced as that many multiply-adds
+  const double cm = CPLX ? 4.0 : 1.0;
+  int bmn = 64, splits = 1;
+  double best = 1e300;
+  for (int e : {64, 32, 16}) {
+    const int64_t t = (int64_t)((g.m + e - 1) / e) * ((g.n + e - 1) / e) * g.batch;
+    for (int s = 1; s <= 64; s *= 2) {
+      if (s > 1 && (g.batch != 1 || g.nosplit || g.k < 4 * BK || g.k / s < 2 * BK)) break;
+      const int kc = s > 1 ? ((g.k + s - 1) / s + BK - 1) / BK * BK : g.k;
+      const int64_t blocks = t * ((g.k + kc - 1) / kc);
+      const int64_t per_sm = (blocks + sms - 1) / sms;
+      double cost = (double)per_sm * e * e * kc * cm;
+      if (s > 1) cost += 2.0e4 * cm + (double)s * e * e * cm * 4.0;
+      if (e == 16) cost *= 1.15;               // one output per thread: more loads per FMA
+      if (cost < best * 0.98) {
+        best = cost;
+        bmn = e;
+        splits = s;
+      }
+    }
   }
   const int kchunk = splits > 1 ? ((g.k + splits - 1) / splits + BK - 1) / BK * BK : g.k;
   if (splits > 1) splits = (g.k + kchunk - 1) / kchunk;
@@ -207,18 +274,32 @@ int launch(fmpt_handle* h, const GemmArgs& g) {
                      grid.z);
   // the split partials live in the handle's workspace (reused in stream order)
   double* ws = nullptr;
+  int* cnt = nullptr;
   if (splits > 1) {
     FMPT_TRY(grow_buffer(h, &h->gemm_ws, &h->gemm_ws_bytes,
                          (size_t)splits * g.m * g.n * sizeof(double) * (CPLX ? 2 : 1)));
     ws = static_cast<double*>(h->gemm_ws);
+    if ((int64_t)grid.x * grid.y * g.batch <= kMaxSplitTiles) {
+      cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+      if (!h->gemm_cnt && cudaStreamIsCapturing(h->stream, &cs) == cudaSuccess &&
+          cs == cudaStreamCaptureStatusNone) {
+        // created outside a stream capture only; inside one the reduction kernel runs
+        FMPT_TRY(grow_buffer(h, &h->gemm_cnt, &h->gemm_cnt_bytes, kMaxSplitTiles * sizeof(int)));
+        FMPT_CUDA(h, cudaMemsetAsync(h->gemm_cnt, 0, kMaxSplitTiles * sizeof(int), h->stream));
+      }
+      cudaGetLastError();
+      cnt = static_cast<int*>(h->gemm_cnt);
+    }
   }
   ProfScope prof(h, FMPT_K_F64_GEMM);
   if (bmn == 64)
-    gemm_kernel<CPLX, 64><<<grid, NT, 0, h->stream>>>(g, splits, kchunk, ws);
+    gemm_kernel<CPLX, 64><<<grid, NT, 0, h->stream>>>(g, splits, kchunk, ws, cnt);
+  else if (bmn == 32)
+    gemm_kernel<CPLX, 32><<<grid, NT, 0, h->stream>>>(g, splits, kchunk, ws, cnt);
   else
-    gemm_kernel<CPLX, 32><<<grid, NT, 0, h->stream>>>(g, splits, kchunk, ws);
+    gemm_kernel<CPLX, 16><<<grid, NT, 0, h->stream>>>(g, splits, kchunk, ws, cnt);
   FMPT_LAUNCHED(h);
-  if (splits > 1) {
+  if (splits > 1 && !cnt) {
     const int64_t mn = (int64_t)g.m * g.n;
     const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((mn + 255) / 256, 4LL * sms));
     split_reduce<CPLX><<<blocks, 256, 0, h->stream>>>(g, splits, ws);

@@ -48,6 +48,9 @@ struct fmpt_handle {
   // reuse on h->stream)
   void* gemm_ws = nullptr;
   size_t gemm_ws_bytes = 0;
+  // per-tile arrival counts of the split FP64 GEMM (zero between launches)
+  void* gemm_cnt = nullptr;
+  size_t gemm_cnt_bytes = 0;
   // partial tiles and arrival counters of the BF16 pair GEMM's K-split last round
   void* tc_ws = nullptr;
   size_t tc_ws_bytes = 0;
