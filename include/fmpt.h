@@ -54,11 +54,13 @@ enum fmpt_dtype { FMPT_F64 = 0, FMPT_C128 = 1 };
  * FP64 is the plain form (CUDA-core FMA, or the handle's FP64 engine, see
  * fmpt_set_f64_engine).  FP64_TC is the same FP64 contraction with every GEMM
  * large enough to gain run on the BF16 tensor cores by the Ozaki scheme: each
- * FP64 operand row becomes 8 exact base-64 digit planes, the 36 digit products
- * up to 48 bits run as tcgen05 MMAs whose FP32 sums are exact, and the partial
- * results are added in FP64 (Frobenius-relative error ~1e-14 on random data,
- * the accuracy class of an FP64 GEMM).  TF32, 3xTF32 and BF16 run on tcgen05
- * with FP32 accumulation (3xTF32 = hi/lo split products). */
+ * FP64 operand row becomes 9 exact base-64 digit planes (every digit within 32,
+ * 53 bits below the row maximum), the 45 digit products of levels up to 10 run
+ * as tcgen05 MMAs whose FP32 sums over each K chunk are exact, and the level
+ * sums are added in FP64 (Frobenius-relative error 1e-15 to 4e-15 against the
+ * FP64 kernel on random data, the accuracy class of an FP64 GEMM).  TF32,
+ * 3xTF32 and BF16 run on tcgen05 with FP32 accumulation (3xTF32 = hi/lo split
+ * products). */
 enum fmpt_precision {
   FMPT_PREC_FP64 = 0,
   FMPT_PREC_TF32X3 = 1,
