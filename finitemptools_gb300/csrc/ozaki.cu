@@ -264,6 +264,163 @@ __global__ void __launch_bounds__(256, 3) oz_digits(SliceSrc src, int rows_out, 
   }
 }
 
+// ------------------------------------------------------------ fast slicing of real operands
+// Real operands whose row or K index has unit stride (with 16-byte aligned rows or columns)
+// take these kernels instead of the generic ones above: 16-byte loads, eight independent
+// loads in flight per thread and no shared-memory staging for the row maxima, the digits
+// of a K-contiguous operand straight from registers.  The generic kernels are bound by
+// memory latency (long-scoreboard stalls, 22-37% of DRAM bandwidth).
+constexpr int RM_KCH = 128;           // K columns per block, row-contiguous row maxima
+constexpr int RK_KCH = 1024;          // K columns per block, K-contiguous row maxima
+
+// rows r, r + 1 of a row-contiguous operand (element (r, c) at p[r + c ld])
+__global__ void __launch_bounds__(256) oz_rowmax_rowfast(const double* __restrict__ p, int64_t ld,
+                                                         int64_t bstride, int rows, int k,
+                                                         unsigned long long* __restrict__ mx) {
+  const int z = blockIdx.z;
+  const int r = (blockIdx.x * 256 + threadIdx.x) * 2;
+  const int c0 = blockIdx.y * RM_KCH, c1 = min(c0 + RM_KCH, k);
+  if (r >= rows) return;
+  const double* b = p + (int64_t)z * bstride + r;
+  uint64_t m0 = 0, m1 = 0;
+  for (int c = c0; c < c1; c += 8) {
+    double2 v[8];
+#pragma unroll
+    for (int u = 0; u < 8; u++)
+      v[u] = c + u < c1 ? __ldg(reinterpret_cast<const double2*>(b + (int64_t)(c + u) * ld))
+                        : make_double2(0.0, 0.0);
+#pragma unroll
+    for (int u = 0; u < 8; u++) {
+      const uint64_t a0 = (uint64_t)__double_as_longlong(v[u].x) & 0x7fffffffffffffffull;
+      const uint64_t a1 = (uint64_t)__double_as_longlong(v[u].y) & 0x7fffffffffffffffull;
+      m0 = a0 > m0 ? a0 : m0;
+      m1 = a1 > m1 ? a1 : m1;
+    }
+  }
+  if (m0) atomicMax(mx + (int64_t)z * rows + r, (unsigned long long)m0);
+  if (m1) atomicMax(mx + (int64_t)z * rows + r + 1, (unsigned long long)m1);
+}
+
+// one warp per row of a K-contiguous operand (element (r, c) at p[r ld + c])
+__global__ void __launch_bounds__(256) oz_rowmax_kfast(const double* __restrict__ p, int64_t ld,
+                                                       int64_t bstride, int rows, int k,
+                                                       unsigned long long* __restrict__ mx) {
+  const int z = blockIdx.z, lane = threadIdx.x & 31;
+  const int r = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (r >= rows) return;                                   // uniform over the warp
+  const int c0 = blockIdx.y * RK_KCH, c1 = min(c0 + RK_KCH, k);
+  const double* b = p + (int64_t)z * bstride + (int64_t)r * ld;
+  uint64_t m = 0;
+  for (int c = c0 + 2 * lane; c < c1; c += 64 * 8) {
+    double2 v[8];
+#pragma unroll
+    for (int u = 0; u < 8; u++)
+      v[u] = c + 64 * u < c1 ? __ldg(reinterpret_cast<const double2*>(b + c + 64 * u))
+                             : make_double2(0.0, 0.0);
+#pragma unroll
+    for (int u = 0; u < 8; u++) {
+      const uint64_t a0 = (uint64_t)__double_as_longlong(v[u].x) & 0x7fffffffffffffffull;
+      const uint64_t a1 = (uint64_t)__double_as_longlong(v[u].y) & 0x7fffffffffffffffull;
+      m = a0 > m ? a0 : m;
+      m = a1 > m ? a1 : m;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const uint64_t y = __shfl_xor_sync(0xffffffffu, m, o);
+    m = y > m ? y : m;
+  }
+  if (lane == 0 && m) atomicMax(mx + (int64_t)z * rows + r, (unsigned long long)m);
+}
+
+// exponent of a row from its maximum's bit pattern (as oz_digits): e, and whether the row
+// holds Inf/NaN
+__device__ __forceinline__ int row_exponent(uint64_t mx, bool& bad) {
+  const int exm = (int)(mx >> 52);
+  bad = exm == 0x7ff;
+  return mx == 0 ? 0 : (exm == 0 ? -1020 : exm - 1021);
+}
+
+// the NS digit planes of 8 consecutive K entries of one row: 16-byte stores at out + cb
+__device__ __forceinline__ void slice8_store(const uint64_t (&bits8)[8], int e, bool bad,
+                                             uint16_t* __restrict__ out, int64_t plane_stride,
+                                             int cb) {
+  uint64_t Mo[8];
+#pragma unroll
+  for (int q = 0; q < 8; q++) {
+    const uint64_t bits = bad ? 0ull : bits8[q];
+    const int ex = (int)((bits >> 52) & 0x7ff);
+    int64_t N = (int64_t)(bits & 0xfffffffffffffull);
+    if (ex) N |= (int64_t)1 << 52;
+    const int sh = (ex ? ex : 1) - 1021 - e;
+    if (sh >= 0) N <<= sh;
+    else N = sh <= -63 ? 0 : (N >> (-sh));
+    if (bits >> 63) N = -N;
+    Mo[q] = (uint64_t)(N + kDigitBias);
+  }
+#pragma unroll
+  for (int i = 0; i < NS; i++) {
+    uint32_t fb[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      if (i == 0) {
+        const int d0 = (int)(uint32_t)(Mo[q] >> 32) >> 16;
+        fb[q] = __float_as_uint(__uint_as_float(0x4B000000u | (uint32_t)(d0 + 64)) - 8388672.0f);
+      } else {
+        const uint32_t u = (uint32_t)(Mo[q] >> (54 - SB * (i + 1))) & 63u;
+        fb[q] = __float_as_uint(__uint_as_float(0x4B000000u | u) - 8388640.0f);
+      }
+    }
+    *reinterpret_cast<uint4*>(out + i * plane_stride + cb) =
+        make_uint4(__byte_perm(fb[0], fb[1], 0x7632), __byte_perm(fb[2], fb[3], 0x7632),
+                   __byte_perm(fb[4], fb[5], 0x7632), __byte_perm(fb[6], fb[7], 0x7632));
+  }
+}
+
+// Digits of a K-contiguous operand: thread (rr, part) of a block owns row r0 + rr and, per
+// 64-column tile, the 8 entries from part * 8; two tiles' loads are in flight at once.
+__global__ void __launch_bounds__(256) oz_digits_kfast(const double* __restrict__ p, int64_t ld,
+                                                       int64_t bstride, int rows_out, int k_out,
+                                                       int ldk,
+                                                       const unsigned long long* __restrict__ mxa,
+                                                       uint16_t* __restrict__ S,
+                                                       int* __restrict__ E) {
+  const int r0 = blockIdx.x * SL_ROWS, kc0 = blockIdx.y * SL_KCH, z = blockIdx.z;
+  const int t = threadIdx.x, rr = t >> 3, part = t & 7;
+  const int r = r0 + rr;
+  if (r >= rows_out) return;
+  bool bad;
+  const int e = row_exponent(mxa[(int64_t)z * rows_out + r], bad);
+  if (blockIdx.y == 0 && part == 0) E[(int64_t)z * rows_out + r] = bad ? E_BAD : e;
+  const int64_t plane_stride = (int64_t)rows_out * ldk;
+  uint16_t* out = S + ((int64_t)z * NS * rows_out + r) * ldk;
+  const double* b = p + (int64_t)z * bstride + (int64_t)r * ld;
+  const int c1 = min(kc0 + SL_KCH, ldk);
+  for (int c0 = kc0; c0 < c1; c0 += 128) {
+    double2 v[2][4];
+#pragma unroll
+    for (int hh = 0; hh < 2; hh++)
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const int cc = c0 + 64 * hh + part * 8 + 2 * u;
+        v[hh][u] = cc < k_out ? __ldg(reinterpret_cast<const double2*>(b + cc))
+                              : make_double2(0.0, 0.0);
+      }
+#pragma unroll
+    for (int hh = 0; hh < 2; hh++) {
+      const int cb = c0 + 64 * hh + part * 8;
+      if (cb >= c1) break;
+      uint64_t bits8[8];
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        bits8[2 * u] = (uint64_t)__double_as_longlong(v[hh][u].x);
+        bits8[2 * u + 1] = (uint64_t)__double_as_longlong(v[hh][u].y);
+      }
+      slice8_store(bits8, e, bad, out, plane_stride, cb);
+    }
+  }
+}
+
 // ------------------------------------------------------------ GEMM kernel
 struct OzEpi {
   double* C;            // direct: output; split: workspace tiles [item][256 cols][256 rows]
@@ -836,18 +993,36 @@ int gemm_f64_ozaki(fmpt_handle* h, const GemmArgs& g) {
     FMPT_CUDA(h, cudaMemsetAsync(MX, 0, (size_t)batch * (M2 + N) * sizeof(uint64_t), h->stream));
     const unsigned kch = (unsigned)((ldk + SL_KCH - 1) / SL_KCH);
     const dim3 ga((M2 + SL_ROWS - 1) / SL_ROWS, kch, batch), gb((N + SL_ROWS - 1) / SL_ROWS, kch, batch);
-    if (!hitA) {
-      oz_rowmax<<<ga, 256, 0, h->stream>>>(sa, M2, K2, MX);
+    // the fast kernels need a real operand with a unit-stride index, 16-byte aligned rows
+    // or columns and an even extent along the unit-stride index
+    auto aligned = [](const SliceSrc& x, int64_t ld) {
+      return !x.cplx && (reinterpret_cast<uintptr_t>(x.p) & 15) == 0 && (ld & 1) == 0 &&
+             (x.bstride & 1) == 0;
+    };
+    auto slice = [&](const SliceSrc& x, int rows, const dim3& grid, unsigned long long* mx,
+                     uint16_t* planes, int* ex) -> int {
+      if (x.sr == 1 && aligned(x, x.sc) && (rows & 1) == 0) {
+        const dim3 g1((unsigned)((rows / 2 + 255) / 256), (unsigned)((K2 + RM_KCH - 1) / RM_KCH),
+                      (unsigned)batch);
+        oz_rowmax_rowfast<<<g1, 256, 0, h->stream>>>(x.p, x.sc, x.bstride, rows, K2, mx);
+      } else if (x.sc == 1 && aligned(x, x.sr) && (K2 & 1) == 0) {
+        const dim3 g1((unsigned)((rows + 7) / 8), (unsigned)((K2 + RK_KCH - 1) / RK_KCH),
+                      (unsigned)batch);
+        oz_rowmax_kfast<<<g1, 256, 0, h->stream>>>(x.p, x.sr, x.bstride, rows, K2, mx);
+      } else {
+        oz_rowmax<<<grid, 256, 0, h->stream>>>(x, rows, K2, mx);
+      }
       FMPT_LAUNCHED(h);
-      oz_digits<<<ga, 256, 0, h->stream>>>(sa, M2, K2, ldk, MX, SA, EA);
+      if (x.sc == 1 && aligned(x, x.sr) && (K2 & 1) == 0)
+        oz_digits_kfast<<<grid, 256, 0, h->stream>>>(x.p, x.sr, x.bstride, rows, K2, ldk, mx,
+                                                      planes, ex);
+      else
+        oz_digits<<<grid, 256, 0, h->stream>>>(x, rows, K2, ldk, mx, planes, ex);
       FMPT_LAUNCHED(h);
-    }
-    if (!hitB) {
-      oz_rowmax<<<gb, 256, 0, h->stream>>>(sb, N, K2, MX + (size_t)batch * M2);
-      FMPT_LAUNCHED(h);
-      oz_digits<<<gb, 256, 0, h->stream>>>(sb, N, K2, ldk, MX + (size_t)batch * M2, SBp, EB);
-      FMPT_LAUNCHED(h);
-    }
+      return FMPT_OK;
+    };
+    if (!hitA) FMPT_TRY(slice(sa, M2, ga, MX, SA, EA));
+    if (!hitB) FMPT_TRY(slice(sb, N, gb, MX + (size_t)batch * M2, SBp, EB));
   }
   for (int side = 0; side < 2; side++) {
     OzCache* c = side == 0 ? g.cacheA : g.cacheB;
