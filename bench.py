@@ -50,7 +50,15 @@ METRIC = "DMRG sweep s & H_eff·x TFLOP/s, mixed vs FP64 on one GB300 at ΔE≤1
 # `bench.py --steps 2 --warmup 3`, averaged over its GEMM 1 and GEMM 2)
 NCU_TRAFFIC = {("bf16", 2048): {"bytes_per_launch": (88.77e6 + 134.09e6 + 334.29e6 + 106.94e6) / 2,
                                 "gemm1_bytes": 88.77e6 + 134.09e6, "gemm2_bytes": 334.29e6 + 106.94e6,
-                                "algorithmic_operand_bytes": {"gemm1": 76.0e6, "gemm2": 210.0e6}}}
+                                "algorithmic_operand_bytes": {"gemm1": 76.0e6, "gemm2": 210.0e6}},
+               # dram__bytes_read + write of the two oz_gemm_pair launches of one application
+               # (ncu --set full, D=2048); the digit planes the GEMMs read are 0.68 GB (GEMM 1)
+               # and 1.89 GB (GEMM 2), the FP64 output tile's epilogue passes add their
+               # read-modify-write
+               ("fp64_tc", 2048): {"bytes_per_launch": (19.81e9 + 6.05e9 + 24.01e9 + 4.75e9) / 2,
+                                   "gemm1_bytes": 19.81e9 + 6.05e9, "gemm2_bytes": 24.01e9 + 4.75e9,
+                                   "algorithmic_digit_plane_bytes": {"gemm1": 0.68e9,
+                                                                     "gemm2": 1.89e9}}}
 UNIT = "TFLOP/s"
 W_MPO, D_PHYS = 5, 2
 OZ_PRODUCTS = 45          # BF16 digit products per FP64 multiply-add of the fp64_tc GEMM

@@ -421,6 +421,79 @@ __global__ void __launch_bounds__(256) oz_digits_kfast(const double* __restrict_
   }
 }
 
+// Digits of a row-contiguous operand (element (r, c) at p[r + c ld]): the 32 x 64 tiles of
+// the block's K chunk stream into a 3-stage shared-memory ring by 8-byte cp.async copies
+// (two tiles in flight, no registers held for them), and thread (rr, part) turns 8
+// consecutive K entries of row rr into one 16-byte store per digit plane.
+constexpr int DR_STAGES = 3;
+constexpr size_t DR_SMEM = (size_t)DR_STAGES * SL_ROWS * 65 * sizeof(uint64_t);
+
+__device__ __forceinline__ void cp_async8(uint64_t* dst, const double* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_u32(dst)), "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+__global__ void __launch_bounds__(256) oz_digits_rowfast(const double* __restrict__ p, int64_t ld,
+                                                         int64_t bstride, int rows_out,
+                                                         int k_out, int ldk,
+                                                         const unsigned long long* __restrict__ mxa,
+                                                         uint16_t* __restrict__ S,
+                                                         int* __restrict__ E) {
+  extern __shared__ __align__(16) uint64_t dr_smem[];
+  auto tile = [&](int st, int lr, int lc) -> uint64_t& {
+    return dr_smem[((size_t)st * SL_ROWS + lr) * 65 + lc];
+  };
+  const int r0 = blockIdx.x * SL_ROWS, kc0 = blockIdx.y * SL_KCH, z = blockIdx.z;
+  const int t = threadIdx.x, rr = t >> 3, part = t & 7;
+  const int r = r0 + rr;
+  bool bad = false;
+  const int e = r < rows_out ? row_exponent(mxa[(int64_t)z * rows_out + r], bad) : 0;
+  if (blockIdx.y == 0 && part == 0 && r < rows_out) E[(int64_t)z * rows_out + r] = bad ? E_BAD : e;
+  const int64_t plane_stride = (int64_t)rows_out * ldk;
+  uint16_t* out = S + ((int64_t)z * NS * rows_out + r) * ldk;
+  const double* b = p + (int64_t)z * bstride;
+  const int c1 = min(kc0 + SL_KCH, ldk);
+  const int ntile = (c1 - kc0 + 63) / 64;
+  // tile j of the chunk into stage j % DR_STAGES: lanes run along rows (contiguous)
+  auto issue = [&](int j) {
+    if (j < ntile) {
+      const int c0 = kc0 + 64 * j, st = j % DR_STAGES;
+#pragma unroll
+      for (int q = 0; q < 8; q++) {
+        const int e2 = t + 256 * q, lr = e2 & 31, lc = e2 >> 5;
+        const int rg = r0 + lr, cg = c0 + lc;
+        if (rg < rows_out && cg < k_out)
+          cp_async8(&tile(st, lr, lc), b + rg + (int64_t)cg * ld);
+        else
+          tile(st, lr, lc) = 0ull;
+      }
+    }
+    cp_async_commit();                      // one group per tile slot (empty past the end)
+  };
+  issue(0);
+  issue(1);
+  for (int j = 0; j < ntile; j++) {
+    issue(j + 2);
+    cp_async_wait<2>();                     // this thread's copies of tile j have landed
+    __syncthreads();                        // and every thread's
+    const int cb = kc0 + 64 * j + part * 8;
+    if (r < rows_out && cb < c1) {
+      uint64_t bits8[8];
+#pragma unroll
+      for (int q = 0; q < 8; q++) bits8[q] = tile(j % DR_STAGES, rr, part * 8 + q);
+      slice8_store(bits8, e, bad, out, plane_stride, cb);
+    }
+    __syncthreads();                        // stage j % 3 is refilled by issue(j + 3)
+  }
+}
+
 // ------------------------------------------------------------ GEMM kernel
 struct OzEpi {
   double* C;            // direct: output; split: workspace tiles [item][256 cols][256 rows]
@@ -931,6 +1004,8 @@ int gemm_f64_ozaki(fmpt_handle* h, const GemmArgs& g) {
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   if (clusters < 0) {
+    FMPT_CUDA(h, cudaFuncSetAttribute(oz_digits_rowfast,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DR_SMEM));
     FMPT_CUDA(h, cudaFuncSetAttribute(oz_gemm_pair, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM));
     cfg.gridDim = dim3(2 * std::max(1, h->sm_count / 2));
     int n = 0;
@@ -1016,6 +1091,9 @@ int gemm_f64_ozaki(fmpt_handle* h, const GemmArgs& g) {
       if (x.sc == 1 && aligned(x, x.sr) && (K2 & 1) == 0)
         oz_digits_kfast<<<grid, 256, 0, h->stream>>>(x.p, x.sr, x.bstride, rows, K2, ldk, mx,
                                                       planes, ex);
+      else if (x.sr == 1 && !x.cplx)
+        oz_digits_rowfast<<<grid, 256, DR_SMEM, h->stream>>>(x.p, x.sc, x.bstride, rows, K2,
+                                                              ldk, mx, planes, ex);
       else
         oz_digits<<<grid, 256, 0, h->stream>>>(x, rows, K2, ldk, mx, planes, ex);
       FMPT_LAUNCHED(h);
