@@ -363,7 +363,8 @@ uint64_t fmpt_graph_launch_count(fmpt_handle* h) { return h ? h->graph_launches 
 
 int fmpt_set_tuning(fmpt_handle* h, int mode) {
   if (!h) return FMPT_ERR_ARG;
-  if (mode < 0 || mode > 2) return fmpt::set_error(h, FMPT_ERR_ARG, "tuning mode must be 0, 1 or 2");
+  if (mode < 0 || mode > 4)
+    return fmpt::set_error(h, FMPT_ERR_ARG, "tuning mode must be 0, 1, 2, 3 or 4");
   h->tune_mode = mode;
   return FMPT_OK;
 }

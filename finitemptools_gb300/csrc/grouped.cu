@@ -29,7 +29,13 @@ namespace fmpt {
 namespace {
 
 constexpr int GK = 8, GNT = 256;
-constexpr int kTile[GP_VARIANTS] = {32, 64};   // tile edge of each kernel variant
+constexpr int kTile[2] = {32, 64};   // tile edge of kernel v & 1
+// Schedules (v >> 1), the order in which the CTAs pull a phase's tiles:
+//   0: blocks by descending work (sum of their segments' k), each block's tiles together;
+//   1: tiles by descending work of their own (block work x the tile's 16-wide groups), so
+//      that the narrow edge tiles of large blocks fall to the end of the phase.
+// The schedule decides only which CTA runs a tile and when; every output tile sums its
+// segments and k in the same order, so no variant changes a result.
 constexpr uint64_t kBarrierTimeoutNs = 2000000000ull;
 
 struct GKArgs {
@@ -242,10 +248,11 @@ __global__ void __launch_bounds__(GNT) grouped_kernel(const GKArgs a) {
   }
 }
 
-int g_occupancy[GP_VARIANTS] = {0, 0};
+int g_occupancy[2] = {0, 0};
 std::mutex g_occ_mu;
 
-int kernel_occupancy(fmpt_handle* h, int v) {
+int kernel_occupancy(fmpt_handle* h, int variant) {
+  const int v = variant & 1;
   std::lock_guard<std::mutex> lock(g_occ_mu);
   if (g_occupancy[v] == 0) {
     int occ = 0;
@@ -348,9 +355,9 @@ int gp_finalize(fmpt_handle* h, GroupedProgram& g) {
   FMPT_TRY(validate(h, g));
   g.tile_prob.clear();
   g.tile_mn.clear();
-  int max_tiles[GP_VARIANTS] = {0, 0};
+  int max_tiles[GP_VARIANTS] = {0, 0, 0, 0};
   for (int v = 0; v < GP_VARIANTS; v++) {
-    const int GT = kTile[v];
+    const int GT = kTile[v & 1], sched = v >> 1;
     g.vtile0[v].assign(g.phases.size(), 0);
     g.vtile1[v].assign(g.phases.size(), 0);
     for (size_t ph = 0; ph < g.phases.size(); ph++) {
@@ -367,6 +374,8 @@ int gp_finalize(fmpt_handle* h, GroupedProgram& g) {
       std::stable_sort(order.begin(), order.end(),
                        [&](int x, int y) { return cost[x - p0] > cost[y - p0]; });
       g.vtile0[v][ph] = (int)g.tile_prob.size();
+      const size_t first = g.tile_prob.size();
+      std::vector<int64_t> tcost;            // schedule 1: work of each emitted tile
       for (int i : order) {
         const GProblem& p = g.probs[i];
         if (p.m <= 0 || p.n <= 0) continue;
@@ -382,7 +391,22 @@ int gp_finalize(fmpt_handle* h, GroupedProgram& g) {
             const int nj = gemm ? std::min(TPR, g16n - b) : TPR;
             g.tile_prob.push_back(i);
             g.tile_mn.push_back((int)tile_word(a, b, mi, nj));
+            tcost.push_back(cost[i - p0] * mi * nj);
           }
+      }
+      if (sched == 1) {
+        const size_t nt = g.tile_prob.size() - first;
+        std::vector<size_t> idx(nt);
+        std::iota(idx.begin(), idx.end(), (size_t)0);
+        std::stable_sort(idx.begin(), idx.end(),
+                         [&](size_t x, size_t y) { return tcost[x] > tcost[y]; });
+        std::vector<int> tp(nt), tm(nt);
+        for (size_t q = 0; q < nt; q++) {
+          tp[q] = g.tile_prob[first + idx[q]];
+          tm[q] = g.tile_mn[first + idx[q]];
+        }
+        std::copy(tp.begin(), tp.end(), g.tile_prob.begin() + first);
+        std::copy(tm.begin(), tm.end(), g.tile_mn.begin() + first);
       }
       g.vtile1[v][ph] = (int)g.tile_prob.size();
       max_tiles[v] = std::max(max_tiles[v], g.vtile1[v][ph] - g.vtile0[v][ph]);
@@ -430,7 +454,7 @@ int gp_finalize(fmpt_handle* h, GroupedProgram& g) {
 }
 
 int gp_autotune(fmpt_handle* h, GroupedProgram& g, double* const* slots, int nslots, int kind) {
-  if (h->tune_mode == 1 || h->tune_mode == 2) {
+  if (h->tune_mode >= 1 && h->tune_mode <= GP_VARIANTS) {
     g.variant = h->tune_mode - 1;
     return FMPT_OK;
   }
@@ -548,7 +572,7 @@ int gp_run(fmpt_handle* h, const GroupedProgram& g, double* const* slots, int ns
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  if (v == 0)
+  if ((v & 1) == 0)
     FMPT_CUDA(h, cudaLaunchKernelEx(&cfg, grouped_kernel<32>, a));
   else
     FMPT_CUDA(h, cudaLaunchKernelEx(&cfg, grouped_kernel<64>, a));

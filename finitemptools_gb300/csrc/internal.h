@@ -223,7 +223,7 @@ int schedule_env(fmpt_handle* h, int cplx, const double* W, int d, int wl, int w
 
 // -------- grouped persistent block-sparse engine (grouped.cu)
 constexpr int GP_MAX_PHASES = 4, GP_SLOTS = 8;
-constexpr int GP_VARIANTS = 2;   // kernel variants: 32x32 and 64x64 output tiles
+constexpr int GP_VARIANTS = 4;   // (tile, schedule): v & 1 -> 32x32 / 64x64 tiles, v >> 1 -> schedule
 enum { GP_GEMM = 0, GP_SUM = 1 };
 // One output block: C (m x n, column-major with ldc) at c_off in the phase's C slot.
 struct GProblem {
@@ -246,7 +246,7 @@ struct GroupedProgram {
   std::vector<GSegment> segs;
   std::vector<int> tile_prob, tile_mn;           // the tiles of every variant, one after another
   std::vector<int> vtile0[GP_VARIANTS], vtile1[GP_VARIANTS];   // per variant and phase
-  int vgrid[GP_VARIANTS] = {0, 0};
+  int vgrid[GP_VARIANTS] = {0, 0, 0, 0};
   int variant = 0;                                // the one gp_run launches by default
   double flops = 0.0;       // 2 m n k over the GEMM segments
   double sum_elems = 0.0;   // output elements x terms of the SUM phases

@@ -572,7 +572,7 @@ int fmpt_u1_op_ac2(fmpt_handle* h, int dtype, const double* W1, const double* W2
 
 int fmpt_op_tile(fmpt_op* op) {
   if (!op || !op->u1) return 0;
-  return static_cast<U1OpState*>(op->u1)->prog.variant == 0 ? 32 : 64;
+  return (static_cast<U1OpState*>(op->u1)->prog.variant & 1) == 0 ? 32 : 64;
 }
 
 int fmpt_op_flops(fmpt_op* op, double* flops) {

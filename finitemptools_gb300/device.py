@@ -76,7 +76,9 @@ class Handle:
         return int(lib().fmpt_graph_launch_count(self.ptr))
 
     def set_tuning(self, mode=0):
-        """Grouped-kernel tile choice: 0 autotune (default), 1 force 32x32, 2 force 64x64."""
+        """Grouped-kernel variant choice: 0 autotune over tiles and block schedules (default),
+        1 / 2 force 32x32 / 64x64 tiles with the blocks-by-work schedule, 3 / 4 the same tiles
+        with the tiles-by-work schedule."""
         self.check(lib().fmpt_set_tuning(self.ptr, int(mode)))
 
     def tuning_info(self):

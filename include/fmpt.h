@@ -108,13 +108,15 @@ int fmpt_set_fused_krylov(fmpt_handle* h, int on);
  * rounding); off, or outside that range, cuSOLVER geqrf + ungqr.  No
  * counterpart in the reference. */
 int fmpt_set_cluster_qr(fmpt_handle* h, int on);
-/* Tile autotuner of the grouped block-sparse kernel.  mode 0 (default): the
- * first time a block-sparse operator or environment update of a new work size
- * (kind, half-octave of FLOPs) is built, every kernel variant (32x32 and 64x64
- * output tiles) is timed on it and the fastest is cached in the handle;
- * mode 1 / 2 force the 32x32 / 64x64 tile.  All variants sum every output in
- * the same order: the choice never changes results.  No counterpart in the
- * reference. */
+/* Autotuner of the grouped block-sparse kernel.  mode 0 (default): the first
+ * time a block-sparse operator or environment update of a new work size (kind,
+ * half-octave of FLOPs) is built, every kernel variant -- 32x32 or 64x64 output
+ * tiles, each with two block schedules (blocks by descending work, or tiles by
+ * descending work of their own) -- is timed on it and the fastest is cached in
+ * the handle; mode 1 / 2 force the 32x32 / 64x64 tile with the first schedule,
+ * mode 3 / 4 the same tiles with the second.
+ * All variants sum every output in the same order: the choice never changes
+ * results.  No counterpart in the reference. */
 int fmpt_set_tuning(fmpt_handle* h, int mode);
 /* Output tile of the tensor-core GEMMs (BF16, TF32, 3xTF32).  mode 0 (default):
  * GEMMs of more than 128 rows run 256x256 tiles on two-CTA clusters

@@ -69,9 +69,10 @@ def test_u1_ac2_apply(L, N, D, site):
 
 @pytest.mark.parametrize("L,N,D,site", [(10, 5, 20, 5), (16, 8, 96, 8), (24, 12, 300, 12)])
 def test_u1_tile_variants_identical(L, N, D, site):
-    """Both grouped-kernel tile variants (32x32, 64x64) sum every output in the
-    same order: forced either way, H_eff*x and the environment update agree
-    bit for bit; the autotuner caches a decision for large programs."""
+    """Every grouped-kernel variant (32x32 or 64x64 tiles, each with both block
+    schedules) sums every output in the same order: forced any way, H_eff*x and the
+    environment update agree bit for bit; the autotuner caches a decision for large
+    programs."""
     Ws, qw, mps, legs, Lm, Rm = _bond(L, N, D, site, 5 * L + D)
     Vl, Vm, Vr = legs[site - 1], legs[site], legs[site + 1]
     W1, W2 = Ws[site - 1], Ws[site]
@@ -82,7 +83,7 @@ def test_u1_tile_variants_identical(L, N, D, site):
     h = dL.h
     ys, es = [], []
     try:
-        for mode, tile in ((1, 32), (2, 64)):
+        for mode, tile in ((1, 32), (2, 64), (3, 32), (4, 64)):
             h.set_tuning(mode)
             op = fm.U1HeffOp(dL, dR, W1, W2, sp(Vl), sp(Vr), QP, QP, qw[site - 1], qw[site],
                              qw[site + 1])
@@ -98,8 +99,8 @@ def test_u1_tile_variants_identical(L, N, D, site):
             assert h.tuning_info()[0] >= 1
     finally:
         h.set_tuning(0)
-    assert np.array_equal(ys[0], ys[1]) and np.array_equal(y_auto, ys[0])
-    assert np.array_equal(es[0], es[1])
+    assert all(np.array_equal(ys[0], y) for y in ys[1:]) and np.array_equal(y_auto, ys[0])
+    assert all(np.array_equal(es[0], e) for e in es[1:])
     assert rel(ys[0], OU.pack2(O.ac2_prime(X, W1, W2, Lm, Rm), Vl, Vr, list(QP), list(QP))) < 1e-13
 
 
