@@ -81,7 +81,9 @@ __device__ bool grid_barrier(const GKArgs& a, int target, int* s_flag) {
     atomicAdd(bar, 1);
     int ok = 1;
     const uint64_t t0 = global_ns();
-    while (ld_acquire(bar) < target + a.hold) {
+    // the count alone is polled; every 32nd poll also looks at the abort flag and the clock
+    for (unsigned polls = 1; ld_acquire(bar) < target + a.hold; polls++) {
+      if ((polls & 31u) != 0) continue;
       if (ld_acquire(abort_flag)) { ok = 0; break; }
       if (global_ns() - t0 > a.wait_ns) {
         atomicExch(abort_flag, 1);
@@ -89,7 +91,6 @@ __device__ bool grid_barrier(const GKArgs& a, int target, int* s_flag) {
         ok = 0;
         break;
       }
-      __nanosleep(128);
     }
     __threadfence();
     *s_flag = ok;

@@ -391,9 +391,11 @@ __device__ bool coop_barrier(const CoopBar& b, int target) {
     atomicAdd(b.count, 1);
     int ok = 1;
     const uint64_t t0 = now_ns();
-    while (ld_acquire_i(b.count) < target + b.hold) {
-      // this launch gave up, or an earlier one of the same solve did (the status word
-      // stays set until the host reads it)
+    // the count alone is polled; every 32nd poll also looks at the abort flag, the status
+    // word (this launch gave up, or an earlier one of the same solve did: the word stays
+    // set until the host reads it) and the clock
+    for (unsigned polls = 1; ld_acquire_i(b.count) < target + b.hold; polls++) {
+      if ((polls & 31u) != 0) continue;
       if (ld_acquire_i(b.abort_flag) || ld_acquire_i(b.status)) { ok = 0; break; }
       if (now_ns() - t0 > b.wait_ns) {
         atomicExch(b.abort_flag, 1);
@@ -401,7 +403,6 @@ __device__ bool coop_barrier(const CoopBar& b, int target) {
         ok = 0;
         break;
       }
-      __nanosleep(64);
     }
     __threadfence();
     ok_s = ok;
