@@ -856,6 +856,46 @@ def ed_heff_case(args):
                       "tflops": flops / (ms / 1e3) / 1e12}), flush=True)
 
 
+def krylov_exp_case(args):
+    """One Krylov exponential of TDVP1 alone: TFI L=40, complex128, D=64 after one FP64
+    TDVP1 step (dt=0.05, stepsize -0.05i), the one-site operator at site 20 (w=3), 20
+    Krylov vectors, exptol 1e-8 as _tdvp1_leftsweep passes it.  Warm-up calls, then timed
+    ones; the timed calls sit between cudaProfilerStart/Stop, which is what an ncu run with
+    --profile-from-start off needs."""
+    import ctypes
+    import finitemptools_gb300 as fm
+    from finitemptools_gb300.derivatives import HeffOp
+    h = fm.default_handle()
+    L, site = 40, 20
+    hs, psi = _tfi_start(fm, h, L=L)
+    env = fm.environments(fm.FiniteMPO(fm.tfi_mpo(hs), L), psi)
+    alg = fm.TDVP1(stepsize=-0.05j, D=64, exptol=1e-8, krylovdim=20, precision="fp64")
+    fm.sweep_(env, alg)
+    mps, mpo, hstore = env.mps, env.mpo, env.hstorage
+    dt = alg.stepsize
+    A = mps[site]
+    op = HeffOp("ac", hstore[site], hstore[site + 1], W1=mpo[site], precision="fp64",
+                dtype=A.dtype)
+    tol = alg.exptol / abs(dt / 2)
+    for _ in range(max(1, args.warmup)):
+        op.exponentiate(dt / 2, A, tol, alg.krylovdim)
+    h.synchronize()
+    import time as _t
+    cuda = ctypes.CDLL("libcuda.so.1")           # cuProfilerStart/Stop: process-wide
+    # the exponential reads its Hessenberg matrix back to the host once per Arnoldi cycle,
+    # so a host clock around synchronised calls times it as well as device events would
+    cuda.cuProfilerStart()
+    t0 = _t.perf_counter()
+    for _ in range(args.steps):
+        op.exponentiate(dt / 2, A, tol, alg.krylovdim)
+    h.synchronize()
+    ms = (_t.perf_counter() - t0) * 1e3 / args.steps
+    cuda.cuProfilerStop()
+    print(json.dumps({"case": "krylov_exp", "L": L, "site": site, "shape": list(A.shape),
+                      "krylovdim": alg.krylovdim, "ms_per_exponential": ms,
+                      "calls": args.steps}), flush=True)
+
+
 def u1_heff_case(args):
     """The block-sparse two-site H_eff*x alone: legs of the centre bond of an L=64,
     total-Sz=0 chain with bond dimension D (sector dimensions from the product-state
@@ -934,6 +974,8 @@ def main():
                          "all 40 fields, central differences on h_20, h_21, h_1, h_40")
     ap.add_argument("--ed-heff", type=int, default=0, metavar="L",
                     help="time the exact-diagonalisation operator of an L-site XXZ chain alone")
+    ap.add_argument("--krylov-exp", action="store_true",
+                    help="one TDVP1 Krylov exponential (TFI L=40 D=64, site 20) alone")
     ap.add_argument("--u1-heff", type=int, default=0, metavar="D",
                     help="only time the block-sparse H_eff*x of an L=64, Sz=0 centre bond "
                          "with bond dimension D (profiling case) and exit")
@@ -943,6 +985,8 @@ def main():
         return run_reference(args)
     if args.u1_heff:
         return u1_heff_case(args)
+    if args.krylov_exp:
+        return krylov_exp_case(args)
     if args.ed_heff:
         return ed_heff_case(args)
 
