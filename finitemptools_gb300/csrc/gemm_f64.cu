@@ -53,34 +53,57 @@ __global__ void __launch_bounds__(NT) gemm_kernel(GemmArgs g, int splits, int kc
 #pragma unroll
     for (int j = 0; j < TPR; j++) { acc[i][j] = 0.0; acci[i][j] = 0.0; }
 
-  for (int k0 = k_lo; k0 < k_hi; k0 += BK) {
-    for (int e = tid; e < BMN * BK; e += NT) {
+  // The K slab k0 .. k0 + BK of A and B goes global -> registers -> shared memory; the
+  // next slab's loads are issued before the current one is multiplied, so that their
+  // latency overlaps the FMAs (a small GEMM runs one block per SM and has nothing else to
+  // hide it behind).  The products are summed in the same order as without it.
+  constexpr int NE = (BMN * BK + NT - 1) / NT;       // slab elements per thread and operand
+  double ra[NE][2], rb[NE][2];
+  auto load_slab = [&](int k0) {
+#pragma unroll
+    for (int q = 0; q < NE; q++) {
+      const int e = tid + q * NT;
+      ra[q][0] = ra[q][1] = rb[q][0] = rb[q][1] = 0.0;
+      if (e >= BMN * BK) continue;
       int mm, kk;
       if (a_mfast) { mm = e % BMN; kk = e / BMN; } else { kk = e % BK; mm = e / BK; }
-      const int gm = m0 + mm, gk = k0 + kk;
-      double vr = 0.0, vi = 0.0;
+      int gm = m0 + mm, gk = k0 + kk;
       if (gm < g.m && gk < k_hi) {
         const int64_t idx = a_index(g.ta, gm, gk, g.lda);
-        vr = __ldg(A + idx);
-        if (CPLX) { vi = __ldg(A + g.planeA + idx); if (conjA) vi = -vi; }
+        ra[q][0] = __ldg(A + idx);
+        if (CPLX) { ra[q][1] = __ldg(A + g.planeA + idx); if (conjA) ra[q][1] = -ra[q][1]; }
       }
-      As[0][kk][mm] = vr;
-      if (CPLX) As[1][kk][mm] = vi;
-    }
-    for (int e = tid; e < BMN * BK; e += NT) {
-      int nn, kk;
+      int nn;
       if (b_kfast) { kk = e % BK; nn = e / BK; } else { nn = e % BMN; kk = e / BMN; }
-      const int gn = n0 + nn, gk = k0 + kk;
-      double vr = 0.0, vi = 0.0;
+      const int gn = n0 + nn;
+      gk = k0 + kk;
       if (gn < g.n && gk < k_hi) {
         const int64_t idx = a_index(g.tb, gk, gn, g.ldb);
-        vr = __ldg(B + idx);
-        if (CPLX) { vi = __ldg(B + g.planeB + idx); if (conjB) vi = -vi; }
+        rb[q][0] = __ldg(B + idx);
+        if (CPLX) { rb[q][1] = __ldg(B + g.planeB + idx); if (conjB) rb[q][1] = -rb[q][1]; }
       }
-      Bs[0][kk][nn] = vr;
-      if (CPLX) Bs[1][kk][nn] = vi;
     }
+  };
+  auto store_slab = [&]() {
+#pragma unroll
+    for (int q = 0; q < NE; q++) {
+      const int e = tid + q * NT;
+      if (e >= BMN * BK) continue;
+      int mm, kk;
+      if (a_mfast) { mm = e % BMN; kk = e / BMN; } else { kk = e % BK; mm = e / BK; }
+      As[0][kk][mm] = ra[q][0];
+      if (CPLX) As[1][kk][mm] = ra[q][1];
+      int nn;
+      if (b_kfast) { kk = e % BK; nn = e / BK; } else { nn = e % BMN; kk = e / BMN; }
+      Bs[0][kk][nn] = rb[q][0];
+      if (CPLX) Bs[1][kk][nn] = rb[q][1];
+    }
+  };
+  if (k_lo < k_hi) load_slab(k_lo);
+  for (int k0 = k_lo; k0 < k_hi; k0 += BK) {
+    store_slab();
     __syncthreads();
+    if (k0 + BK < k_hi) load_slab(k0 + BK);
 #pragma unroll
     for (int kk = 0; kk < BK; kk++) {
       double a[TPR], b[TPR], ai[TPR], bi[TPR];
