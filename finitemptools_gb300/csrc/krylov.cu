@@ -52,11 +52,14 @@ __device__ __forceinline__ void warp_sum_many(double (&a)[K]) {
   for (; o > 0; o >>= 1) a[0] += __shfl_xor_sync(0xffffffffu, a[0], o);
 }
 
-__device__ double block_sum(double v) {
+// Warps at or above nw hold exact zeros (the threads of a block past its elements) and skip
+// their shuffle sums: the result is the same, and their FP64 adds no longer queue on the
+// SM's FP64 pipe in front of the warps with data.
+__device__ double block_sum(double v, int nw = KT / 32) {
   __shared__ double red[KT / 32];
   __shared__ double total;
-  v = warp_sum(v);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  if ((threadIdx.x >> 5) < nw) v = warp_sum(v);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = (threadIdx.x >> 5) < nw ? v : 0.0;
   __syncthreads();
   if (threadIdx.x < 32) {
     double w = threadIdx.x < KT / 32 ? red[threadIdx.x] : 0.0;
@@ -73,7 +76,7 @@ __device__ double block_sum(double v) {
 __device__ double sum_parts(const double* part, int G) {
   double s = 0.0;
   for (int i = threadIdx.x; i < G; i += KT) s += part[i];
-  return block_sum(s);
+  return block_sum(s, G >= KT ? KT / 32 : (G + 31) / 32);
 }
 
 // part[b] = sum x*y over a grid-stride slice (real view of length n)
@@ -175,10 +178,12 @@ __device__ __forceinline__ void multidot_body(int cplx, int64_t n, int j,
       v[2 * c] = sr[c];
       v[2 * c + 1] = si[c];
     }
-    warp_sum_many<2 * MD_CH>(v);
+    // warps past the block's elements hold zeros: they store them without the shuffle sums
+    const bool holds = wid * 32 < epb;
+    if (holds) warp_sum_many<2 * MD_CH>(v);
     {
       constexpr int sh = MD_CH == 16 ? 0 : (MD_CH == 8 ? 1 : (MD_CH == 4 ? 2 : 3));
-      if ((lane & ((1 << sh) - 1)) == 0) red[wid][lane >> sh] = v[0];
+      if ((lane & ((1 << sh) - 1)) == 0) red[wid][lane >> sh] = holds ? v[0] : 0.0;
     }
     __syncthreads();
     if (threadIdx.x < 2 * MD_CH) {
@@ -285,7 +290,7 @@ __device__ __forceinline__ void multi_axpy_body(int cplx, int64_t n, int j,
     s = fma(zr, zr, s);
     if (cplx) s = fma(zi, zi, s);
   }
-  s = block_sum(s);
+  s = block_sum(s, (epb + 31) / 32);
   if (threadIdx.x == 0) part[blockIdx.x] = s;
 }
 
@@ -1085,9 +1090,11 @@ int op_project(fmpt_op* op, double* y, const int* gate) {
 }
 
 // Grid of the Arnoldi orthogonalisation kernels: EPB_A vector elements (complex elements
-// for complex data) per block and pass, so that a D = 64 vector (8192 elements) spreads its
-// FP64 work over 128 SMs instead of 32; at most two blocks per SM.
-constexpr int EPB_A = 64;
+// for complex data) per block and pass.  A D = 64 vector (8192 elements) runs on 64 blocks
+// whose four element-holding warps spread over the SM's four FP64 sub-partitions (one
+// exponential of 20 vectors: 1.92 ms, against 1.97 ms with 64 elements per block on 128
+// SMs and 2.18 ms with 32); at most two blocks per SM.
+constexpr int EPB_A = 128;
 int arnoldi_grid(fmpt_handle* h, int64_t n) {
   const int64_t g = (n + EPB_A - 1) / EPB_A;
   const int64_t cap = 2LL * std::max(1, h->sm_count);
